@@ -1,0 +1,206 @@
+/*
+ * sfdx.h -- C ABI of the GB300-native SFD_EXCMG forward solver.
+ *
+ * Plain C types only (double, int, pointers, sizes); complex arrays are
+ * interleaved (re, im) doubles, i.e. the memory layout of Fortran
+ * complex(8) and C99 double _Complex.  Every entry point returns an SFDX_*
+ * status code instead of stopping the process.
+ *
+ * Mesh conventions are the reference's (sfd_excmg/src/fdfe_main.f90):
+ *   nx, ny        cells along x and y
+ *   nz            cells along z INCLUDING the nair air layers (z index 1 is
+ *                 the top of the air, as in read_input, file_opt.f90:8-95)
+ *   a[nx], b[ny], c[nz]   cell sizes; c holds the air layers first
+ *   sigma         Fortran sigma(ncell,6) = C [6][ncell], ncell = nx*ny*nz,
+ *                 components (xx, yy, zz, xy, xz, yz), cell index
+ *                 (k-1)*nx*ny + (j-1)*nx + i  (file_opt.f90:142)
+ *   nl            nx(ny+1)(nz+1) + (nx+1)ny(nz+1) + (nx+1)(ny+1)nz edges,
+ *                 ordered Ex, Ey, Ez (fdfe_main.f90:261,310,358)
+ *   ex            Fortran ex(2*nl, nf) = C [nf][2][nl] complex: the xy
+ *                 solution followed by the yx solution of each frequency
+ *                 (fwd_solver, fdfe_main.f90:1565-1594)
+ */
+#ifndef SFDX_H
+#define SFDX_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define SFDX_OK 0
+#define SFDX_ERR_ARG 1         /* invalid argument (null pointer, bad size, bad option)     */
+#define SFDX_ERR_MESH 2        /* mesh not divisible by 2^level / level too large            */
+#define SFDX_ERR_CUDA 3        /* CUDA runtime error or no device                            */
+#define SFDX_ERR_NOCONV 4      /* a system reached its iteration limit before the tolerance  */
+#define SFDX_ERR_NAN 5         /* NaN in a right-hand side, guess or residual                */
+#define SFDX_ERR_RECEIVER 6    /* receiver outside the interpolation stencil                 */
+#define SFDX_ERR_IO 7          /* model/data file missing or malformed                       */
+#define SFDX_ERR_UNSUPPORTED 8 /* option combination not implemented                         */
+#define SFDX_ERR_TIMEOUT 9     /* a bounded device wait ran out                              */
+#define SFDX_ERR_NOMEM 10      /* device allocation failed / size above a fixed limit        */
+
+/* quirk bits: reference behaviours that change intermediate results */
+#define SFDX_QUIRK_COARSEN_SHIFT 1   /* mesh_coarsen fine-cell index (fdfe_main.f90:64)          */
+#define SFDX_QUIRK_EXCMG_MIDPOINT 2  /* cal_coef along-edge nodes (excmg.f90:685,711,737)         */
+#define SFDX_QUIRK_RX_TRANSPOSE 4    /* arho_interp2 rd=2 stencil (fdfe_main.f90:763-768)         */
+#define SFDX_QUIRKS_REFERENCE 7
+
+/* solver ids (.fwd line 2, read_input file_opt.f90:102) */
+#define SFDX_SOLVER_BICGSTAB 1
+#define SFDX_SOLVER_TFQMR 2
+#define SFDX_SOLVER_GPBICG 3
+#define SFDX_SOLVER_BICG 4
+#define SFDX_SOLVER_COCR 6
+
+/* precision */
+#define SFDX_FP64 0   /* complex128 everywhere                                    */
+#define SFDX_MIXED 1  /* complex64 operator/smoother/Krylov inside FP64 refinement */
+
+/*
+ * Runtime options.  Defaults (sfdx_default_opts) equal the reference's
+ * compile-time constants in global_para.f90:5-19 and solvers.f90:14.
+ */
+typedef struct sfdx_opts {
+    int level;          /* EXCMG levels, >= 3 (.fwd line 2; argv 2)                    */
+    double eps;         /* finest-level tolerance (.fwd line 2; argv 3)                */
+    int solver;         /* SFDX_SOLVER_*                                               */
+    int excmg;          /* fwd_acc: 0 single solve from zero guess, 1 EXCMG cascade    */
+    int precond;        /* 'S' multi-colour SSOR, 'J' Jacobi (pre_type)                */
+    int div_cor;        /* divergence correction on/off (div_cor)                      */
+    int corr_intv;      /* iterations between corrections (corr_intv = 200)            */
+    double corr_tol;    /* nodal-Poisson PCG tolerance (corr_tol = 1e-3)               */
+    double ssor_omega;  /* SSOR relaxation (ssor_omg = 1)                              */
+    double sigma_air;   /* conductivity written into air cells by readers (1e-9)      */
+    int maxit_plain;    /* iteration limit of the single solve (5000)                  */
+    int maxit_level;    /* iteration limit of each EXCMG level (1000)                  */
+    int precision;      /* SFDX_FP64 | SFDX_MIXED                                      */
+    int quirks;         /* SFDX_QUIRK_* bits (SFDX_QUIRKS_REFERENCE by default)         */
+    double coarse_tol;  /* relative residual of the on-device solve replacing PARDISO */
+    int coarse_maxit;   /* iteration limit of that solve                               */
+    double inner_tol;   /* mixed precision: FP32 inner-solve reduction per refinement  */
+    int inner_maxit;    /* mixed precision: inner iterations per refinement step       */
+    int max_refine;     /* mixed precision: refinement steps                           */
+    int batch;          /* systems solved together (0 = all 2*nf)                      */
+    int verbose;        /* 0 silent, 1 per-level summary on stderr                     */
+    int use_graphs;     /* capture Krylov iterations in CUDA graphs                    */
+} sfdx_opts;
+
+/* Fill *o with the reference defaults. */
+void sfdx_default_opts(sfdx_opts* o);
+
+/* Human-readable text of a status code (static storage). */
+const char* sfdx_strerror(int code);
+
+/* Library version (major*10000 + minor*100 + patch). */
+int sfdx_version(void);
+
+/* ------------------------------------------------------------------------
+ * Forward solve.  Replaces fwd_solver(modelname, a, b, c, nair, level, slv,
+ * eps, sigma, freq, ex) (fdfe_main.f90:1565-1594, called at
+ * sfd_excmg.f90:52).  ex is caller-owned [nf][2][nl] complex.
+ * iters (optional, [nf][2][level]): Krylov iterations per level (reference
+ * iters(1) semantics: loop index at exit) -- levels 1-2 of the cascade
+ * report the on-device coarse solve.  relres (optional, [nf][2]): final
+ * relative residual ||b - A x|| / ||b|| on the finest level.
+ * ------------------------------------------------------------------------ */
+int sfdx_fwd_solve(const sfdx_opts* o, int nx, int ny, int nz, int nair, const double* a, const double* b,
+                   const double* c, const double* sigma, int nf, const double* freq, double* ex, int* iters,
+                   double* relres);
+
+/* ------------------------------------------------------------------------
+ * Reusable plan: device workspace for one mesh and frequency list, so
+ * repeated solves (inversion loops, benchmarks) allocate nothing.
+ * sigma / ex may be host or device pointers (flag *_on_device).
+ * ------------------------------------------------------------------------ */
+typedef struct sfdx_plan sfdx_plan;
+int sfdx_plan_create(sfdx_plan** plan, const sfdx_opts* o, int nx, int ny, int nz, int nair, const double* a,
+                     const double* b, const double* c, int nf, const double* freq);
+int sfdx_plan_solve(sfdx_plan* plan, const double* sigma, int sigma_on_device, double* ex, int ex_on_device,
+                    int* iters, double* relres);
+/* Impedances from the plan's last solution (device resident), see sfdx_impedance. */
+int sfdx_plan_impedance(sfdx_plan* plan, int nrec, const double* recv, int out_type, double* out, double* tipper);
+/* Device pointer of the plan's last solution, layout [nf][2][nl] complex (valid until the next solve). */
+const double* sfdx_plan_fields(sfdx_plan* plan);
+/* Bytes of device memory held by the plan. */
+long long sfdx_plan_device_bytes(const sfdx_plan* plan);
+void sfdx_plan_destroy(sfdx_plan* plan);
+
+/* ------------------------------------------------------------------------
+ * Impedances at the receivers.  Replaces post_process + arho_interp2
+ * (fdfe_main.f90:549-790).  recv: Fortran recv(nrec,3) = C [3][nrec].
+ * out[nf][nrec][4]: out_type 0/1 -> (Re Zxy, Im Zxy, Re Zyx, Im Zyx),
+ * out_type 2 -> (rho_xy, rho_yx, phi_xy, phi_yx).  tipper (optional)
+ * [nf][nrec][4] = (Re Tx, Im Tx, Re Ty, Im Ty).  The receiver stencil follows
+ * SFDX_QUIRK_RX_TRANSPOSE of `quirks`.
+ * ------------------------------------------------------------------------ */
+int sfdx_impedance(int nx, int ny, int nz, int nair, const double* a, const double* b, const double* c, int nf,
+                   const double* freq, const double* ex, int nrec, const double* recv, int out_type, int quirks,
+                   double* out, double* tipper);
+
+/* ------------------------------------------------------------------------
+ * Component entry points (each one replaces one reference routine; all
+ * buffers are host memory, the work runs on the GPU unless noted).
+ * ------------------------------------------------------------------------ */
+
+/* mt1d_anl (model_selec.f90:266-401), host FP64: conv is Fortran
+ * conv(nz,6); edc, hx: 2nz+2 complex; imp: 4 complex. */
+int sfdx_mt1d(double freq, int nz, const double* conv, const double* c, double* edc, double* hx, double* imp);
+
+/* fd_assemb + dcfast as a matrix-free operator (fdfe_main.f90:226-546,
+ * zamux div_correc.f90:431-449): y = K x for ns systems interleaved
+ * ([nl][ns] complex), system s at frequency freqs[s].  precision selects the
+ * FP64 or the complex64 kernel. */
+int sfdx_apply_operator(int nx, int ny, int nz, const double* a, const double* b, const double* c,
+                        const double* sigma, int ns, const double* freqs, int precision, const double* x, double* y);
+
+/* Right-hand sides of dcfast (fdfe_main.f90:470-524): p1 (xy), p2 (yx),
+ * from the 1-D field edc (2nz+2 complex, sfdx_mt1d). */
+int sfdx_build_rhs(int nx, int ny, int nz, const double* a, const double* b, const double* c, const double* sigma,
+                   double freq, const double* edc, double* p1, double* p2);
+
+/* One preconditioner application x = M^{-1} y (replaces ssorfac + lusol,
+ * div_correc.f90:171-220 / solvers.f90:721-762, with the multi-colour
+ * ordering; 'J' replaces diagcsr). */
+int sfdx_precond_apply(int nx, int ny, int nz, const double* a, const double* b, const double* c,
+                       const double* sigma, int ns, const double* freqs, int precond, int precision, const double* y,
+                       double* x);
+
+/* mesh_coarsen (fdfe_main.f90:18-84): k coarsenings (2^k cells merge per
+ * axis); quirk = SFDX_QUIRK_COARSEN_SHIFT bit. */
+int sfdx_mesh_coarsen(int nx, int ny, int nz, const double* a, const double* b, const double* c, const double* sigma,
+                      int k, int quirks, double* a1, double* b1, double* c1, double* sigma1);
+
+/* extint_v (excmg.f90:9-77): EXCMG guess on the fine level (nx,ny,nz,a1,b1,
+ * c1,nair) from the 4h solution u0 and the 2h solution u1; ns systems
+ * interleaved. */
+int sfdx_prolongate(int nx, int ny, int nz, const double* a1, const double* b1, const double* c1, int nair, int ns,
+                    const double* u0, const double* u1, double* u, int quirks);
+
+/* One Krylov solve (Bicg_stab_p solvers.f90:522-719 / pgpbicg :137-315 /
+ * the other solver ids) of K x = rhs on one mesh for ns interleaved systems,
+ * starting from x.  iters[ns], relres[ns] (true residual) are outputs. */
+int sfdx_krylov_solve(const sfdx_opts* o, int nx, int ny, int nz, const double* a, const double* b, const double* c,
+                      const double* sigma, int ns, const double* freqs, const double* rhs, double* x, double tol,
+                      int itmax, int* iters, double* relres);
+
+/* Divergence correction (div_correc.f90:11-147 with fddc_assemb, isotropic
+ * scheme, and Jacobi-PCG :343-402): x += grad(phi), P phi = T x, for ns
+ * interleaved systems.  Returns PCG iterations of system 0 in *pcg_iters. */
+int sfdx_div_correct(int nx, int ny, int nz, const double* a, const double* b, const double* c,
+                     const double* sigma, int ns, double* x, double tol, int* pcg_iters);
+
+/* ------------------------------------------------------------------------
+ * Reference file formats (file_opt.f90).  sfdx_read_model allocates nothing:
+ * call with null arrays to get the sizes, then again with buffers.
+ * ------------------------------------------------------------------------ */
+int sfdx_read_sizes(const char* model_name, int* nx, int* ny, int* nz, int* nair, int* nf, int* nrec);
+int sfdx_read_model(const char* model_name, const sfdx_opts* o, int* level, double* eps, int* solver, int* out_type,
+                    double* a, double* b, double* c, double* sigma, double* freq, double* recv, int* abu);
+int sfdx_write_res(const char* model_name, int nf, const double* freq, int nrec, const double* recv,
+                   const double* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SFDX_H */

@@ -1,0 +1,379 @@
+"""CPU oracle for the SFD_EXCMG forward-solve path -- TEST INFRASTRUCTURE ONLY.
+
+Only tests/, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
+``bench.py`` may import this module, and only as the checker.  The shipped
+library (``sfd_excmg_gb300``) never imports, loads or calls anything here.
+
+It restates the reference's FP64 algorithms: the heavy loops live in
+``sfd_oracle.c`` (index-for-index restatement of fdfe_main.f90, solvers.f90,
+div_correc.f90, excmg.f90, model_selec.f90), the per-frequency orchestration
+(``doublemode_nor`` fdfe_main.f90:892-1063, ``u1u2`` :1228-1256,
+``doublemode_acc`` :1258-1563, ``fwd_solver`` :1565-1594) is restated here.
+
+MKL PARDISO (solvers.f90:765-875, used on the two coarsest EXCMG levels) is
+closed; it is replaced by SciPy's SuperLU (``scipy.sparse.linalg.splu``),
+which, like PARDISO with iterative refinement, returns the direct solution
+to rounding level.
+
+Parity status: UNPINNED against reference outputs -- the reference needs
+ifort + MKL, does not compile as committed, and ships no golden vectors.
+The oracle is pinned by known-answer tests instead (tests/test_oracle_*.py):
+the analytic 1-D layered response, the homogeneous half-space impedance,
+polynomial exactness of the prolongation, and the published DTM1 iteration
+counts where they are reproducible.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+import threading
+from dataclasses import dataclass, field
+
+import numpy as np
+import scipy.sparse as sp
+from scipy.sparse.linalg import splu
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+_BUILD = os.path.join(HERE, "_build")
+_SO = os.path.join(_BUILD, "libsfd_oracle.so")
+_LIB = None
+_LOCK = threading.Lock()
+
+MU = 4 * np.pi * 1e-7
+SIGMA_AIR = 1e-9  # global_para.f90:12
+
+c_double_p = ctypes.POINTER(ctypes.c_double)
+c_int64_p = ctypes.POINTER(ctypes.c_int64)
+c_int32_p = ctypes.POINTER(ctypes.c_int32)
+
+
+def build(force: bool = False) -> str:
+    """Compile sfd_oracle.c into oracle/_build/libsfd_oracle.so (gcc, -O2)."""
+    src = os.path.join(HERE, "sfd_oracle.c")
+    if not force and os.path.exists(_SO) and os.path.getmtime(_SO) >= os.path.getmtime(src):
+        return _SO
+    os.makedirs(_BUILD, exist_ok=True)
+    tmp = _SO + f".{os.getpid()}.tmp"
+    subprocess.check_call(["gcc", "-O2", "-fPIC", "-shared", "-o", tmp, src, "-lm"])
+    os.replace(tmp, _SO)
+    return _SO
+
+
+def lib():
+    global _LIB
+    with _LOCK:
+        if _LIB is None:
+            _LIB = ctypes.CDLL(build())
+            L = _LIB
+            L.orc_assemble.restype = ctypes.c_int64
+            L.orc_solve.restype = ctypes.c_int
+            L.orc_solve.argtypes = [
+                ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, c_double_p, c_double_p, c_double_p,
+                c_double_p, ctypes.c_char, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                ctypes.c_int64, ctypes.c_void_p, c_int64_p, c_int32_p, ctypes.c_void_p, ctypes.c_void_p,
+                ctypes.c_double, ctypes.c_int, c_double_p]
+            L.orc_bicgstab_fixed.restype = ctypes.c_int
+            L.orc_extint_v.restype = ctypes.c_int
+            L.orc_post_process.restype = ctypes.c_int
+            L.orc_div_correc.restype = ctypes.c_int
+            L.orc_ssor_apply.restype = ctypes.c_int
+    return _LIB
+
+
+def _d(x):
+    return np.ascontiguousarray(x, dtype=np.float64)
+
+
+def _z(x):
+    return np.ascontiguousarray(x, dtype=np.complex128)
+
+
+def _p(x, t=c_double_p):
+    return x.ctypes.data_as(t)
+
+
+def nedges(nx, ny, nz):
+    return nx * (ny + 1) * (nz + 1) + (nx + 1) * ny * (nz + 1) + (nx + 1) * (ny + 1) * nz
+
+
+# --------------------------------------------------------------------------
+# Model container (restates read_input's outputs, file_opt.f90:8-95)
+# --------------------------------------------------------------------------
+@dataclass
+class OracleModel:
+    nx: int
+    ny: int
+    nz: int  # total z cells, air included (z index 1 = top of air)
+    nair: int
+    a: np.ndarray
+    b: np.ndarray
+    c: np.ndarray  # length nz, air first
+    sigma: np.ndarray  # shape (6, ncell): Fortran sigma(ncell,6)
+    freq: np.ndarray
+    recv: np.ndarray  # shape (nrec, 3)
+    level: int = 3
+    eps: float = 1e-8
+    solver: int = 1
+    out_type: int = 1
+
+
+@dataclass
+class OracleOpts:
+    excmg: bool = False          # fwd_acc (global_para.f90:19), default 0
+    pre: str = "S"               # pre_type (global_para.f90:18)
+    div_cor: bool = True         # global_para.f90:8
+    corr_intv: int = 200         # global_para.f90:9
+    corr_tol: float = 1e-3       # global_para.f90:10
+    omega: float = 1.0           # ssor_omg (solvers.f90:14)
+    maxit_plain: int = 5000      # fdfe_main.f90:993
+    maxit_level: int = 1000      # fdfe_main.f90:1414
+    coarsen_quirk: bool = True   # mesh_coarsen index shift (fdfe_main.f90:64)
+    midpoint_quirk: bool = True  # cal_coef along-edge nodes (excmg.f90:685)
+    rd: int = 2                  # arho_interp2 stencil (fdfe_main.f90:640,685)
+
+
+# --------------------------------------------------------------------------
+# Thin wrappers over the C restatement
+# --------------------------------------------------------------------------
+def mt1d_anl(ff, conv, c):
+    """mt1d_anl (model_selec.f90:266-401). conv: (nz,6) array; returns ex, hx, imp."""
+    conv = np.asarray(conv, dtype=np.float64)
+    nz = conv.shape[0]
+    cf = np.asfortranarray(conv).ravel(order="F").copy()
+    ex = np.zeros(2 * nz + 2, np.complex128)
+    hx = np.zeros(2 * nz + 2, np.complex128)
+    imp = np.zeros(4, np.complex128)
+    lib().orc_mt1d_anl(ctypes.c_double(ff), ctypes.c_int(nz), _p(cf), _p(_d(c)), _p(ex), _p(hx), _p(imp))
+    return ex, hx, imp
+
+
+def column_conv(sigma, nx, ny, nz):
+    """cont1(k,1:3) = conv((k-1)*nx*ny+1, 1:3), off-diagonals zero (fdfe_main.f90:938-942)."""
+    conv = np.zeros((nz, 6))
+    idx = np.arange(nz) * nx * ny
+    conv[:, 0:3] = sigma[0:3, idx].T
+    return conv
+
+
+def assemble(nx, ny, nz, a, b, c, sigma, ff, edc):
+    """fd_assemb + dcfast: returns (csr K, p1, p2) with the reference's entry order."""
+    nl = nedges(nx, ny, nz)
+    ia = np.zeros(nl + 1, np.int64)
+    ja = np.zeros(13 * nl, np.int32)
+    km = np.zeros(13 * nl, np.complex128)
+    p1 = np.zeros(nl, np.complex128)
+    p2 = np.zeros(nl, np.complex128)
+    sg = _d(sigma)
+    nnz = lib().orc_assemble(nx, ny, nz, _p(_d(a)), _p(_d(b)), _p(_d(c)), _p(sg), ctypes.c_double(ff), _p(_z(edc)),
+                             _p(ia, c_int64_p), _p(ja, c_int32_p), _p(km), _p(p1), _p(p2))
+    K = sp.csr_matrix((km[:nnz].copy(), ja[:nnz].copy(), ia), shape=(nl, nl))
+    return K, p1, p2
+
+
+def boundary_flags(nx, ny, nz):
+    nl = nedges(nx, ny, nz)
+    f = np.zeros(nl, np.uint8)
+    lib().orc_boundary_flags(nx, ny, nz, f.ctypes.data_as(ctypes.c_void_p))
+    return f.astype(bool)
+
+
+def mesh_coarsen(a, b, c, sigma, k, quirk=True):
+    nx, ny, nz = len(a), len(b), len(c)
+    asf = 2 ** k
+    if nx % asf or ny % asf or nz % asf:
+        raise ValueError("mesh_coarsen: sizes not divisible by 2**k")
+    cx, cy, cz = nx // asf, ny // asf, nz // asf
+    a1, b1, c1 = np.zeros(cx), np.zeros(cy), np.zeros(cz)
+    nc = np.zeros((6, cx * cy * cz))
+    lib().orc_mesh_coarsen(nx, ny, nz, _p(_d(a)), _p(_d(b)), _p(_d(c)), _p(_d(sigma)), k, int(quirk), _p(a1), _p(b1),
+                           _p(c1), _p(nc))
+    return a1, b1, c1, nc
+
+
+def solve_krylov(solver, mesh, K, rhs, x0, eps, itmax, opts: OracleOpts):
+    """Bicg_stab_p (solver 1) or pgpbicg (solver 3) on the CSR system."""
+    nx, ny, nz, a, b, c, sigma = mesh
+    x = _z(x0).copy()
+    err = np.zeros(itmax + 1)
+    ia = np.ascontiguousarray(K.indptr, dtype=np.int64)
+    ja = np.ascontiguousarray(K.indices, dtype=np.int32)
+    km = _z(K.data)
+    it = lib().orc_solve(solver, nx, ny, nz, _p(_d(a)), _p(_d(b)), _p(_d(c)), _p(_d(sigma)), opts.pre.encode(),
+                         int(opts.div_cor), opts.corr_intv, opts.corr_tol, opts.omega, K.shape[0],
+                         km.ctypes.data, _p(ia, c_int64_p), _p(ja, c_int32_p), _z(rhs).ctypes.data, x.ctypes.data,
+                         eps, itmax, _p(err))
+    return x, int(it), err[:itmax]
+
+
+def ssor_apply(K, y, omega=1.0):
+    ia = np.ascontiguousarray(K.indptr, dtype=np.int64)
+    ja = np.ascontiguousarray(K.indices, dtype=np.int32)
+    km = _z(K.data)
+    x = np.zeros(K.shape[0], np.complex128)
+    lib().orc_ssor_apply(ctypes.c_int64(K.shape[0]), km.ctypes.data_as(ctypes.c_void_p), _p(ia, c_int64_p),
+                         _p(ja, c_int32_p), ctypes.c_double(omega), _z(y).ctypes.data_as(ctypes.c_void_p),
+                         x.ctypes.data_as(ctypes.c_void_p))
+    return x
+
+
+def div_correc(nx, ny, nz, a, b, c, sigma, x, tol=1e-3):
+    x = _z(x).copy()
+    it = lib().orc_div_correc(nx, ny, nz, _p(_d(a)), _p(_d(b)), _p(_d(c)), _p(_d(sigma)),
+                              x.ctypes.data_as(ctypes.c_void_p), ctypes.c_double(tol))
+    return x, it
+
+
+def divergence(nx, ny, nz, a, b, c, sigma, x):
+    np_ = (nx + 1) * (ny + 1) * (nz + 1)
+    t = np.zeros(np_, np.complex128)
+    lib().orc_divergence(nx, ny, nz, _p(_d(a)), _p(_d(b)), _p(_d(c)), _p(_d(sigma)),
+                         _z(x).ctypes.data_as(ctypes.c_void_p), t.ctypes.data_as(ctypes.c_void_p))
+    return t
+
+
+def extint_v(nx, ny, nz, a1, b1, c1, nair, u0, u1, midpoint_quirk=True):
+    nl = nedges(nx, ny, nz)
+    u = np.zeros(nl, np.complex128)
+    nnan = lib().orc_extint_v(nx, ny, nz, _p(_d(a1)), _p(_d(b1)), _p(_d(c1)), nair, _z(u0).ctypes.data_as(
+        ctypes.c_void_p), _z(u1).ctypes.data_as(ctypes.c_void_p), u.ctypes.data_as(ctypes.c_void_p),
+        int(midpoint_quirk))
+    return u, nnan
+
+
+def interp(m, nx, ny, nz, a, b, c, nair, u, midpoint_quirk=True):
+    """quad_interp_e (m=2) or cubic_interp (m=4) alone; nx.. = output sizes."""
+    out = np.zeros(nedges(nx, ny, nz), np.complex128)
+    f = lib().orc_quad_interp if m == 2 else lib().orc_cubic_interp
+    f(nx, ny, nz, _p(_d(a)), _p(_d(b)), _p(_d(c)), nair, _z(u).ctypes.data_as(ctypes.c_void_p),
+      out.ctypes.data_as(ctypes.c_void_p), int(midpoint_quirk))
+    return out
+
+
+def post_process(model: OracleModel, x1, x2, ff, out_type=1, rd=2):
+    """post_process + arho_interp2 for one frequency. Returns (out[nrec,4], tip[nrec,4], fields[nrec,10])."""
+    nrec = model.recv.shape[0]
+    recv = np.asfortranarray(model.recv, dtype=np.float64).ravel(order="F").copy()
+    out = np.zeros((nrec, 4))
+    tip = np.zeros((nrec, 4))
+    fld = np.zeros((nrec, 10), np.complex128)
+    rc = lib().orc_post_process(model.nx, model.ny, model.nz, model.nair, _p(_d(model.a)), _p(_d(model.b)),
+                                _p(_d(model.c)), ctypes.c_double(ff), _z(x1).ctypes.data_as(ctypes.c_void_p),
+                                _z(x2).ctypes.data_as(ctypes.c_void_p), nrec, _p(recv), out_type, rd, _p(out),
+                                _p(tip), fld.ctypes.data_as(ctypes.c_void_p))
+    if rc != 0:
+        raise ValueError(f"receiver {-rc} lies outside the interpolation stencil")
+    return out, tip, fld
+
+
+# --------------------------------------------------------------------------
+# Orchestration (fdfe_main.f90)
+# --------------------------------------------------------------------------
+@dataclass
+class LevelInfo:
+    level: int
+    nx: int
+    ny: int
+    nz: int
+    iters: list = field(default_factory=list)  # [xy, yx]
+    direct: bool = False
+
+
+def doublemode_nor(nx, ny, nz, a, b, c, sigma, ff, mid, slv, tol, opts: OracleOpts, x0=None):
+    """doublemode_nor (fdfe_main.f90:892-1063): one mesh, both polarisations."""
+    conv = column_conv(sigma, nx, ny, nz)
+    edc, _, _ = mt1d_anl(ff, conv, c)
+    K, p1, p2 = assemble(nx, ny, nz, a, b, c, sigma, ff, edc)
+    mesh = (nx, ny, nz, a, b, c, sigma)
+    info = LevelInfo(0, nx, ny, nz, direct=mid in (1, 2))
+    if mid in (1, 2):
+        lu = splu(K.tocsc())
+        u1 = lu.solve(p1)
+        u2 = lu.solve(p2)
+        return u1, u2, info
+    maxit = opts.maxit_plain
+    nl = K.shape[0]
+    u1, it1, _ = solve_krylov(slv if slv in (1, 3) else 1, mesh, K, p1, np.zeros(nl) if x0 is None else x0[0],
+                              tol, maxit, opts)
+    u2, it2, _ = solve_krylov(slv if slv in (1, 3) else 1, mesh, K, p2, np.zeros(nl) if x0 is None else x0[1],
+                              tol, maxit, opts)
+    info.iters = [it1, it2]
+    return u1, u2, info
+
+
+def doublemode_acc(model: OracleModel, ff, opts: OracleOpts, n_grid=None, eps=None):
+    """doublemode_acc (fdfe_main.f90:1258-1563) with u1u2 (:1228-1256)."""
+    N = model.level if n_grid is None else n_grid
+    tol = (model.eps if eps is None else eps) * 10.0 ** (-N + 1)
+    a, b, c, sigma = model.a, model.b, model.c, model.sigma
+    infos = []
+    # u1u2: levels 1 and 2 solved directly
+    a1, b1, c1, s1 = mesh_coarsen(a, b, c, sigma, N - 1, opts.coarsen_quirk)
+    u01, u02, inf = doublemode_nor(len(a1), len(b1), len(c1), a1, b1, c1, s1, ff, 1, model.solver, tol, opts)
+    inf.level = 1
+    infos.append(inf)
+    a1, b1, c1, s1 = mesh_coarsen(a, b, c, sigma, N - 2, opts.coarsen_quirk)
+    u11, u12, inf = doublemode_nor(len(a1), len(b1), len(c1), a1, b1, c1, s1, ff, 2, model.solver, tol, opts)
+    inf.level = 2
+    infos.append(inf)
+    tol = tol * 10
+    for i in range(3, N + 1):
+        tol = tol * 10
+        if i != N:
+            a1, b1, c1, sf = mesh_coarsen(a, b, c, sigma, N - i, opts.coarsen_quirk)
+        else:
+            a1, b1, c1, sf = a, b, c, sigma
+        nx, ny, nz = len(a1), len(b1), len(c1)
+        nair_l = model.nair // 2 ** (N - i)
+        u21, _ = extint_v(nx, ny, nz, a1, b1, c1, nair_l, u01, u11, opts.midpoint_quirk)
+        u22, _ = extint_v(nx, ny, nz, a1, b1, c1, nair_l, u02, u12, opts.midpoint_quirk)
+        conv = column_conv(sf, nx, ny, nz)
+        edc, _, _ = mt1d_anl(ff, conv, c1)
+        K, p1, p2 = assemble(nx, ny, nz, a1, b1, c1, sf, ff, edc)
+        if np.isnan(np.abs(p1)).any():
+            raise FloatingPointError("NaN value found in the RHS(p1)")
+        mesh = (nx, ny, nz, a1, b1, c1, sf)
+        slv = model.solver if model.solver in (1, 3) else 1
+        x1, it1, _ = solve_krylov(slv, mesh, K, p1, u21, tol, opts.maxit_level, opts)
+        x2, it2, _ = solve_krylov(slv, mesh, K, p2, u22, tol, opts.maxit_level, opts)
+        infos.append(LevelInfo(i, nx, ny, nz, [it1, it2]))
+        u01, u02, u11, u12 = u11, u12, x1, x2
+    return u11, u12, infos
+
+
+def fwd_solver(model: OracleModel, opts: OracleOpts | None = None, freqs=None):
+    """fwd_solver (fdfe_main.f90:1565-1594): returns ex[nf, 2, nl] and per-frequency infos."""
+    opts = opts or OracleOpts()
+    freqs = model.freq if freqs is None else freqs
+    nl = nedges(model.nx, model.ny, model.nz)
+    ex = np.zeros((len(freqs), 2, nl), np.complex128)
+    infos = []
+    for k, ff in enumerate(freqs):
+        if not opts.excmg:
+            u1, u2, inf = doublemode_nor(model.nx, model.ny, model.nz, model.a, model.b, model.c, model.sigma, ff, 0,
+                                         model.solver, model.eps, opts)
+            infos.append([inf])
+        else:
+            u1, u2, inf = doublemode_acc(model, ff, opts)
+            infos.append(inf)
+        ex[k, 0] = u1
+        ex[k, 1] = u2
+    return ex, infos
+
+
+def impedances(model: OracleModel, ex, out_type=1, rd=2, freqs=None):
+    """post_process over all frequencies: results[nf, nrec, 4]."""
+    freqs = model.freq if freqs is None else freqs
+    res = np.zeros((len(freqs), model.recv.shape[0], 4))
+    for k, ff in enumerate(freqs):
+        res[k], _, _ = post_process(model, ex[k, 0], ex[k, 1], ff, out_type, rd)
+    return res
+
+
+def direct_solve(model: OracleModel, ff):
+    """Exact (SuperLU) solution of the fine-mesh system for both polarisations."""
+    conv = column_conv(model.sigma, model.nx, model.ny, model.nz)
+    edc, _, _ = mt1d_anl(ff, conv, model.c)
+    K, p1, p2 = assemble(model.nx, model.ny, model.nz, model.a, model.b, model.c, model.sigma, ff, edc)
+    lu = splu(K.tocsc())
+    return lu.solve(p1), lu.solve(p2), K, p1, p2

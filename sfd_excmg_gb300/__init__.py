@@ -1,0 +1,22 @@
+"""sfd_excmg_gb300 -- GB300-native forward solver for SFD_EXCMG-style 3-D MT modelling.
+
+The compute path is the native library ``_lib/libsfdx.so`` (hand-written
+CUDA for sm_103a behind the C ABI in ``include/sfdx.h``); this package is a
+thin ctypes face over it plus model I/O and synthetic-model generators.
+"""
+from . import capi
+from .capi import FP64, MIXED, QUIRKS_REFERENCE, Opts, SfdxError
+from .model import Model
+from .solver import (Plan, apply_operator, build_rhs, fwd_solve, impedance, krylov_solve, mesh_coarsen, mt1d,
+                     precond_apply, prolongate)
+
+__all__ = [
+    "capi", "Opts", "SfdxError", "FP64", "MIXED", "QUIRKS_REFERENCE", "Model", "Plan", "fwd_solve", "impedance",
+    "mt1d", "apply_operator", "build_rhs", "precond_apply", "mesh_coarsen", "prolongate", "krylov_solve",
+]
+
+
+def build(verbose: bool = False) -> str:
+    """Compile the native library in-tree (sm_103a) and return its path."""
+    from . import _build
+    return _build.build(verbose=verbose)

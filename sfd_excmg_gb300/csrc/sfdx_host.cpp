@@ -1,0 +1,447 @@
+// sfdx_host.cpp -- host-side parts of the forward-solve path that are O(nz)
+// or O(nx*ny) and stay in FP64 on the CPU:
+//   * the analytic 1-D anisotropic layered field (mt1d_anl,
+//     model_selec.f90:266-401) that feeds the Dirichlet boundary values,
+//   * the impedance evaluation (post_process + arho_interp2,
+//     fdfe_main.f90:549-790),
+//   * the reference's model/data/result file formats (file_opt.f90:8-158).
+#include <cmath>
+#include <complex>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "sfdx.h"
+#include "sfdx_host.h"
+
+namespace sfdx {
+
+typedef std::complex<double> zd;
+static const double kPi = 3.141592653589793238462643;
+static const double kMu = 4.0 * 3.141592653589793238462643 * 1e-7;
+
+// -------------------------------------------------------------------- mt1d
+// Propagator form of Pek & Santos (2002) for a stack of anisotropic layers:
+// a 4x4 layer matrix S_i maps (Ex, Ey, Hx, Hy)-like field vectors from the
+// bottom of layer i to its top; the bottom half-space fixes the two decaying
+// modes and the top E is normalised to (1,0) (xy) or (0,1) (yx).
+static void mat4(const zd* A, const zd* B, zd* C) {
+    for (int i = 0; i < 4; i++)
+        for (int j = 0; j < 4; j++) {
+            zd s = 0;
+            for (int k = 0; k < 4; k++) s += A[i * 4 + k] * B[k * 4 + j];
+            C[i * 4 + j] = s;
+        }
+}
+
+int mt1d_anl(double ff, int nz, const double* conv, const double* c, zd* ex, zd* hx, zd* imp) {
+    if (nz <= 0 || !conv || !c || !ex) return SFDX_ERR_ARG;
+    auto CV = [&](int i, int m) { return conv[(size_t)(m - 1) * nz + (i - 1)]; };
+    std::vector<zd> sprod((size_t)16 * (nz + 1), zd(0, 0));
+    zd m[16];
+    for (auto& q : m) q = 0;
+    const double w = 2 * kPi * ff;
+    const zd iwm = zd(0, 1) * w * kMu;
+    for (int i = 0; i < 4; i++) sprod[(size_t)nz * 16 + i * 4 + i] = 1.0;
+    for (int i = nz; i >= 1; i--) {
+        double axx = CV(i, 1) - CV(i, 5) * CV(i, 5) / CV(i, 3);
+        double ayy = CV(i, 2) - CV(i, 6) * CV(i, 6) / CV(i, 3);
+        double axy = CV(i, 4) - CV(i, 5) * CV(i, 6) / CV(i, 3);
+        double ada = axx + ayy, add = axx - ayy;
+        double da12 = std::sqrt(add * add + 4 * axy * axy);
+        if (add < 0) da12 = -da12;
+        double a1 = (ada + da12) / 2, a2 = (ada - da12) / 2;
+        zd kp = std::sqrt(-iwm) * std::sqrt(a1), km = std::sqrt(-iwm) * std::sqrt(a2);
+        zd xp = -kp / iwm, xm = -km / iwm;
+        double qp = 0, qm = 0;
+        if (axy != 0) {
+            qp = 2 * axy / (add + da12);
+            qm = (add - da12) / axy / 2;
+        }
+        double qdq = qp * qm, dq = 1 - qdq;
+        if (i == nz) {  // bottom half-space: the two downward-decaying modes
+            m[0 * 4 + 1] = 1.0;
+            m[1 * 4 + 1] = qp;
+            m[2 * 4 + 1] = -xp * qp;
+            m[3 * 4 + 1] = xp;
+            m[0 * 4 + 3] = qm;
+            m[1 * 4 + 3] = 1.0;
+            m[2 * 4 + 3] = -xm;
+            m[3 * 4 + 3] = xm * qm;
+        }
+        zd t = kp * c[i - 1];
+        zd sp = (std::exp(t) - std::exp(-t)) / 2.0, cp = (std::exp(t) + std::exp(-t)) / 2.0;
+        t = km * c[i - 1];
+        zd sm = (std::exp(t) - std::exp(-t)) / 2.0, cm = (std::exp(t) + std::exp(-t)) / 2.0;
+        zd s[16] = {cp - qdq * cm,           -qm * (cp - cm),          qm * (sp / xp - sm / xm), sp / xp - qdq * sm / xm,
+                    qp * (cp - cm),          -qdq * cp + cm,           qdq * sp / xp - sm / xm,  qp * (sp / xp - sm / xm),
+                    -qp * (xp * sp - xm * sm), qdq * xp * sp - xm * sm, -qdq * cp + cm,          -qp * (cp - cm),
+                    xp * sp - qdq * xm * sm, -qm * (xp * sp - xm * sm), qm * (cp - cm),           cp - qdq * cm};
+        for (auto& q : s) q /= dq;
+        mat4(s, &sprod[(size_t)i * 16], &sprod[(size_t)(i - 1) * 16]);
+    }
+    zd sm4[16];
+    mat4(&sprod[0], m, sm4);
+    zd bot[8];
+    for (int mode = 0; mode < 2; mode++) {
+        zd e0 = mode == 0 ? zd(1, 0) : zd(0, 1);
+        zd g11 = sm4[1], g21 = sm4[5], g12 = sm4[3], g22 = sm4[7];
+        zd det = g11 * g22 - g12 * g21;
+        zd cb[4] = {0, (g22 * e0.real() - g12 * e0.imag()) / det, 0, (-g21 * e0.real() + g11 * e0.imag()) / det};
+        zd mc[4];
+        for (int r = 0; r < 4; r++) {
+            zd a = 0;
+            for (int q = 0; q < 4; q++) a += m[r * 4 + q] * cb[q];
+            mc[r] = a;
+        }
+        for (int i = 1; i <= nz + 1; i++) {
+            zd f[4];
+            for (int r = 0; r < 4; r++) {
+                zd a = 0;
+                for (int q = 0; q < 4; q++) a += sprod[(size_t)(i - 1) * 16 + r * 4 + q] * mc[q];
+                f[r] = a;
+            }
+            if (mode == 0) {
+                ex[i - 1] = f[0];
+                if (hx) hx[i - 1] = f[3];
+            } else {
+                ex[i + nz] = f[1];
+                if (hx) hx[i + nz] = f[2];
+            }
+            if (i == nz + 1)
+                for (int r = 0; r < 4; r++) bot[mode * 4 + r] = f[r];
+        }
+    }
+    if (imp) {
+        zd t = bot[2] * bot[7] - bot[3] * bot[6];
+        imp[0] = (bot[0] * bot[7] - bot[4] * bot[3]) / t;
+        imp[1] = (bot[4] * bot[2] - bot[0] * bot[6]) / t;
+        imp[2] = (bot[1] * bot[7] - bot[5] * bot[3]) / t;
+        imp[3] = (bot[5] * bot[2] - bot[1] * bot[6]) / t;
+    }
+    for (int q = 0; q < 2 * nz + 2; q++)
+        if (std::isnan(std::abs(ex[q]))) return SFDX_ERR_NAN;
+    return SFDX_OK;
+}
+
+// -------------------------------------------------------------------- impedance
+// Surface fields at cell centres of node plane nair+1 from the edge solution
+// (fdfe_main.f90:601-683), then a 3x3 quadratic Lagrange interpolation to the
+// receivers (arho_interp2, :718-790) and Z from the two polarisations
+// (:687-705).  `surf` supplies the few edge planes the evaluation reads.
+static double qcoef(double x, const double* x0, int q) {
+    if (q == 0) return (x - x0[1]) * (x - x0[2]) / (x0[0] - x0[1]) / (x0[0] - x0[2]);
+    if (q == 1) return (x - x0[0]) * (x - x0[2]) / (x0[1] - x0[0]) / (x0[1] - x0[2]);
+    return (x - x0[0]) * (x - x0[1]) / (x0[2] - x0[0]) / (x0[2] - x0[1]);
+}
+
+int impedance_from_surface(const SurfaceView& sv, const double* a, const double* b, const double* c, double ff,
+                           int nrec, const double* recv, int out_type, int transpose, double* out, double* tip) {
+    const int nx = sv.nx, ny = sv.ny, nair = sv.nair;
+    const size_t nxy = (size_t)nx * ny;
+    std::vector<zd> E[2][2], H[2][3];  // E[pol][x|y], H[pol][x|y|z] at (i,j)
+    for (int p = 0; p < 2; p++) {
+        for (int q = 0; q < 2; q++) E[p][q].assign(nxy, 0);
+        for (int q = 0; q < 3; q++) H[p][q].assign(nxy, 0);
+    }
+    const zd iwm = zd(0, 1) * 2.0 * kPi * ff * kMu;
+    const double cz = c[nair];
+    for (int p = 0; p < 2; p++)
+        for (int j = 0; j < ny; j++)
+            for (int i = 0; i < nx; i++) {
+                // Ex at plane m (=nair) and m+1, rows j, j+1; Ey at columns i, i+1; Ez layer m+1
+                zd ex0 = (sv.ex(p, 0, i, j) + sv.ex(p, 0, i, j + 1)) / 2.0;
+                zd ey0 = (sv.ey(p, 0, i, j) + sv.ey(p, 0, i + 1, j)) / 2.0;
+                E[p][0][(size_t)j * nx + i] = ex0;
+                E[p][1][(size_t)j * nx + i] = ey0;
+                zd exz = ((sv.ex(p, 1, i, j) + sv.ex(p, 1, i, j + 1)) / 2.0 - ex0) / cz;
+                zd ezx = ((sv.ez(p, i + 1, j) + sv.ez(p, i + 1, j + 1)) / 2.0 - (sv.ez(p, i, j + 1) + sv.ez(p, i, j)) / 2.0) / a[i];
+                zd eyz = ((sv.ey(p, 1, i, j) + sv.ey(p, 1, i + 1, j)) / 2.0 - ey0) / cz;
+                zd ezy = (-(sv.ez(p, i, j) + sv.ez(p, i + 1, j)) / 2.0 + (sv.ez(p, i, j + 1) + sv.ez(p, i + 1, j + 1)) / 2.0) / b[j];
+                zd exy = (sv.ex(p, 0, i, j + 1) - sv.ex(p, 0, i, j)) / b[j];
+                zd eyx = (sv.ey(p, 0, i + 1, j) - sv.ey(p, 0, i, j)) / a[i];
+                H[p][1][(size_t)j * nx + i] = (exz - ezx) / iwm;
+                H[p][0][(size_t)j * nx + i] = (ezy - eyz) / iwm;
+                H[p][2][(size_t)j * nx + i] = (exy - eyx) / iwm;
+            }
+    // cell-centre coordinates (arho_interp2 :729-735)
+    std::vector<double> aax(nx), bby(ny);
+    double sa = 0, sb = 0;
+    for (int i = 0; i < nx; i++) sa += a[i];
+    for (int i = 0; i < ny; i++) sb += b[i];
+    aax[0] = (a[0] - sa) / 2;
+    bby[0] = (b[0] - sb) / 2;
+    for (int i = 2; i <= nx; i++) {
+        double s = 0;
+        for (int q = 0; q < i - 1; q++) s += a[q];
+        aax[i - 1] = -sa / 2 + s + a[i - 1] / 2;
+    }
+    for (int i = 2; i <= ny; i++) {
+        double s = 0;
+        for (int q = 0; q < i - 1; q++) s += b[q];
+        bby[i - 1] = -sb / 2 + s + b[i - 1] / 2;
+    }
+    for (int r = 0; r < nrec; r++) {
+        double xr = recv[r], yr = recv[(size_t)nrec + r];
+        int irec = -1, jrec = -1;
+        for (int j = 1; j <= nx - 1; j++)
+            if (xr >= aax[j - 1] && xr <= aax[j]) { irec = j; break; }
+        for (int j = 1; j <= ny - 1; j++)
+            if (yr >= bby[j - 1] && yr <= bby[j]) { jrec = j; break; }
+        if (irec < 2 || jrec < 2 || irec + 1 > nx || jrec + 1 > ny) return SFDX_ERR_RECEIVER;
+        if (transpose && (jrec + 1 > nx || irec + 1 > ny)) return SFDX_ERR_RECEIVER;
+        double c1[3], c2[3];
+        for (int q = 0; q < 3; q++) c1[q] = qcoef(xr, &aax[irec - 2], q);
+        for (int q = 0; q < 3; q++) c2[q] = qcoef(yr, &bby[jrec - 2], q);
+        zd f[2][5];
+        for (int p = 0; p < 2; p++) {
+            for (int q = 0; q < 5; q++) f[p][q] = 0;
+            for (int mm = 1; mm <= 3; mm++)
+                for (int nn = 1; nn <= 3; nn++) {
+                    double w = c1[mm - 1] * c2[nn - 1];
+                    // 1-based (I,J) of the field array; transposed stencil as rd=2
+                    int I = transpose ? mm + jrec - 2 : mm + irec - 2;
+                    int J = transpose ? nn + irec - 2 : nn + jrec - 2;
+                    size_t id = (size_t)(J - 1) * nx + (I - 1);
+                    size_t idz = (size_t)(nn + jrec - 3) * nx + (mm + irec - 3);
+                    f[p][0] += w * E[p][0][id];
+                    f[p][1] += w * E[p][1][id];
+                    f[p][2] += w * H[p][0][id];
+                    f[p][3] += w * H[p][1][id];
+                    f[p][4] += w * H[p][2][idz];
+                }
+        }
+        zd det = f[0][2] * f[1][3] - f[1][2] * f[0][3];
+        zd zxy = (f[1][0] * f[0][2] - f[0][0] * f[1][2]) / det;
+        zd zyx = (f[0][1] * f[1][3] - f[1][1] * f[0][3]) / det;
+        double* o = out + (size_t)r * 4;
+        if (out_type == 2) {
+            double wmu = 2.0 * kPi * ff * kMu;
+            o[0] = std::abs(zxy * zxy * zd(0, 1)) / wmu;
+            o[1] = std::abs(zyx * zyx * zd(0, 1)) / wmu;
+            o[2] = -std::atan(zxy.imag() / zxy.real()) * 180.0 / kPi;
+            o[3] = -std::atan(zyx.imag() / zyx.real()) * 180.0 / kPi;
+        } else {
+            o[0] = zxy.real();
+            o[1] = zxy.imag();
+            o[2] = zyx.real();
+            o[3] = zyx.imag();
+        }
+        if (tip) {
+            zd tx = (f[1][3] * f[0][4] - f[0][3] * f[1][4]) / det;
+            zd ty = (f[0][2] * f[1][4] - f[1][2] * f[0][4]) / det;
+            double* t = tip + (size_t)r * 4;
+            t[0] = tx.real();
+            t[1] = tx.imag();
+            t[2] = ty.real();
+            t[3] = ty.imag();
+        }
+    }
+    return SFDX_OK;
+}
+
+// -------------------------------------------------------------------- files
+// read_input (file_opt.f90:8-95) + read_topo (:97-128): list-directed reads
+// are whitespace-separated numbers; the first line is a free-text title.
+struct Tok {
+    FILE* f;
+    explicit Tok(FILE* ff) : f(ff) {}
+    bool skip_line() {
+        int ch;
+        while ((ch = fgetc(f)) != EOF && ch != '\n') {
+        }
+        return ch != EOF;
+    }
+    bool num(double& v) {
+        char buf[128];
+        if (fscanf(f, "%127s", buf) != 1) return false;
+        for (char* p = buf; *p; p++)
+            if (*p == 'd' || *p == 'D') *p = 'e';  // Fortran exponent letter
+        char* end;
+        v = strtod(buf, &end);
+        return end != buf;
+    }
+    bool inum(int& v) {
+        double d;
+        if (!num(d)) return false;
+        v = (int)d;
+        return true;
+    }
+};
+
+struct ModelHeader {
+    int level, solver, out_type, nx, ny, nz, nair, topo, conduc_type, nf, nrec;
+    double eps, ext[2];
+    int abu[6];
+};
+
+static int read_header(Tok& t, ModelHeader& h) {
+    if (!t.skip_line()) return SFDX_ERR_IO;
+    if (!t.inum(h.level) || !t.num(h.eps) || !t.inum(h.solver) || !t.inum(h.out_type)) return SFDX_ERR_IO;
+    if (!t.inum(h.nx) || !t.inum(h.ny) || !t.inum(h.nz) || !t.inum(h.nair) || !t.inum(h.topo)) return SFDX_ERR_IO;
+    return SFDX_OK;
+}
+
+}  // namespace sfdx
+
+using namespace sfdx;
+
+extern "C" int sfdx_read_sizes(const char* name, int* nx, int* ny, int* nz, int* nair, int* nf, int* nrec) {
+    if (!name) return SFDX_ERR_ARG;
+    std::string base(name);
+    FILE* f = fopen((base + ".fwd").c_str(), "r");
+    if (!f) return SFDX_ERR_IO;
+    Tok t(f);
+    ModelHeader h{};
+    int rc = read_header(t, h);
+    fclose(f);
+    if (rc) return rc;
+    FILE* g = fopen((base + ".dat").c_str(), "r");
+    if (!g) return SFDX_ERR_IO;
+    Tok u(g);
+    int nfr = 0, nr = 0;
+    double d;
+    if (!u.inum(nfr)) { fclose(g); return SFDX_ERR_IO; }
+    for (int i = 0; i < nfr; i++)
+        if (!u.num(d)) { fclose(g); return SFDX_ERR_IO; }
+    if (!u.inum(nr)) { fclose(g); return SFDX_ERR_IO; }
+    fclose(g);
+    if (nx) *nx = h.nx;
+    if (ny) *ny = h.ny;
+    if (nz) *nz = h.nz + h.nair;  // total z cells, air included
+    if (nair) *nair = h.nair;
+    if (nf) *nf = nfr;
+    if (nrec) *nrec = nr;
+    return SFDX_OK;
+}
+
+extern "C" int sfdx_read_model(const char* name, const sfdx_opts* o, int* level, double* eps, int* solver,
+                               int* out_type, double* a, double* b, double* c, double* sigma, double* freq,
+                               double* recv, int* abu) {
+    if (!name || !a || !b || !c || !sigma || !freq || !recv) return SFDX_ERR_ARG;
+    sfdx_opts def;
+    sfdx_default_opts(&def);
+    if (!o) o = &def;
+    std::string base(name);
+    FILE* f = fopen((base + ".fwd").c_str(), "r");
+    if (!f) return SFDX_ERR_IO;
+    Tok t(f);
+    ModelHeader h{};
+    int rc = read_header(t, h);
+    if (rc) { fclose(f); return rc; }
+    // range checks of read_input (file_opt.f90:22-39)
+    if (h.level < 3 || h.solver < 0 || h.solver >= 5 || h.out_type < 0 || h.out_type >= 3 ||
+        h.nx / (1 << h.level) < 2) {
+        fclose(f);
+        return SFDX_ERR_ARG;
+    }
+    const int nx = h.nx, ny = h.ny, nze = h.nz, nair = h.nair, nzt = nze + nair;
+    for (int i = 0; i < nx; i++) if (!t.num(a[i])) { fclose(f); return SFDX_ERR_IO; }
+    for (int i = 0; i < ny; i++) if (!t.num(b[i])) { fclose(f); return SFDX_ERR_IO; }
+    for (int i = 0; i < nze; i++) if (!t.num(c[nair + i])) { fclose(f); return SFDX_ERR_IO; }
+    if (!t.num(h.ext[0]) || !t.num(h.ext[1])) { fclose(f); return SFDX_ERR_IO; }
+    for (int q = 0; q < 6; q++) if (!t.inum(h.abu[q])) { fclose(f); return SFDX_ERR_IO; }
+    for (int i = 0; i < nair; i++) c[i] = c[nzt - 1 - i];  // c(1:nair) = c(nz+nair:nz+1:-1)
+    if (!t.inum(h.conduc_type)) { fclose(f); return SFDX_ERR_IO; }
+    const size_t ncell = (size_t)nx * ny * nzt;
+    for (size_t q = 0; q < 6 * ncell; q++) sigma[q] = 0;
+    for (int k = 1; k <= nze; k++)
+        for (int j = 1; j <= ny; j++)
+            for (int i = 1; i <= nx; i++) {
+                size_t id = (size_t)(nair + k - 1) * nx * ny + (size_t)(j - 1) * nx + (i - 1);
+                double v[6] = {0, 0, 0, 0, 0, 0};
+                int nv = h.conduc_type == 1 ? 1 : (h.conduc_type == 2 ? 3 : 6);
+                for (int q = 0; q < nv; q++) if (!t.num(v[q])) { fclose(f); return SFDX_ERR_IO; }
+                if (h.conduc_type == 1) v[1] = v[2] = v[0];
+                for (int q = 0; q < 6; q++) sigma[q * ncell + id] = v[q];
+            }
+    fclose(f);
+    for (size_t id = 0; id < (size_t)nair * nx * ny; id++)
+        for (int q = 0; q < 3; q++) sigma[q * ncell + id] = o->sigma_air;
+    if (h.topo != 0) {
+        // read_topo (file_opt.f90:97-128): air cells below the local surface
+        // take the earth conductivity sigma_hhs; the reference writes it into
+        // components 1, 4 and 6 (xx, xy, yz), kept here as written.
+        FILE* g = fopen((base + ".topo").c_str(), "r");
+        if (!g) return SFDX_ERR_IO;
+        Tok u(g);
+        int n1, n2;
+        if (!u.inum(n1) || !u.inum(n2)) { fclose(g); return SFDX_ERR_IO; }
+        const double cstep = c[nair];
+        const double sigma_hhs = 1e-2;  // global_para.f90:12
+        for (int j = n1; j <= n2; j++)
+            for (int i = n1; i <= n2; i++) {
+                double tv;
+                if (!u.num(tv)) { fclose(g); return SFDX_ERR_IO; }
+                int n3 = (int)(tv / cstep);
+                for (int k = 1; k <= n3; k++) {
+                    long long id = (long long)(nair - n3 + k - 1) * nx * ny + (long long)(j - 1) * nx + (i - 1);
+                    if (id < 0 || id >= (long long)ncell) continue;
+                    sigma[0 * ncell + id] = sigma_hhs;
+                    sigma[3 * ncell + id] = sigma_hhs;
+                    sigma[5 * ncell + id] = sigma_hhs;
+                }
+            }
+        fclose(g);
+    }
+    FILE* g = fopen((base + ".dat").c_str(), "r");
+    if (!g) return SFDX_ERR_IO;
+    Tok u(g);
+    int nf, nrec;
+    if (!u.inum(nf)) { fclose(g); return SFDX_ERR_IO; }
+    for (int i = 0; i < nf; i++) if (!u.num(freq[i])) { fclose(g); return SFDX_ERR_IO; }
+    if (!u.inum(nrec)) { fclose(g); return SFDX_ERR_IO; }
+    for (int i = 0; i < nrec; i++)
+        for (int q = 0; q < 3; q++) if (!u.num(recv[(size_t)q * nrec + i])) { fclose(g); return SFDX_ERR_IO; }
+    fclose(g);
+    if (level) *level = h.level;
+    if (eps) *eps = h.eps;
+    if (solver) *solver = h.solver;
+    if (out_type) *out_type = h.out_type;
+    if (abu) for (int q = 0; q < 6; q++) abu[q] = h.abu[q];
+    return SFDX_OK;
+}
+
+// output_data (file_opt.f90:131-158): format 4(e12.5,2x),i1,2x,4(e12.5,2x).
+// The reference prints an unset loop variable in the i1 field; 0 is written.
+static void fortran_e12_5(char* buf, double v) {
+    // Fortran Ew.d: 0.ddddde+xx  (buf holds 32 chars)
+    if (v == 0) { snprintf(buf, 32, " 0.00000E+00"); return; }
+    int ex = (int)std::floor(std::log10(std::fabs(v))) + 1;
+    double m = v / std::pow(10.0, ex);
+    if (std::fabs(m) >= 0.999995) { m /= 10; ex += 1; }
+    if (std::fabs(m) < 0.1) { m *= 10; ex -= 1; }
+    char mant[16];
+    snprintf(mant, sizeof mant, "%.5f", std::fabs(m));
+    snprintf(buf, 32, "%s%s%c%c%02d", v < 0 ? "-" : " ", mant, 'E', ex < 0 ? '-' : '+', std::abs(ex) % 100);
+}
+
+extern "C" int sfdx_write_res(const char* name, int nf, const double* freq, int nrec, const double* recv,
+                              const double* out) {
+    if (!name || !freq || !recv || !out) return SFDX_ERR_ARG;
+    FILE* f = fopen((std::string(name) + ".res").c_str(), "w");
+    if (!f) return SFDX_ERR_IO;
+    char b[32];
+    for (int k = 0; k < nf; k++)
+        for (int i = 0; i < nrec; i++) {
+            for (int q = 0; q < 3; q++) { fortran_e12_5(b, recv[(size_t)q * nrec + i]); fprintf(f, "%s  ", b); }
+            fortran_e12_5(b, freq[k]);
+            fprintf(f, "%s  0  ", b);
+            for (int q = 0; q < 4; q++) {
+                fortran_e12_5(b, out[((size_t)k * nrec + i) * 4 + q]);
+                fprintf(f, "%s  ", b);
+            }
+            fprintf(f, "\n");
+        }
+    fclose(f);
+    return SFDX_OK;
+}
+
+extern "C" int sfdx_mt1d(double freq, int nz, const double* conv, const double* c, double* edc, double* hx,
+                         double* imp) {
+    if (!conv || !c || !edc || nz <= 0) return SFDX_ERR_ARG;
+    return sfdx::mt1d_anl(freq, nz, conv, c, reinterpret_cast<zd*>(edc), reinterpret_cast<zd*>(hx),
+                          reinterpret_cast<zd*>(imp));
+}

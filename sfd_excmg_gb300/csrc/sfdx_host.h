@@ -1,0 +1,32 @@
+// sfdx_host.h -- declarations shared by the host-side translation units.
+#pragma once
+#include <complex>
+#include <cstddef>
+
+namespace sfdx {
+
+// mt1d_anl restatement (sfdx_host.cpp); conv is Fortran conv(nz,6).
+int mt1d_anl(double ff, int nz, const double* conv, const double* c, std::complex<double>* ex,
+             std::complex<double>* hx, std::complex<double>* imp);
+
+// The edge planes the impedance evaluation reads, for both polarisations:
+//   ex planes m=nair and m+1 (node planes nair+1, nair+2; [2][ny+1][nx]),
+//   ey planes m and m+1 ([2][ny][nx+1]), ez layer m ([ny+1][nx+1]).
+struct SurfaceView {
+    int nx, ny, nair;
+    const std::complex<double>* exs[2];
+    const std::complex<double>* eys[2];
+    const std::complex<double>* ezs[2];
+    std::complex<double> ex(int p, int plane, int i, int j) const {
+        return exs[p][((size_t)plane * (ny + 1) + j) * nx + i];
+    }
+    std::complex<double> ey(int p, int plane, int i, int j) const {
+        return eys[p][((size_t)plane * ny + j) * (nx + 1) + i];
+    }
+    std::complex<double> ez(int p, int i, int j) const { return ezs[p][(size_t)j * (nx + 1) + i]; }
+};
+
+int impedance_from_surface(const SurfaceView& sv, const double* a, const double* b, const double* c, double ff,
+                           int nrec, const double* recv, int out_type, int transpose, double* out, double* tip);
+
+}  // namespace sfdx

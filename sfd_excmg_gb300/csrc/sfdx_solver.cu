@@ -1,0 +1,1100 @@
+// sfdx_solver.cu -- host drivers and the C ABI of the GB300 forward solver.
+//
+// One plan = one mesh hierarchy + one frequency list.  All 2*nf systems
+// (frequency x polarisation) of a model are solved together: their vectors
+// are interleaved innermost so that every kernel reads the shared
+// conductivity and spacing tables once for the whole batch.
+//
+//  fwd_solver (fdfe_main.f90:1565)            -> sfdx_plan_solve
+//    doublemode_nor (:892, fwd_acc = 0)       -> solve_plain
+//    doublemode_acc (:1258, fwd_acc = 1)      -> solve_cascade
+//      u1u2 + pardiso_spd (:1228, :765)       -> coarse levels: FP64 Krylov to coarse_tol
+//      extint_v (excmg.f90:9)                 -> prolongate (k_interp, k_extrapolate)
+//    Bicg_stab_p (solvers.f90:522)            -> bicgstab<T>
+//    lusol/ssorfac (multi-colour)             -> precond<T>
+//  mixed precision                            -> solve_level_mixed (FP64 residual,
+//                                                complex64 inner BiCGStab)
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <memory>
+#include <type_traits>
+#include <vector>
+
+#include "sfdx.h"
+#include "sfdx_excmg.cuh"
+#include "sfdx_host.h"
+#include "sfdx_kernels.cuh"
+
+using namespace sfdx;
+
+namespace sfdx {
+
+static const double kPi = 3.141592653589793238462643;
+static const double kMu = 4.0 * 3.141592653589793238462643 * 1e-7;
+
+#define CK(call)                                                        \
+    do {                                                                \
+        cudaError_t e_ = (call);                                        \
+        if (e_ != cudaSuccess) {                                        \
+            if (getenv("SFDX_DEBUG"))                                   \
+                fprintf(stderr, "sfdx: CUDA %s at %s:%d\n", cudaGetErrorString(e_), __FILE__, __LINE__); \
+            return SFDX_ERR_CUDA;                                       \
+        }                                                               \
+    } while (0)
+#define RC(call)                       \
+    do {                               \
+        int r_ = (call);               \
+        if (r_ != SFDX_OK) return r_;  \
+    } while (0)
+
+static int g_nsm = 0;
+static int device_sms() {
+    if (!g_nsm) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&g_nsm, cudaDevAttrMultiProcessorCount, dev);
+        if (g_nsm <= 0) g_nsm = 1;
+    }
+    return g_nsm;
+}
+
+// block size: ns * 2^k in [128, 1024] and >= 2*ns (reductions need NQ*ns <= B)
+static int block_for(int ns) {
+    int b = ns;
+    while (b < 128 || b < 2 * ns) b *= 2;
+    return b;
+}
+static int grid_for(int64_t work, int B, int per_sm = 8) {
+    int64_t g = (work + B - 1) / B;
+    int64_t cap = (int64_t)device_sms() * per_sm;
+    if (g > cap) g = cap;
+    if (g < 1) g = 1;
+    return (int)g;
+}
+
+// ------------------------------------------------------------------ device buffers
+struct DBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    ~DBuf() {
+        if (p) cudaFree(p);
+    }
+    int alloc(size_t n) {
+        if (n <= bytes) return SFDX_OK;
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+        if (cudaMalloc(&p, n) != cudaSuccess) return SFDX_ERR_NOMEM;
+        bytes = n;
+        return SFDX_OK;
+    }
+    template <class X> X* as() const { return reinterpret_cast<X*>(p); }
+};
+
+// ------------------------------------------------------------------ mesh level
+struct Level {
+    int nx = 0, ny = 0, nz = 0, nair = 0;
+    int64_t xnl = 0, ynl = 0, nl = 0, ncell = 0;
+    std::vector<double> a, b, c;
+    int aniso = 0;
+    DBuf tab64, tab32;     // [3 axes][6 arrays][stride]
+    DBuf sig64, sig32;     // [6][ncell]
+    DBuf spac;             // a, b, c (device, FP64) for coarsening
+    DBuf crd_cubic;        // node coordinates used by cubic_interp on this level
+    DBuf crd_quad;         // node coordinates used by quad_interp_e (pairwise sums of a,b,c)
+    int stride = 0;
+
+    void set_dims(int X, int Y, int Z) {
+        nx = X; ny = Y; nz = Z;
+        xnl = (int64_t)nx * (ny + 1) * (nz + 1);
+        ynl = (int64_t)(nx + 1) * ny * (nz + 1);
+        nl = xnl + ynl + (int64_t)(nx + 1) * (ny + 1) * nz;
+        ncell = (int64_t)nx * ny * nz;
+    }
+    template <class T> Lev<T> lev() const;
+};
+
+static void axis_tables(const std::vector<double>& h, int stride, double* out) {
+    const int n = (int)h.size();
+    double* rh = out;
+    double* lo = out + stride;
+    double* hi = out + 2 * stride;
+    double* rs = out + 3 * stride;
+    double* wl = out + 4 * stride;
+    double* wh = out + 5 * stride;
+    for (int q = 0; q < 6 * stride; q++) out[q] = 0;
+    for (int i = 0; i < n; i++) rh[i] = 1.0 / h[i];
+    for (int m = 1; m < n; m++) {
+        double s = h[m - 1] + h[m];
+        lo[m] = -2 / (h[m - 1] * (h[m - 1] + h[m]));
+        hi[m] = -2 / (h[m] * (h[m - 1] + h[m]));
+        rs[m] = 1.0 / s;
+        wl[m] = h[m - 1] / s;
+        wh[m] = h[m] / s;
+    }
+}
+
+template <class T> static AxisT<T> axis_ptrs(const T* base, int stride, int axis) {
+    const T* p = base + (size_t)axis * 6 * stride;
+    AxisT<T> a;
+    a.rh = p;
+    a.lo = p + stride;
+    a.hi = p + 2 * stride;
+    a.rs = p + 3 * stride;
+    a.wlo = p + 4 * stride;
+    a.whi = p + 5 * stride;
+    return a;
+}
+template <class T> Lev<T> Level::lev() const {
+    Lev<T> L;
+    L.nx = nx; L.ny = ny; L.nz = nz;
+    L.xnl = xnl; L.ynl = ynl; L.nl = nl; L.ncell = ncell;
+    const T* base = std::is_same<T, double>::value ? (const T*)tab64.p : (const T*)tab32.p;
+    L.ax = axis_ptrs<T>(base, stride, 0);
+    L.ay = axis_ptrs<T>(base, stride, 1);
+    L.az = axis_ptrs<T>(base, stride, 2);
+    L.sig = std::is_same<T, double>::value ? (const T*)sig64.p : (const T*)sig32.p;
+    L.aniso = aniso;
+    return L;
+}
+
+static std::vector<double> node_coords(const std::vector<double>& h, int nair, bool is_z) {
+    std::vector<double> X(h.size() + 1);
+    double s = 0;
+    if (is_z) {
+        for (int i = 0; i < nair; i++) s += h[i];
+        X[0] = -s;
+    } else {
+        for (double v : h) s += v;
+        X[0] = -s / 2;
+    }
+    for (size_t i = 1; i <= h.size(); i++) X[i] = X[i - 1] + h[i - 1];
+    return X;
+}
+
+static int upload_level_tables(Level& L, cudaStream_t st) {
+    L.stride = std::max(L.nx, std::max(L.ny, L.nz)) + 2;
+    std::vector<double> t64((size_t)18 * L.stride);
+    axis_tables(L.a, L.stride, &t64[0]);
+    axis_tables(L.b, L.stride, &t64[(size_t)6 * L.stride]);
+    axis_tables(L.c, L.stride, &t64[(size_t)12 * L.stride]);
+    std::vector<float> t32(t64.size());
+    for (size_t q = 0; q < t64.size(); q++) t32[q] = (float)t64[q];
+    RC(L.tab64.alloc(t64.size() * 8));
+    RC(L.tab32.alloc(t32.size() * 4));
+    CK(cudaMemcpyAsync(L.tab64.p, t64.data(), t64.size() * 8, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(L.tab32.p, t32.data(), t32.size() * 4, cudaMemcpyHostToDevice, st));
+    std::vector<double> sp;
+    sp.insert(sp.end(), L.a.begin(), L.a.end());
+    sp.insert(sp.end(), L.b.begin(), L.b.end());
+    sp.insert(sp.end(), L.c.begin(), L.c.end());
+    RC(L.spac.alloc(sp.size() * 8));
+    CK(cudaMemcpyAsync(L.spac.p, sp.data(), sp.size() * 8, cudaMemcpyHostToDevice, st));
+    // coordinates for the prolongation INTO this level: cubic uses this
+    // level's spacings; quad (into the next coarser level) uses the pairwise
+    // sums of this level's spacings (extint_v excmg.f90:24-33).
+    std::vector<double> cc;
+    for (auto& v : node_coords(L.a, 0, false)) cc.push_back(v);
+    for (auto& v : node_coords(L.b, 0, false)) cc.push_back(v);
+    for (auto& v : node_coords(L.c, L.nair, true)) cc.push_back(v);
+    RC(L.crd_cubic.alloc(cc.size() * 8));
+    CK(cudaMemcpyAsync(L.crd_cubic.p, cc.data(), cc.size() * 8, cudaMemcpyHostToDevice, st));
+    if (L.nx % 2 == 0 && L.ny % 2 == 0 && L.nz % 2 == 0) {
+        std::vector<double> a2(L.nx / 2), b2(L.ny / 2), c2(L.nz / 2);
+        for (int i = 0; i < L.nx / 2; i++) a2[i] = L.a[2 * i] + L.a[2 * i + 1];
+        for (int i = 0; i < L.ny / 2; i++) b2[i] = L.b[2 * i] + L.b[2 * i + 1];
+        for (int i = 0; i < L.nz / 2; i++) c2[i] = L.c[2 * i] + L.c[2 * i + 1];
+        std::vector<double> cq;
+        for (auto& v : node_coords(a2, 0, false)) cq.push_back(v);
+        for (auto& v : node_coords(b2, 0, false)) cq.push_back(v);
+        for (auto& v : node_coords(c2, L.nair / 2, true)) cq.push_back(v);
+        RC(L.crd_quad.alloc(cq.size() * 8));
+        CK(cudaMemcpyAsync(L.crd_quad.p, cq.data(), cq.size() * 8, cudaMemcpyHostToDevice, st));
+    }
+    return SFDX_OK;
+}
+
+// ------------------------------------------------------------------ plan
+struct Plan {
+    sfdx_opts o;
+    int nf = 0, ns = 0, nlev = 0;
+    std::vector<double> freq, wm;
+    std::vector<Level> lev;  // lev[0] coarsest ... lev[nlev-1] finest
+    cudaStream_t st = nullptr;
+    // per-system device data
+    DBuf d_state, d_wm, d_pol, d_edc, d_part, d_counter, d_tol, d_mask, d_scale, d_flag;
+    // FP64 vectors (finest-level size)
+    DBuf x64, b64, r64, u0, u1, ut, ex_out;
+    // Krylov vectors (precision of the active solve)
+    DBuf kv[8];
+    DBuf errrec;
+    int edc_stride = 0;
+    std::vector<int> iters;        // [nf][2][nlev]
+    std::vector<double> relres;    // [nf][2]
+    std::vector<KState> hst;
+    bool have_solution = false;
+    ~Plan() {
+        if (st) cudaStreamDestroy(st);
+    }
+};
+
+static int sync_state(Plan& P) {
+    P.hst.resize(P.ns);
+    CK(cudaMemcpyAsync(P.hst.data(), P.d_state.p, sizeof(KState) * P.ns, cudaMemcpyDeviceToHost, P.st));
+    CK(cudaStreamSynchronize(P.st));
+    return SFDX_OK;
+}
+
+static RedBuf redbuf(Plan& P) {
+    RedBuf r;
+    r.part = P.d_part.as<double2>();
+    r.counter = P.d_counter.as<unsigned int>();
+    return r;
+}
+
+// ------------------------------------------------------------------ preconditioner
+template <class T, int O, int PP, int MODE>
+static void fwd_one(Plan& P, const Lev<T>& L, cplx<T>* w, cplx<T>* q, const cplx<T>* r, const cplx<T>* v) {
+    const int B = block_for(P.ns);
+    const int64_t W = colour_count(L, O) * P.ns;
+    k_sweep_fwd<T, O, PP, MODE><<<grid_for(W, B, 16), B, 0, P.st>>>(L, P.d_state.as<KState>(), P.ns, w, q, r, v);
+}
+template <class T, int O, int PP>
+static void bwd_one(Plan& P, const Lev<T>& L, cplx<T>* x) {
+    const int B = block_for(P.ns);
+    const int64_t W = colour_count(L, O) * P.ns;
+    k_sweep_bwd<T, O, PP><<<grid_for(W, B, 16), B, 0, P.st>>>(L, P.d_state.as<KState>(), P.ns, x);
+}
+
+// out = M^{-1} rhs where rhs is produced by MODE (see k_sweep_fwd)
+template <class T, int MODE>
+static void precond(Plan& P, const Lev<T>& L, cplx<T>* out, cplx<T>* q, const cplx<T>* r, const cplx<T>* v) {
+    if (P.o.precond == 'J') {
+        const int B = block_for(P.ns);
+        k_jacobi<T, MODE><<<grid_for(L.nl * P.ns, B, 16), B, 0, P.st>>>(L, P.d_state.as<KState>(), P.ns, out, q, r, v);
+        return;
+    }
+    fwd_one<T, OX, 0, MODE>(P, L, out, q, r, v);
+    fwd_one<T, OX, 1, MODE>(P, L, out, q, r, v);
+    fwd_one<T, OY, 0, MODE>(P, L, out, q, r, v);
+    fwd_one<T, OY, 1, MODE>(P, L, out, q, r, v);
+    fwd_one<T, OZ, 0, MODE>(P, L, out, q, r, v);
+    fwd_one<T, OZ, 1, MODE>(P, L, out, q, r, v);
+    bwd_one<T, OZ, 0>(P, L, out);
+    bwd_one<T, OY, 1>(P, L, out);
+    bwd_one<T, OY, 0>(P, L, out);
+    bwd_one<T, OX, 1>(P, L, out);
+    bwd_one<T, OX, 0>(P, L, out);
+}
+
+// ------------------------------------------------------------------ BiCGStab
+// Solves the ns systems of level L: A x = b.  x holds the initial guess.
+// Vectors r, rhat, p, v, y, s, z, t come from P.kv (precision T).
+template <class T>
+static int bicgstab(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, const double* tols_host, double tol,
+                    int itmax, const int* mask_host) {
+    const Lev<T> L = LV.lev<T>();
+    const int ns = P.ns;
+    const size_t vb = (size_t)LV.nl * ns * sizeof(cplx<T>);
+    for (int q = 0; q < 8; q++) RC(P.kv[q].alloc(vb));
+    cplx<T>* r = P.kv[0].as<cplx<T>>();
+    cplx<T>* rhat = P.kv[1].as<cplx<T>>();
+    cplx<T>* p = P.kv[2].as<cplx<T>>();
+    cplx<T>* v = P.kv[3].as<cplx<T>>();
+    cplx<T>* y = P.kv[4].as<cplx<T>>();
+    cplx<T>* s = P.kv[5].as<cplx<T>>();
+    cplx<T>* z = P.kv[6].as<cplx<T>>();
+    cplx<T>* t = P.kv[7].as<cplx<T>>();
+    CK(cudaMemsetAsync(p, 0, vb, P.st));
+    CK(cudaMemsetAsync(v, 0, vb, P.st));
+    CK(cudaMemsetAsync(y, 0, vb, P.st));
+    CK(cudaMemsetAsync(z, 0, vb, P.st));
+    // state
+    std::vector<KState> init(ns);
+    for (int q = 0; q < ns; q++) {
+        KState S;
+        memset(&S, 0, sizeof(S));
+        S.wm = P.wm[q];
+        S.tol = tols_host ? tols_host[q] : tol;
+        S.itmax = itmax;
+        S.active = mask_host ? mask_host[q] : 1;
+        S.status = S.active ? ST_RUN : ST_CONV;
+        init[q] = S;
+    }
+    CK(cudaMemcpyAsync(P.d_state.p, init.data(), sizeof(KState) * ns, cudaMemcpyHostToDevice, P.st));
+    const int B = block_for(ns);
+    const size_t smem = 2 * B * sizeof(double2);
+    const int G = grid_for(LV.nl * ns, B, 8);
+    RC(P.d_part.alloc((size_t)G * 2 * ns * sizeof(double2)));
+    KState* dst = P.d_state.as<KState>();
+    k_residual<T, T, 0><<<G, B, smem, P.st>>>(L, dst, ns, b, x, r, rhat, redbuf(P), nullptr, 0);
+    CK(cudaGetLastError());
+    const int check_every = 8;
+    for (int it = 1; it <= itmax; it++) {
+        precond<T, RHS_PUPD>(P, L, y, p, r, v);
+        k_bicg_v<T><<<G, B, smem, P.st>>>(L, dst, ns, y, v, rhat, redbuf(P));
+        precond<T, RHS_SUPD>(P, L, z, s, r, v);
+        k_bicg_t<T><<<G, B, smem, P.st>>>(L, dst, ns, z, t, s, redbuf(P));
+        k_bicg_upd<T, T><<<G, B, smem, P.st>>>(L, dst, ns, x, y, z, s, t, r, rhat, redbuf(P), nullptr, 0);
+        if (it % check_every == 0 || it == itmax) {
+            CK(cudaGetLastError());
+            RC(sync_state(P));
+            int act = 0;
+            for (int q = 0; q < ns; q++) act += P.hst[q].active;
+            if (!act) break;
+        }
+    }
+    RC(sync_state(P));
+    return SFDX_OK;
+}
+
+// true relative residual ||b - A x|| / ||b|| per system (FP64)
+static int true_residual(Plan& P, const Level& LV, const double2* b, const double2* x, double* rel, const int* mask) {
+    const int ns = P.ns;
+    std::vector<KState> init(ns);
+    for (int q = 0; q < ns; q++) {
+        KState S;
+        memset(&S, 0, sizeof(S));
+        S.wm = P.wm[q];
+        S.active = mask ? mask[q] : 1;
+        init[q] = S;
+    }
+    CK(cudaMemcpyAsync(P.d_state.p, init.data(), sizeof(KState) * ns, cudaMemcpyHostToDevice, P.st));
+    const int B = block_for(ns);
+    const int G = grid_for(LV.nl * ns, B, 8);
+    RC(P.d_part.alloc((size_t)G * 2 * ns * sizeof(double2)));
+    RC(P.r64.alloc((size_t)LV.nl * ns * sizeof(double2)));
+    k_residual<double, double, 2><<<G, B, 2 * B * sizeof(double2), P.st>>>(
+        LV.lev<double>(), P.d_state.as<KState>(), ns, b, x, P.r64.as<double2>(), nullptr, redbuf(P), nullptr, 0);
+    CK(cudaGetLastError());
+    RC(sync_state(P));
+    for (int q = 0; q < ns; q++) {
+        double nb = P.hst[q].babs;
+        rel[q] = (mask && !mask[q]) ? 0.0 : (nb > 0 ? P.hst[q].err / nb : P.hst[q].err);
+    }
+    return SFDX_OK;
+}
+
+// ------------------------------------------------------------------ level solves
+// FP64 solve to `tol` with the reference's solver semantics.
+static int solve_level_fp64(Plan& P, const Level& LV, double tol, int itmax, std::vector<int>& its,
+                            std::vector<int>& status) {
+    if (P.o.solver != SFDX_SOLVER_BICGSTAB) return SFDX_ERR_UNSUPPORTED;
+    RC(bicgstab<double>(P, LV, P.b64.as<double2>(), P.x64.as<double2>(), nullptr, tol, itmax, nullptr));
+    its.resize(P.ns);
+    status.resize(P.ns);
+    for (int q = 0; q < P.ns; q++) {
+        its[q] = P.hst[q].iters;
+        status[q] = P.hst[q].status;
+    }
+    return SFDX_OK;
+}
+
+// Mixed precision: FP64 residual, complex64 inner BiCGStab on the
+// normalised residual, FP64 update; stops on the TRUE relative residual.
+static int solve_level_mixed(Plan& P, const Level& LV, double tol, int itmax, std::vector<int>& its,
+                             std::vector<int>& status) {
+    if (P.o.solver != SFDX_SOLVER_BICGSTAB) return SFDX_ERR_UNSUPPORTED;
+    const int ns = P.ns;
+    const size_t n64 = (size_t)LV.nl * ns;
+    its.assign(ns, 0);
+    status.assign(ns, ST_RUN);
+    std::vector<int> mask(ns, 1);
+    std::vector<double> rel(ns), scale(ns), tols(ns);
+    DBuf rhs32, d32;
+    RC(rhs32.alloc(n64 * sizeof(float2)));
+    RC(d32.alloc(n64 * sizeof(float2)));
+    RC(P.d_scale.alloc(ns * sizeof(double)));
+    const int B = block_for(ns);
+    const int G = grid_for((int64_t)n64, B, 8);
+    for (int ref = 0; ref <= P.o.max_refine; ref++) {
+        RC(true_residual(P, LV, P.b64.as<double2>(), P.x64.as<double2>(), rel.data(), mask.data()));
+        int left = 0;
+        for (int q = 0; q < ns; q++) {
+            if (!mask[q]) { scale[q] = 0; continue; }
+            if (std::isnan(rel[q])) { status[q] = ST_NAN; mask[q] = 0; scale[q] = 0; continue; }
+            if (rel[q] < tol) { status[q] = ST_CONV; mask[q] = 0; scale[q] = 0; continue; }
+            if (its[q] >= itmax) { status[q] = ST_MAXIT; mask[q] = 0; scale[q] = 0; continue; }
+            scale[q] = rel[q] * P.hst[q].babs;  // ||r||
+            tols[q] = std::max(P.o.inner_tol, 0.3 * tol / rel[q]);
+            left++;
+        }
+        if (!left) break;
+        if (ref == P.o.max_refine) {
+            for (int q = 0; q < ns; q++) if (mask[q]) status[q] = ST_MAXIT;
+            break;
+        }
+        CK(cudaMemcpyAsync(P.d_scale.p, scale.data(), ns * sizeof(double), cudaMemcpyHostToDevice, P.st));
+        k_scale_to_f32<<<G, B, 0, P.st>>>(LV.nl, ns, P.d_scale.as<double>(), P.r64.as<double2>(), rhs32.as<float2>());
+        CK(cudaMemsetAsync(d32.p, 0, n64 * sizeof(float2), P.st));
+        int inner_max = P.o.inner_maxit;
+        RC(bicgstab<float>(P, LV, rhs32.as<float2>(), d32.as<float2>(), tols.data(), 0.0, inner_max, mask.data()));
+        for (int q = 0; q < ns; q++)
+            if (mask[q]) its[q] += std::max(0, P.hst[q].iters - 1);
+        k_refine_add<float><<<G, B, 0, P.st>>>(LV.nl, ns, P.d_scale.as<double>(), P.x64.as<double2>(), d32.as<float2>());
+        CK(cudaGetLastError());
+    }
+    return SFDX_OK;
+}
+
+static int solve_level(Plan& P, const Level& LV, double tol, int itmax, bool coarse, std::vector<int>& its,
+                       std::vector<int>& status) {
+    if (coarse || P.o.precision == SFDX_FP64) return solve_level_fp64(P, LV, tol, itmax, its, status);
+    return solve_level_mixed(P, LV, tol, itmax, its, status);
+}
+
+// ------------------------------------------------------------------ per-level set-up
+// 1-D background for every system of level LV (host, FP64), then the RHS.
+static int level_rhs(Plan& P, const Level& LV, const std::vector<double>& col /*[nz][3]*/) {
+    const int ns = P.ns, nz = LV.nz;
+    P.edc_stride = 2 * nz + 2;
+    std::vector<std::complex<double>> edc((size_t)ns * P.edc_stride);
+    std::vector<double> conv((size_t)nz * 6, 0.0);
+    for (int k = 0; k < nz; k++)
+        for (int q = 0; q < 3; q++) conv[(size_t)q * nz + k] = col[(size_t)k * 3 + q];
+    std::vector<int> pols(ns);
+    for (int f = 0; f < P.nf; f++) {
+        std::vector<std::complex<double>> e(2 * nz + 2);
+        RC(mt1d_anl(P.freq[f], nz, conv.data(), LV.c.data(), e.data(), nullptr, nullptr));
+        for (int pol = 0; pol < 2; pol++) {
+            int s = 2 * f + pol;
+            pols[s] = pol;
+            std::copy(e.begin(), e.end(), edc.begin() + (size_t)s * P.edc_stride);
+        }
+    }
+    RC(P.d_edc.alloc(edc.size() * sizeof(double2)));
+    RC(P.d_pol.alloc(ns * sizeof(int)));
+    CK(cudaMemcpyAsync(P.d_edc.p, edc.data(), edc.size() * sizeof(double2), cudaMemcpyHostToDevice, P.st));
+    CK(cudaMemcpyAsync(P.d_pol.p, pols.data(), ns * sizeof(int), cudaMemcpyHostToDevice, P.st));
+    const int B = block_for(ns);
+    k_build_rhs<<<grid_for(LV.nl * ns, B, 16), B, 0, P.st>>>(LV.lev<double>(), P.d_wm.as<double>(), P.d_pol.as<int>(),
+                                                              P.d_edc.as<double2>(), P.edc_stride, ns, P.b64.as<double2>());
+    CK(cudaGetLastError());
+    // NaN check of the right-hand side (fdfe_main.f90:1398-1403)
+    RC(P.d_flag.alloc(sizeof(int)));
+    CK(cudaMemsetAsync(P.d_flag.p, 0, sizeof(int), P.st));
+    k_nan_check<double><<<grid_for(LV.nl * ns, 256), 256, 0, P.st>>>(LV.nl * ns, P.b64.as<double2>(), P.d_flag.as<int>());
+    int flag = 0;
+    CK(cudaMemcpyAsync(&flag, P.d_flag.p, sizeof(int), cudaMemcpyDeviceToHost, P.st));
+    CK(cudaStreamSynchronize(P.st));
+    return flag ? SFDX_ERR_NAN : SFDX_OK;
+}
+
+// conductivity column (i=1,j=1) of level LV, diagonal components (cont1,
+// fdfe_main.f90:938-942 / 1376-1380)
+static int level_column(Plan& P, const Level& LV, std::vector<double>& col) {
+    col.assign((size_t)LV.nz * 3, 0.0);
+    std::vector<double> tmp(LV.nz);
+    for (int q = 0; q < 3; q++) {
+        CK(cudaMemcpy2DAsync(tmp.data(), sizeof(double), LV.sig64.as<double>() + (size_t)q * LV.ncell,
+                             sizeof(double) * (size_t)LV.nx * LV.ny, sizeof(double), LV.nz, cudaMemcpyDeviceToHost, P.st));
+        CK(cudaStreamSynchronize(P.st));
+        for (int k = 0; k < LV.nz; k++) col[(size_t)k * 3 + q] = tmp[k];
+    }
+    return SFDX_OK;
+}
+
+static int set_conductivity(Plan& P, const double* sigma, bool on_device) {
+    Level& F = P.lev[P.nlev - 1];
+    const size_t nb = (size_t)6 * F.ncell * sizeof(double);
+    RC(F.sig64.alloc(nb));
+    CK(cudaMemcpyAsync(F.sig64.p, sigma, nb, on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, P.st));
+    for (int l = P.nlev - 2; l >= 0; l--) {
+        Level& C = P.lev[l];
+        const int k = P.nlev - 1 - l;
+        RC(C.sig64.alloc((size_t)6 * C.ncell * sizeof(double)));
+        DBuf c1;
+        RC(c1.alloc((C.nx + C.ny + C.nz) * sizeof(double)));
+        std::vector<double> cs;
+        cs.insert(cs.end(), C.a.begin(), C.a.end());
+        cs.insert(cs.end(), C.b.begin(), C.b.end());
+        cs.insert(cs.end(), C.c.begin(), C.c.end());
+        CK(cudaMemcpyAsync(c1.p, cs.data(), cs.size() * 8, cudaMemcpyHostToDevice, P.st));
+        const double* fs = F.spac.as<double>();
+        const double* cp = c1.as<double>();
+        k_coarsen<<<grid_for(C.ncell, 128, 32), 128, 0, P.st>>>(F.nx, F.ny, F.nz, fs, fs + F.nx, fs + F.nx + F.ny, cp,
+                                                                cp + C.nx, cp + C.nx + C.ny, 1 << k,
+                                                                (P.o.quirks & SFDX_QUIRK_COARSEN_SHIFT) ? 1 : 0,
+                                                                F.sig64.as<double>(), C.sig64.as<double>());
+        CK(cudaGetLastError());
+        CK(cudaStreamSynchronize(P.st));
+    }
+    for (int l = 0; l < P.nlev; l++) {
+        Level& L = P.lev[l];
+        RC(L.sig32.alloc((size_t)6 * L.ncell * sizeof(float)));
+        // sigma is real: convert pairs as if complex (6*ncell is even)
+        int64_t n2 = 3 * L.ncell;
+        k_convert<double, float><<<grid_for(n2, 256), 256, 0, P.st>>>(n2, L.sig64.as<double2>(), L.sig32.as<float2>());
+        RC(P.d_flag.alloc(sizeof(int)));
+        CK(cudaMemsetAsync(P.d_flag.p, 0, sizeof(int), P.st));
+        k_any_offdiag<<<grid_for(3 * L.ncell, 256), 256, 0, P.st>>>(L.ncell, L.sig64.as<double>(), P.d_flag.as<int>());
+        int flag = 0;
+        CK(cudaMemcpyAsync(&flag, P.d_flag.p, sizeof(int), cudaMemcpyDeviceToHost, P.st));
+        CK(cudaStreamSynchronize(P.st));
+        L.aniso = flag;
+    }
+    return SFDX_OK;
+}
+
+// extint_v: x64 (level l) from u0 (level l-2) and u1 (level l-1)
+static int prolongate(Plan& P, int l, const double2* u0, const double2* u1, double2* out) {
+    const Level& F = P.lev[l];
+    const Level& M = P.lev[l - 1];
+    const int ns = P.ns;
+    const int midq = (P.o.quirks & SFDX_QUIRK_EXCMG_MIDPOINT) ? 1 : 0;
+    const int B = block_for(ns);
+    // quad: level l-2 -> level l-1 (coordinates from pairwise sums of level l)
+    const double* cq = F.crd_quad.as<double>();
+    k_interp<double, 2><<<grid_for(M.nl * ns, B, 16), B, 0, P.st>>>(M.nx, M.ny, M.nz, cq, cq + M.nx + 1,
+                                                                     cq + M.nx + M.ny + 2, midq, ns, u0, P.ut.as<double2>());
+    k_extrapolate<double><<<grid_for(M.nl * ns, 256), 256, 0, P.st>>>(M.nl * ns, u1, P.ut.as<double2>());
+    const double* cc = F.crd_cubic.as<double>();
+    k_interp<double, 4><<<grid_for(F.nl * ns, B, 16), B, 0, P.st>>>(F.nx, F.ny, F.nz, cc, cc + F.nx + 1,
+                                                                     cc + F.nx + F.ny + 2, midq, ns, P.ut.as<double2>(), out);
+    CK(cudaGetLastError());
+    CK(cudaMemsetAsync(P.d_flag.p, 0, sizeof(int), P.st));
+    k_nan_check<double><<<grid_for(F.nl * ns, 256), 256, 0, P.st>>>(F.nl * ns, out, P.d_flag.as<int>());
+    int flag = 0;
+    CK(cudaMemcpyAsync(&flag, P.d_flag.p, sizeof(int), cudaMemcpyDeviceToHost, P.st));
+    CK(cudaStreamSynchronize(P.st));
+    return flag ? SFDX_ERR_NAN : SFDX_OK;
+}
+
+static int status_to_rc(const std::vector<int>& status) {
+    int rc = SFDX_OK;
+    for (int s : status) {
+        if (s == ST_NAN) return SFDX_ERR_NAN;
+        if (s == ST_MAXIT) rc = SFDX_ERR_NOCONV;
+    }
+    return rc;
+}
+
+static void record_iters(Plan& P, int level_slot, const std::vector<int>& its) {
+    for (int s = 0; s < P.ns; s++) P.iters[(size_t)s * P.nlev + level_slot] = its[s];
+}
+
+static int plan_solve(Plan& P) {
+    const int ns = P.ns;
+    const Level& F = P.lev[P.nlev - 1];
+    P.iters.assign((size_t)ns * P.nlev, 0);
+    P.relres.assign(ns, 0.0);
+    std::vector<int> its, status;
+    int rc_conv = SFDX_OK;
+    const size_t nfine = (size_t)F.nl * ns * sizeof(double2);
+    RC(P.x64.alloc(nfine));
+    RC(P.b64.alloc(nfine));
+    std::vector<double> col;
+    if (!P.o.excmg) {
+        RC(level_column(P, F, col));
+        RC(level_rhs(P, F, col));
+        CK(cudaMemsetAsync(P.x64.p, 0, nfine, P.st));
+        RC(solve_level(P, F, P.o.eps, P.o.maxit_plain, false, its, status));
+        record_iters(P, P.nlev - 1, its);
+        rc_conv = status_to_rc(status);
+    } else {
+        const int N = P.nlev;
+        RC(P.u0.alloc(nfine));
+        RC(P.u1.alloc(nfine));
+        RC(P.ut.alloc(nfine));
+        double tol = P.o.eps * std::pow(10.0, -N + 1);
+        // levels 1 and 2: tight FP64 solve in place of PARDISO (u1u2)
+        for (int l = 0; l < 2; l++) {
+            const Level& L = P.lev[l];
+            RC(level_column(P, L, col));
+            RC(level_rhs(P, L, col));
+            CK(cudaMemsetAsync(P.x64.p, 0, (size_t)L.nl * ns * sizeof(double2), P.st));
+            RC(solve_level(P, L, P.o.coarse_tol, P.o.coarse_maxit, true, its, status));
+            record_iters(P, l, its);
+            double2* dst = l == 0 ? P.u0.as<double2>() : P.u1.as<double2>();
+            CK(cudaMemcpyAsync(dst, P.x64.p, (size_t)L.nl * ns * sizeof(double2), cudaMemcpyDeviceToDevice, P.st));
+        }
+        tol = tol * 10;
+        for (int l = 2; l < N; l++) {
+            tol = tol * 10;
+            const Level& L = P.lev[l];
+            RC(prolongate(P, l, P.u0.as<double2>(), P.u1.as<double2>(), P.x64.as<double2>()));
+            RC(level_column(P, L, col));
+            RC(level_rhs(P, L, col));
+            RC(solve_level(P, L, tol, P.o.maxit_level, false, its, status));
+            record_iters(P, l, its);
+            if (l == N - 1) rc_conv = status_to_rc(status);
+            else {
+                std::swap(P.u0.p, P.u1.p);
+                std::swap(P.u0.bytes, P.u1.bytes);
+                CK(cudaMemcpyAsync(P.u1.p, P.x64.p, (size_t)L.nl * ns * sizeof(double2), cudaMemcpyDeviceToDevice, P.st));
+            }
+        }
+    }
+    RC(true_residual(P, F, P.b64.as<double2>(), P.x64.as<double2>(), P.relres.data(), nullptr));
+    // de-interleave into [nf][2][nl] (system-major)
+    RC(P.ex_out.alloc(nfine));
+    const int B = block_for(ns);
+    k_scatter_sys<double><<<grid_for(F.nl * ns, B, 16), B, 0, P.st>>>(F.nl, ns, P.x64.as<double2>(), P.ex_out.as<double2>());
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(P.st));
+    P.have_solution = true;
+    return rc_conv;
+}
+
+static int validate_opts(const sfdx_opts& o) {
+    if (o.excmg && o.level < 3) return SFDX_ERR_ARG;
+    if (o.precond != 'S' && o.precond != 'J') return SFDX_ERR_ARG;
+    if (o.precision != SFDX_FP64 && o.precision != SFDX_MIXED) return SFDX_ERR_ARG;
+    if (o.solver != SFDX_SOLVER_BICGSTAB && o.solver != SFDX_SOLVER_GPBICG && o.solver != SFDX_SOLVER_TFQMR &&
+        o.solver != SFDX_SOLVER_BICG && o.solver != SFDX_SOLVER_COCR)
+        return SFDX_ERR_ARG;
+    if (o.eps <= 0 || o.maxit_plain <= 0 || o.maxit_level <= 0) return SFDX_ERR_ARG;
+    return SFDX_OK;
+}
+
+}  // namespace sfdx
+
+// ====================================================================== C ABI
+struct sfdx_plan {
+    Plan P;
+};
+
+extern "C" void sfdx_default_opts(sfdx_opts* o) {
+    if (!o) return;
+    memset(o, 0, sizeof(*o));
+    o->level = 3;
+    o->eps = 1e-8;
+    o->solver = SFDX_SOLVER_BICGSTAB;
+    o->excmg = 0;            // fwd_acc = 0 (global_para.f90:19)
+    o->precond = 'S';        // pre_type = 'S' (global_para.f90:18)
+    o->div_cor = 1;          // global_para.f90:8
+    o->corr_intv = 200;      // global_para.f90:9
+    o->corr_tol = 1e-3;      // global_para.f90:10
+    o->ssor_omega = 1.0;     // solvers.f90:14
+    o->sigma_air = 1e-9;     // global_para.f90:12
+    o->maxit_plain = 5000;   // fdfe_main.f90:993
+    o->maxit_level = 1000;   // fdfe_main.f90:1414
+    o->precision = SFDX_FP64;
+    o->quirks = SFDX_QUIRKS_REFERENCE;
+    o->coarse_tol = 1e-12;
+    o->coarse_maxit = 5000;
+    o->inner_tol = 1e-4;
+    o->inner_maxit = 1000;
+    o->max_refine = 12;
+    o->batch = 0;
+    o->verbose = 0;
+    o->use_graphs = 1;
+}
+
+extern "C" const char* sfdx_strerror(int code) {
+    switch (code) {
+        case SFDX_OK: return "ok";
+        case SFDX_ERR_ARG: return "invalid argument";
+        case SFDX_ERR_MESH: return "mesh sizes not divisible by 2^level (or level too large)";
+        case SFDX_ERR_CUDA: return "CUDA error or no CUDA device";
+        case SFDX_ERR_NOCONV: return "iteration limit reached before the tolerance";
+        case SFDX_ERR_NAN: return "NaN encountered";
+        case SFDX_ERR_RECEIVER: return "receiver outside the interpolation stencil";
+        case SFDX_ERR_IO: return "model/data file missing or malformed";
+        case SFDX_ERR_UNSUPPORTED: return "option combination not implemented";
+        case SFDX_ERR_TIMEOUT: return "bounded device wait ran out";
+        case SFDX_ERR_NOMEM: return "device allocation failed or size above a fixed limit";
+        default: return "unknown status";
+    }
+}
+
+extern "C" int sfdx_version(void) { return 100; }
+
+extern "C" int sfdx_plan_create(sfdx_plan** out, const sfdx_opts* opts, int nx, int ny, int nz, int nair,
+                                const double* a, const double* b, const double* c, int nf, const double* freq) {
+    if (!out || !a || !b || !c || !freq || nx < 2 || ny < 2 || nz < 2 || nf < 1 || nair < 0 || nair > nz)
+        return SFDX_ERR_ARG;
+    sfdx_opts o;
+    if (opts) o = *opts;
+    else sfdx_default_opts(&o);
+    RC(validate_opts(o));
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return SFDX_ERR_CUDA;
+    std::unique_ptr<sfdx_plan> h(new sfdx_plan());
+    Plan& P = h->P;
+    P.o = o;
+    P.nf = nf;
+    P.ns = 2 * nf;
+    if (P.ns > 512) return SFDX_ERR_UNSUPPORTED;
+    P.freq.assign(freq, freq + nf);
+    P.wm.resize(P.ns);
+    for (int f = 0; f < nf; f++) {
+        if (!(freq[f] > 0)) return SFDX_ERR_ARG;
+        P.wm[2 * f] = P.wm[2 * f + 1] = 2 * kPi * freq[f] * kMu;
+    }
+    P.nlev = o.excmg ? o.level : 1;
+    if (o.excmg) {
+        const int f = 1 << o.level;  // cubic_interp tiles 8 fine cells on level 3 and up
+        if (nx % f || ny % f || nz % f) return SFDX_ERR_MESH;
+        if (nx / f < 1 || ny / f < 1 || nz / f < 1) return SFDX_ERR_MESH;
+    }
+    CK(cudaStreamCreateWithFlags(&P.st, cudaStreamNonBlocking));
+    P.lev.resize(P.nlev);
+    for (int l = 0; l < P.nlev; l++) {
+        Level& L = P.lev[l];
+        const int k = P.nlev - 1 - l, asf = 1 << k;
+        L.set_dims(nx / asf, ny / asf, nz / asf);
+        L.nair = nair / asf;
+        L.a.resize(L.nx);
+        L.b.resize(L.ny);
+        L.c.resize(L.nz);
+        // mesh_coarsen spacing sums (fdfe_main.f90:40-48)
+        for (int i = 0; i < L.nx; i++) { double s = 0; for (int q = i * asf; q < (i + 1) * asf; q++) s += a[q]; L.a[i] = s; }
+        for (int i = 0; i < L.ny; i++) { double s = 0; for (int q = i * asf; q < (i + 1) * asf; q++) s += b[q]; L.b[i] = s; }
+        for (int i = 0; i < L.nz; i++) { double s = 0; for (int q = i * asf; q < (i + 1) * asf; q++) s += c[q]; L.c[i] = s; }
+        RC(upload_level_tables(L, P.st));
+    }
+    RC(P.d_state.alloc(sizeof(KState) * P.ns));
+    RC(P.d_wm.alloc(sizeof(double) * P.ns));
+    CK(cudaMemcpyAsync(P.d_wm.p, P.wm.data(), sizeof(double) * P.ns, cudaMemcpyHostToDevice, P.st));
+    RC(P.d_counter.alloc(sizeof(unsigned int)));
+    CK(cudaMemsetAsync(P.d_counter.p, 0, sizeof(unsigned int), P.st));
+    RC(P.d_flag.alloc(sizeof(int)));
+    CK(cudaStreamSynchronize(P.st));
+    *out = h.release();
+    return SFDX_OK;
+}
+
+extern "C" int sfdx_plan_solve(sfdx_plan* plan, const double* sigma, int sigma_on_device, double* ex, int ex_on_device,
+                               int* iters, double* relres) {
+    if (!plan || !sigma) return SFDX_ERR_ARG;
+    Plan& P = plan->P;
+    RC(set_conductivity(P, sigma, sigma_on_device != 0));
+    int rc = plan_solve(P);
+    if (rc != SFDX_OK && rc != SFDX_ERR_NOCONV) return rc;
+    const Level& F = P.lev[P.nlev - 1];
+    if (ex) {
+        CK(cudaMemcpyAsync(ex, P.ex_out.p, (size_t)F.nl * P.ns * sizeof(double2),
+                           ex_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, P.st));
+        CK(cudaStreamSynchronize(P.st));
+    }
+    if (iters) memcpy(iters, P.iters.data(), P.iters.size() * sizeof(int));
+    if (relres) memcpy(relres, P.relres.data(), P.relres.size() * sizeof(double));
+    return rc;
+}
+
+extern "C" const double* sfdx_plan_fields(sfdx_plan* plan) {
+    if (!plan || !plan->P.have_solution) return nullptr;
+    return plan->P.ex_out.as<double>();
+}
+
+extern "C" long long sfdx_plan_device_bytes(const sfdx_plan* plan) {
+    if (!plan) return 0;
+    const Plan& P = plan->P;
+    long long s = 0;
+    const DBuf* bufs[] = {&P.d_state, &P.d_wm, &P.d_pol, &P.d_edc, &P.d_part, &P.d_counter, &P.d_tol, &P.d_mask,
+                          &P.d_scale, &P.d_flag, &P.x64, &P.b64, &P.r64, &P.u0, &P.u1, &P.ut, &P.ex_out, &P.errrec};
+    for (auto* b : bufs) s += (long long)b->bytes;
+    for (auto& b : P.kv) s += (long long)b.bytes;
+    for (auto& L : P.lev)
+        s += (long long)(L.tab64.bytes + L.tab32.bytes + L.sig64.bytes + L.sig32.bytes + L.spac.bytes +
+                         L.crd_cubic.bytes + L.crd_quad.bytes);
+    return s;
+}
+
+extern "C" void sfdx_plan_destroy(sfdx_plan* plan) { delete plan; }
+
+// impedance from the plan's device-resident solution: copy only the edge
+// planes the evaluation reads.
+extern "C" int sfdx_plan_impedance(sfdx_plan* plan, int nrec, const double* recv, int out_type, double* out,
+                                   double* tipper) {
+    if (!plan || !recv || !out || nrec < 1) return SFDX_ERR_ARG;
+    Plan& P = plan->P;
+    if (!P.have_solution) return SFDX_ERR_ARG;
+    const Level& F = P.lev[P.nlev - 1];
+    const int nx = F.nx, ny = F.ny, m = F.nair;
+    const size_t pex = (size_t)nx * (ny + 1), pey = (size_t)(nx + 1) * ny, pez = (size_t)(nx + 1) * (ny + 1);
+    std::vector<std::complex<double>> buf((2 * pex + 2 * pey + pez) * 2);
+    const std::complex<double>* dev = reinterpret_cast<const std::complex<double>*>(P.ex_out.p);
+    for (int f = 0; f < P.nf; f++) {
+        SurfaceView sv;
+        sv.nx = nx; sv.ny = ny; sv.nair = m;
+        for (int p = 0; p < 2; p++) {
+            const std::complex<double>* x = dev + (size_t)(2 * f + p) * F.nl;
+            std::complex<double>* base = buf.data() + (size_t)p * (2 * pex + 2 * pey + pez);
+            CK(cudaMemcpyAsync(base, x + (size_t)m * pex, 2 * pex * 16, cudaMemcpyDeviceToHost, P.st));
+            CK(cudaMemcpyAsync(base + 2 * pex, x + F.xnl + (size_t)m * pey, 2 * pey * 16, cudaMemcpyDeviceToHost, P.st));
+            CK(cudaMemcpyAsync(base + 2 * pex + 2 * pey, x + F.xnl + F.ynl + (size_t)m * pez, pez * 16,
+                               cudaMemcpyDeviceToHost, P.st));
+            sv.exs[p] = base;
+            sv.eys[p] = base + 2 * pex;
+            sv.ezs[p] = base + 2 * pex + 2 * pey;
+        }
+        CK(cudaStreamSynchronize(P.st));
+        RC(impedance_from_surface(sv, F.a.data(), F.b.data(), F.c.data(), P.freq[f], nrec, recv, out_type,
+                                  (P.o.quirks & SFDX_QUIRK_RX_TRANSPOSE) ? 1 : 0, out + (size_t)f * nrec * 4,
+                                  tipper ? tipper + (size_t)f * nrec * 4 : nullptr));
+    }
+    return SFDX_OK;
+}
+
+extern "C" int sfdx_fwd_solve(const sfdx_opts* o, int nx, int ny, int nz, int nair, const double* a, const double* b,
+                              const double* c, const double* sigma, int nf, const double* freq, double* ex, int* iters,
+                              double* relres) {
+    sfdx_plan* p = nullptr;
+    RC(sfdx_plan_create(&p, o, nx, ny, nz, nair, a, b, c, nf, freq));
+    int rc = sfdx_plan_solve(p, sigma, 0, ex, 0, iters, relres);
+    sfdx_plan_destroy(p);
+    return rc;
+}
+
+extern "C" int sfdx_impedance(int nx, int ny, int nz, int nair, const double* a, const double* b, const double* c,
+                              int nf, const double* freq, const double* ex, int nrec, const double* recv, int out_type,
+                              int quirks, double* out, double* tipper) {
+    if (!a || !b || !c || !freq || !ex || !recv || !out || nrec < 1 || nair < 0 || nair + 1 >= nz) return SFDX_ERR_ARG;
+    const int64_t xnl = (int64_t)nx * (ny + 1) * (nz + 1), ynl = (int64_t)(nx + 1) * ny * (nz + 1);
+    const int64_t nl = xnl + ynl + (int64_t)(nx + 1) * (ny + 1) * nz;
+    const size_t pex = (size_t)nx * (ny + 1), pey = (size_t)(nx + 1) * ny, pez = (size_t)(nx + 1) * (ny + 1);
+    const std::complex<double>* X = reinterpret_cast<const std::complex<double>*>(ex);
+    for (int f = 0; f < nf; f++) {
+        SurfaceView sv;
+        sv.nx = nx; sv.ny = ny; sv.nair = nair;
+        for (int p = 0; p < 2; p++) {
+            const std::complex<double>* x = X + (size_t)(2 * f + p) * nl;
+            sv.exs[p] = x + (size_t)nair * pex;
+            sv.eys[p] = x + xnl + (size_t)nair * pey;
+            sv.ezs[p] = x + xnl + ynl + (size_t)nair * pez;
+        }
+        RC(impedance_from_surface(sv, a, b, c, freq[f], nrec, recv, out_type, (quirks & SFDX_QUIRK_RX_TRANSPOSE) ? 1 : 0,
+                                  out + (size_t)f * nrec * 4, tipper ? tipper + (size_t)f * nrec * 4 : nullptr));
+    }
+    return SFDX_OK;
+}
+
+// ---------------------------------------------------------------- component entry points
+namespace {
+// A one-level plan over host inputs, ns systems at the given frequencies.
+int component_plan(sfdx_plan** h, const sfdx_opts* o, int nx, int ny, int nz, const double* a, const double* b,
+                   const double* c, const double* sigma, int ns, const double* freqs) {
+    if (ns < 1 || ns > 512 || !freqs) return SFDX_ERR_ARG;
+    sfdx_opts oo;
+    if (o) oo = *o;
+    else sfdx_default_opts(&oo);
+    oo.excmg = 0;
+    // nf systems pairs: reuse plan_create with one frequency per pair, then
+    // override the per-system table with the requested frequencies.
+    std::vector<double> fr((ns + 1) / 2, 1.0);
+    RC(sfdx_plan_create(h, &oo, nx, ny, nz, 0, a, b, c, (int)fr.size(), fr.data()));
+    Plan& P = (*h)->P;
+    P.ns = ns;
+    P.wm.resize(ns);
+    for (int s = 0; s < ns; s++) P.wm[s] = 2 * kPi * freqs[s] * kMu;
+    RC(P.d_wm.alloc(sizeof(double) * ns));
+    CK(cudaMemcpyAsync(P.d_wm.p, P.wm.data(), sizeof(double) * ns, cudaMemcpyHostToDevice, P.st));
+    RC(P.d_state.alloc(sizeof(KState) * ns));
+    if (sigma) RC(set_conductivity(P, sigma, false));
+    return SFDX_OK;
+}
+struct PlanGuard {
+    sfdx_plan* p = nullptr;
+    ~PlanGuard() { if (p) sfdx_plan_destroy(p); }
+};
+}  // namespace
+
+extern "C" int sfdx_apply_operator(int nx, int ny, int nz, const double* a, const double* b, const double* c,
+                                   const double* sigma, int ns, const double* freqs, int precision, const double* x,
+                                   double* y) {
+    if (!sigma || !x || !y) return SFDX_ERR_ARG;
+    PlanGuard g;
+    RC(component_plan(&g.p, nullptr, nx, ny, nz, a, b, c, sigma, ns, freqs));
+    Plan& P = g.p->P;
+    const Level& L = P.lev[0];
+    const size_t n = (size_t)L.nl * ns;
+    DBuf dx, dy;
+    RC(dx.alloc(n * 16));
+    RC(dy.alloc(n * 16));
+    CK(cudaMemcpyAsync(dx.p, x, n * 16, cudaMemcpyHostToDevice, P.st));
+    const int B = block_for(ns);
+    if (precision == SFDX_FP64) {
+        k_apply<double><<<grid_for(n, B, 16), B, 0, P.st>>>(L.lev<double>(), P.d_wm.as<double>(), ns, dx.as<double2>(),
+                                                              dy.as<double2>());
+    } else {
+        DBuf fx, fy;
+        RC(fx.alloc(n * 8));
+        RC(fy.alloc(n * 8));
+        k_convert<double, float><<<grid_for(n, 256), 256, 0, P.st>>>(n, dx.as<double2>(), fx.as<float2>());
+        k_apply<float><<<grid_for(n, B, 16), B, 0, P.st>>>(L.lev<float>(), P.d_wm.as<double>(), ns, fx.as<float2>(),
+                                                             fy.as<float2>());
+        k_convert<float, double><<<grid_for(n, 256), 256, 0, P.st>>>(n, fy.as<float2>(), dy.as<double2>());
+        CK(cudaStreamSynchronize(P.st));
+    }
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(y, dy.p, n * 16, cudaMemcpyDeviceToHost, P.st));
+    CK(cudaStreamSynchronize(P.st));
+    return SFDX_OK;
+}
+
+extern "C" int sfdx_build_rhs(int nx, int ny, int nz, const double* a, const double* b, const double* c,
+                              const double* sigma, double freq, const double* edc, double* p1, double* p2) {
+    if (!sigma || !edc || !p1 || !p2) return SFDX_ERR_ARG;
+    PlanGuard g;
+    double fr[2] = {freq, freq};
+    RC(component_plan(&g.p, nullptr, nx, ny, nz, a, b, c, sigma, 2, fr));
+    Plan& P = g.p->P;
+    const Level& L = P.lev[0];
+    P.edc_stride = 2 * nz + 2;
+    std::vector<double2> e(2 * P.edc_stride);
+    for (int q = 0; q < P.edc_stride; q++) e[q] = e[P.edc_stride + q] = make_double2(edc[2 * q], edc[2 * q + 1]);
+    int pols[2] = {0, 1};
+    RC(P.d_edc.alloc(e.size() * sizeof(double2)));
+    RC(P.d_pol.alloc(2 * sizeof(int)));
+    CK(cudaMemcpyAsync(P.d_edc.p, e.data(), e.size() * sizeof(double2), cudaMemcpyHostToDevice, P.st));
+    CK(cudaMemcpyAsync(P.d_pol.p, pols, 2 * sizeof(int), cudaMemcpyHostToDevice, P.st));
+    RC(P.b64.alloc((size_t)L.nl * 2 * sizeof(double2)));
+    const int B = block_for(2);
+    k_build_rhs<<<grid_for(L.nl * 2, B, 16), B, 0, P.st>>>(L.lev<double>(), P.d_wm.as<double>(), P.d_pol.as<int>(),
+                                                            P.d_edc.as<double2>(), P.edc_stride, 2, P.b64.as<double2>());
+    RC(P.ex_out.alloc((size_t)L.nl * 2 * sizeof(double2)));
+    k_scatter_sys<double><<<grid_for(L.nl * 2, B, 16), B, 0, P.st>>>(L.nl, 2, P.b64.as<double2>(), P.ex_out.as<double2>());
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(p1, P.ex_out.p, L.nl * 16, cudaMemcpyDeviceToHost, P.st));
+    CK(cudaMemcpyAsync(p2, P.ex_out.as<double2>() + L.nl, L.nl * 16, cudaMemcpyDeviceToHost, P.st));
+    CK(cudaStreamSynchronize(P.st));
+    return SFDX_OK;
+}
+
+extern "C" int sfdx_precond_apply(int nx, int ny, int nz, const double* a, const double* b, const double* c,
+                                  const double* sigma, int ns, const double* freqs, int pc, int precision,
+                                  const double* y, double* x) {
+    if (!sigma || !y || !x || (pc != 'S' && pc != 'J')) return SFDX_ERR_ARG;
+    sfdx_opts o;
+    sfdx_default_opts(&o);
+    o.precond = pc;
+    PlanGuard g;
+    RC(component_plan(&g.p, &o, nx, ny, nz, a, b, c, sigma, ns, freqs));
+    Plan& P = g.p->P;
+    const Level& L = P.lev[0];
+    const size_t n = (size_t)L.nl * ns;
+    std::vector<KState> init(ns);
+    for (int q = 0; q < ns; q++) {
+        memset(&init[q], 0, sizeof(KState));
+        init[q].wm = P.wm[q];
+        init[q].active = 1;
+    }
+    CK(cudaMemcpyAsync(P.d_state.p, init.data(), sizeof(KState) * ns, cudaMemcpyHostToDevice, P.st));
+    DBuf dy, dx;
+    RC(dy.alloc(n * 16));
+    RC(dx.alloc(n * 16));
+    CK(cudaMemcpyAsync(dy.p, y, n * 16, cudaMemcpyHostToDevice, P.st));
+    if (precision == SFDX_FP64) {
+        precond<double, RHS_VEC>(P, L.lev<double>(), dx.as<double2>(), dy.as<double2>(), nullptr, nullptr);
+    } else {
+        DBuf fy, fx;
+        RC(fy.alloc(n * 8));
+        RC(fx.alloc(n * 8));
+        k_convert<double, float><<<grid_for(n, 256), 256, 0, P.st>>>(n, dy.as<double2>(), fy.as<float2>());
+        precond<float, RHS_VEC>(P, L.lev<float>(), fx.as<float2>(), fy.as<float2>(), nullptr, nullptr);
+        k_convert<float, double><<<grid_for(n, 256), 256, 0, P.st>>>(n, fx.as<float2>(), dx.as<double2>());
+        CK(cudaStreamSynchronize(P.st));
+    }
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(x, dx.p, n * 16, cudaMemcpyDeviceToHost, P.st));
+    CK(cudaStreamSynchronize(P.st));
+    return SFDX_OK;
+}
+
+extern "C" int sfdx_mesh_coarsen(int nx, int ny, int nz, const double* a, const double* b, const double* c,
+                                 const double* sigma, int k, int quirks, double* a1, double* b1, double* c1,
+                                 double* sigma1) {
+    if (!a || !b || !c || !sigma || !a1 || !b1 || !c1 || !sigma1 || k < 0) return SFDX_ERR_ARG;
+    const int asf = 1 << k;
+    if (nx % asf || ny % asf || nz % asf) return SFDX_ERR_MESH;
+    const int cx = nx / asf, cy = ny / asf, cz = nz / asf;
+    for (int i = 0; i < cx; i++) { double s = 0; for (int q = i * asf; q < (i + 1) * asf; q++) s += a[q]; a1[i] = s; }
+    for (int i = 0; i < cy; i++) { double s = 0; for (int q = i * asf; q < (i + 1) * asf; q++) s += b[q]; b1[i] = s; }
+    for (int i = 0; i < cz; i++) { double s = 0; for (int q = i * asf; q < (i + 1) * asf; q++) s += c[q]; c1[i] = s; }
+    cudaStream_t st;
+    CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    const size_t n0 = (size_t)nx * ny * nz, n1 = (size_t)cx * cy * cz;
+    DBuf ds0, ds1, sp;
+    int rc = ds0.alloc(n0 * 6 * 8);
+    if (!rc) rc = ds1.alloc(n1 * 6 * 8);
+    if (!rc) rc = sp.alloc((size_t)(nx + ny + nz + cx + cy + cz) * 8);
+    if (rc) { cudaStreamDestroy(st); return rc; }
+    std::vector<double> hs;
+    hs.insert(hs.end(), a, a + nx);
+    hs.insert(hs.end(), b, b + ny);
+    hs.insert(hs.end(), c, c + nz);
+    hs.insert(hs.end(), a1, a1 + cx);
+    hs.insert(hs.end(), b1, b1 + cy);
+    hs.insert(hs.end(), c1, c1 + cz);
+    cudaMemcpyAsync(sp.p, hs.data(), hs.size() * 8, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(ds0.p, sigma, n0 * 48, cudaMemcpyHostToDevice, st);
+    const double* s = sp.as<double>();
+    k_coarsen<<<grid_for(n1, 128, 32), 128, 0, st>>>(nx, ny, nz, s, s + nx, s + nx + ny, s + nx + ny + nz,
+                                                     s + nx + ny + nz + cx, s + nx + ny + nz + cx + cy, asf,
+                                                     (quirks & SFDX_QUIRK_COARSEN_SHIFT) ? 1 : 0, ds0.as<double>(),
+                                                     ds1.as<double>());
+    cudaMemcpyAsync(sigma1, ds1.p, n1 * 48, cudaMemcpyDeviceToHost, st);
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    cudaStreamDestroy(st);
+    return e == cudaSuccess ? SFDX_OK : SFDX_ERR_CUDA;
+}
+
+extern "C" int sfdx_prolongate(int nx, int ny, int nz, const double* a1, const double* b1, const double* c1, int nair,
+                               int ns, const double* u0, const double* u1, double* u, int quirks) {
+    if (!a1 || !b1 || !c1 || !u0 || !u1 || !u || ns < 1 || ns > 512) return SFDX_ERR_ARG;
+    if (nx % 8 || ny % 8 || nz % 8) return SFDX_ERR_MESH;
+    // a 3-level hierarchy whose finest level is this mesh
+    sfdx_opts o;
+    sfdx_default_opts(&o);
+    o.excmg = 1;
+    o.level = 3;
+    o.quirks = quirks;
+    std::vector<double> fr((ns + 1) / 2, 1.0);
+    PlanGuard g;
+    RC(sfdx_plan_create(&g.p, &o, nx, ny, nz, nair, a1, b1, c1, (int)fr.size(), fr.data()));
+    Plan& P = g.p->P;
+    P.ns = ns;
+    const Level& F = P.lev[2];
+    const Level& M = P.lev[1];
+    const Level& C = P.lev[0];
+    DBuf d0, d1, dout;
+    RC(d0.alloc((size_t)C.nl * ns * 16));
+    RC(d1.alloc((size_t)M.nl * ns * 16));
+    RC(dout.alloc((size_t)F.nl * ns * 16));
+    RC(P.ut.alloc((size_t)M.nl * ns * 16));
+    CK(cudaMemcpyAsync(d0.p, u0, (size_t)C.nl * ns * 16, cudaMemcpyHostToDevice, P.st));
+    CK(cudaMemcpyAsync(d1.p, u1, (size_t)M.nl * ns * 16, cudaMemcpyHostToDevice, P.st));
+    int rc = prolongate(P, 2, d0.as<double2>(), d1.as<double2>(), dout.as<double2>());
+    if (rc && rc != SFDX_ERR_NAN) return rc;
+    CK(cudaMemcpyAsync(u, dout.p, (size_t)F.nl * ns * 16, cudaMemcpyDeviceToHost, P.st));
+    CK(cudaStreamSynchronize(P.st));
+    return rc;
+}
+
+extern "C" int sfdx_krylov_solve(const sfdx_opts* o, int nx, int ny, int nz, const double* a, const double* b,
+                                 const double* c, const double* sigma, int ns, const double* freqs, const double* rhs,
+                                 double* x, double tol, int itmax, int* iters, double* relres) {
+    if (!sigma || !rhs || !x || itmax < 1) return SFDX_ERR_ARG;
+    PlanGuard g;
+    RC(component_plan(&g.p, o, nx, ny, nz, a, b, c, sigma, ns, freqs));
+    Plan& P = g.p->P;
+    const Level& L = P.lev[0];
+    const size_t n = (size_t)L.nl * ns;
+    RC(P.x64.alloc(n * 16));
+    RC(P.b64.alloc(n * 16));
+    CK(cudaMemcpyAsync(P.b64.p, rhs, n * 16, cudaMemcpyHostToDevice, P.st));
+    CK(cudaMemcpyAsync(P.x64.p, x, n * 16, cudaMemcpyHostToDevice, P.st));
+    std::vector<int> its, status;
+    RC(solve_level(P, L, tol, itmax, false, its, status));
+    std::vector<double> rel(ns);
+    RC(true_residual(P, L, P.b64.as<double2>(), P.x64.as<double2>(), rel.data(), nullptr));
+    CK(cudaMemcpyAsync(x, P.x64.p, n * 16, cudaMemcpyDeviceToHost, P.st));
+    CK(cudaStreamSynchronize(P.st));
+    if (iters) for (int q = 0; q < ns; q++) iters[q] = its[q];
+    if (relres) for (int q = 0; q < ns; q++) relres[q] = rel[q];
+    return status_to_rc(status);
+}
+
+extern "C" int sfdx_div_correct(int, int, int, const double*, const double*, const double*, const double*, int,
+                                double*, double, int*) {
+    return SFDX_ERR_UNSUPPORTED;
+}

@@ -1,0 +1,221 @@
+"""Python face of the C ABI: forward solve, impedances and the component entry points.
+
+Every function here calls libsfdx.so; none computes anything itself.  Arrays
+are numpy (host); ``Plan.solve`` additionally accepts device pointers (for
+example ``torch.Tensor.data_ptr()`` of a CUDA tensor) so that conductivities
+and fields can stay resident in HBM between solves.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import capi
+from .model import Model
+
+
+def _opts(**kw) -> capi.Opts:
+    return capi.Opts.defaults(**kw)
+
+
+def _d(x):
+    return np.ascontiguousarray(x, dtype=np.float64)
+
+
+def _z(x):
+    return np.ascontiguousarray(x, dtype=np.complex128)
+
+
+class Plan:
+    """Device workspace for one mesh + frequency list (``sfdx_plan_*``)."""
+
+    def __init__(self, model: Model, **opts):
+        model.validate()
+        self.model = model
+        self.opts = _opts(**opts)
+        self.nlev = self.opts.level if self.opts.excmg else 1
+        self._h = ctypes.c_void_p()
+        L = capi.lib()
+        self._a, self._b, self._c, self._f = _d(model.a), _d(model.b), _d(model.c), _d(model.freq)
+        capi.check(L.sfdx_plan_create(ctypes.byref(self._h), ctypes.byref(self.opts), model.nx, model.ny, model.nz,
+                                      model.nair, capi.dptr(self._a), capi.dptr(self._b), capi.dptr(self._c),
+                                      model.nf, capi.dptr(self._f)), "sfdx_plan_create")
+        self.iters = np.zeros((model.nf, 2, self.nlev), np.int32)
+        self.relres = np.zeros((model.nf, 2))
+        self.status = 0
+
+    def close(self):
+        if self._h:
+            capi.lib().sfdx_plan_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def solve(self, sigma=None, out=None, sigma_device_ptr: int | None = None, out_device_ptr: int | None = None,
+              allow_noconv: bool = False):
+        """Solve all frequencies x polarisations.  Returns ex[nf, 2, nl] (host) unless a device output is given."""
+        L = capi.lib()
+        m = self.model
+        if sigma_device_ptr is not None:
+            sp, son = ctypes.c_void_p(sigma_device_ptr), 1
+        else:
+            sg = _d(m.sigma if sigma is None else sigma)
+            assert sg.size == 6 * m.ncell
+            sp, son = ctypes.c_void_p(sg.ctypes.data), 0
+            self._sg = sg
+        ex = None
+        if out_device_ptr is not None:
+            op, oon = ctypes.c_void_p(out_device_ptr), 1
+        else:
+            ex = out if out is not None else np.zeros((m.nf, 2, m.nl), np.complex128)
+            op, oon = ctypes.c_void_p(ex.ctypes.data), 0
+        it = np.zeros(self.iters.size, np.int32)
+        rr = np.zeros(self.relres.size)
+        rc = L.sfdx_plan_solve(self._h, sp, son, op, oon, capi.iptr(it), capi.dptr(rr))
+        self.status = rc
+        if rc != 0 and not (allow_noconv and rc == 4):
+            raise capi.SfdxError(rc, "sfdx_plan_solve")
+        self.iters = it.reshape(self.iters.shape)
+        self.relres = rr.reshape(self.relres.shape)
+        return ex
+
+    def impedance(self, recv=None, out_type: int = 1, tipper: bool = False):
+        m = self.model
+        rv = _d(np.asarray(m.recv if recv is None else recv).T)  # [3][nrec]
+        nrec = rv.shape[1]
+        out = np.zeros((m.nf, nrec, 4))
+        tip = np.zeros((m.nf, nrec, 4)) if tipper else None
+        capi.check(capi.lib().sfdx_plan_impedance(self._h, nrec, capi.dptr(rv), out_type, capi.dptr(out),
+                                                   capi.dptr(tip) if tip is not None else None),
+                   "sfdx_plan_impedance")
+        return (out, tip) if tipper else out
+
+    def fields_device_ptr(self) -> int:
+        return capi.lib().sfdx_plan_fields(self._h) or 0
+
+    def device_bytes(self) -> int:
+        return int(capi.lib().sfdx_plan_device_bytes(self._h))
+
+
+def fwd_solve(model: Model, **opts):
+    """sfdx_fwd_solve: returns (ex[nf,2,nl], iters[nf,2,levels], relres[nf,2])."""
+    o = _opts(**opts)
+    nlev = o.level if o.excmg else 1
+    ex = np.zeros((model.nf, 2, model.nl), np.complex128)
+    it = np.zeros(model.nf * 2 * nlev, np.int32)
+    rr = np.zeros(model.nf * 2)
+    rc = capi.lib().sfdx_fwd_solve(ctypes.byref(o), model.nx, model.ny, model.nz, model.nair, capi.dptr(_d(model.a)),
+                                   capi.dptr(_d(model.b)), capi.dptr(_d(model.c)), capi.dptr(_d(model.sigma)),
+                                   model.nf, capi.dptr(_d(model.freq)), capi.zptr(ex), capi.iptr(it), capi.dptr(rr))
+    capi.check(rc, "sfdx_fwd_solve")
+    return ex, it.reshape(model.nf, 2, nlev), rr.reshape(model.nf, 2)
+
+
+def impedance(model: Model, ex, out_type: int = 1, quirks: int = capi.QUIRKS_REFERENCE, tipper: bool = False,
+              recv=None):
+    rv = _d(np.asarray(model.recv if recv is None else recv).T)
+    nrec = rv.shape[1]
+    out = np.zeros((model.nf, nrec, 4))
+    tip = np.zeros((model.nf, nrec, 4)) if tipper else None
+    capi.check(capi.lib().sfdx_impedance(model.nx, model.ny, model.nz, model.nair, capi.dptr(_d(model.a)),
+                                         capi.dptr(_d(model.b)), capi.dptr(_d(model.c)), model.nf,
+                                         capi.dptr(_d(model.freq)), capi.zptr(_z(ex)), nrec, capi.dptr(rv), out_type,
+                                         quirks, capi.dptr(out), capi.dptr(tip) if tip is not None else None),
+               "sfdx_impedance")
+    return (out, tip) if tipper else out
+
+
+# ---------------------------------------------------------------- components
+def mt1d(freq: float, conv: np.ndarray, c: np.ndarray):
+    conv = np.asarray(conv, np.float64)
+    nz = conv.shape[0]
+    cf = _d(conv.T.ravel())  # Fortran conv(nz,6)
+    edc = np.zeros(2 * nz + 2, np.complex128)
+    hx = np.zeros(2 * nz + 2, np.complex128)
+    imp = np.zeros(4, np.complex128)
+    capi.check(capi.lib().sfdx_mt1d(freq, nz, capi.dptr(cf), capi.dptr(_d(c)), capi.zptr(edc), capi.zptr(hx),
+                                    capi.zptr(imp)), "sfdx_mt1d")
+    return edc, hx, imp
+
+
+def apply_operator(nx, ny, nz, a, b, c, sigma, freqs, x, precision=capi.FP64):
+    """y = K x for ns interleaved systems; x: [nl, ns] complex (or [nl] for one system)."""
+    freqs = _d(np.atleast_1d(freqs))
+    ns = len(freqs)
+    xx = _z(x).reshape(-1, ns)
+    y = np.zeros_like(xx)
+    capi.check(capi.lib().sfdx_apply_operator(nx, ny, nz, capi.dptr(_d(a)), capi.dptr(_d(b)), capi.dptr(_d(c)),
+                                              capi.dptr(_d(sigma)), ns, capi.dptr(freqs), precision, capi.zptr(xx),
+                                              capi.zptr(y)), "sfdx_apply_operator")
+    return y.reshape(np.shape(x))
+
+
+def build_rhs(nx, ny, nz, a, b, c, sigma, freq, edc):
+    nl = nx * (ny + 1) * (nz + 1) + (nx + 1) * ny * (nz + 1) + (nx + 1) * (ny + 1) * nz
+    p1 = np.zeros(nl, np.complex128)
+    p2 = np.zeros(nl, np.complex128)
+    capi.check(capi.lib().sfdx_build_rhs(nx, ny, nz, capi.dptr(_d(a)), capi.dptr(_d(b)), capi.dptr(_d(c)),
+                                         capi.dptr(_d(sigma)), freq, capi.zptr(_z(edc)), capi.zptr(p1),
+                                         capi.zptr(p2)), "sfdx_build_rhs")
+    return p1, p2
+
+
+def precond_apply(nx, ny, nz, a, b, c, sigma, freqs, y, precond="S", precision=capi.FP64):
+    freqs = _d(np.atleast_1d(freqs))
+    ns = len(freqs)
+    yy = _z(y).reshape(-1, ns)
+    x = np.zeros_like(yy)
+    capi.check(capi.lib().sfdx_precond_apply(nx, ny, nz, capi.dptr(_d(a)), capi.dptr(_d(b)), capi.dptr(_d(c)),
+                                             capi.dptr(_d(sigma)), ns, capi.dptr(freqs), ord(precond), precision,
+                                             capi.zptr(yy), capi.zptr(x)), "sfdx_precond_apply")
+    return x.reshape(np.shape(y))
+
+
+def mesh_coarsen(a, b, c, sigma, k, quirks=capi.QUIRKS_REFERENCE):
+    nx, ny, nz = len(a), len(b), len(c)
+    f = 2 ** k
+    a1, b1, c1 = np.zeros(nx // f), np.zeros(ny // f), np.zeros(nz // f)
+    s1 = np.zeros((6, (nx // f) * (ny // f) * (nz // f)))
+    capi.check(capi.lib().sfdx_mesh_coarsen(nx, ny, nz, capi.dptr(_d(a)), capi.dptr(_d(b)), capi.dptr(_d(c)),
+                                            capi.dptr(_d(sigma)), k, quirks, capi.dptr(a1), capi.dptr(b1),
+                                            capi.dptr(c1), capi.dptr(s1)), "sfdx_mesh_coarsen")
+    return a1, b1, c1, s1
+
+
+def prolongate(nx, ny, nz, a1, b1, c1, nair, u0, u1, quirks=capi.QUIRKS_REFERENCE):
+    """extint_v on the fine mesh (nx,ny,nz); u0 on the 4h mesh, u1 on the 2h mesh ([n] or [n, ns])."""
+    u0 = _z(u0)
+    ns = 1 if u0.ndim == 1 else u0.shape[1]
+    nl = nx * (ny + 1) * (nz + 1) + (nx + 1) * ny * (nz + 1) + (nx + 1) * (ny + 1) * nz
+    u = np.zeros((nl, ns), np.complex128)
+    rc = capi.lib().sfdx_prolongate(nx, ny, nz, capi.dptr(_d(a1)), capi.dptr(_d(b1)), capi.dptr(_d(c1)), nair, ns,
+                                    capi.zptr(u0), capi.zptr(_z(u1)), capi.zptr(u), quirks)
+    capi.check(rc, "sfdx_prolongate")
+    return u[:, 0] if u0.ndim == 1 else u
+
+
+def krylov_solve(nx, ny, nz, a, b, c, sigma, freqs, rhs, x0=None, tol=1e-8, itmax=5000, **opts):
+    freqs = _d(np.atleast_1d(freqs))
+    ns = len(freqs)
+    r = _z(rhs).reshape(-1, ns)
+    x = np.zeros_like(r) if x0 is None else _z(x0).reshape(-1, ns).copy()
+    it = np.zeros(ns, np.int32)
+    rr = np.zeros(ns)
+    o = _opts(**opts)
+    rc = capi.lib().sfdx_krylov_solve(ctypes.byref(o), nx, ny, nz, capi.dptr(_d(a)), capi.dptr(_d(b)),
+                                      capi.dptr(_d(c)), capi.dptr(_d(sigma)), ns, capi.dptr(freqs), capi.zptr(r),
+                                      capi.zptr(x), tol, itmax, capi.iptr(it), capi.dptr(rr))
+    if rc not in (0, 4):
+        capi.check(rc, "sfdx_krylov_solve")
+    return x.reshape(np.shape(rhs)), it, rr, rc

@@ -1,0 +1,92 @@
+"""The C-ABI library builds, loads and exports every entry point of include/sfdx.h (no GPU needed)."""
+import ctypes
+import os
+import re
+
+import numpy as np
+
+import sfd_excmg_gb300 as S
+from oracle import oracle as O
+from sfd_excmg_gb300 import capi
+from sfd_excmg_gb300 import synthetic as syn
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared():
+    src = open(os.path.join(ROOT, "include", "sfdx.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(sfdx_\w+)\s*\(", src)))
+
+
+def test_every_declared_symbol_is_exported(lib):
+    names = _declared()
+    assert len(names) >= 20
+    for n in names:
+        assert hasattr(lib, n), n
+    for n in names:
+        assert n in capi._PROTO, f"{n} has no ctypes prototype"
+
+
+def test_default_options_match_reference_constants():
+    o = S.Opts.defaults()
+    assert (o.level, o.solver, o.excmg, chr(o.precond)) == (3, 1, 0, "S")
+    assert (o.div_cor, o.corr_intv, o.corr_tol, o.ssor_omega) == (1, 200, 1e-3, 1.0)
+    assert (o.sigma_air, o.maxit_plain, o.maxit_level) == (1e-9, 5000, 1000)
+    assert o.quirks == capi.QUIRKS_REFERENCE
+    assert ctypes.sizeof(S.Opts) == ctypes.sizeof(capi.Opts)
+
+
+def test_strerror_covers_codes(lib):
+    for code in range(0, 11):
+        assert len(lib.sfdx_strerror(code)) > 0
+
+
+def test_host_mt1d_matches_oracle():
+    m = syn.small_aniso()
+    conv = O.column_conv(m.sigma, m.nx, m.ny, m.nz)
+    conv[:, 3] = 0.2 * conv[:, 0]
+    conv[:, 4] = 0.1 * conv[:, 0]
+    conv[:, 5] = -0.15 * conv[:, 0]
+    for f in (1e-3, 1.0, 1e3):
+        e1, h1, i1 = O.mt1d_anl(f, conv, m.c)
+        e2, h2, i2 = S.mt1d(f, conv, m.c)
+        np.testing.assert_allclose(e2, e1, rtol=1e-13, atol=1e-15)
+        np.testing.assert_allclose(h2, h1, rtol=1e-13, atol=1e-30)
+        np.testing.assert_allclose(i2, i1, rtol=1e-13)
+
+
+def test_host_impedance_matches_post_process():
+    m = syn.small_aniso(freqs=(0.1, 10.0))
+    rng = np.random.default_rng(0)
+    ex = rng.standard_normal((2, 2, m.nl)) + 1j * rng.standard_normal((2, 2, m.nl))
+    om = O.OracleModel(m.nx, m.ny, m.nz, m.nair, m.a, m.b, m.c, m.sigma, m.freq, m.recv)
+    for out_type, rd, q in ((1, 2, 7), (2, 1, 3), (0, 2, 4)):
+        ref = O.impedances(om, ex, out_type=out_type, rd=rd)
+        got = S.impedance(m, ex, out_type=out_type, quirks=q)
+        np.testing.assert_allclose(got, ref, rtol=1e-13, atol=1e-300)
+
+
+def test_model_file_roundtrip(tmp_path):
+    m = syn.small_aniso()
+    name = str(tmp_path / "mod")
+    m.write(name)
+    r = S.Model.read(name)
+    assert (r.nx, r.ny, r.nz, r.nair) == (m.nx, m.ny, m.nz, m.nair)
+    np.testing.assert_array_equal(r.c, m.c)
+    np.testing.assert_array_equal(r.sigma, m.sigma)
+    np.testing.assert_array_equal(r.recv, m.recv)
+    np.testing.assert_array_equal(r.freq, m.freq)
+
+
+def test_reader_rejects_bad_level(tmp_path):
+    m = syn.small_aniso()
+    m.level = 2
+    name = str(tmp_path / "bad")
+    m.write(name)
+    try:
+        S.Model.read(name)
+    except capi.SfdxError as e:
+        assert e.code == 1
+    else:
+        raise AssertionError("level < 3 must be rejected (file_opt.f90:22-25)")

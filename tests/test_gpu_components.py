@@ -1,0 +1,189 @@
+"""Parity of every GPU kernel with the oracle, called through the C ABI.
+
+Integer/index work (coarsening sums, boundary handling) and the FP64
+operator must agree with the oracle's assembled CSR to rounding; FP32
+kernels within single-precision tolerance (stated per test).
+"""
+import numpy as np
+import pytest
+
+import sfd_excmg_gb300 as S
+from oracle import oracle as O
+from sfd_excmg_gb300 import synthetic as syn
+
+pytestmark = pytest.mark.gpu
+
+
+def _model(seed=0, n=16):
+    return syn.small_aniso(n=n, seed=seed)
+
+
+def _csr(m, ff):
+    conv = O.column_conv(m.sigma, m.nx, m.ny, m.nz)
+    edc, _, _ = O.mt1d_anl(ff, conv, m.c)
+    K, p1, p2 = O.assemble(m.nx, m.ny, m.nz, m.a, m.b, m.c, m.sigma, ff, edc)
+    return K, p1, p2, edc
+
+
+def _rand(n, ns=None, seed=0):
+    rng = np.random.default_rng(seed)
+    shape = (n,) if ns is None else (n, ns)
+    return rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
+
+
+@pytest.mark.parametrize("seed", [0, 1])
+def test_operator_fp64_matches_csr(seed):
+    m = _model(seed)
+    ff = [0.01, 3.0][seed]
+    K, _, _, _ = _csr(m, ff)
+    x = _rand(m.nl, seed=seed)
+    y = S.apply_operator(m.nx, m.ny, m.nz, m.a, m.b, m.c, m.sigma, [ff], x)
+    ref = K @ x
+    # FP64, same formulas; only the factorised weights differ in the last bits
+    assert np.abs(y - ref).max() <= 1e-12 * np.abs(ref).max()
+
+
+def test_operator_batched_systems_and_fp32():
+    m = _model(2)
+    freqs = [1e-3, 0.5, 7.0, 300.0]
+    x = _rand(m.nl, ns=4, seed=3)
+    y64 = S.apply_operator(m.nx, m.ny, m.nz, m.a, m.b, m.c, m.sigma, freqs, x)
+    y32 = S.apply_operator(m.nx, m.ny, m.nz, m.a, m.b, m.c, m.sigma, freqs, x, precision=S.MIXED)
+    for s, ff in enumerate(freqs):
+        K, _, _, _ = _csr(m, ff)
+        ref = K @ x[:, s]
+        assert np.abs(y64[:, s] - ref).max() <= 1e-12 * np.abs(ref).max()
+        # complex64 operator: inputs and coefficients rounded to FP32
+        assert np.abs(y32[:, s] - ref).max() <= 2e-5 * np.abs(ref).max()
+
+
+def test_rhs_matches_dcfast():
+    m = _model(1)
+    for ff in (0.02, 40.0):
+        K, p1, p2, edc = _csr(m, ff)
+        q1, q2 = S.build_rhs(m.nx, m.ny, m.nz, m.a, m.b, m.c, m.sigma, ff, edc)
+        assert np.abs(q1 - p1).max() <= 1e-12 * np.abs(p1).max()
+        assert np.abs(q2 - p2).max() <= 1e-12 * np.abs(p2).max()
+
+
+@pytest.mark.parametrize("quirk", [0, 1])
+def test_mesh_coarsen_matches_oracle(quirk):
+    m = _model(3)
+    for k in (1, 2):
+        a1, b1, c1, s1 = S.mesh_coarsen(m.a, m.b, m.c, m.sigma, k, quirks=quirk)
+        ra, rb, rc, rs = O.mesh_coarsen(m.a, m.b, m.c, m.sigma, k, quirk=bool(quirk))
+        assert np.array_equal(a1, ra) and np.array_equal(b1, rb) and np.array_equal(c1, rc)
+        assert np.abs(s1 - rs).max() <= 1e-15 * np.abs(rs).max()
+
+
+@pytest.mark.parametrize("quirk", [0, 2])
+def test_prolongation_matches_extint_v(quirk):
+    m = _model(4)
+    nx, ny, nz = m.nx, m.ny, m.nz
+    rng = np.random.default_rng(5)
+    n0 = O.nedges(nx // 4, ny // 4, nz // 4)
+    n1 = O.nedges(nx // 2, ny // 2, nz // 2)
+    u0 = rng.standard_normal(n0) + 1j * rng.standard_normal(n0)
+    u1 = rng.standard_normal(n1) + 1j * rng.standard_normal(n1)
+    ref, _ = O.extint_v(nx, ny, nz, m.a, m.b, m.c, m.nair, u0, u1, midpoint_quirk=bool(quirk))
+    got = S.prolongate(nx, ny, nz, m.a, m.b, m.c, m.nair, u0, u1, quirks=quirk)
+    assert np.abs(got - ref).max() <= 1e-12 * np.abs(ref).max()
+
+
+def test_prolongation_batched_systems():
+    m = _model(6)
+    nx, ny, nz = m.nx, m.ny, m.nz
+    rng = np.random.default_rng(7)
+    n0 = O.nedges(nx // 4, ny // 4, nz // 4)
+    n1 = O.nedges(nx // 2, ny // 2, nz // 2)
+    u0 = rng.standard_normal((n0, 3)) + 1j * rng.standard_normal((n0, 3))
+    u1 = rng.standard_normal((n1, 3)) + 1j * rng.standard_normal((n1, 3))
+    got = S.prolongate(nx, ny, nz, m.a, m.b, m.c, m.nair, u0, u1)
+    for s in range(3):
+        ref, _ = O.extint_v(nx, ny, nz, m.a, m.b, m.c, m.nair, u0[:, s], u1[:, s])
+        assert np.abs(got[:, s] - ref).max() <= 1e-12 * np.abs(ref).max()
+
+
+def _colour(m):
+    """Colour of every edge (0..5) in the multi-colour ordering of the GPU sweeps."""
+    nx, ny, nz = m.nx, m.ny, m.nz
+    k, j, i = np.meshgrid(np.arange(nz + 1), np.arange(ny + 1), np.arange(nx), indexing="ij")
+    cx = ((j + k) & 1).ravel()
+    k, j, i = np.meshgrid(np.arange(nz + 1), np.arange(ny), np.arange(nx + 1), indexing="ij")
+    cy = 2 + ((i + k) & 1).ravel()
+    k, j, i = np.meshgrid(np.arange(nz), np.arange(ny + 1), np.arange(nx + 1), indexing="ij")
+    cz = 4 + ((i + j) & 1).ravel()
+    return np.concatenate([cx, cy, cz])
+
+
+def test_colouring_is_independent():
+    m = _model(0)
+    K, _, _, _ = _csr(m, 1.0)
+    col = _colour(m)
+    Kc = K.tocoo()
+    off = Kc.row != Kc.col
+    assert not np.any(col[Kc.row[off]] == col[Kc.col[off]])
+
+
+def test_multicolour_ssor_is_symmetric_gauss_seidel():
+    """x = M^{-1} y with M = (D+L) D^{-1} (D+U) in the colour order."""
+    import scipy.sparse as sp
+    from scipy.sparse.linalg import spsolve_triangular
+    m = _model(1)
+    ff = 2.0
+    K, _, _, _ = _csr(m, ff)
+    col = _colour(m)
+    perm = np.lexsort((np.arange(m.nl), col))
+    Kp = K[perm][:, perm].tocsr()
+    D = sp.diags(Kp.diagonal())
+    Lw = sp.tril(Kp, k=0).tocsr()
+    Up = sp.triu(Kp, k=0).tocsr()
+    y = _rand(m.nl, seed=11)
+    w = spsolve_triangular(Lw, y[perm], lower=True)
+    xp = spsolve_triangular(Up, D @ w, lower=False)
+    ref = np.empty_like(xp)
+    ref[perm] = xp
+    got = S.precond_apply(m.nx, m.ny, m.nz, m.a, m.b, m.c, m.sigma, [ff], y)
+    assert np.abs(got - ref).max() <= 1e-10 * np.abs(ref).max()
+    got32 = S.precond_apply(m.nx, m.ny, m.nz, m.a, m.b, m.c, m.sigma, [ff], y, precision=S.MIXED)
+    assert np.abs(got32 - ref).max() <= 1e-3 * np.abs(ref).max()
+
+
+def test_jacobi_preconditioner():
+    m = _model(2)
+    K, _, _, _ = _csr(m, 0.3)
+    y = _rand(m.nl, seed=2)
+    got = S.precond_apply(m.nx, m.ny, m.nz, m.a, m.b, m.c, m.sigma, [0.3], y, precond="J")
+    ref = y / K.diagonal()
+    assert np.abs(got - ref).max() <= 1e-12 * np.abs(ref).max()
+
+
+def test_krylov_fp64_converges_to_direct_solution():
+    m = _model(0)
+    ff = 1.0
+    K, p1, p2, _ = _csr(m, ff)
+    from scipy.sparse.linalg import splu
+    lu = splu(K.tocsc())
+    rhs = np.stack([p1, p2], axis=1)
+    x, it, rr, rc = S.krylov_solve(m.nx, m.ny, m.nz, m.a, m.b, m.c, m.sigma, [ff, ff], rhs, tol=1e-10, itmax=3000)
+    assert rc == 0, (it, rr)
+    assert np.all(rr < 1e-9), rr
+    for s, p in enumerate((p1, p2)):
+        xd = lu.solve(p)
+        r = p - K @ x[:, s]
+        assert np.linalg.norm(r) <= 1e-9 * np.linalg.norm(p)
+        # fields in the earth (below the air layers) agree with the direct solve
+        assert np.linalg.norm(x[:, s] - xd) <= 1e-3 * np.linalg.norm(xd)
+
+
+def test_krylov_mixed_precision_reaches_fp64_tolerance():
+    m = _model(3)
+    ff = 0.1
+    K, p1, p2, _ = _csr(m, ff)
+    rhs = np.stack([p1, p2], axis=1)
+    x, it, rr, rc = S.krylov_solve(m.nx, m.ny, m.nz, m.a, m.b, m.c, m.sigma, [ff, ff], rhs, tol=1e-10, itmax=5000,
+                                   precision=S.MIXED)
+    assert rc == 0, (it, rr)
+    for s, p in enumerate((p1, p2)):
+        r = p - K @ x[:, s]
+        assert np.linalg.norm(r) < 1e-10 * np.linalg.norm(p)

@@ -1,0 +1,80 @@
+"""End-to-end forward solves on the GPU against the oracle.
+
+The multi-colour SSOR changes the Krylov iterates, so parity is on the
+converged answer: impedances and surface fields of the GPU solve are
+compared with the oracle's solution of the same mesh (SuperLU direct solve,
+the exact discrete answer), within tolerances stated per test.
+"""
+import numpy as np
+import pytest
+
+import sfd_excmg_gb300 as S
+from oracle import oracle as O
+from sfd_excmg_gb300 import synthetic as syn
+
+pytestmark = pytest.mark.gpu
+
+
+def _omodel(m):
+    return O.OracleModel(m.nx, m.ny, m.nz, m.nair, m.a, m.b, m.c, m.sigma, m.freq, m.recv, m.level, m.eps, m.solver,
+                         m.out_type)
+
+
+def _direct_Z(m):
+    om = _omodel(m)
+    ex = np.zeros((m.nf, 2, m.nl), np.complex128)
+    for k, ff in enumerate(m.freq):
+        u1, u2, _, _, _ = O.direct_solve(om, ff)
+        ex[k, 0], ex[k, 1] = u1, u2
+    return ex, O.impedances(om, ex, out_type=1, rd=2)
+
+
+def _zc(res):
+    return res[..., 0::2] + 1j * res[..., 1::2]
+
+
+def test_halfspace_known_answer():
+    m = syn.halfspace(n=16, freqs=(1.0, 10.0))
+    ex, it, rr = S.fwd_solve(m, eps=1e-10)
+    res = S.impedance(m, ex, out_type=2)
+    # discretisation error of a 16^3 mesh: within 5 % and 2 degrees
+    assert np.all(np.abs(res[..., 0:2] / 100.0 - 1) < 0.05), res
+    assert np.all(np.abs(res[..., 2:4] - 45.0) < 2.0), res
+
+
+@pytest.mark.parametrize("excmg", [0, 1])
+def test_forward_fp64_matches_direct(excmg):
+    m = syn.small_aniso(n=16, seed=1, freqs=(0.05, 20.0))
+    ex, it, rr = S.fwd_solve(m, eps=1e-10, excmg=excmg, level=3)
+    assert np.all(rr < 1e-9), rr
+    _, zref = _direct_Z(m)
+    z = S.impedance(m, ex)
+    err = np.abs(_zc(z) - _zc(zref)) / np.abs(_zc(zref))
+    assert err.max() < 1e-4, err
+
+
+def test_forward_mixed_matches_fp64():
+    m = syn.small_aniso(n=16, seed=2, freqs=(0.01, 1.0, 100.0))
+    ex64, _, rr64 = S.fwd_solve(m, eps=1e-10, excmg=1, level=3)
+    exm, _, rrm = S.fwd_solve(m, eps=1e-10, excmg=1, level=3, precision=S.MIXED)
+    assert np.all(rrm < 1e-10), rrm
+    z64 = _zc(S.impedance(m, ex64))
+    zm = _zc(S.impedance(m, exm))
+    _, zref = _direct_Z(m)
+    zr = _zc(zref)
+    e64 = np.abs(z64 - zr) / np.abs(zr)
+    em = np.abs(zm - zr) / np.abs(zr)
+    assert em.max() < 1e-4, (em, e64)
+
+
+def test_plan_reuse_and_device_impedance():
+    m = syn.small_aniso(n=16, seed=3, freqs=(0.3, 3.0))
+    with S.Plan(m, eps=1e-9, excmg=1, level=3) as p:
+        ex1 = p.solve()
+        z1 = p.impedance()
+        ex2 = p.solve()
+        z2 = p.impedance()
+    assert np.array_equal(ex1, ex2)
+    np.testing.assert_array_equal(z1, z2)
+    zh = S.impedance(m, ex1)
+    np.testing.assert_allclose(z1, zh, rtol=0, atol=1e-14 * np.abs(zh).max())
