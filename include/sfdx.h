@@ -124,6 +124,8 @@ int sfdx_plan_impedance(sfdx_plan* plan, int nrec, const double* recv, int out_t
 const double* sfdx_plan_fields(sfdx_plan* plan);
 /* Bytes of device memory held by the plan. */
 long long sfdx_plan_device_bytes(const sfdx_plan* plan);
+/* Wall time (ms) of each level of the last solve, coarsest first (n >= levels). */
+int sfdx_plan_level_times(const sfdx_plan* plan, double* ms, int n);
 void sfdx_plan_destroy(sfdx_plan* plan);
 
 /* ------------------------------------------------------------------------

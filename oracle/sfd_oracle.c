@@ -479,7 +479,7 @@ void orc_mesh_coarsen(int nx0, int ny0, int nz0, const double *a, const double *
                             if (quirk) {
                                 ind = ((int64_t)(m - 1) * asf + r) * nx * ny * asf * asf +
                                       ((int64_t)(j - 1) * asf + s) * nx * asf + (int64_t)(i - 1) * asf + t;
-                                if (ind > ncell0) ind -= (int64_t)nx0 * ny0;
+                                while (ind > ncell0) ind -= (int64_t)nx0 * ny0;
                             } else {
                                 ind = ((int64_t)(m - 1) * asf + r - 1) * nx0 * ny0 +
                                       ((int64_t)(j - 1) * asf + s - 1) * nx0 + (int64_t)(i - 1) * asf + t;

@@ -312,6 +312,10 @@ __global__ void k_bicg_v(Lev<T> L, KState* st, int ns, const cplx<T>* __restrict
         double2 rho = st[ss].rho;
         double den = d.x * d.x + d.y * d.y;
         st[ss].alpha = make_double2((rho.x * d.x + rho.y * d.y) / den, (rho.y * d.x - rho.x * d.y) / den);
+        if (!isfinite(st[ss].alpha.x) || !isfinite(st[ss].alpha.y)) {  // breakdown: keep the last iterate
+            st[ss].active = 0;
+            st[ss].status = ST_BREAK;
+        }
     }
 }
 
@@ -345,6 +349,11 @@ __global__ void k_bicg_t(Lev<T> L, KState* st, int ns, const cplx<T>* __restrict
         double2 ts = smem[B + ss];
         double tt = smem[B + ns + ss].x;
         st[ss].omega = make_double2(ts.x / tt, ts.y / tt);
+        if (!isfinite(st[ss].omega.x) || !isfinite(st[ss].omega.y) ||
+            (st[ss].omega.x == 0.0 && st[ss].omega.y == 0.0)) {  // breakdown: keep the last iterate
+            st[ss].active = 0;
+            st[ss].status = ST_BREAK;
+        }
     }
 }
 

@@ -22,11 +22,13 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <ctime>
 #include <memory>
 #include <type_traits>
 #include <vector>
 
 #include "sfdx.h"
+#include "sfdx_divcorr.cuh"
 #include "sfdx_excmg.cuh"
 #include "sfdx_host.h"
 #include "sfdx_kernels.cuh"
@@ -233,9 +235,13 @@ struct Plan {
     DBuf x64, b64, r64, u0, u1, ut, ex_out;
     // Krylov vectors (precision of the active solve)
     DBuf kv[8];
+    // divergence correction: t, r, p, v, phi (nodes) and the PCG state
+    DBuf dcv[5], d_pst;
+    int dc_calls = 0, dc_last_iters = 0;
     DBuf errrec;
     int edc_stride = 0;
     std::vector<int> iters;        // [nf][2][nlev]
+    std::vector<double> level_ms;  // wall time per level of the last solve
     std::vector<double> relres;    // [nf][2]
     std::vector<KState> hst;
     bool have_solution = false;
@@ -293,6 +299,57 @@ static void precond(Plan& P, const Lev<T>& L, cplx<T>* out, cplx<T>* q, const cp
     bwd_one<T, OX, 0>(P, L, out);
 }
 
+// ------------------------------------------------------------------ divergence correction
+static NodeGeo node_geo(const Level& LV) {
+    NodeGeo G;
+    G.nx = LV.nx; G.ny = LV.ny; G.nz = LV.nz;
+    G.np = (int64_t)(LV.nx + 1) * (LV.ny + 1) * (LV.nz + 1);
+    G.xnl = LV.xnl; G.ynl = LV.ynl; G.ncell = LV.ncell;
+    const double* sp = LV.spac.as<double>();
+    G.a = sp; G.b = sp + LV.nx; G.c = sp + LV.nx + LV.ny;
+    G.sig = LV.sig64.as<double>();
+    return G;
+}
+
+// x += grad(phi), P phi = T x  for the systems active in P.d_state
+static int div_correct(Plan& P, const Level& LV, double2* x) {
+    const int ns = P.ns;
+    const NodeGeo G = node_geo(LV);
+    const size_t nb = (size_t)G.np * ns * sizeof(double2);
+    for (int q = 0; q < 5; q++) RC(P.dcv[q].alloc(nb));
+    RC(P.d_pst.alloc(sizeof(KState) * ns));
+    double2 *t = P.dcv[0].as<double2>(), *r = P.dcv[1].as<double2>(), *p = P.dcv[2].as<double2>();
+    double2 *v = P.dcv[3].as<double2>(), *phi = P.dcv[4].as<double2>();
+    const int B = block_for(ns);
+    const int G1 = grid_for(G.np * ns, B, 8);
+    RC(P.d_part.alloc(std::max(P.d_part.bytes, (size_t)G1 * 2 * ns * sizeof(double2))));
+    const size_t sm = 2 * B * sizeof(double2);
+    KState* pst = P.d_pst.as<KState>();
+    k_dc_div<<<G1, B, sm, P.st>>>(G, P.d_state.as<KState>(), ns, x, t, r, p, phi, redbuf(P), pst);
+    const int maxit = 2000;  // pcg itmax (div_correc.f90:57)
+    int it = 0;
+    std::vector<KState> h(ns);
+    for (; it < maxit; it++) {
+        k_dc_Ap<<<G1, B, sm, P.st>>>(G, pst, ns, p, v, redbuf(P));
+        k_dc_upd<<<G1, B, sm, P.st>>>(G, pst, ns, p, v, phi, r, redbuf(P), P.o.corr_tol, maxit);
+        k_dc_p<<<G1, B, 0, P.st>>>(G, pst, ns, r, p);
+        if ((it + 1) % 16 == 0) {
+            CK(cudaMemcpyAsync(h.data(), pst, sizeof(KState) * ns, cudaMemcpyDeviceToHost, P.st));
+            CK(cudaStreamSynchronize(P.st));
+            int act = 0;
+            for (auto& q : h) act += q.active;
+            if (!act) break;
+        }
+    }
+    CK(cudaMemcpyAsync(h.data(), pst, sizeof(KState) * ns, cudaMemcpyDeviceToHost, P.st));
+    k_dc_grad<<<grid_for(LV.nl * ns, B, 16), B, 0, P.st>>>(G, P.d_state.as<KState>(), ns, phi, x);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(P.st));
+    P.dc_calls++;
+    P.dc_last_iters = h[0].iters;
+    return SFDX_OK;
+}
+
 // ------------------------------------------------------------------ BiCGStab
 // Solves the ns systems of level L: A x = b.  x holds the initial guess.
 // Vectors r, rhat, p, v, y, s, z, t come from P.kv (precision T).
@@ -337,6 +394,12 @@ static int bicgstab(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, cons
     CK(cudaGetLastError());
     const int check_every = 8;
     for (int it = 1; it <= itmax; it++) {
+        // top of iteration `it` (solvers.f90:630-640): divergence correction and
+        // residual restart every corr_intv iterations (FP64 solves only)
+        if (std::is_same<T, double>::value && P.o.div_cor && it % P.o.corr_intv == 0) {
+            RC(div_correct(P, LV, reinterpret_cast<double2*>(x)));
+            k_residual<T, T, 1><<<G, B, smem, P.st>>>(L, dst, ns, b, x, r, rhat, redbuf(P), nullptr, 0);
+        }
         precond<T, RHS_PUPD>(P, L, y, p, r, v);
         k_bicg_v<T><<<G, B, smem, P.st>>>(L, dst, ns, y, v, rhat, redbuf(P));
         precond<T, RHS_SUPD>(P, L, z, s, r, v);
@@ -579,6 +642,25 @@ static void record_iters(Plan& P, int level_slot, const std::vector<int>& its) {
     for (int s = 0; s < P.ns; s++) P.iters[(size_t)s * P.nlev + level_slot] = its[s];
 }
 
+static double now_ms() {
+    timespec ts;
+    clock_gettime(CLOCK_MONOTONIC, &ts);
+    return ts.tv_sec * 1e3 + ts.tv_nsec * 1e-6;
+}
+
+static void log_level(Plan& P, int l, const std::vector<int>& its, const std::vector<int>& status, double ms) {
+    if (!P.o.verbose && !getenv("SFDX_VERBOSE")) return;
+    const Level& L = P.lev[l];
+    int mn = 1 << 30, mx = 0, cnt[5] = {0, 0, 0, 0, 0};
+    for (int q = 0; q < P.ns; q++) {
+        mn = std::min(mn, its[q]);
+        mx = std::max(mx, its[q]);
+        if (status[q] >= 0 && status[q] < 5) cnt[status[q]]++;
+    }
+    fprintf(stderr, "sfdx: level %d (%dx%dx%d, nl=%lld) iters %d..%d conv %d maxit %d nan %d break %d  %.1f ms\n", l + 1,
+            L.nx, L.ny, L.nz, (long long)L.nl, mn, mx, cnt[ST_CONV], cnt[ST_MAXIT], cnt[ST_NAN], cnt[ST_BREAK], ms);
+}
+
 static int plan_solve(Plan& P) {
     const int ns = P.ns;
     const Level& F = P.lev[P.nlev - 1];
@@ -590,13 +672,18 @@ static int plan_solve(Plan& P) {
     RC(P.x64.alloc(nfine));
     RC(P.b64.alloc(nfine));
     std::vector<double> col;
+    P.level_ms.assign(P.nlev, 0.0);
     if (!P.o.excmg) {
+        double t0 = now_ms();
         RC(level_column(P, F, col));
         RC(level_rhs(P, F, col));
         CK(cudaMemsetAsync(P.x64.p, 0, nfine, P.st));
         RC(solve_level(P, F, P.o.eps, P.o.maxit_plain, false, its, status));
         record_iters(P, P.nlev - 1, its);
         rc_conv = status_to_rc(status);
+        CK(cudaStreamSynchronize(P.st));
+        P.level_ms[0] = now_ms() - t0;
+        log_level(P, 0, its, status, P.level_ms[0]);
     } else {
         const int N = P.nlev;
         RC(P.u0.alloc(nfine));
@@ -605,6 +692,7 @@ static int plan_solve(Plan& P) {
         double tol = P.o.eps * std::pow(10.0, -N + 1);
         // levels 1 and 2: tight FP64 solve in place of PARDISO (u1u2)
         for (int l = 0; l < 2; l++) {
+            double t0 = now_ms();
             const Level& L = P.lev[l];
             RC(level_column(P, L, col));
             RC(level_rhs(P, L, col));
@@ -613,16 +701,23 @@ static int plan_solve(Plan& P) {
             record_iters(P, l, its);
             double2* dst = l == 0 ? P.u0.as<double2>() : P.u1.as<double2>();
             CK(cudaMemcpyAsync(dst, P.x64.p, (size_t)L.nl * ns * sizeof(double2), cudaMemcpyDeviceToDevice, P.st));
+            CK(cudaStreamSynchronize(P.st));
+            P.level_ms[l] = now_ms() - t0;
+            log_level(P, l, its, status, P.level_ms[l]);
         }
         tol = tol * 10;
         for (int l = 2; l < N; l++) {
             tol = tol * 10;
+            double t0 = now_ms();
             const Level& L = P.lev[l];
             RC(prolongate(P, l, P.u0.as<double2>(), P.u1.as<double2>(), P.x64.as<double2>()));
             RC(level_column(P, L, col));
             RC(level_rhs(P, L, col));
             RC(solve_level(P, L, tol, P.o.maxit_level, false, its, status));
             record_iters(P, l, its);
+            CK(cudaStreamSynchronize(P.st));
+            P.level_ms[l] = now_ms() - t0;
+            log_level(P, l, its, status, P.level_ms[l]);
             if (l == N - 1) rc_conv = status_to_rc(status);
             else {
                 std::swap(P.u0.p, P.u1.p);
@@ -799,6 +894,13 @@ extern "C" long long sfdx_plan_device_bytes(const sfdx_plan* plan) {
 }
 
 extern "C" void sfdx_plan_destroy(sfdx_plan* plan) { delete plan; }
+
+extern "C" int sfdx_plan_level_times(const sfdx_plan* plan, double* ms, int n) {
+    if (!plan || !ms) return SFDX_ERR_ARG;
+    const Plan& P = plan->P;
+    for (int l = 0; l < n; l++) ms[l] = l < (int)P.level_ms.size() ? P.level_ms[l] : 0.0;
+    return SFDX_OK;
+}
 
 // impedance from the plan's device-resident solution: copy only the edge
 // planes the evaluation reads.
@@ -1094,7 +1196,29 @@ extern "C" int sfdx_krylov_solve(const sfdx_opts* o, int nx, int ny, int nz, con
     return status_to_rc(status);
 }
 
-extern "C" int sfdx_div_correct(int, int, int, const double*, const double*, const double*, const double*, int,
-                                double*, double, int*) {
-    return SFDX_ERR_UNSUPPORTED;
+extern "C" int sfdx_div_correct(int nx, int ny, int nz, const double* a, const double* b, const double* c,
+                                const double* sigma, int ns, double* x, double tol, int* pcg_iters) {
+    if (!sigma || !x || ns < 1) return SFDX_ERR_ARG;
+    std::vector<double> fr(ns, 1.0);
+    sfdx_opts o;
+    sfdx_default_opts(&o);
+    o.corr_tol = tol;
+    PlanGuard g;
+    RC(component_plan(&g.p, &o, nx, ny, nz, a, b, c, sigma, ns, fr.data()));
+    Plan& P = g.p->P;
+    const Level& L = P.lev[0];
+    const size_t n = (size_t)L.nl * ns;
+    std::vector<KState> init(ns);
+    for (int q = 0; q < ns; q++) {
+        memset(&init[q], 0, sizeof(KState));
+        init[q].active = 1;
+    }
+    CK(cudaMemcpyAsync(P.d_state.p, init.data(), sizeof(KState) * ns, cudaMemcpyHostToDevice, P.st));
+    RC(P.x64.alloc(n * 16));
+    CK(cudaMemcpyAsync(P.x64.p, x, n * 16, cudaMemcpyHostToDevice, P.st));
+    RC(div_correct(P, L, P.x64.as<double2>()));
+    CK(cudaMemcpyAsync(x, P.x64.p, n * 16, cudaMemcpyDeviceToHost, P.st));
+    CK(cudaStreamSynchronize(P.st));
+    if (pcg_iters) *pcg_iters = P.dc_last_iters;
+    return SFDX_OK;
 }

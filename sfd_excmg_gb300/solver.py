@@ -104,6 +104,11 @@ class Plan:
     def fields_device_ptr(self) -> int:
         return capi.lib().sfdx_plan_fields(self._h) or 0
 
+    def level_times(self) -> np.ndarray:
+        ms = np.zeros(self.nlev)
+        capi.check(capi.lib().sfdx_plan_level_times(self._h, capi.dptr(ms), self.nlev), "sfdx_plan_level_times")
+        return ms
+
     def device_bytes(self) -> int:
         return int(capi.lib().sfdx_plan_device_bytes(self._h))
 

@@ -187,3 +187,24 @@ def test_krylov_mixed_precision_reaches_fp64_tolerance():
     for s, p in enumerate((p1, p2)):
         r = p - K @ x[:, s]
         assert np.linalg.norm(r) < 1e-10 * np.linalg.norm(p)
+
+
+def test_divergence_correction_matches_div_correc():
+    m = _model(5)
+    rng = np.random.default_rng(9)
+    x = rng.standard_normal(m.nl) + 1j * rng.standard_normal(m.nl)
+    ref, it_ref = O.div_correc(m.nx, m.ny, m.nz, m.a, m.b, m.c, m.sigma, x, tol=1e-3)
+    from sfd_excmg_gb300 import capi
+    import ctypes
+    got = np.ascontiguousarray(x.copy())
+    it = ctypes.c_int()
+    capi.check(capi.lib().sfdx_div_correct(m.nx, m.ny, m.nz, capi.dptr(np.ascontiguousarray(m.a)),
+                                           capi.dptr(np.ascontiguousarray(m.b)), capi.dptr(np.ascontiguousarray(m.c)),
+                                           capi.dptr(np.ascontiguousarray(m.sigma)), 1, capi.zptr(got), 1e-3,
+                                           ctypes.byref(it)), "sfdx_div_correct")
+    assert it.value == it_ref
+    assert np.abs(got - ref).max() <= 1e-9 * np.abs(ref).max()
+    # the correction removes most of the nodal divergence
+    d0 = np.linalg.norm(O.divergence(m.nx, m.ny, m.nz, m.a, m.b, m.c, m.sigma, x))
+    d1 = np.linalg.norm(O.divergence(m.nx, m.ny, m.nz, m.a, m.b, m.c, m.sigma, got))
+    assert d1 < 1e-2 * d0
