@@ -1,0 +1,360 @@
+#!/usr/bin/env python3
+"""Benchmark: MT forward solves/s of the GB300 solver on the config-2 workload.
+
+Workload (configs[1] of the benchmark set): anisotropic model with Gaussian
+hills, 64x64x48 core cells of 50 m (80x80x80 with padding and air, 1,574,640
+complex edge unknowns), 8 frequencies over 0.001-1000 Hz x 2 polarisations =
+16 systems, EXCMG with 3 levels, finest tolerance 1e-8, 32x32 receivers.
+Synthetic, seeded (numpy default_rng(0)); the reference publishes no model
+files for it.
+
+A step = one complete forward solve of all 16 systems (both coarse levels,
+prolongations, the finest level) followed by the impedances at the 1024
+receivers.  `value` is solves/s with the conductivity resident in HBM;
+`e2e` is the same through the C-ABI call sfdx_fwd_solve with host buffers
+(H2D of sigma and D2H of all fields inside the timed region) followed by
+sfdx_impedance.  The per-step working set (~4 GB) is far larger than L2, so
+no flush is needed between steps.
+
+`--impl reference` times the reference algorithm's CPU restatement (the
+oracle: FP64 CSR, lexicographic SSOR-BiCGStab, serial per system) on the
+host cores, one thread per system, as a bounded sample scaled to full solves
+(see cpu_sample()).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+FALLBACK_HBM_GBS = 6800.0
+REF_SAMPLE_ITERS = 6
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, index=0):
+        self.path = tempfile.mktemp(suffix=".csv")
+        self.p = None
+        self.index = index
+
+    def start(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.f = open(self.path, "w")
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                       "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except Exception:
+            self.p.kill()
+        self.f.close()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as td
+        td.barrier()
+
+
+def max_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as td
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    td.all_reduce(t, op=td.ReduceOp.MAX)
+    return float(t.item())
+
+
+def solve_opts(precision):
+    import sfd_excmg_gb300 as S
+    return dict(excmg=1, level=3, eps=1e-8, precision=S.MIXED if precision == "mixed" else S.FP64, div_cor=0)
+
+
+def cpu_sample(model, freqs_idx, threads, iters=REF_SAMPLE_ITERS):
+    """Bounded sample of the reference algorithm on the host cores.
+
+    Per system (one thread each, the oracle releases the GIL): assembly of the
+    finest-level CSR (fd_assemb + dcfast), then `iters` iterations of
+    SSOR-BiCGStab (ssorfac + lusol + zamux, serial).  Returns the wall time of
+    the parallel sample and the mean per-iteration / set-up seconds.
+    """
+    from concurrent.futures import ThreadPoolExecutor
+
+    from oracle import oracle as O
+    import ctypes
+
+    L = O.lib()
+
+    def one(k):
+        ff = float(model.freq[k])
+        t0 = time.perf_counter()
+        conv = O.column_conv(model.sigma, model.nx, model.ny, model.nz)
+        edc, _, _ = O.mt1d_anl(ff, conv, model.c)
+        K, p1, _ = O.assemble(model.nx, model.ny, model.nz, model.a, model.b, model.c, model.sigma, ff, edc)
+        t1 = time.perf_counter()
+        ia = np.ascontiguousarray(K.indptr, np.int64)
+        ja = np.ascontiguousarray(K.indices, np.int32)
+        km = np.ascontiguousarray(K.data)
+        x = np.zeros(model.nl, np.complex128)
+        L.orc_bicgstab_fixed(ctypes.c_int64(model.nl), km.ctypes.data_as(ctypes.c_void_p),
+                             ia.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
+                             ja.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), p1.ctypes.data_as(ctypes.c_void_p),
+                             x.ctypes.data_as(ctypes.c_void_p), iters)
+        t2 = time.perf_counter()
+        return t1 - t0, (t2 - t1) / iters
+
+    t = time.perf_counter()
+    with ThreadPoolExecutor(max_workers=threads) as ex:
+        res = list(ex.map(one, freqs_idx))
+    wall = time.perf_counter() - t
+    return wall, float(np.mean([r[1] for r in res])), float(np.mean([r[0] for r in res]))
+
+
+def reference_iterations():
+    """Iterations the reference algorithm needs per cfg2 system (tests/golden/cfg2_reference, made by
+    tests/golden/make_cfg2_reference.py: plain path, zero guess, lexicographic SSOR + divergence correction)."""
+    d = os.path.join(ROOT, "tests", "golden", "cfg2_reference")
+    its = []
+    if os.path.isdir(d):
+        for fn in sorted(os.listdir(d)):
+            if fn.endswith(".json"):
+                with open(os.path.join(d, fn)) as f:
+                    its += [p["iters"] for p in json.load(f)["pol"]]
+    return its
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    from sfd_excmg_gb300 import synthetic as syn
+    m = syn.config2(seed=0)
+    ns = 2 * m.nf
+    threads = max(1, min(ns, os.cpu_count() or 1))
+    its = reference_iterations()
+    n_it = float(np.mean(its)) if its else float("nan")
+    vals = []
+    for w in range(args.warmup):
+        cpu_sample(m, list(range(m.nf)) * 2, threads, iters=2)
+    samples = []
+    for k in range(args.steps):
+        wall, t_it, t_setup = cpu_sample(m, list(range(m.nf)) * 2, threads)
+        # projected time of the full solve of all systems on `threads` cores
+        per_system = t_setup + n_it * t_it
+        proj = per_system * ns / threads
+        vals.append(ns / proj)
+        samples.append((wall, t_it, t_setup))
+    v = float(np.median(vals))
+    line = {
+        "impl": "reference", "metric": "MT solves/s", "value": v, "unit": "solves/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+        "ms_per_step": float(np.median([s[0] for s in samples]) * 1e3),
+        "config": {"workload": "cfg2 anisotropic+hills 80x80x80 (1,574,640 edges), 8 freqs x 2 pols",
+                   "solver": "SSOR-BiCGStab FP64 CSR (reference algorithm, oracle restatement)"},
+        "cpu_baseline": {"value": v, "unit": "solves/s", "cores": threads, "kind": "port",
+                         "sample": (f"per system: finest-level assembly + {REF_SAMPLE_ITERS} SSOR-BiCGStab iterations; "
+                                    f"scaled by the reference algorithm's mean iteration count {n_it:.0f} "
+                                    f"(tests/golden/cfg2_reference); {threads} systems in parallel")},
+        "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "data": "synthetic",
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, rank, world, local):
+    import torch
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as td
+        td.init_process_group("nccl")
+    import sfd_excmg_gb300 as S
+    from sfd_excmg_gb300 import capi
+    from sfd_excmg_gb300 import synthetic as syn
+
+    m = syn.config2(seed=0)
+    ns = 2 * m.nf
+    opts = solve_opts(args.precision)
+    plan = S.Plan(m, **opts)
+    stream = torch.cuda.Stream()
+    plan.set_stream(stream.cuda_stream)
+    sig = torch.from_numpy(np.ascontiguousarray(m.sigma)).to("cuda")
+    fields = torch.empty((m.nf, 2, m.nl, 2), dtype=torch.float64, device="cuda")
+    L = capi.lib()
+
+    def step():
+        plan.solve(sigma_device_ptr=sig.data_ptr(), out_device_ptr=fields.data_ptr(), allow_noconv=True)
+        return plan.impedance()
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    barrier(world)
+    clocks = Clocks(local)
+    clocks.start()
+    l0 = L.sfdx_launch_count()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    z = None
+    for _ in range(args.steps):
+        z = step()
+    e1.record(stream)
+    e1.synchronize()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    launches = (L.sfdx_launch_count() - l0) / args.steps
+    clk = clocks.stop()
+    ms = max_over_ranks(ms, world)
+    barrier(world)
+    value = ns * args.steps * world / (ms / 1e3)
+    status, iters, relres, lt = plan.status, plan.iters.copy(), plan.relres.copy(), plan.level_times()
+
+    # kernel rooflines on the finest level (CUDA events on the plan's stream)
+    hbm, src = peaks()
+    kern = {}
+    for kid, name in ((2, "mc_ssor_c64"), (0, "operator_c64")):
+        kms, kb = plan.kernel_time(kid, reps=10)
+        kern[name] = {"ms": kms, "bytes": kb, "gbs": kb / (kms / 1e3) / 1e9}
+
+    # end to end through the C ABI with host buffers
+    e2e_steps = max(1, args.steps // 2)
+    h2d = m.sigma.nbytes
+    d2h = m.nf * 2 * m.nl * 16 + m.nf * m.recv.shape[0] * 4 * 8
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    for _ in range(e2e_steps):
+        ex, _, _ = S.fwd_solve(m, **opts) if args.e2e_allow_noconv is False else _fwd_noconv(S, m, opts)
+        S.impedance(m, ex)
+    e2e_s = (time.perf_counter() - t) / e2e_steps
+    e2e_s = max_over_ranks(e2e_s, world)
+
+    extra = {}
+    if args.compare_fp64 and rank == 0:
+        p64 = S.Plan(m, **solve_opts("fp64"))
+        t = time.perf_counter()
+        p64.solve(allow_noconv=True)
+        t64 = time.perf_counter() - t
+        z64 = p64.impedance()
+        zc = z[..., 0::2] + 1j * z[..., 1::2]
+        z64c = z64[..., 0::2] + 1j * z64[..., 1::2]
+        rel = np.abs(zc - z64c) / np.abs(z64c)
+        extra = {"z_rel_err_vs_fp64": float(rel.max()), "z_rel_err_vs_fp64_median": float(np.median(rel)),
+                 "fp64_solves_per_s": ns / t64, "fp64_status": int(p64.status),
+                 "fp64_fine_iters": p64.iters[:, :, -1].ravel().tolist()}
+        p64.close()
+
+    if rank != 0:
+        plan.close()
+        return
+    dom = kern["mc_ssor_c64"]
+    cpu = None
+    if args.cpu_baseline:
+        its = reference_iterations()
+        wall, t_it, t_setup = cpu_sample(m, [0], 1)
+        n_it = float(np.mean(its)) if its else float("nan")
+        cpu = {"value": 1.0 / (t_setup + n_it * t_it), "unit": "solves/s", "cores": 1, "kind": "port",
+               "sample": (f"one system: finest-level assembly + {REF_SAMPLE_ITERS} serial SSOR-BiCGStab iterations "
+                          f"({t_it:.3f} s/it), scaled by the reference algorithm's mean iteration count {n_it:.0f}")}
+    line = {
+        "metric": "MT solves/s", "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "c64+c128" if args.precision == "mixed" else "c128", "data": "synthetic",
+        "config": {"workload": "cfg2: anisotropic 20-block model with Gaussian hills, 64x64x48 core cells of 50 m "
+                               "(80x80x80, 1,574,640 edges), 8 freqs 1e-3..1e3 Hz x 2 pols, EXCMG 3 levels, tol 1e-8, "
+                               "32x32 receivers",
+                   "precision": args.precision, "systems_per_step": ns, "l2": "working set > L2 (no flush)"},
+        "e2e": {"value": ns / e2e_s, "unit": "solves/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "hbm", "achieved": dom["gbs"], "peak": hbm, "unit": "GB/s", "frac": dom["gbs"] / hbm,
+                     "traffic": None, "kernel": "mc_ssor_c64 (11 colour sweeps)", "peak_source": src},
+        "kernels": kern,
+        "cpu_baseline": cpu,
+        "clocks": clk,
+        "solve": {"status": int(status), "fine_iters": iters[:, :, -1].ravel().tolist(),
+                  "relres_max": float(relres.max()), "level_ms": [float(x) for x in lt]},
+    }
+    line.update(extra)
+    print(json.dumps(line), flush=True)
+    plan.close()
+
+
+def _fwd_noconv(S, m, opts):
+    with S.Plan(m, **opts) as p:
+        ex = p.solve(allow_noconv=True)
+    return ex, None, None
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--no-compare-fp64", dest="compare_fp64", action="store_false")
+    ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    ap.add_argument("--e2e-strict", dest="e2e_allow_noconv", action="store_false")
+    args = ap.parse_args()
+    rank, world, local = dist()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_ours(args, rank, world, local)
+
+
+if __name__ == "__main__":
+    main()

@@ -95,6 +95,9 @@ const char* sfdx_strerror(int code);
 /* Library version (major*10000 + minor*100 + patch). */
 int sfdx_version(void);
 
+/* Number of CUDA kernel launches this library has issued in this process. */
+long long sfdx_launch_count(void);
+
 /* ------------------------------------------------------------------------
  * Forward solve.  Replaces fwd_solver(modelname, a, b, c, nair, level, slv,
  * eps, sigma, freq, ex) (fdfe_main.f90:1565-1594, called at
@@ -124,6 +127,11 @@ int sfdx_plan_impedance(sfdx_plan* plan, int nrec, const double* recv, int out_t
 const double* sfdx_plan_fields(sfdx_plan* plan);
 /* Bytes of device memory held by the plan. */
 long long sfdx_plan_device_bytes(const sfdx_plan* plan);
+/* Issue the plan's work on `stream` (a cudaStream_t; null = the plan's own stream). */
+int sfdx_plan_set_stream(sfdx_plan* plan, void* stream);
+/* CUDA-event time (ms per launch) of one kernel family on the finest level and its
+ * algorithmic HBM bytes: 0 operator c64, 1 operator c128, 2 MC-SSOR c64, 3 MC-SSOR c128. */
+int sfdx_plan_kernel_time(sfdx_plan* plan, int kernel, int reps, double* ms, double* bytes);
 /* Wall time (ms) of each level of the last solve, coarsest first (n >= levels). */
 int sfdx_plan_level_times(const sfdx_plan* plan, double* ms, int n);
 void sfdx_plan_destroy(sfdx_plan* plan);

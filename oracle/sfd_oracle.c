@@ -529,8 +529,9 @@ typedef struct {
     int64_t *jlu; /* 1-based */
     int64_t *ju;  /* 1-based */
     double w;
-    char pre; /* 'S' or 'J' */
+    char pre; /* 'S', 'J' or 'M' */
     zc *mj;   /* Jacobi diagonal */
+    void *mc; /* multi-colour data ('M') */
 } precond_t;
 
 static int ssorfac(int64_t n, const zc *a, const int64_t *ia0, const int32_t *ja0, double omega, precond_t *P) {
@@ -542,6 +543,7 @@ static int ssorfac(int64_t n, const zc *a, const int64_t *ia0, const int32_t *ja
     P->jlu = (int64_t *)calloc((size_t)(nnz + n + 2), sizeof(int64_t));
     P->ju = (int64_t *)calloc((size_t)(n + 2), sizeof(int64_t));
     P->mj = NULL;
+    P->mc = NULL;
     int64_t ju0 = n + 2;
     P->jlu[1] = ju0;
     for (int64_t ii = 1; ii <= n; ii++) {
@@ -568,6 +570,7 @@ static void jacobifac(int64_t n, const zc *a, const int64_t *ia0, const int32_t 
     P->pre = 'J';
     P->alu = NULL;
     P->jlu = P->ju = NULL;
+    P->mc = NULL;
     P->mj = (zc *)calloc((size_t)n, sizeof(zc));
     for (int64_t i = 0; i < n; i++)
         for (int64_t j = ia0[i]; j < ia0[i + 1]; j++)
@@ -579,6 +582,61 @@ static void precond_free(precond_t *P) {
     free(P->jlu);
     free(P->ju);
     free(P->mj);
+    P->alu = NULL;
+    P->jlu = P->ju = NULL;
+    P->mj = NULL;
+}
+
+/* Multi-colour symmetric Gauss-Seidel ('M'): the GPU's preconditioner,
+ * restated on the assembled CSR.  colour[i] in 0..5 (Ex (j+k)&1, Ey (i+k)&1,
+ * Ez (i+j)&1, orientation-major); forward sweep in increasing colour,
+ * backward in decreasing colour, x = (D+U)^{-1} D (D+L)^{-1} y with L, U the
+ * parts coupling to earlier / later colours.  Not part of the reference: it
+ * is the oracle of the multi-colour kernels. */
+typedef struct {
+    int64_t n;
+    const zc *a;
+    const int64_t *ia;
+    const int32_t *ja;
+    unsigned char *col;
+    zc *diag;
+} mcpre_t;
+
+static void mc_colours(int nx, int ny, int nz, unsigned char *col) {
+    int64_t q = 0;
+    for (int k = 0; k <= nz; k++)
+        for (int j = 0; j <= ny; j++)
+            for (int i = 0; i < nx; i++) col[q++] = (unsigned char)((j + k) & 1);
+    for (int k = 0; k <= nz; k++)
+        for (int j = 0; j < ny; j++)
+            for (int i = 0; i <= nx; i++) col[q++] = (unsigned char)(2 + ((i + k) & 1));
+    for (int k = 0; k < nz; k++)
+        for (int j = 0; j <= ny; j++)
+            for (int i = 0; i <= nx; i++) col[q++] = (unsigned char)(4 + ((i + j) & 1));
+}
+
+static void mc_psolve(const mcpre_t *M, const zc *y, zc *x) {
+    int64_t n = M->n;
+    for (int c = 0; c < 6; c++)
+        for (int64_t i = 0; i < n; i++) {
+            if (M->col[i] != c) continue;
+            zc s = y[i];
+            for (int64_t k = M->ia[i]; k < M->ia[i + 1]; k++) {
+                int32_t j = M->ja[k];
+                if (M->col[j] < c) s -= M->a[k] * x[j];
+            }
+            x[i] = s / M->diag[i];
+        }
+    for (int c = 5; c >= 0; c--)
+        for (int64_t i = 0; i < n; i++) {
+            if (M->col[i] != c) continue;
+            zc s = 0;
+            for (int64_t k = M->ia[i]; k < M->ia[i + 1]; k++) {
+                int32_t j = M->ja[k];
+                if (M->col[j] > c) s += M->a[k] * x[j];
+            }
+            x[i] = x[i] - s / M->diag[i];
+        }
 }
 
 /* x = M^{-1} y.  For 'S' this is lusol with pre_type='S' including the
@@ -589,6 +647,10 @@ static void psolve(const precond_t *P, const zc *y, zc *xo) {
     int64_t n = P->n;
     if (P->pre == 'J') {
         for (int64_t i = 0; i < n; i++) xo[i] = y[i] / P->mj[i];
+        return;
+    }
+    if (P->pre == 'M') {
+        mc_psolve((const mcpre_t *)P->mc, y, xo);
         return;
     }
     const zc *alu = P->alu;
@@ -902,9 +964,30 @@ typedef struct {
     double corr_tol, omega;
 } korc_opts;
 
+/* multi-colour preconditioner data: one per calling thread, colour buffer reused across solves */
+static __thread mcpre_t t_mc;
+static __thread int64_t t_mc_cap;
+
 static int make_precond(const korc_opts *o, int64_t n, const zc *K, const int64_t *ia, const int32_t *ja, precond_t *P) {
     if (o->pre == 'J') {
         jacobifac(n, K, ia, ja, P);
+        return 0;
+    }
+    if (o->pre == 'M') {
+        jacobifac(n, K, ia, ja, P); /* diagonal */
+        P->pre = 'M';
+        t_mc.n = n;
+        t_mc.a = K;
+        t_mc.ia = ia;
+        t_mc.ja = ja;
+        if (t_mc_cap < n) {
+            free(t_mc.col);
+            t_mc.col = (unsigned char *)malloc((size_t)n);
+            t_mc_cap = n;
+        }
+        mc_colours(o->nx, o->ny, o->nz, t_mc.col);
+        t_mc.diag = P->mj;
+        P->mc = &t_mc;
         return 0;
     }
     return ssorfac(n, K, ia, ja, o->omega, P);

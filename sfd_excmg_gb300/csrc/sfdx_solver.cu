@@ -17,6 +17,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <complex>
 #include <cstdio>
@@ -56,6 +57,9 @@ static const double kMu = 4.0 * 3.141592653589793238462643 * 1e-7;
     } while (0)
 
 static int g_nsm = 0;
+// kernel launches issued by this library (process-wide)
+static std::atomic<long long> g_launches{0};
+#define KL(...) (g_launches.fetch_add(1, std::memory_order_relaxed), __VA_ARGS__)
 static int device_sms() {
     if (!g_nsm) {
         int dev = 0;
@@ -228,7 +232,8 @@ struct Plan {
     int nf = 0, ns = 0, nlev = 0;
     std::vector<double> freq, wm;
     std::vector<Level> lev;  // lev[0] coarsest ... lev[nlev-1] finest
-    cudaStream_t st = nullptr;
+    cudaStream_t st = nullptr;      // stream all work of the plan is issued on
+    cudaStream_t own_st = nullptr;  // stream created by the plan (destroyed with it)
     // per-system device data
     DBuf d_state, d_wm, d_pol, d_edc, d_part, d_counter, d_tol, d_mask, d_scale, d_flag;
     // FP64 vectors (finest-level size)
@@ -246,7 +251,7 @@ struct Plan {
     std::vector<KState> hst;
     bool have_solution = false;
     ~Plan() {
-        if (st) cudaStreamDestroy(st);
+        if (own_st) cudaStreamDestroy(own_st);
     }
 };
 
@@ -269,13 +274,13 @@ template <class T, int O, int PP, int MODE>
 static void fwd_one(Plan& P, const Lev<T>& L, cplx<T>* w, cplx<T>* q, const cplx<T>* r, const cplx<T>* v) {
     const int B = block_for(P.ns);
     const int64_t W = colour_count(L, O) * P.ns;
-    k_sweep_fwd<T, O, PP, MODE><<<grid_for(W, B, 16), B, 0, P.st>>>(L, P.d_state.as<KState>(), P.ns, w, q, r, v);
+    KL(k_sweep_fwd<T, O, PP, MODE><<<grid_for(W, B, 16), B, 0, P.st>>>(L, P.d_state.as<KState>(), P.ns, w, q, r, v));
 }
 template <class T, int O, int PP>
 static void bwd_one(Plan& P, const Lev<T>& L, cplx<T>* x) {
     const int B = block_for(P.ns);
     const int64_t W = colour_count(L, O) * P.ns;
-    k_sweep_bwd<T, O, PP><<<grid_for(W, B, 16), B, 0, P.st>>>(L, P.d_state.as<KState>(), P.ns, x);
+    KL(k_sweep_bwd<T, O, PP><<<grid_for(W, B, 16), B, 0, P.st>>>(L, P.d_state.as<KState>(), P.ns, x));
 }
 
 // out = M^{-1} rhs where rhs is produced by MODE (see k_sweep_fwd)
@@ -283,7 +288,7 @@ template <class T, int MODE>
 static void precond(Plan& P, const Lev<T>& L, cplx<T>* out, cplx<T>* q, const cplx<T>* r, const cplx<T>* v) {
     if (P.o.precond == 'J') {
         const int B = block_for(P.ns);
-        k_jacobi<T, MODE><<<grid_for(L.nl * P.ns, B, 16), B, 0, P.st>>>(L, P.d_state.as<KState>(), P.ns, out, q, r, v);
+        KL(k_jacobi<T, MODE><<<grid_for(L.nl * P.ns, B, 16), B, 0, P.st>>>(L, P.d_state.as<KState>(), P.ns, out, q, r, v));
         return;
     }
     fwd_one<T, OX, 0, MODE>(P, L, out, q, r, v);
@@ -325,14 +330,14 @@ static int div_correct(Plan& P, const Level& LV, double2* x) {
     RC(P.d_part.alloc(std::max(P.d_part.bytes, (size_t)G1 * 2 * ns * sizeof(double2))));
     const size_t sm = 2 * B * sizeof(double2);
     KState* pst = P.d_pst.as<KState>();
-    k_dc_div<<<G1, B, sm, P.st>>>(G, P.d_state.as<KState>(), ns, x, t, r, p, phi, redbuf(P), pst);
+    KL(k_dc_div<<<G1, B, sm, P.st>>>(G, P.d_state.as<KState>(), ns, x, t, r, p, phi, redbuf(P), pst));
     const int maxit = 2000;  // pcg itmax (div_correc.f90:57)
     int it = 0;
     std::vector<KState> h(ns);
     for (; it < maxit; it++) {
-        k_dc_Ap<<<G1, B, sm, P.st>>>(G, pst, ns, p, v, redbuf(P));
-        k_dc_upd<<<G1, B, sm, P.st>>>(G, pst, ns, p, v, phi, r, redbuf(P), P.o.corr_tol, maxit);
-        k_dc_p<<<G1, B, 0, P.st>>>(G, pst, ns, r, p);
+        KL(k_dc_Ap<<<G1, B, sm, P.st>>>(G, pst, ns, p, v, redbuf(P)));
+        KL(k_dc_upd<<<G1, B, sm, P.st>>>(G, pst, ns, p, v, phi, r, redbuf(P), P.o.corr_tol, maxit));
+        KL(k_dc_p<<<G1, B, 0, P.st>>>(G, pst, ns, r, p));
         if ((it + 1) % 16 == 0) {
             CK(cudaMemcpyAsync(h.data(), pst, sizeof(KState) * ns, cudaMemcpyDeviceToHost, P.st));
             CK(cudaStreamSynchronize(P.st));
@@ -342,7 +347,7 @@ static int div_correct(Plan& P, const Level& LV, double2* x) {
         }
     }
     CK(cudaMemcpyAsync(h.data(), pst, sizeof(KState) * ns, cudaMemcpyDeviceToHost, P.st));
-    k_dc_grad<<<grid_for(LV.nl * ns, B, 16), B, 0, P.st>>>(G, P.d_state.as<KState>(), ns, phi, x);
+    KL(k_dc_grad<<<grid_for(LV.nl * ns, B, 16), B, 0, P.st>>>(G, P.d_state.as<KState>(), ns, phi, x));
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(P.st));
     P.dc_calls++;
@@ -390,7 +395,7 @@ static int bicgstab(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, cons
     const int G = grid_for(LV.nl * ns, B, 8);
     RC(P.d_part.alloc((size_t)G * 2 * ns * sizeof(double2)));
     KState* dst = P.d_state.as<KState>();
-    k_residual<T, T, 0><<<G, B, smem, P.st>>>(L, dst, ns, b, x, r, rhat, redbuf(P), nullptr, 0);
+    KL(k_residual<T, T, 0><<<G, B, smem, P.st>>>(L, dst, ns, b, x, r, rhat, redbuf(P), nullptr, 0));
     CK(cudaGetLastError());
     const int check_every = 8;
     for (int it = 1; it <= itmax; it++) {
@@ -398,13 +403,13 @@ static int bicgstab(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, cons
         // residual restart every corr_intv iterations (FP64 solves only)
         if (std::is_same<T, double>::value && P.o.div_cor && it % P.o.corr_intv == 0) {
             RC(div_correct(P, LV, reinterpret_cast<double2*>(x)));
-            k_residual<T, T, 1><<<G, B, smem, P.st>>>(L, dst, ns, b, x, r, rhat, redbuf(P), nullptr, 0);
+            KL(k_residual<T, T, 1><<<G, B, smem, P.st>>>(L, dst, ns, b, x, r, rhat, redbuf(P), nullptr, 0));
         }
         precond<T, RHS_PUPD>(P, L, y, p, r, v);
-        k_bicg_v<T><<<G, B, smem, P.st>>>(L, dst, ns, y, v, rhat, redbuf(P));
+        KL(k_bicg_v<T><<<G, B, smem, P.st>>>(L, dst, ns, y, v, rhat, redbuf(P)));
         precond<T, RHS_SUPD>(P, L, z, s, r, v);
-        k_bicg_t<T><<<G, B, smem, P.st>>>(L, dst, ns, z, t, s, redbuf(P));
-        k_bicg_upd<T, T><<<G, B, smem, P.st>>>(L, dst, ns, x, y, z, s, t, r, rhat, redbuf(P), nullptr, 0);
+        KL(k_bicg_t<T><<<G, B, smem, P.st>>>(L, dst, ns, z, t, s, redbuf(P)));
+        KL(k_bicg_upd<T, T><<<G, B, smem, P.st>>>(L, dst, ns, x, y, z, s, t, r, rhat, redbuf(P), nullptr, 0));
         if (it % check_every == 0 || it == itmax) {
             CK(cudaGetLastError());
             RC(sync_state(P));
@@ -433,8 +438,8 @@ static int true_residual(Plan& P, const Level& LV, const double2* b, const doubl
     const int G = grid_for(LV.nl * ns, B, 8);
     RC(P.d_part.alloc((size_t)G * 2 * ns * sizeof(double2)));
     RC(P.r64.alloc((size_t)LV.nl * ns * sizeof(double2)));
-    k_residual<double, double, 2><<<G, B, 2 * B * sizeof(double2), P.st>>>(
-        LV.lev<double>(), P.d_state.as<KState>(), ns, b, x, P.r64.as<double2>(), nullptr, redbuf(P), nullptr, 0);
+    KL(k_residual<double, double, 2><<<G, B, 2 * B * sizeof(double2), P.st>>>(
+        LV.lev<double>(), P.d_state.as<KState>(), ns, b, x, P.r64.as<double2>(), nullptr, redbuf(P), nullptr, 0));
     CK(cudaGetLastError());
     RC(sync_state(P));
     for (int q = 0; q < ns; q++) {
@@ -476,16 +481,38 @@ static int solve_level_mixed(Plan& P, const Level& LV, double tol, int itmax, st
     RC(P.d_scale.alloc(ns * sizeof(double)));
     const int B = block_for(ns);
     const int G = grid_for((int64_t)n64, B, 8);
+    std::vector<double> prev(ns, 0.0), applied(ns, 0.0), undo(ns, 0.0);
+    std::vector<int> bad(ns, 0);
     for (int ref = 0; ref <= P.o.max_refine; ref++) {
         RC(true_residual(P, LV, P.b64.as<double2>(), P.x64.as<double2>(), rel.data(), mask.data()));
+        // safeguard: a correction that raised the true residual is taken back
+        bool any_undo = false;
+        for (int q = 0; q < ns; q++) {
+            undo[q] = 0;
+            if (mask[q] && applied[q] != 0 && !(rel[q] < prev[q])) {
+                undo[q] = -applied[q];
+                any_undo = true;
+                rel[q] = prev[q];
+                bad[q]++;
+            }
+            applied[q] = 0;
+        }
+        if (any_undo) {
+            CK(cudaMemcpyAsync(P.d_scale.p, undo.data(), ns * sizeof(double), cudaMemcpyHostToDevice, P.st));
+            KL(k_refine_add<float><<<G, B, 0, P.st>>>(LV.nl, ns, P.d_scale.as<double>(), P.x64.as<double2>(),
+                                                   d32.as<float2>()));
+            RC(true_residual(P, LV, P.b64.as<double2>(), P.x64.as<double2>(), rel.data(), mask.data()));
+        }
         int left = 0;
         for (int q = 0; q < ns; q++) {
             if (!mask[q]) { scale[q] = 0; continue; }
             if (std::isnan(rel[q])) { status[q] = ST_NAN; mask[q] = 0; scale[q] = 0; continue; }
             if (rel[q] < tol) { status[q] = ST_CONV; mask[q] = 0; scale[q] = 0; continue; }
-            if (its[q] >= itmax) { status[q] = ST_MAXIT; mask[q] = 0; scale[q] = 0; continue; }
+            if (its[q] >= itmax || bad[q] >= 2) { status[q] = ST_MAXIT; mask[q] = 0; scale[q] = 0; continue; }
             scale[q] = rel[q] * P.hst[q].babs;  // ||r||
-            tols[q] = std::max(P.o.inner_tol, 0.3 * tol / rel[q]);
+            // ask the FP32 solve for what is still missing, but not below what
+            // single precision can deliver; tighter after a rejected step
+            tols[q] = std::max(P.o.inner_tol / (bad[q] ? 10.0 : 1.0), 0.3 * tol / rel[q]);
             left++;
         }
         if (!left) break;
@@ -494,14 +521,30 @@ static int solve_level_mixed(Plan& P, const Level& LV, double tol, int itmax, st
             break;
         }
         CK(cudaMemcpyAsync(P.d_scale.p, scale.data(), ns * sizeof(double), cudaMemcpyHostToDevice, P.st));
-        k_scale_to_f32<<<G, B, 0, P.st>>>(LV.nl, ns, P.d_scale.as<double>(), P.r64.as<double2>(), rhs32.as<float2>());
+        KL(k_scale_to_f32<<<G, B, 0, P.st>>>(LV.nl, ns, P.d_scale.as<double>(), P.r64.as<double2>(), rhs32.as<float2>()));
         CK(cudaMemsetAsync(d32.p, 0, n64 * sizeof(float2), P.st));
-        int inner_max = P.o.inner_maxit;
+        int inner_max = std::min(P.o.inner_maxit, std::max(1, itmax - *std::min_element(its.begin(), its.end())));
         RC(bicgstab<float>(P, LV, rhs32.as<float2>(), d32.as<float2>(), tols.data(), 0.0, inner_max, mask.data()));
-        for (int q = 0; q < ns; q++)
-            if (mask[q]) its[q] += std::max(0, P.hst[q].iters - 1);
-        k_refine_add<float><<<G, B, 0, P.st>>>(LV.nl, ns, P.d_scale.as<double>(), P.x64.as<double2>(), d32.as<float2>());
+        for (int q = 0; q < ns; q++) {
+            if (!mask[q]) continue;
+            its[q] += std::max(0, P.hst[q].iters - 1);
+            // apply the correction only if the inner solve reduced its residual
+            const KState& S = P.hst[q];
+            if (!(S.err < 1.0) || S.status == ST_NAN) {
+                scale[q] = 0;
+                bad[q]++;
+            }
+            prev[q] = rel[q];
+            applied[q] = scale[q];
+        }
+        CK(cudaMemcpyAsync(P.d_scale.p, scale.data(), ns * sizeof(double), cudaMemcpyHostToDevice, P.st));
+        KL(k_refine_add<float><<<G, B, 0, P.st>>>(LV.nl, ns, P.d_scale.as<double>(), P.x64.as<double2>(), d32.as<float2>()));
         CK(cudaGetLastError());
+        if (P.o.verbose || getenv("SFDX_VERBOSE")) {
+            fprintf(stderr, "sfdx:   refine %d rel:", ref);
+            for (int q = 0; q < ns; q++) fprintf(stderr, " %.1e", rel[q]);
+            fprintf(stderr, "\n");
+        }
     }
     return SFDX_OK;
 }
@@ -536,13 +579,13 @@ static int level_rhs(Plan& P, const Level& LV, const std::vector<double>& col /*
     CK(cudaMemcpyAsync(P.d_edc.p, edc.data(), edc.size() * sizeof(double2), cudaMemcpyHostToDevice, P.st));
     CK(cudaMemcpyAsync(P.d_pol.p, pols.data(), ns * sizeof(int), cudaMemcpyHostToDevice, P.st));
     const int B = block_for(ns);
-    k_build_rhs<<<grid_for(LV.nl * ns, B, 16), B, 0, P.st>>>(LV.lev<double>(), P.d_wm.as<double>(), P.d_pol.as<int>(),
-                                                              P.d_edc.as<double2>(), P.edc_stride, ns, P.b64.as<double2>());
+    KL(k_build_rhs<<<grid_for(LV.nl * ns, B, 16), B, 0, P.st>>>(LV.lev<double>(), P.d_wm.as<double>(), P.d_pol.as<int>(),
+                                                              P.d_edc.as<double2>(), P.edc_stride, ns, P.b64.as<double2>()));
     CK(cudaGetLastError());
     // NaN check of the right-hand side (fdfe_main.f90:1398-1403)
     RC(P.d_flag.alloc(sizeof(int)));
     CK(cudaMemsetAsync(P.d_flag.p, 0, sizeof(int), P.st));
-    k_nan_check<double><<<grid_for(LV.nl * ns, 256), 256, 0, P.st>>>(LV.nl * ns, P.b64.as<double2>(), P.d_flag.as<int>());
+    KL(k_nan_check<double><<<grid_for(LV.nl * ns, 256), 256, 0, P.st>>>(LV.nl * ns, P.b64.as<double2>(), P.d_flag.as<int>()));
     int flag = 0;
     CK(cudaMemcpyAsync(&flag, P.d_flag.p, sizeof(int), cudaMemcpyDeviceToHost, P.st));
     CK(cudaStreamSynchronize(P.st));
@@ -581,10 +624,10 @@ static int set_conductivity(Plan& P, const double* sigma, bool on_device) {
         CK(cudaMemcpyAsync(c1.p, cs.data(), cs.size() * 8, cudaMemcpyHostToDevice, P.st));
         const double* fs = F.spac.as<double>();
         const double* cp = c1.as<double>();
-        k_coarsen<<<grid_for(C.ncell, 128, 32), 128, 0, P.st>>>(F.nx, F.ny, F.nz, fs, fs + F.nx, fs + F.nx + F.ny, cp,
+        KL(k_coarsen<<<grid_for(C.ncell, 128, 32), 128, 0, P.st>>>(F.nx, F.ny, F.nz, fs, fs + F.nx, fs + F.nx + F.ny, cp,
                                                                 cp + C.nx, cp + C.nx + C.ny, 1 << k,
                                                                 (P.o.quirks & SFDX_QUIRK_COARSEN_SHIFT) ? 1 : 0,
-                                                                F.sig64.as<double>(), C.sig64.as<double>());
+                                                                F.sig64.as<double>(), C.sig64.as<double>()));
         CK(cudaGetLastError());
         CK(cudaStreamSynchronize(P.st));
     }
@@ -593,10 +636,10 @@ static int set_conductivity(Plan& P, const double* sigma, bool on_device) {
         RC(L.sig32.alloc((size_t)6 * L.ncell * sizeof(float)));
         // sigma is real: convert pairs as if complex (6*ncell is even)
         int64_t n2 = 3 * L.ncell;
-        k_convert<double, float><<<grid_for(n2, 256), 256, 0, P.st>>>(n2, L.sig64.as<double2>(), L.sig32.as<float2>());
+        KL(k_convert<double, float><<<grid_for(n2, 256), 256, 0, P.st>>>(n2, L.sig64.as<double2>(), L.sig32.as<float2>()));
         RC(P.d_flag.alloc(sizeof(int)));
         CK(cudaMemsetAsync(P.d_flag.p, 0, sizeof(int), P.st));
-        k_any_offdiag<<<grid_for(3 * L.ncell, 256), 256, 0, P.st>>>(L.ncell, L.sig64.as<double>(), P.d_flag.as<int>());
+        KL(k_any_offdiag<<<grid_for(3 * L.ncell, 256), 256, 0, P.st>>>(L.ncell, L.sig64.as<double>(), P.d_flag.as<int>()));
         int flag = 0;
         CK(cudaMemcpyAsync(&flag, P.d_flag.p, sizeof(int), cudaMemcpyDeviceToHost, P.st));
         CK(cudaStreamSynchronize(P.st));
@@ -614,15 +657,15 @@ static int prolongate(Plan& P, int l, const double2* u0, const double2* u1, doub
     const int B = block_for(ns);
     // quad: level l-2 -> level l-1 (coordinates from pairwise sums of level l)
     const double* cq = F.crd_quad.as<double>();
-    k_interp<double, 2><<<grid_for(M.nl * ns, B, 16), B, 0, P.st>>>(M.nx, M.ny, M.nz, cq, cq + M.nx + 1,
-                                                                     cq + M.nx + M.ny + 2, midq, ns, u0, P.ut.as<double2>());
-    k_extrapolate<double><<<grid_for(M.nl * ns, 256), 256, 0, P.st>>>(M.nl * ns, u1, P.ut.as<double2>());
+    KL(k_interp<double, 2><<<grid_for(M.nl * ns, B, 16), B, 0, P.st>>>(M.nx, M.ny, M.nz, cq, cq + M.nx + 1,
+                                                                     cq + M.nx + M.ny + 2, midq, ns, u0, P.ut.as<double2>()));
+    KL(k_extrapolate<double><<<grid_for(M.nl * ns, 256), 256, 0, P.st>>>(M.nl * ns, u1, P.ut.as<double2>()));
     const double* cc = F.crd_cubic.as<double>();
-    k_interp<double, 4><<<grid_for(F.nl * ns, B, 16), B, 0, P.st>>>(F.nx, F.ny, F.nz, cc, cc + F.nx + 1,
-                                                                     cc + F.nx + F.ny + 2, midq, ns, P.ut.as<double2>(), out);
+    KL(k_interp<double, 4><<<grid_for(F.nl * ns, B, 16), B, 0, P.st>>>(F.nx, F.ny, F.nz, cc, cc + F.nx + 1,
+                                                                     cc + F.nx + F.ny + 2, midq, ns, P.ut.as<double2>(), out));
     CK(cudaGetLastError());
     CK(cudaMemsetAsync(P.d_flag.p, 0, sizeof(int), P.st));
-    k_nan_check<double><<<grid_for(F.nl * ns, 256), 256, 0, P.st>>>(F.nl * ns, out, P.d_flag.as<int>());
+    KL(k_nan_check<double><<<grid_for(F.nl * ns, 256), 256, 0, P.st>>>(F.nl * ns, out, P.d_flag.as<int>()));
     int flag = 0;
     CK(cudaMemcpyAsync(&flag, P.d_flag.p, sizeof(int), cudaMemcpyDeviceToHost, P.st));
     CK(cudaStreamSynchronize(P.st));
@@ -730,7 +773,7 @@ static int plan_solve(Plan& P) {
     // de-interleave into [nf][2][nl] (system-major)
     RC(P.ex_out.alloc(nfine));
     const int B = block_for(ns);
-    k_scatter_sys<double><<<grid_for(F.nl * ns, B, 16), B, 0, P.st>>>(F.nl, ns, P.x64.as<double2>(), P.ex_out.as<double2>());
+    KL(k_scatter_sys<double><<<grid_for(F.nl * ns, B, 16), B, 0, P.st>>>(F.nl, ns, P.x64.as<double2>(), P.ex_out.as<double2>()));
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(P.st));
     P.have_solution = true;
@@ -772,8 +815,11 @@ extern "C" void sfdx_default_opts(sfdx_opts* o) {
     o->maxit_level = 1000;   // fdfe_main.f90:1414
     o->precision = SFDX_FP64;
     o->quirks = SFDX_QUIRKS_REFERENCE;
-    o->coarse_tol = 1e-12;
-    o->coarse_maxit = 5000;
+    // The two coarsest levels only feed the extrapolated guess: its residual on
+    // the next level is the same for a coarse solve to 1e-6 as for an exact
+    // (direct) one, so 1e-6 in FP64 stands in for PARDISO.
+    o->coarse_tol = 1e-6;
+    o->coarse_maxit = 1000;
     o->inner_tol = 1e-4;
     o->inner_maxit = 1000;
     o->max_refine = 12;
@@ -829,7 +875,8 @@ extern "C" int sfdx_plan_create(sfdx_plan** out, const sfdx_opts* opts, int nx, 
         if (nx % f || ny % f || nz % f) return SFDX_ERR_MESH;
         if (nx / f < 1 || ny / f < 1 || nz / f < 1) return SFDX_ERR_MESH;
     }
-    CK(cudaStreamCreateWithFlags(&P.st, cudaStreamNonBlocking));
+    CK(cudaStreamCreateWithFlags(&P.own_st, cudaStreamNonBlocking));
+    P.st = P.own_st;
     P.lev.resize(P.nlev);
     for (int l = 0; l < P.nlev; l++) {
         Level& L = P.lev[l];
@@ -894,6 +941,74 @@ extern "C" long long sfdx_plan_device_bytes(const sfdx_plan* plan) {
 }
 
 extern "C" void sfdx_plan_destroy(sfdx_plan* plan) { delete plan; }
+
+extern "C" long long sfdx_launch_count(void) { return g_launches.load(); }
+
+extern "C" int sfdx_plan_set_stream(sfdx_plan* plan, void* stream) {
+    if (!plan) return SFDX_ERR_ARG;
+    CK(cudaStreamSynchronize(plan->P.st));
+    plan->P.st = stream ? (cudaStream_t)stream : plan->P.own_st;
+    return SFDX_OK;
+}
+
+// Times `reps` launches of one kernel family on the plan's finest level
+// with CUDA events on the plan's stream (the plan must have solved once so
+// that the conductivity is resident).  kernel: 0 operator (complex64),
+// 1 operator (complex128), 2 multi-colour SSOR application (complex64, all
+// 11 colour launches), 3 multi-colour SSOR (complex128), 4 prolongation
+// 2h->h (complex128).  bytes: algorithmic HBM bytes of one application.
+extern "C" int sfdx_plan_kernel_time(sfdx_plan* plan, int kernel, int reps, double* ms, double* bytes) {
+    if (!plan || !ms || reps < 1) return SFDX_ERR_ARG;
+    Plan& P = plan->P;
+    if (!P.have_solution) return SFDX_ERR_ARG;
+    const Level& F = P.lev[P.nlev - 1];
+    const int ns = P.ns;
+    const size_t n = (size_t)F.nl * ns;
+    const bool f32 = (kernel == 0 || kernel == 2);
+    const size_t es = f32 ? 8 : 16;
+    for (int q = 0; q < 3; q++) RC(P.kv[q].alloc(n * es));
+    std::vector<KState> init(ns);
+    for (int q = 0; q < ns; q++) {
+        memset(&init[q], 0, sizeof(KState));
+        init[q].wm = P.wm[q];
+        init[q].active = 1;
+    }
+    CK(cudaMemcpyAsync(P.d_state.p, init.data(), sizeof(KState) * ns, cudaMemcpyHostToDevice, P.st));
+    // deterministic non-zero input
+    if (f32) KL(k_convert<double, float><<<grid_for(n, 256), 256, 0, P.st>>>(n, P.ex_out.as<double2>(), P.kv[0].as<float2>()));
+    else CK(cudaMemcpyAsync(P.kv[0].p, P.ex_out.p, n * 16, cudaMemcpyDeviceToDevice, P.st));
+    const int B = block_for(ns);
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    auto launch = [&]() {
+        switch (kernel) {
+            case 0: KL(k_apply<float><<<grid_for(n, B, 16), B, 0, P.st>>>(F.lev<float>(), P.d_wm.as<double>(), ns, P.kv[0].as<float2>(), P.kv[1].as<float2>())); break;
+            case 1: KL(k_apply<double><<<grid_for(n, B, 16), B, 0, P.st>>>(F.lev<double>(), P.d_wm.as<double>(), ns, P.kv[0].as<double2>(), P.kv[1].as<double2>())); break;
+            case 2: precond<float, RHS_VEC>(P, F.lev<float>(), P.kv[1].as<float2>(), P.kv[0].as<float2>(), nullptr, nullptr); break;
+            case 3: precond<double, RHS_VEC>(P, F.lev<double>(), P.kv[1].as<double2>(), P.kv[0].as<double2>(), nullptr, nullptr); break;
+            default: break;
+        }
+    };
+    launch();
+    CK(cudaEventRecord(e0, P.st));
+    for (int r = 0; r < reps; r++) launch();
+    CK(cudaEventRecord(e1, P.st));
+    CK(cudaEventSynchronize(e1));
+    float t = 0;
+    CK(cudaEventElapsedTime(&t, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    CK(cudaGetLastError());
+    *ms = t / reps;
+    // algorithmic bytes: read x, write y (complex, per edge and system) and
+    // the six conductivities per cell once per launch
+    const double p = f32 ? 4.0 : 8.0;
+    double b1 = (double)F.nl * ns * 4 * p + (double)F.ncell * 6 * p;
+    if (kernel == 2 || kernel == 3) b1 *= 2;  // forward + backward sweep
+    if (bytes) *bytes = b1;
+    return SFDX_OK;
+}
 
 extern "C" int sfdx_plan_level_times(const sfdx_plan* plan, double* ms, int n) {
     if (!plan || !ms) return SFDX_ERR_ARG;
@@ -1014,16 +1129,16 @@ extern "C" int sfdx_apply_operator(int nx, int ny, int nz, const double* a, cons
     CK(cudaMemcpyAsync(dx.p, x, n * 16, cudaMemcpyHostToDevice, P.st));
     const int B = block_for(ns);
     if (precision == SFDX_FP64) {
-        k_apply<double><<<grid_for(n, B, 16), B, 0, P.st>>>(L.lev<double>(), P.d_wm.as<double>(), ns, dx.as<double2>(),
-                                                              dy.as<double2>());
+        KL(k_apply<double><<<grid_for(n, B, 16), B, 0, P.st>>>(L.lev<double>(), P.d_wm.as<double>(), ns, dx.as<double2>(),
+                                                              dy.as<double2>()));
     } else {
         DBuf fx, fy;
         RC(fx.alloc(n * 8));
         RC(fy.alloc(n * 8));
-        k_convert<double, float><<<grid_for(n, 256), 256, 0, P.st>>>(n, dx.as<double2>(), fx.as<float2>());
-        k_apply<float><<<grid_for(n, B, 16), B, 0, P.st>>>(L.lev<float>(), P.d_wm.as<double>(), ns, fx.as<float2>(),
-                                                             fy.as<float2>());
-        k_convert<float, double><<<grid_for(n, 256), 256, 0, P.st>>>(n, fy.as<float2>(), dy.as<double2>());
+        KL(k_convert<double, float><<<grid_for(n, 256), 256, 0, P.st>>>(n, dx.as<double2>(), fx.as<float2>()));
+        KL(k_apply<float><<<grid_for(n, B, 16), B, 0, P.st>>>(L.lev<float>(), P.d_wm.as<double>(), ns, fx.as<float2>(),
+                                                             fy.as<float2>()));
+        KL(k_convert<float, double><<<grid_for(n, 256), 256, 0, P.st>>>(n, fy.as<float2>(), dy.as<double2>()));
         CK(cudaStreamSynchronize(P.st));
     }
     CK(cudaGetLastError());
@@ -1050,10 +1165,10 @@ extern "C" int sfdx_build_rhs(int nx, int ny, int nz, const double* a, const dou
     CK(cudaMemcpyAsync(P.d_pol.p, pols, 2 * sizeof(int), cudaMemcpyHostToDevice, P.st));
     RC(P.b64.alloc((size_t)L.nl * 2 * sizeof(double2)));
     const int B = block_for(2);
-    k_build_rhs<<<grid_for(L.nl * 2, B, 16), B, 0, P.st>>>(L.lev<double>(), P.d_wm.as<double>(), P.d_pol.as<int>(),
-                                                            P.d_edc.as<double2>(), P.edc_stride, 2, P.b64.as<double2>());
+    KL(k_build_rhs<<<grid_for(L.nl * 2, B, 16), B, 0, P.st>>>(L.lev<double>(), P.d_wm.as<double>(), P.d_pol.as<int>(),
+                                                            P.d_edc.as<double2>(), P.edc_stride, 2, P.b64.as<double2>()));
     RC(P.ex_out.alloc((size_t)L.nl * 2 * sizeof(double2)));
-    k_scatter_sys<double><<<grid_for(L.nl * 2, B, 16), B, 0, P.st>>>(L.nl, 2, P.b64.as<double2>(), P.ex_out.as<double2>());
+    KL(k_scatter_sys<double><<<grid_for(L.nl * 2, B, 16), B, 0, P.st>>>(L.nl, 2, P.b64.as<double2>(), P.ex_out.as<double2>()));
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(p1, P.ex_out.p, L.nl * 16, cudaMemcpyDeviceToHost, P.st));
     CK(cudaMemcpyAsync(p2, P.ex_out.as<double2>() + L.nl, L.nl * 16, cudaMemcpyDeviceToHost, P.st));
@@ -1090,9 +1205,9 @@ extern "C" int sfdx_precond_apply(int nx, int ny, int nz, const double* a, const
         DBuf fy, fx;
         RC(fy.alloc(n * 8));
         RC(fx.alloc(n * 8));
-        k_convert<double, float><<<grid_for(n, 256), 256, 0, P.st>>>(n, dy.as<double2>(), fy.as<float2>());
+        KL(k_convert<double, float><<<grid_for(n, 256), 256, 0, P.st>>>(n, dy.as<double2>(), fy.as<float2>()));
         precond<float, RHS_VEC>(P, L.lev<float>(), fx.as<float2>(), fy.as<float2>(), nullptr, nullptr);
-        k_convert<float, double><<<grid_for(n, 256), 256, 0, P.st>>>(n, fx.as<float2>(), dx.as<double2>());
+        KL(k_convert<float, double><<<grid_for(n, 256), 256, 0, P.st>>>(n, fx.as<float2>(), dx.as<double2>()));
         CK(cudaStreamSynchronize(P.st));
     }
     CK(cudaGetLastError());
@@ -1129,10 +1244,10 @@ extern "C" int sfdx_mesh_coarsen(int nx, int ny, int nz, const double* a, const 
     cudaMemcpyAsync(sp.p, hs.data(), hs.size() * 8, cudaMemcpyHostToDevice, st);
     cudaMemcpyAsync(ds0.p, sigma, n0 * 48, cudaMemcpyHostToDevice, st);
     const double* s = sp.as<double>();
-    k_coarsen<<<grid_for(n1, 128, 32), 128, 0, st>>>(nx, ny, nz, s, s + nx, s + nx + ny, s + nx + ny + nz,
+    KL(k_coarsen<<<grid_for(n1, 128, 32), 128, 0, st>>>(nx, ny, nz, s, s + nx, s + nx + ny, s + nx + ny + nz,
                                                      s + nx + ny + nz + cx, s + nx + ny + nz + cx + cy, asf,
                                                      (quirks & SFDX_QUIRK_COARSEN_SHIFT) ? 1 : 0, ds0.as<double>(),
-                                                     ds1.as<double>());
+                                                     ds1.as<double>()));
     cudaMemcpyAsync(sigma1, ds1.p, n1 * 48, cudaMemcpyDeviceToHost, st);
     cudaError_t e = cudaStreamSynchronize(st);
     if (e == cudaSuccess) e = cudaGetLastError();

@@ -109,6 +109,17 @@ class Plan:
         capi.check(capi.lib().sfdx_plan_level_times(self._h, capi.dptr(ms), self.nlev), "sfdx_plan_level_times")
         return ms
 
+    def set_stream(self, stream_handle: int | None) -> None:
+        """Issue the plan's kernels on a caller's CUDA stream (e.g. torch.cuda.current_stream().cuda_stream)."""
+        capi.check(capi.lib().sfdx_plan_set_stream(self._h, ctypes.c_void_p(stream_handle or 0)), "sfdx_plan_set_stream")
+
+    def kernel_time(self, kernel: int, reps: int = 20):
+        """(ms per launch, algorithmic bytes per launch) of one kernel family on the finest level."""
+        ms, b = ctypes.c_double(), ctypes.c_double()
+        capi.check(capi.lib().sfdx_plan_kernel_time(self._h, kernel, reps, ctypes.byref(ms), ctypes.byref(b)),
+                   "sfdx_plan_kernel_time")
+        return ms.value, b.value
+
     def device_bytes(self) -> int:
         return int(capi.lib().sfdx_plan_device_bytes(self._h))
 

@@ -208,3 +208,20 @@ def test_divergence_correction_matches_div_correc():
     d0 = np.linalg.norm(O.divergence(m.nx, m.ny, m.nz, m.a, m.b, m.c, m.sigma, x))
     d1 = np.linalg.norm(O.divergence(m.nx, m.ny, m.nz, m.a, m.b, m.c, m.sigma, got))
     assert d1 < 1e-2 * d0
+
+
+@pytest.mark.parametrize("ff", [0.01, 5.0])
+def test_bicgstab_iterates_match_multicolour_oracle(ff):
+    """Same algorithm (Bicg_stab_p with the multi-colour SSOR) on CPU and GPU:
+    the stopping iteration must agree and the solutions match closely."""
+    m = _model(7)
+    K, p1, p2, _ = _csr(m, ff)
+    mesh = (m.nx, m.ny, m.nz, m.a, m.b, m.c, m.sigma)
+    opts = O.OracleOpts(pre="M", div_cor=False)
+    rhs = np.stack([p1, p2], axis=1)
+    x, it, rr, rc = S.krylov_solve(m.nx, m.ny, m.nz, m.a, m.b, m.c, m.sigma, [ff, ff], rhs, tol=1e-8, itmax=2000,
+                                   div_cor=0)
+    for s, p in enumerate((p1, p2)):
+        xo, ito, _ = O.solve_krylov(1, mesh, K, p, np.zeros(m.nl), 1e-8, 2000, opts)
+        assert abs(int(it[s]) - ito) <= 1, (it, ito)
+        assert np.linalg.norm(x[:, s] - xo) <= 1e-6 * np.linalg.norm(xo)
