@@ -119,9 +119,13 @@ def max_over_ranks(x, world):
     return float(t.item())
 
 
-def solve_opts(precision):
+SOLVER = {"bicgstab": 1, "gpbicg": 3}
+
+
+def solve_opts(precision, solver="bicgstab"):
     import sfd_excmg_gb300 as S
-    return dict(excmg=1, level=3, eps=1e-8, precision=S.MIXED if precision == "mixed" else S.FP64, div_cor=0)
+    return dict(excmg=1, level=3, eps=1e-8, precision=S.MIXED if precision == "mixed" else S.FP64, div_cor=0,
+                solver=SOLVER[solver])
 
 
 def cpu_sample(model, freqs_idx, threads, iters=REF_SAMPLE_ITERS):
@@ -226,7 +230,7 @@ def run_ours(args, rank, world, local):
 
     m = syn.config2(seed=0)
     ns = 2 * m.nf
-    opts = solve_opts(args.precision)
+    opts = solve_opts(args.precision, args.solver)
     plan = S.Plan(m, **opts)
     stream = torch.cuda.Stream()
     plan.set_stream(stream.cuda_stream)
@@ -284,7 +288,7 @@ def run_ours(args, rank, world, local):
 
     extra = {}
     if args.compare_fp64 and rank == 0:
-        p64 = S.Plan(m, **solve_opts("fp64"))
+        p64 = S.Plan(m, **solve_opts("fp64", args.solver))
         t = time.perf_counter()
         p64.solve(allow_noconv=True)
         t64 = time.perf_counter() - t
@@ -345,6 +349,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--solver", default="bicgstab", choices=list(SOLVER))
     ap.add_argument("--no-compare-fp64", dest="compare_fp64", action="store_false")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     ap.add_argument("--e2e-strict", dest="e2e_allow_noconv", action="store_false")

@@ -78,9 +78,7 @@ typedef struct sfdx_opts {
     int quirks;         /* SFDX_QUIRK_* bits (SFDX_QUIRKS_REFERENCE by default)         */
     double coarse_tol;  /* relative residual of the on-device solve replacing PARDISO */
     int coarse_maxit;   /* iteration limit of that solve                               */
-    double inner_tol;   /* mixed precision: FP32 inner-solve reduction per refinement  */
-    int inner_maxit;    /* mixed precision: inner iterations per refinement step       */
-    int max_refine;     /* mixed precision: refinement steps                           */
+    int reliable_every; /* mixed precision: iterations between FP64 residual updates */
     int batch;          /* systems solved together (0 = all 2*nf)                      */
     int verbose;        /* 0 silent, 1 per-level summary on stderr                     */
     int use_graphs;     /* capture Krylov iterations in CUDA graphs                    */

@@ -48,7 +48,7 @@ class Opts(ctypes.Structure):
         ("corr_tol", ctypes.c_double), ("ssor_omega", ctypes.c_double), ("sigma_air", ctypes.c_double),
         ("maxit_plain", ctypes.c_int), ("maxit_level", ctypes.c_int), ("precision", ctypes.c_int),
         ("quirks", ctypes.c_int), ("coarse_tol", ctypes.c_double), ("coarse_maxit", ctypes.c_int),
-        ("inner_tol", ctypes.c_double), ("inner_maxit", ctypes.c_int), ("max_refine", ctypes.c_int),
+        ("reliable_every", ctypes.c_int),
         ("batch", ctypes.c_int), ("verbose", ctypes.c_int), ("use_graphs", ctypes.c_int),
     ]
 

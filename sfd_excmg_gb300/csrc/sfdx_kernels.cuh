@@ -488,9 +488,120 @@ __global__ void k_residual(Lev<XT> L, KState* st, int ns, const cplx<XT>* __rest
             double2 q1 = make_double2((a.x * b.x + a.y * b.y) / bd, (a.y * b.x - a.x * b.y) / bd);
             double2 q2 = make_double2((al2.x * om2.x + al2.y * om2.y) / od, (al2.y * om2.x - al2.x * om2.y) / od);
             S.beta = make_double2(q1.x * q2.x - q1.y * q2.y, q1.x * q2.y + q1.y * q2.x);
-        } else {
+        } else if (MODE == 2) {
             S.err = nr;  // absolute residual norm; the host driver scales
             S.babs = sqrt(v.y);
+        } else if (MODE == 3) {  // GPBiCG start (solvers.f90:203-221): no stopping test before iteration 1
+            S.babs = sqrt(v.y);
+            S.err = nr / S.babs;
+            S.it = 1;
+            S.iters = 0;
+            S.beta = make_double2(0.0, 0.0);
+            if (isnan(S.err)) {
+                S.status = ST_NAN;
+                S.active = 0;
+            }
+        }
+        // MODE 4: residual restart only (GPBiCG after a divergence correction)
+    }
+}
+
+// ------------------------------------------------------------------ reliable updates
+// Mixed precision: the Krylov iteration runs in complex64 on a partial
+// solution x32; every few iterations (and whenever the complex64 recurrence
+// claims convergence) the partial solution is folded into the complex128
+// solution, the residual is recomputed in FP64 and handed back to the
+// complex64 iteration, whose search directions are kept (reliable updated
+// residuals, Sleijpen & van der Vorst 1996).  Convergence is decided on the
+// FP64 residual only.
+enum { ST_VCONV = 5 };
+
+// systems whose complex64 recurrence converged become active again until the
+// FP64 residual confirms it
+__global__ void k_reactivate(KState* st, int ns) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < ns && st[s].status == ST_CONV) {
+        st[s].status = ST_RUN;
+        st[s].active = 1;
+    }
+}
+
+// x64 += x32 ; x32 = 0  (active systems)
+template <class T>
+__global__ void k_flush(int64_t nl, const KState* st, int ns, double2* __restrict__ x64, cplx<T>* __restrict__ x32) {
+    const int64_t W = nl * ns;
+    for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < W; g += (int64_t)gridDim.x * blockDim.x) {
+        const int s = (int)(g % ns);
+        if (!st[s].active) continue;
+        cplx<T> d = x32[g];
+        double2 v = x64[g];
+        x64[g] = make_double2(v.x + (double)d.x, v.y + (double)d.y);
+        x32[g] = zero<T>();
+    }
+}
+
+// r32 = b64 - A64 x64 ; FP64 convergence test ; re-synchronise the scalar
+// recurrences with the new residual.  solver: 1 BiCGStab (rho = <rhat, r>,
+// beta = rho/rhoold * alpha/omega), 3 GPBiCG (beta = alpha/omega *
+// <r0, r>/<r0, r_old>).
+template <class T>
+__global__ void k_reliable(Lev<double> L, KState* st, int ns, const double2* __restrict__ b, const double2* __restrict__ x,
+                           cplx<T>* __restrict__ r, const cplx<T>* __restrict__ rhat, int solver, RedBuf rb) {
+    extern __shared__ double2 smem[];
+    const int s = threadIdx.x % ns;
+    const bool act = st[s].active;
+    const double wm = st[s].wm;
+    double rr = 0, hr = 0, hi = 0;
+    const int64_t W = L.nl * ns;
+    if (act)
+        for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < W; g += (int64_t)gridDim.x * blockDim.x) {
+            int o, i, j, k;
+            edecode(L, g / ns, o, i, j, k);
+            double2 ax = apply_row<double>(L, o, i, j, k, wm, x, ns, s, x[g]);
+            double2 rv = b[g] - ax;
+            cplx<T> rt = mk<T>((T)rv.x, (T)rv.y);
+            r[g] = rt;
+            rr += rv.x * rv.x + rv.y * rv.y;
+            cplx<T> h = rhat[g];
+            hr += (double)h.x * rv.x + (double)h.y * rv.y;
+            hi += (double)h.x * rv.y - (double)h.y * rv.x;
+        }
+    double2 acc[2] = {make_double2(rr, 0.0), make_double2(hr, hi)};
+    if (!block_reduce_and_last<2, double>(acc, ns, rb, smem)) return;
+    const int B = blockDim.x;
+    for (int ss = threadIdx.x; ss < ns; ss += B) {
+        KState& S = st[ss];
+        if (!S.active) continue;
+        S.err = sqrt(smem[B + ss].x) / S.babs;
+        double2 h = smem[B + ns + ss];
+        if (isnan(S.err)) {
+            S.status = ST_NAN;
+            S.active = 0;
+            continue;
+        }
+        if (S.err < S.tol) {
+            S.status = ST_VCONV;
+            S.active = 0;
+            continue;
+        }
+        if (S.it > S.itmax) {
+            S.status = ST_MAXIT;
+            S.active = 0;
+            continue;
+        }
+        if (solver == 3) {
+            double2 a = S.alpha, o = S.omega, ro = S.rho;
+            double od = o.x * o.x + o.y * o.y, rd = ro.x * ro.x + ro.y * ro.y;
+            double2 q1 = make_double2((a.x * o.x + a.y * o.y) / od, (a.y * o.x - a.x * o.y) / od);
+            double2 q2 = make_double2((h.x * ro.x + h.y * ro.y) / rd, (h.y * ro.x - h.x * ro.y) / rd);
+            S.beta = make_double2(q1.x * q2.x - q1.y * q2.y, q1.x * q2.y + q1.y * q2.x);
+        } else {
+            S.rho = h;
+            double2 a = S.rho, bb = S.rhoold, al2 = S.alpha, om2 = S.omega;
+            double bd = bb.x * bb.x + bb.y * bb.y, od = om2.x * om2.x + om2.y * om2.y;
+            double2 q1 = make_double2((a.x * bb.x + a.y * bb.y) / bd, (a.y * bb.x - a.x * bb.y) / bd);
+            double2 q2 = make_double2((al2.x * om2.x + al2.y * om2.y) / od, (al2.y * om2.x - al2.x * om2.y) / od);
+            S.beta = make_double2(q1.x * q2.x - q1.y * q2.y, q1.x * q2.y + q1.y * q2.x);
         }
     }
 }

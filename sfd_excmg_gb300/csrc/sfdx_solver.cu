@@ -31,6 +31,7 @@
 #include "sfdx.h"
 #include "sfdx_divcorr.cuh"
 #include "sfdx_excmg.cuh"
+#include "sfdx_gpbicg.cuh"
 #include "sfdx_host.h"
 #include "sfdx_kernels.cuh"
 
@@ -71,9 +72,9 @@ static int device_sms() {
 }
 
 // block size: ns * 2^k in [128, 1024] and >= 2*ns (reductions need NQ*ns <= B)
-static int block_for(int ns) {
+static int block_for(int ns, int nq = 2) {
     int b = ns;
-    while (b < 128 || b < 2 * ns) b *= 2;
+    while (b < 128 || b < nq * ns) b *= 2;
     return b;
 }
 static int grid_for(int64_t work, int B, int per_sm = 8) {
@@ -239,7 +240,7 @@ struct Plan {
     // FP64 vectors (finest-level size)
     DBuf x64, b64, r64, u0, u1, ut, ex_out;
     // Krylov vectors (precision of the active solve)
-    DBuf kv[8];
+    DBuf kv[14];
     // divergence correction: t, r, p, v, phi (nodes) and the PCG state
     DBuf dcv[5], d_pst;
     int dc_calls = 0, dc_last_iters = 0;
@@ -355,12 +356,56 @@ static int div_correct(Plan& P, const Level& LV, double2* x) {
     return SFDX_OK;
 }
 
-// ------------------------------------------------------------------ BiCGStab
-// Solves the ns systems of level L: A x = b.  x holds the initial guess.
-// Vectors r, rhat, p, v, y, s, z, t come from P.kv (precision T).
+// ------------------------------------------------------------------ Krylov drivers
+// Reliable-update context of a mixed-precision solve: the FP64 right-hand
+// side and solution; the complex64 iteration works on a partial solution.
+struct Reliable {
+    const double2* b64;
+    double2* x64;
+    int every;  // iterations between FP64 residual replacements
+};
+
+static void init_states(Plan& P, const double* tols_host, double tol, int itmax, const int* mask_host,
+                        std::vector<KState>& init) {
+    init.resize(P.ns);
+    for (int q = 0; q < P.ns; q++) {
+        KState S;
+        memset(&S, 0, sizeof(S));
+        S.wm = P.wm[q];
+        S.tol = tols_host ? tols_host[q] : tol;
+        S.itmax = itmax;
+        S.active = mask_host ? mask_host[q] : 1;
+        S.status = S.active ? ST_RUN : ST_CONV;
+        init[q] = S;
+    }
+}
+
+// FP64 residual replacement for the systems still running or whose complex64
+// recurrence claims convergence; returns the number of systems left active.
+template <class T>
+static int reliable_update(Plan& P, const Level& LV, const Reliable& rel, cplx<T>* x32, cplx<T>* r, const cplx<T>* rhat,
+                           int solver, int& active) {
+    const int ns = P.ns;
+    const int B = block_for(ns, 4);
+    KState* dst = P.d_state.as<KState>();
+    KL(k_reactivate<<<(ns + 127) / 128, 128, 0, P.st>>>(dst, ns));
+    KL(k_flush<T><<<grid_for(LV.nl * ns, B, 16), B, 0, P.st>>>(LV.nl, dst, ns, rel.x64, x32));
+    KL(k_reliable<T><<<grid_for(LV.nl * ns, B, 8), B, 4 * B * sizeof(double2), P.st>>>(
+        LV.lev<double>(), dst, ns, rel.b64, rel.x64, r, rhat, solver, redbuf(P)));
+    CK(cudaGetLastError());
+    RC(sync_state(P));
+    active = 0;
+    for (int q = 0; q < ns; q++) active += P.hst[q].active;
+    return SFDX_OK;
+}
+
+// Bicg_stab_p (solvers.f90:522-719) for the ns systems of level L: A x = b.
+// Plain: x holds the initial guess (precision T).  With `rel` (mixed
+// precision) b/x are the complex64 work vectors and the FP64 b64/x64 of
+// `rel` define the system.
 template <class T>
 static int bicgstab(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, const double* tols_host, double tol,
-                    int itmax, const int* mask_host) {
+                    int itmax, const int* mask_host, const Reliable* rel = nullptr) {
     const Lev<T> L = LV.lev<T>();
     const int ns = P.ns;
     const size_t vb = (size_t)LV.nl * ns * sizeof(cplx<T>);
@@ -373,35 +418,29 @@ static int bicgstab(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, cons
     cplx<T>* s = P.kv[5].as<cplx<T>>();
     cplx<T>* z = P.kv[6].as<cplx<T>>();
     cplx<T>* t = P.kv[7].as<cplx<T>>();
-    CK(cudaMemsetAsync(p, 0, vb, P.st));
-    CK(cudaMemsetAsync(v, 0, vb, P.st));
-    CK(cudaMemsetAsync(y, 0, vb, P.st));
-    CK(cudaMemsetAsync(z, 0, vb, P.st));
-    // state
-    std::vector<KState> init(ns);
-    for (int q = 0; q < ns; q++) {
-        KState S;
-        memset(&S, 0, sizeof(S));
-        S.wm = P.wm[q];
-        S.tol = tols_host ? tols_host[q] : tol;
-        S.itmax = itmax;
-        S.active = mask_host ? mask_host[q] : 1;
-        S.status = S.active ? ST_RUN : ST_CONV;
-        init[q] = S;
-    }
+    for (cplx<T>* q : {p, v, y, z}) CK(cudaMemsetAsync(q, 0, vb, P.st));
+    std::vector<KState> init;
+    init_states(P, tols_host, tol, itmax, mask_host, init);
     CK(cudaMemcpyAsync(P.d_state.p, init.data(), sizeof(KState) * ns, cudaMemcpyHostToDevice, P.st));
-    const int B = block_for(ns);
-    const size_t smem = 2 * B * sizeof(double2);
+    const int B = block_for(ns, 4);
+    const size_t smem = 4 * B * sizeof(double2);
     const int G = grid_for(LV.nl * ns, B, 8);
-    RC(P.d_part.alloc((size_t)G * 2 * ns * sizeof(double2)));
+    RC(P.d_part.alloc(std::max(P.d_part.bytes, (size_t)G * 4 * ns * sizeof(double2))));
     KState* dst = P.d_state.as<KState>();
-    KL(k_residual<T, T, 0><<<G, B, smem, P.st>>>(L, dst, ns, b, x, r, rhat, redbuf(P), nullptr, 0));
+    if (rel) {
+        CK(cudaMemsetAsync(x, 0, vb, P.st));
+        KL(k_residual<T, double, 0><<<G, B, smem, P.st>>>(LV.lev<double>(), dst, ns, rel->b64, rel->x64, r, rhat,
+                                                            redbuf(P), nullptr, 0));
+    } else {
+        KL(k_residual<T, T, 0><<<G, B, smem, P.st>>>(L, dst, ns, b, x, r, rhat, redbuf(P), nullptr, 0));
+    }
     CK(cudaGetLastError());
     const int check_every = 8;
+    int last_rel = 0;
     for (int it = 1; it <= itmax; it++) {
         // top of iteration `it` (solvers.f90:630-640): divergence correction and
         // residual restart every corr_intv iterations (FP64 solves only)
-        if (std::is_same<T, double>::value && P.o.div_cor && it % P.o.corr_intv == 0) {
+        if (!rel && std::is_same<T, double>::value && P.o.div_cor && it % P.o.corr_intv == 0) {
             RC(div_correct(P, LV, reinterpret_cast<double2*>(x)));
             KL(k_residual<T, T, 1><<<G, B, smem, P.st>>>(L, dst, ns, b, x, r, rhat, redbuf(P), nullptr, 0));
         }
@@ -413,11 +452,91 @@ static int bicgstab(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, cons
         if (it % check_every == 0 || it == itmax) {
             CK(cudaGetLastError());
             RC(sync_state(P));
-            int act = 0;
-            for (int q = 0; q < ns; q++) act += P.hst[q].active;
+            int act = 0, cand = 0;
+            for (int q = 0; q < ns; q++) {
+                act += P.hst[q].active;
+                cand += P.hst[q].status == ST_CONV;
+            }
+            if (rel && (cand || it - last_rel >= rel->every || it == itmax)) {
+                RC(reliable_update<T>(P, LV, *rel, x, r, rhat, 1, act));
+                last_rel = it;
+            }
             if (!act) break;
         }
     }
+    if (rel) KL(k_flush<T><<<grid_for(LV.nl * ns, B, 16), B, 0, P.st>>>(LV.nl, dst, ns, rel->x64, x));
+    RC(sync_state(P));
+    return SFDX_OK;
+}
+
+// pgpbicg (solvers.f90:137-315) for the ns systems of level L (same calling
+// convention as bicgstab).
+template <class T>
+static int gpbicg(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, const double* tols_host, double tol,
+                  int itmax, const int* mask_host, const Reliable* rel = nullptr) {
+    const Lev<T> L = LV.lev<T>();
+    const int ns = P.ns;
+    const size_t vb = (size_t)LV.nl * ns * sizeof(cplx<T>);
+    for (int q = 0; q < 14; q++) RC(P.kv[q].alloc(vb));
+    cplx<T>* V[14];
+    for (int q = 0; q < 14; q++) V[q] = P.kv[q].as<cplx<T>>();
+    cplx<T> *r = V[0], *r0 = V[1], *rp = V[2], *y = V[3], *p = V[4], *u = V[5], *w = V[6], *t = V[7];
+    cplx<T>* tp[2] = {V[8], V[9]};
+    cplx<T> *ap = V[10], *at = V[11], *z = V[12], *tmp = V[13];
+    for (cplx<T>* q : {u, w, t, tp[0], tp[1], z}) CK(cudaMemsetAsync(q, 0, vb, P.st));
+    std::vector<KState> init;
+    init_states(P, tols_host, tol, itmax, mask_host, init);
+    CK(cudaMemcpyAsync(P.d_state.p, init.data(), sizeof(KState) * ns, cudaMemcpyHostToDevice, P.st));
+    const int B = block_for(ns, 4);
+    const size_t smem = 4 * B * sizeof(double2);
+    const int G = grid_for(LV.nl * ns, B, 8);
+    RC(P.d_part.alloc(std::max(P.d_part.bytes, (size_t)G * 4 * ns * sizeof(double2))));
+    KState* dst = P.d_state.as<KState>();
+    if (rel) {
+        CK(cudaMemsetAsync(x, 0, vb, P.st));
+        KL(k_residual<T, double, 3><<<G, B, smem, P.st>>>(LV.lev<double>(), dst, ns, rel->b64, rel->x64, r, r0,
+                                                            redbuf(P), nullptr, 0));
+    } else {
+        KL(k_residual<T, T, 3><<<G, B, smem, P.st>>>(L, dst, ns, b, x, r, r0, redbuf(P), nullptr, 0));
+    }
+    precond<T, RHS_VEC>(P, L, rp, r, nullptr, nullptr);
+    CK(cudaMemcpyAsync(p, rp, vb, cudaMemcpyDeviceToDevice, P.st));
+    const int Ge = grid_for(LV.nl * ns, B, 16);
+    int cur = 0, last_rel = 0;
+    for (int it = 1; it <= itmax; it++) {
+        if (!rel && std::is_same<T, double>::value && P.o.div_cor && it % P.o.corr_intv == 0) {
+            // solvers.f90:223-235: correct x, restart r and r0 (rp is kept)
+            RC(div_correct(P, LV, reinterpret_cast<double2*>(x)));
+            KL(k_residual<T, T, 4><<<G, B, smem, P.st>>>(L, dst, ns, b, x, r, r0, redbuf(P), nullptr, 0));
+        }
+        KL(k_gp_ap<T><<<G, B, smem, P.st>>>(L, dst, ns, p, ap, r0, r, redbuf(P)));
+        KL(k_gp_yt<T><<<Ge, B, 0, P.st>>>(LV.nl, dst, ns, y, t, r, w, ap));
+        precond<T, RHS_VEC>(P, L, tmp, ap, nullptr, nullptr);
+        KL(k_gp_tp<T><<<Ge, B, 0, P.st>>>(LV.nl, dst, ns, tp[cur], rp, tmp));
+        KL(k_gp_at<T><<<G, B, smem, P.st>>>(L, dst, ns, tp[cur], at, t, y, redbuf(P)));
+        KL(k_gp_upd<T, T><<<G, B, smem, P.st>>>(LV.nl, dst, ns, u, z, x, r, tmp, tp[cur ^ 1], rp, p, t, y, at, r0,
+                                                 redbuf(P), nullptr, 0));
+        bool stop = false;
+        if (it % 8 == 0 || it == itmax) {
+            CK(cudaGetLastError());
+            RC(sync_state(P));
+            int act = 0, cand = 0;
+            for (int q = 0; q < ns; q++) {
+                act += P.hst[q].active;
+                cand += P.hst[q].status == ST_CONV;
+            }
+            if (rel && (cand || it - last_rel >= rel->every || it == itmax)) {
+                RC(reliable_update<T>(P, LV, *rel, x, r, r0, 3, act));
+                last_rel = it;
+            }
+            stop = !act;
+        }
+        if (stop) break;
+        precond<T, RHS_VEC>(P, L, rp, r, nullptr, nullptr);
+        KL(k_gp_pw<T><<<Ge, B, 0, P.st>>>(LV.nl, dst, ns, w, p, at, ap, rp, u));
+        cur ^= 1;
+    }
+    if (rel) KL(k_flush<T><<<grid_for(LV.nl * ns, B, 16), B, 0, P.st>>>(LV.nl, dst, ns, rel->x64, x));
     RC(sync_state(P));
     return SFDX_OK;
 }
@@ -453,8 +572,12 @@ static int true_residual(Plan& P, const Level& LV, const double2* b, const doubl
 // FP64 solve to `tol` with the reference's solver semantics.
 static int solve_level_fp64(Plan& P, const Level& LV, double tol, int itmax, std::vector<int>& its,
                             std::vector<int>& status) {
-    if (P.o.solver != SFDX_SOLVER_BICGSTAB) return SFDX_ERR_UNSUPPORTED;
-    RC(bicgstab<double>(P, LV, P.b64.as<double2>(), P.x64.as<double2>(), nullptr, tol, itmax, nullptr));
+    if (P.o.solver == SFDX_SOLVER_BICGSTAB)
+        RC(bicgstab<double>(P, LV, P.b64.as<double2>(), P.x64.as<double2>(), nullptr, tol, itmax, nullptr));
+    else if (P.o.solver == SFDX_SOLVER_GPBICG)
+        RC(gpbicg<double>(P, LV, P.b64.as<double2>(), P.x64.as<double2>(), nullptr, tol, itmax, nullptr));
+    else
+        return SFDX_ERR_UNSUPPORTED;
     its.resize(P.ns);
     status.resize(P.ns);
     for (int q = 0; q < P.ns; q++) {
@@ -464,87 +587,27 @@ static int solve_level_fp64(Plan& P, const Level& LV, double tol, int itmax, std
     return SFDX_OK;
 }
 
-// Mixed precision: FP64 residual, complex64 inner BiCGStab on the
-// normalised residual, FP64 update; stops on the TRUE relative residual.
+// Mixed precision: complex64 operator, smoother and Krylov recurrences;
+// complex128 solution, residual and convergence test (reliable updates).
 static int solve_level_mixed(Plan& P, const Level& LV, double tol, int itmax, std::vector<int>& its,
                              std::vector<int>& status) {
-    if (P.o.solver != SFDX_SOLVER_BICGSTAB) return SFDX_ERR_UNSUPPORTED;
     const int ns = P.ns;
-    const size_t n64 = (size_t)LV.nl * ns;
-    its.assign(ns, 0);
-    status.assign(ns, ST_RUN);
-    std::vector<int> mask(ns, 1);
-    std::vector<double> rel(ns), scale(ns), tols(ns);
-    DBuf rhs32, d32;
-    RC(rhs32.alloc(n64 * sizeof(float2)));
-    RC(d32.alloc(n64 * sizeof(float2)));
-    RC(P.d_scale.alloc(ns * sizeof(double)));
-    const int B = block_for(ns);
-    const int G = grid_for((int64_t)n64, B, 8);
-    std::vector<double> prev(ns, 0.0), applied(ns, 0.0), undo(ns, 0.0);
-    std::vector<int> bad(ns, 0);
-    for (int ref = 0; ref <= P.o.max_refine; ref++) {
-        RC(true_residual(P, LV, P.b64.as<double2>(), P.x64.as<double2>(), rel.data(), mask.data()));
-        // safeguard: a correction that raised the true residual is taken back
-        bool any_undo = false;
-        for (int q = 0; q < ns; q++) {
-            undo[q] = 0;
-            if (mask[q] && applied[q] != 0 && !(rel[q] < prev[q])) {
-                undo[q] = -applied[q];
-                any_undo = true;
-                rel[q] = prev[q];
-                bad[q]++;
-            }
-            applied[q] = 0;
-        }
-        if (any_undo) {
-            CK(cudaMemcpyAsync(P.d_scale.p, undo.data(), ns * sizeof(double), cudaMemcpyHostToDevice, P.st));
-            KL(k_refine_add<float><<<G, B, 0, P.st>>>(LV.nl, ns, P.d_scale.as<double>(), P.x64.as<double2>(),
-                                                   d32.as<float2>()));
-            RC(true_residual(P, LV, P.b64.as<double2>(), P.x64.as<double2>(), rel.data(), mask.data()));
-        }
-        int left = 0;
-        for (int q = 0; q < ns; q++) {
-            if (!mask[q]) { scale[q] = 0; continue; }
-            if (std::isnan(rel[q])) { status[q] = ST_NAN; mask[q] = 0; scale[q] = 0; continue; }
-            if (rel[q] < tol) { status[q] = ST_CONV; mask[q] = 0; scale[q] = 0; continue; }
-            if (its[q] >= itmax || bad[q] >= 2) { status[q] = ST_MAXIT; mask[q] = 0; scale[q] = 0; continue; }
-            scale[q] = rel[q] * P.hst[q].babs;  // ||r||
-            // ask the FP32 solve for what is still missing, but not below what
-            // single precision can deliver; tighter after a rejected step
-            tols[q] = std::max(P.o.inner_tol / (bad[q] ? 10.0 : 1.0), 0.3 * tol / rel[q]);
-            left++;
-        }
-        if (!left) break;
-        if (ref == P.o.max_refine) {
-            for (int q = 0; q < ns; q++) if (mask[q]) status[q] = ST_MAXIT;
-            break;
-        }
-        CK(cudaMemcpyAsync(P.d_scale.p, scale.data(), ns * sizeof(double), cudaMemcpyHostToDevice, P.st));
-        KL(k_scale_to_f32<<<G, B, 0, P.st>>>(LV.nl, ns, P.d_scale.as<double>(), P.r64.as<double2>(), rhs32.as<float2>()));
-        CK(cudaMemsetAsync(d32.p, 0, n64 * sizeof(float2), P.st));
-        int inner_max = std::min(P.o.inner_maxit, std::max(1, itmax - *std::min_element(its.begin(), its.end())));
-        RC(bicgstab<float>(P, LV, rhs32.as<float2>(), d32.as<float2>(), tols.data(), 0.0, inner_max, mask.data()));
-        for (int q = 0; q < ns; q++) {
-            if (!mask[q]) continue;
-            its[q] += std::max(0, P.hst[q].iters - 1);
-            // apply the correction only if the inner solve reduced its residual
-            const KState& S = P.hst[q];
-            if (!(S.err < 1.0) || S.status == ST_NAN) {
-                scale[q] = 0;
-                bad[q]++;
-            }
-            prev[q] = rel[q];
-            applied[q] = scale[q];
-        }
-        CK(cudaMemcpyAsync(P.d_scale.p, scale.data(), ns * sizeof(double), cudaMemcpyHostToDevice, P.st));
-        KL(k_refine_add<float><<<G, B, 0, P.st>>>(LV.nl, ns, P.d_scale.as<double>(), P.x64.as<double2>(), d32.as<float2>()));
-        CK(cudaGetLastError());
-        if (P.o.verbose || getenv("SFDX_VERBOSE")) {
-            fprintf(stderr, "sfdx:   refine %d rel:", ref);
-            for (int q = 0; q < ns; q++) fprintf(stderr, " %.1e", rel[q]);
-            fprintf(stderr, "\n");
-        }
+    const size_t n = (size_t)LV.nl * ns;
+    DBuf x32;
+    RC(x32.alloc(n * sizeof(float2)));
+    Reliable rel{P.b64.as<double2>(), P.x64.as<double2>(), P.o.reliable_every > 0 ? P.o.reliable_every : 40};
+    if (P.o.solver == SFDX_SOLVER_GPBICG)
+        RC(gpbicg<float>(P, LV, nullptr, x32.as<float2>(), nullptr, tol, itmax, nullptr, &rel));
+    else if (P.o.solver == SFDX_SOLVER_BICGSTAB)
+        RC(bicgstab<float>(P, LV, nullptr, x32.as<float2>(), nullptr, tol, itmax, nullptr, &rel));
+    else
+        return SFDX_ERR_UNSUPPORTED;
+    its.resize(ns);
+    status.resize(ns);
+    for (int q = 0; q < ns; q++) {
+        its[q] = P.hst[q].iters;
+        int st = P.hst[q].status;
+        status[q] = (st == ST_VCONV) ? ST_CONV : (st == ST_CONV || st == ST_RUN ? ST_MAXIT : st);
     }
     return SFDX_OK;
 }
@@ -820,9 +883,7 @@ extern "C" void sfdx_default_opts(sfdx_opts* o) {
     // (direct) one, so 1e-6 in FP64 stands in for PARDISO.
     o->coarse_tol = 1e-6;
     o->coarse_maxit = 1000;
-    o->inner_tol = 1e-4;
-    o->inner_maxit = 1000;
-    o->max_refine = 12;
+    o->reliable_every = 40;
     o->batch = 0;
     o->verbose = 0;
     o->use_graphs = 1;

@@ -158,31 +158,47 @@ def test_jacobi_preconditioner():
     assert np.abs(got - ref).max() <= 1e-12 * np.abs(ref).max()
 
 
-def test_krylov_fp64_converges_to_direct_solution():
+def _earth_edges(m):
+    """Edges whose both end nodes lie at or below the air-earth interface.  Above it the
+    operator is nearly singular (air conductivity 1e-9: discrete gradients are an almost
+    null space), so iterative and direct solutions differ there without changing any
+    observable; fields are compared on the earth edges."""
+    nx, ny, nz, na = m.nx, m.ny, m.nz, m.nair
+    kx = np.repeat(np.arange(nz + 1), (ny + 1) * nx)
+    ky = np.repeat(np.arange(nz + 1), ny * (nx + 1))
+    kz = np.repeat(np.arange(nz), (ny + 1) * (nx + 1))
+    return np.concatenate([kx >= na, ky >= na, kz >= na])
+
+
+@pytest.mark.parametrize("solver", [1, 3])
+def test_krylov_fp64_converges_to_direct_solution(solver):
     m = _model(0)
     ff = 1.0
     K, p1, p2, _ = _csr(m, ff)
     from scipy.sparse.linalg import splu
     lu = splu(K.tocsc())
     rhs = np.stack([p1, p2], axis=1)
-    x, it, rr, rc = S.krylov_solve(m.nx, m.ny, m.nz, m.a, m.b, m.c, m.sigma, [ff, ff], rhs, tol=1e-10, itmax=3000)
+    x, it, rr, rc = S.krylov_solve(m.nx, m.ny, m.nz, m.a, m.b, m.c, m.sigma, [ff, ff], rhs, tol=1e-10, itmax=3000,
+                                   div_cor=0, solver=solver)
     assert rc == 0, (it, rr)
     assert np.all(rr < 1e-9), rr
+    earth = _earth_edges(m)
     for s, p in enumerate((p1, p2)):
         xd = lu.solve(p)
         r = p - K @ x[:, s]
         assert np.linalg.norm(r) <= 1e-9 * np.linalg.norm(p)
-        # fields in the earth (below the air layers) agree with the direct solve
-        assert np.linalg.norm(x[:, s] - xd) <= 1e-3 * np.linalg.norm(xd)
+        # relative residual 1e-10 on this mesh leaves ~1e-6 in the earth fields
+        assert np.linalg.norm((x[:, s] - xd)[earth]) <= 1e-5 * np.linalg.norm(xd[earth])
 
 
-def test_krylov_mixed_precision_reaches_fp64_tolerance():
+@pytest.mark.parametrize("solver", [1, 3])
+def test_krylov_mixed_precision_reaches_fp64_tolerance(solver):
     m = _model(3)
     ff = 0.1
     K, p1, p2, _ = _csr(m, ff)
     rhs = np.stack([p1, p2], axis=1)
     x, it, rr, rc = S.krylov_solve(m.nx, m.ny, m.nz, m.a, m.b, m.c, m.sigma, [ff, ff], rhs, tol=1e-10, itmax=5000,
-                                   precision=S.MIXED)
+                                   precision=S.MIXED, solver=solver)
     assert rc == 0, (it, rr)
     for s, p in enumerate((p1, p2)):
         r = p - K @ x[:, s]
@@ -210,18 +226,23 @@ def test_divergence_correction_matches_div_correc():
     assert d1 < 1e-2 * d0
 
 
+@pytest.mark.parametrize("solver", [1, 3])
 @pytest.mark.parametrize("ff", [0.01, 5.0])
-def test_bicgstab_iterates_match_multicolour_oracle(ff):
-    """Same algorithm (Bicg_stab_p with the multi-colour SSOR) on CPU and GPU:
-    the stopping iteration must agree and the solutions match closely."""
+def test_krylov_iterates_match_multicolour_oracle(ff, solver):
+    """Same algorithm (Bicg_stab_p / pgpbicg with the multi-colour SSOR) on CPU and
+    GPU: the stopping iteration agrees and the converged fields match."""
     m = _model(7)
     K, p1, p2, _ = _csr(m, ff)
     mesh = (m.nx, m.ny, m.nz, m.a, m.b, m.c, m.sigma)
     opts = O.OracleOpts(pre="M", div_cor=False)
     rhs = np.stack([p1, p2], axis=1)
     x, it, rr, rc = S.krylov_solve(m.nx, m.ny, m.nz, m.a, m.b, m.c, m.sigma, [ff, ff], rhs, tol=1e-8, itmax=2000,
-                                   div_cor=0)
+                                   div_cor=0, solver=solver)
+    earth = _earth_edges(m)
     for s, p in enumerate((p1, p2)):
-        xo, ito, _ = O.solve_krylov(1, mesh, K, p, np.zeros(m.nl), 1e-8, 2000, opts)
+        xo, ito, _ = O.solve_krylov(solver, mesh, K, p, np.zeros(m.nl), 1e-8, 2000, opts)
+        # summation order differs (tree vs sequential dot products): allow a
+        # one-iteration shift of the stopping test
         assert abs(int(it[s]) - ito) <= 1, (it, ito)
-        assert np.linalg.norm(x[:, s] - xo) <= 1e-6 * np.linalg.norm(xo)
+        assert np.linalg.norm(p - K @ x[:, s]) <= 1.01e-8 * np.linalg.norm(p)
+        assert np.linalg.norm((x[:, s] - xo)[earth]) <= 1e-4 * np.linalg.norm(xo[earth])

@@ -35,7 +35,7 @@ def _zc(res):
 
 def test_halfspace_known_answer():
     m = syn.halfspace(n=16, freqs=(1.0, 10.0))
-    ex, it, rr = S.fwd_solve(m, eps=1e-10)
+    ex, it, rr = S.fwd_solve(m, eps=1e-10, div_cor=0)
     res = S.impedance(m, ex, out_type=2)
     # discretisation error of a 16^3 mesh: within 5 % and 2 degrees
     assert np.all(np.abs(res[..., 0:2] / 100.0 - 1) < 0.05), res
@@ -45,7 +45,7 @@ def test_halfspace_known_answer():
 @pytest.mark.parametrize("excmg", [0, 1])
 def test_forward_fp64_matches_direct(excmg):
     m = syn.small_aniso(n=16, seed=1, freqs=(0.05, 20.0))
-    ex, it, rr = S.fwd_solve(m, eps=1e-10, excmg=excmg, level=3)
+    ex, it, rr = S.fwd_solve(m, eps=1e-10, excmg=excmg, level=3, div_cor=0)
     assert np.all(rr < 1e-9), rr
     _, zref = _direct_Z(m)
     z = S.impedance(m, ex)
@@ -55,7 +55,7 @@ def test_forward_fp64_matches_direct(excmg):
 
 def test_forward_mixed_matches_fp64():
     m = syn.small_aniso(n=16, seed=2, freqs=(0.01, 1.0, 100.0))
-    ex64, _, rr64 = S.fwd_solve(m, eps=1e-10, excmg=1, level=3)
+    ex64, _, rr64 = S.fwd_solve(m, eps=1e-10, excmg=1, level=3, div_cor=0)
     exm, _, rrm = S.fwd_solve(m, eps=1e-10, excmg=1, level=3, precision=S.MIXED)
     assert np.all(rrm < 1e-10), rrm
     z64 = _zc(S.impedance(m, ex64))
@@ -69,7 +69,7 @@ def test_forward_mixed_matches_fp64():
 
 def test_plan_reuse_and_device_impedance():
     m = syn.small_aniso(n=16, seed=3, freqs=(0.3, 3.0))
-    with S.Plan(m, eps=1e-9, excmg=1, level=3) as p:
+    with S.Plan(m, eps=1e-9, excmg=1, level=3, div_cor=0) as p:
         ex1 = p.solve()
         z1 = p.impedance()
         ex2 = p.solve()
