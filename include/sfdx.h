@@ -187,10 +187,12 @@ int sfdx_prolongate(int nx, int ny, int nz, const double* a1, const double* b1, 
 
 /* One Krylov solve (Bicg_stab_p solvers.f90:522-719 / pgpbicg :137-315 /
  * the other solver ids) of K x = rhs on one mesh for ns interleaved systems,
- * starting from x.  iters[ns], relres[ns] (true residual) are outputs. */
+ * starting from x.  iters[ns], relres[ns] (true residual) are outputs;
+ * history (optional, [ns][itmax]) receives the recurrence residual recorded at
+ * the top of each iteration (the .ccv history of solvers.f90:687-704). */
 int sfdx_krylov_solve(const sfdx_opts* o, int nx, int ny, int nz, const double* a, const double* b, const double* c,
                       const double* sigma, int ns, const double* freqs, const double* rhs, double* x, double tol,
-                      int itmax, int* iters, double* relres);
+                      int itmax, int* iters, double* relres, double* history);
 
 /* Divergence correction (div_correc.f90:11-147 with fddc_assemb, isotropic
  * scheme, and Jacobi-PCG :343-402): x += grad(phi), P phi = T x, for ns

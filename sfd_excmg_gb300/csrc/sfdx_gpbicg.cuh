@@ -182,6 +182,15 @@ __global__ void k_gp_upd(int64_t nl, KState* st, int ns, cplx<T>* __restrict__ u
         S.err = nr / S.babs;
         if (err_rec && S.it <= S.itmax) err_rec[(size_t)ss * err_stride + S.it - 1] = S.err;
         S.iters = S.it;
+        // beta = alpha/omega * <r0, r_new> / <r0, r_old>, computed before the
+        // stopping tests so that a resumed system (mixed precision re-check)
+        // continues with consistent scalars
+        double2 a = S.alpha, o = S.omega, ro = S.rho;
+        double od = o.x * o.x + o.y * o.y, rd = ro.x * ro.x + ro.y * ro.y;
+        double2 q1 = make_double2((a.x * o.x + a.y * o.y) / od, (a.y * o.x - a.x * o.y) / od);
+        double2 q2 = make_double2((rn.x * ro.x + rn.y * ro.y) / rd, (rn.y * ro.x - rn.x * ro.y) / rd);
+        S.beta = make_double2(q1.x * q2.x - q1.y * q2.y, q1.x * q2.y + q1.y * q2.x);
+        S.it += 1;
         if (isnan(S.err)) {
             S.status = ST_NAN;
             S.active = 0;
@@ -192,18 +201,11 @@ __global__ void k_gp_upd(int64_t nl, KState* st, int ns, cplx<T>* __restrict__ u
             S.active = 0;
             continue;
         }
-        if (S.it >= S.itmax) {
+        if (S.iters >= S.itmax) {
             S.status = ST_MAXIT;
             S.active = 0;
             continue;
         }
-        // beta = alpha/omega * <r0, r_new> / <r0, r_old>
-        double2 a = S.alpha, o = S.omega, ro = S.rho;
-        double od = o.x * o.x + o.y * o.y, rd = ro.x * ro.x + ro.y * ro.y;
-        double2 q1 = make_double2((a.x * o.x + a.y * o.y) / od, (a.y * o.x - a.x * o.y) / od);
-        double2 q2 = make_double2((rn.x * ro.x + rn.y * ro.y) / rd, (rn.y * ro.x - rn.x * ro.y) / rd);
-        S.beta = make_double2(q1.x * q2.x - q1.y * q2.y, q1.x * q2.y + q1.y * q2.x);
-        S.it += 1;
     }
 }
 

@@ -395,6 +395,15 @@ __global__ void k_bicg_upd(Lev<T> L, KState* st, int ns, cplx<XT>* __restrict__ 
         S.err = nr / S.babs;
         S.it += 1;
         if (err_rec && S.it <= S.itmax) err_rec[(size_t)ss * err_stride + S.it - 1] = S.err;
+        // scalars of the next iteration first: a system stopped below may be
+        // resumed (mixed precision re-check) and must continue consistently
+        S.rhoold = S.rho;
+        S.rho = rh;
+        double2 a = S.rho, b = S.rhoold, al2 = S.alpha, om2 = S.omega;
+        double bd = b.x * b.x + b.y * b.y, od = om2.x * om2.x + om2.y * om2.y;
+        double2 q1 = make_double2((a.x * b.x + a.y * b.y) / bd, (a.y * b.x - a.x * b.y) / bd);
+        double2 q2 = make_double2((al2.x * om2.x + al2.y * om2.y) / od, (al2.y * om2.x - al2.x * om2.y) / od);
+        S.beta = make_double2(q1.x * q2.x - q1.y * q2.y, q1.x * q2.y + q1.y * q2.x);
         if (isnan(S.err)) {  // solvers.f90:683
             S.status = ST_NAN;
             S.active = 0;
@@ -413,13 +422,6 @@ __global__ void k_bicg_upd(Lev<T> L, KState* st, int ns, cplx<XT>* __restrict__ 
             S.active = 0;
             continue;
         }
-        S.rhoold = S.rho;
-        S.rho = rh;
-        double2 a = S.rho, b = S.rhoold, al2 = S.alpha, om2 = S.omega;
-        double bd = b.x * b.x + b.y * b.y, od = om2.x * om2.x + om2.y * om2.y;
-        double2 q1 = make_double2((a.x * b.x + a.y * b.y) / bd, (a.y * b.x - a.x * b.y) / bd);
-        double2 q2 = make_double2((al2.x * om2.x + al2.y * om2.y) / od, (al2.y * om2.x - al2.x * om2.y) / od);
-        S.beta = make_double2(q1.x * q2.x - q1.y * q2.y, q1.x * q2.y + q1.y * q2.x);
     }
 }
 

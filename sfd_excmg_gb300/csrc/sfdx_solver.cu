@@ -246,6 +246,8 @@ struct Plan {
     int dc_calls = 0, dc_last_iters = 0;
     DBuf errrec;
     int edc_stride = 0;
+    double* hist = nullptr;  // optional device residual history [ns][hist_stride]
+    int hist_stride = 0;
     std::vector<int> iters;        // [nf][2][nlev]
     std::vector<double> level_ms;  // wall time per level of the last solve
     std::vector<double> relres;    // [nf][2]
@@ -430,9 +432,9 @@ static int bicgstab(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, cons
     if (rel) {
         CK(cudaMemsetAsync(x, 0, vb, P.st));
         KL(k_residual<T, double, 0><<<G, B, smem, P.st>>>(LV.lev<double>(), dst, ns, rel->b64, rel->x64, r, rhat,
-                                                            redbuf(P), nullptr, 0));
+                                                            redbuf(P), P.hist, P.hist_stride));
     } else {
-        KL(k_residual<T, T, 0><<<G, B, smem, P.st>>>(L, dst, ns, b, x, r, rhat, redbuf(P), nullptr, 0));
+        KL(k_residual<T, T, 0><<<G, B, smem, P.st>>>(L, dst, ns, b, x, r, rhat, redbuf(P), P.hist, P.hist_stride));
     }
     CK(cudaGetLastError());
     const int check_every = 8;
@@ -448,7 +450,7 @@ static int bicgstab(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, cons
         KL(k_bicg_v<T><<<G, B, smem, P.st>>>(L, dst, ns, y, v, rhat, redbuf(P)));
         precond<T, RHS_SUPD>(P, L, z, s, r, v);
         KL(k_bicg_t<T><<<G, B, smem, P.st>>>(L, dst, ns, z, t, s, redbuf(P)));
-        KL(k_bicg_upd<T, T><<<G, B, smem, P.st>>>(L, dst, ns, x, y, z, s, t, r, rhat, redbuf(P), nullptr, 0));
+        KL(k_bicg_upd<T, T><<<G, B, smem, P.st>>>(L, dst, ns, x, y, z, s, t, r, rhat, redbuf(P), P.hist, P.hist_stride));
         if (it % check_every == 0 || it == itmax) {
             CK(cudaGetLastError());
             RC(sync_state(P));
@@ -515,7 +517,7 @@ static int gpbicg(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, const 
         KL(k_gp_tp<T><<<Ge, B, 0, P.st>>>(LV.nl, dst, ns, tp[cur], rp, tmp));
         KL(k_gp_at<T><<<G, B, smem, P.st>>>(L, dst, ns, tp[cur], at, t, y, redbuf(P)));
         KL(k_gp_upd<T, T><<<G, B, smem, P.st>>>(LV.nl, dst, ns, u, z, x, r, tmp, tp[cur ^ 1], rp, p, t, y, at, r0,
-                                                 redbuf(P), nullptr, 0));
+                                                 redbuf(P), P.hist, P.hist_stride));
         bool stop = false;
         if (it % 8 == 0 || it == itmax) {
             CK(cudaGetLastError());
@@ -1350,7 +1352,7 @@ extern "C" int sfdx_prolongate(int nx, int ny, int nz, const double* a1, const d
 
 extern "C" int sfdx_krylov_solve(const sfdx_opts* o, int nx, int ny, int nz, const double* a, const double* b,
                                  const double* c, const double* sigma, int ns, const double* freqs, const double* rhs,
-                                 double* x, double tol, int itmax, int* iters, double* relres) {
+                                 double* x, double tol, int itmax, int* iters, double* relres, double* history) {
     if (!sigma || !rhs || !x || itmax < 1) return SFDX_ERR_ARG;
     PlanGuard g;
     RC(component_plan(&g.p, o, nx, ny, nz, a, b, c, sigma, ns, freqs));
@@ -1361,8 +1363,18 @@ extern "C" int sfdx_krylov_solve(const sfdx_opts* o, int nx, int ny, int nz, con
     RC(P.b64.alloc(n * 16));
     CK(cudaMemcpyAsync(P.b64.p, rhs, n * 16, cudaMemcpyHostToDevice, P.st));
     CK(cudaMemcpyAsync(P.x64.p, x, n * 16, cudaMemcpyHostToDevice, P.st));
+    if (history) {
+        RC(P.errrec.alloc((size_t)ns * itmax * sizeof(double)));
+        CK(cudaMemsetAsync(P.errrec.p, 0, (size_t)ns * itmax * sizeof(double), P.st));
+        P.hist = P.errrec.as<double>();
+        P.hist_stride = itmax;
+    }
     std::vector<int> its, status;
     RC(solve_level(P, L, tol, itmax, false, its, status));
+    if (history) {
+        CK(cudaMemcpyAsync(history, P.hist, (size_t)ns * itmax * sizeof(double), cudaMemcpyDeviceToHost, P.st));
+        P.hist = nullptr;
+    }
     std::vector<double> rel(ns);
     RC(true_residual(P, L, P.b64.as<double2>(), P.x64.as<double2>(), rel.data(), nullptr));
     CK(cudaMemcpyAsync(x, P.x64.p, n * 16, cudaMemcpyDeviceToHost, P.st));

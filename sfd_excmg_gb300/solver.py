@@ -221,17 +221,21 @@ def prolongate(nx, ny, nz, a1, b1, c1, nair, u0, u1, quirks=capi.QUIRKS_REFERENC
     return u[:, 0] if u0.ndim == 1 else u
 
 
-def krylov_solve(nx, ny, nz, a, b, c, sigma, freqs, rhs, x0=None, tol=1e-8, itmax=5000, **opts):
+def krylov_solve(nx, ny, nz, a, b, c, sigma, freqs, rhs, x0=None, tol=1e-8, itmax=5000, history=False, **opts):
+    """One Krylov solve of ns interleaved systems.  Returns (x, iters, relres, rc[, history[ns, itmax]])."""
     freqs = _d(np.atleast_1d(freqs))
     ns = len(freqs)
     r = _z(rhs).reshape(-1, ns)
     x = np.zeros_like(r) if x0 is None else _z(x0).reshape(-1, ns).copy()
     it = np.zeros(ns, np.int32)
     rr = np.zeros(ns)
+    hist = np.zeros((ns, itmax)) if history else None
     o = _opts(**opts)
     rc = capi.lib().sfdx_krylov_solve(ctypes.byref(o), nx, ny, nz, capi.dptr(_d(a)), capi.dptr(_d(b)),
                                       capi.dptr(_d(c)), capi.dptr(_d(sigma)), ns, capi.dptr(freqs), capi.zptr(r),
-                                      capi.zptr(x), tol, itmax, capi.iptr(it), capi.dptr(rr))
+                                      capi.zptr(x), tol, itmax, capi.iptr(it), capi.dptr(rr),
+                                      capi.dptr(hist) if hist is not None else None)
     if rc not in (0, 4):
         capi.check(rc, "sfdx_krylov_solve")
-    return x.reshape(np.shape(rhs)), it, rr, rc
+    out = (x.reshape(np.shape(rhs)), it, rr, rc)
+    return out + (hist,) if history else out

@@ -45,7 +45,7 @@ def test_halfspace_known_answer():
 @pytest.mark.parametrize("excmg", [0, 1])
 def test_forward_fp64_matches_direct(excmg):
     m = syn.small_aniso(n=16, seed=1, freqs=(0.05, 20.0))
-    ex, it, rr = S.fwd_solve(m, eps=1e-10, excmg=excmg, level=3, div_cor=0)
+    ex, it, rr = S.fwd_solve(m, eps=1e-10, excmg=excmg, level=3, div_cor=0, solver=3)
     assert np.all(rr < 1e-9), rr
     _, zref = _direct_Z(m)
     z = S.impedance(m, ex)
@@ -55,8 +55,8 @@ def test_forward_fp64_matches_direct(excmg):
 
 def test_forward_mixed_matches_fp64():
     m = syn.small_aniso(n=16, seed=2, freqs=(0.01, 1.0, 100.0))
-    ex64, _, rr64 = S.fwd_solve(m, eps=1e-10, excmg=1, level=3, div_cor=0)
-    exm, _, rrm = S.fwd_solve(m, eps=1e-10, excmg=1, level=3, precision=S.MIXED)
+    ex64, _, rr64 = S.fwd_solve(m, eps=1e-10, excmg=1, level=3, div_cor=0, solver=3)
+    exm, _, rrm = S.fwd_solve(m, eps=1e-10, excmg=1, level=3, precision=S.MIXED, solver=3)
     assert np.all(rrm < 1e-10), rrm
     z64 = _zc(S.impedance(m, ex64))
     zm = _zc(S.impedance(m, exm))
