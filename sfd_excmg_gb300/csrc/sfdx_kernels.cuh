@@ -15,6 +15,7 @@ struct KState {
     double2 eta, tau;        // GPBiCG / spare
     double babs, err, tol;
     double wm;               // omega*mu of the system's frequency
+    double errv;             // last FP64-verified relative residual (mixed precision)
     int it, itmax, active, status, iters;
     int pad[3];
 };
@@ -462,6 +463,7 @@ __global__ void k_residual(Lev<XT> L, KState* st, int ns, const cplx<XT>* __rest
         if (MODE == 0) {
             S.babs = sqrt(v.y);
             S.err = nr / S.babs;
+            S.errv = S.err;
             S.rho = make_double2(1.0, 0.0);
             S.alpha = make_double2(1.0, 0.0);
             S.omega = make_double2(1.0, 0.0);
@@ -496,6 +498,7 @@ __global__ void k_residual(Lev<XT> L, KState* st, int ns, const cplx<XT>* __rest
         } else if (MODE == 3) {  // GPBiCG start (solvers.f90:203-221): no stopping test before iteration 1
             S.babs = sqrt(v.y);
             S.err = nr / S.babs;
+            S.errv = S.err;
             S.it = 1;
             S.iters = 0;
             S.beta = make_double2(0.0, 0.0);
@@ -530,15 +533,26 @@ __global__ void k_reactivate(KState* st, int ns) {
 
 // x64 += x32 ; x32 = 0  (active systems)
 template <class T>
-__global__ void k_flush(int64_t nl, const KState* st, int ns, double2* __restrict__ x64, cplx<T>* __restrict__ x32) {
+__global__ void k_flush(int64_t nl, const KState* st, int ns, double2* __restrict__ x64, cplx<T>* __restrict__ x32,
+                        double2* __restrict__ xb) {
     const int64_t W = nl * ns;
     for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < W; g += (int64_t)gridDim.x * blockDim.x) {
         const int s = (int)(g % ns);
         if (!st[s].active) continue;
         cplx<T> d = x32[g];
         double2 v = x64[g];
+        if (xb) xb[g] = v;  // kept until the FP64 residual accepts the update
         x64[g] = make_double2(v.x + (double)d.x, v.y + (double)d.y);
         x32[g] = zero<T>();
+    }
+}
+
+// x64 = xb for the systems whose last update was rejected (status ST_BREAK)
+__global__ void k_restore(int64_t nl, const KState* st, int ns, double2* __restrict__ x64, const double2* __restrict__ xb) {
+    const int64_t W = nl * ns;
+    for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < W; g += (int64_t)gridDim.x * blockDim.x) {
+        const int s = (int)(g % ns);
+        if (st[s].status == ST_BREAK && st[s].pad[0] == 1) x64[g] = xb[g];
     }
 }
 
@@ -576,11 +590,16 @@ __global__ void k_reliable(Lev<double> L, KState* st, int ns, const double2* __r
         if (!S.active) continue;
         S.err = sqrt(smem[B + ss].x) / S.babs;
         double2 h = smem[B + ns + ss];
-        if (isnan(S.err)) {
-            S.status = ST_NAN;
+        if (isnan(S.err) || (S.errv > 0 && S.err > 10.0 * S.errv)) {
+            // the complex64 correction made the FP64 residual worse (kappa * eps32 > 1
+            // for this system): take it back (k_restore) and stop the mixed iteration
+            S.status = ST_BREAK;
             S.active = 0;
+            S.pad[0] = 1;  // restore marker for k_restore
+            S.err = S.errv;
             continue;
         }
+        S.errv = S.err;
         if (S.err < S.tol) {
             S.status = ST_VCONV;
             S.active = 0;

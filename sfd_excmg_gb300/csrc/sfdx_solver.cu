@@ -364,7 +364,8 @@ static int div_correct(Plan& P, const Level& LV, double2* x) {
 struct Reliable {
     const double2* b64;
     double2* x64;
-    int every;  // iterations between FP64 residual replacements
+    int every;    // iterations between FP64 residual replacements
+    double2* xb;  // copy of x64 before the last update (restored on rejection)
 };
 
 static void init_states(Plan& P, const double* tols_host, double tol, int itmax, const int* mask_host,
@@ -391,13 +392,21 @@ static int reliable_update(Plan& P, const Level& LV, const Reliable& rel, cplx<T
     const int B = block_for(ns, 4);
     KState* dst = P.d_state.as<KState>();
     KL(k_reactivate<<<(ns + 127) / 128, 128, 0, P.st>>>(dst, ns));
-    KL(k_flush<T><<<grid_for(LV.nl * ns, B, 16), B, 0, P.st>>>(LV.nl, dst, ns, rel.x64, x32));
+    KL(k_flush<T><<<grid_for(LV.nl * ns, B, 16), B, 0, P.st>>>(LV.nl, dst, ns, rel.x64, x32, rel.xb));
     KL(k_reliable<T><<<grid_for(LV.nl * ns, B, 8), B, 4 * B * sizeof(double2), P.st>>>(
         LV.lev<double>(), dst, ns, rel.b64, rel.x64, r, rhat, solver, redbuf(P)));
     CK(cudaGetLastError());
     RC(sync_state(P));
     active = 0;
-    for (int q = 0; q < ns; q++) active += P.hst[q].active;
+    int rejected = 0;
+    for (int q = 0; q < ns; q++) {
+        active += P.hst[q].active;
+        rejected += P.hst[q].status == ST_BREAK && P.hst[q].pad[0] == 1;
+    }
+    if (rejected) {
+        KL(k_restore<<<grid_for(LV.nl * ns, B, 16), B, 0, P.st>>>(LV.nl, dst, ns, rel.x64, rel.xb));
+        CK(cudaGetLastError());
+    }
     return SFDX_OK;
 }
 
@@ -466,7 +475,7 @@ static int bicgstab(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, cons
             if (!act) break;
         }
     }
-    if (rel) KL(k_flush<T><<<grid_for(LV.nl * ns, B, 16), B, 0, P.st>>>(LV.nl, dst, ns, rel->x64, x));
+    if (rel) KL(k_flush<T><<<grid_for(LV.nl * ns, B, 16), B, 0, P.st>>>(LV.nl, dst, ns, rel->x64, x, nullptr));
     RC(sync_state(P));
     return SFDX_OK;
 }
@@ -538,7 +547,7 @@ static int gpbicg(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, const 
         KL(k_gp_pw<T><<<Ge, B, 0, P.st>>>(LV.nl, dst, ns, w, p, at, ap, rp, u));
         cur ^= 1;
     }
-    if (rel) KL(k_flush<T><<<grid_for(LV.nl * ns, B, 16), B, 0, P.st>>>(LV.nl, dst, ns, rel->x64, x));
+    if (rel) KL(k_flush<T><<<grid_for(LV.nl * ns, B, 16), B, 0, P.st>>>(LV.nl, dst, ns, rel->x64, x, nullptr));
     RC(sync_state(P));
     return SFDX_OK;
 }
@@ -595,9 +604,11 @@ static int solve_level_mixed(Plan& P, const Level& LV, double tol, int itmax, st
                              std::vector<int>& status) {
     const int ns = P.ns;
     const size_t n = (size_t)LV.nl * ns;
-    DBuf x32;
+    DBuf x32, xb;
     RC(x32.alloc(n * sizeof(float2)));
-    Reliable rel{P.b64.as<double2>(), P.x64.as<double2>(), P.o.reliable_every > 0 ? P.o.reliable_every : 40};
+    RC(xb.alloc(n * sizeof(double2)));
+    Reliable rel{P.b64.as<double2>(), P.x64.as<double2>(), P.o.reliable_every > 0 ? P.o.reliable_every : 40,
+                 xb.as<double2>()};
     if (P.o.solver == SFDX_SOLVER_GPBICG)
         RC(gpbicg<float>(P, LV, nullptr, x32.as<float2>(), nullptr, tol, itmax, nullptr, &rel));
     else if (P.o.solver == SFDX_SOLVER_BICGSTAB)
@@ -606,10 +617,39 @@ static int solve_level_mixed(Plan& P, const Level& LV, double tol, int itmax, st
         return SFDX_ERR_UNSUPPORTED;
     its.resize(ns);
     status.resize(ns);
+    std::vector<int> left(ns, 0);
+    int nleft = 0, used_max = 0;
     for (int q = 0; q < ns; q++) {
         its[q] = P.hst[q].iters;
         int st = P.hst[q].status;
         status[q] = (st == ST_VCONV) ? ST_CONV : (st == ST_CONV || st == ST_RUN ? ST_MAXIT : st);
+        // complex64 steps stalled (correction rejected) before the iteration
+        // limit: finish this system in FP64 from its current FP64 iterate
+        if (st == ST_BREAK && its[q] < itmax) {
+            left[q] = 1;
+            nleft++;
+            used_max = std::max(used_max, its[q]);
+        }
+    }
+    if (nleft) {
+        std::vector<int> its64, st64;
+        const int save = P.o.div_cor;
+        P.o.div_cor = 0;  // the FP64 finish is a continuation, not a reference restart
+        int rc;
+        if (P.o.solver == SFDX_SOLVER_GPBICG)
+            rc = gpbicg<double>(P, LV, P.b64.as<double2>(), P.x64.as<double2>(), nullptr, tol, itmax - used_max,
+                                left.data());
+        else
+            rc = bicgstab<double>(P, LV, P.b64.as<double2>(), P.x64.as<double2>(), nullptr, tol, itmax - used_max,
+                                  left.data());
+        P.o.div_cor = save;
+        RC(rc);
+        for (int q = 0; q < ns; q++) {
+            if (!left[q]) continue;
+            its[q] += P.hst[q].iters;
+            status[q] = P.hst[q].status;
+        }
+        if (P.o.verbose || getenv("SFDX_VERBOSE")) fprintf(stderr, "sfdx:   %d system(s) finished in FP64\n", nleft);
     }
     return SFDX_OK;
 }
