@@ -336,6 +336,21 @@ def run_ours(args, rank, world, local):
     plan.close()
 
 
+def run_profile(args):
+    """Kernel families on the finest level of the workload, CUDA-event timed (few launches)."""
+    import sfd_excmg_gb300 as S
+    from sfd_excmg_gb300 import synthetic as syn
+    m = syn.config2(seed=0)
+    hbm, src = peaks()
+    with S.Plan(m, **solve_opts(args.precision, args.solver)) as p:
+        p.load()
+        out = {}
+        for kid, name in ((2, "mc_ssor_c64"), (0, "operator_c64"), (1, "operator_c128")):
+            ms, b = p.kernel_time(kid, reps=2)
+            out[name] = {"ms": ms, "alg_bytes": b, "gbs": b / (ms / 1e3) / 1e9, "frac_of_" + src: b / (ms / 1e3) / 1e9 / hbm}
+    print(json.dumps(out), flush=True)
+
+
 def _fwd_noconv(S, m, opts):
     with S.Plan(m, **opts) as p:
         ex = p.solve(allow_noconv=True)
@@ -349,13 +364,18 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
-    ap.add_argument("--solver", default="bicgstab", choices=list(SOLVER))
+    ap.add_argument("--solver", default="gpbicg", choices=list(SOLVER))
     ap.add_argument("--no-compare-fp64", dest="compare_fp64", action="store_false")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     ap.add_argument("--e2e-strict", dest="e2e_allow_noconv", action="store_false")
+    ap.add_argument("--profile", action="store_true",
+                    help="only load the workload's conductivity and time each kernel family a few times "
+                         "(a short launch sequence for ncu captures)")
     args = ap.parse_args()
     rank, world, local = dist()
-    if args.impl == "reference":
+    if args.profile:
+        run_profile(args)
+    elif args.impl == "reference":
         run_reference(args, rank, world)
     else:
         run_ours(args, rank, world, local)

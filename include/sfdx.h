@@ -119,6 +119,8 @@ int sfdx_plan_create(sfdx_plan** plan, const sfdx_opts* o, int nx, int ny, int n
                      const double* b, const double* c, int nf, const double* freq);
 int sfdx_plan_solve(sfdx_plan* plan, const double* sigma, int sigma_on_device, double* ex, int ex_on_device,
                     int* iters, double* relres);
+/* Load (and coarsen) the conductivity without solving. */
+int sfdx_plan_load(sfdx_plan* plan, const double* sigma, int sigma_on_device);
 /* Impedances from the plan's last solution (device resident), see sfdx_impedance. */
 int sfdx_plan_impedance(sfdx_plan* plan, int nrec, const double* recv, int out_type, double* out, double* tipper);
 /* Device pointer of the plan's last solution, layout [nf][2][nl] complex (valid until the next solve). */

@@ -82,6 +82,7 @@ _PROTO = {
     "sfdx_plan_impedance": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, c_double_p, ctypes.c_int, c_double_p,
                                            c_double_p]),
     "sfdx_plan_fields": (ctypes.c_void_p, [ctypes.c_void_p]),
+    "sfdx_plan_load": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]),
     "sfdx_plan_device_bytes": (ctypes.c_longlong, [ctypes.c_void_p]),
     "sfdx_plan_destroy": (None, [ctypes.c_void_p]),
     "sfdx_plan_level_times": (ctypes.c_int, [ctypes.c_void_p, c_double_p, ctypes.c_int]),

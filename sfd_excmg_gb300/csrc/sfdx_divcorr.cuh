@@ -70,7 +70,7 @@ __device__ __forceinline__ int64_t node_id(const NodeGeo& G, int i, int j, int k
 }
 
 // t = T x (boundary nodes 0); also r = t, p = r/m and the PCG start-up sums.
-__global__ void k_dc_div(NodeGeo G, const KState* st, int ns, const double2* __restrict__ x, double2* __restrict__ t,
+static __global__ void k_dc_div(NodeGeo G, const KState* st, int ns, const double2* __restrict__ x, double2* __restrict__ t,
                          double2* __restrict__ r, double2* __restrict__ p, double2* __restrict__ u, RedBuf rb,
                          KState* pst) {
     extern __shared__ double2 smem[];
@@ -129,7 +129,7 @@ __global__ void k_dc_div(NodeGeo G, const KState* st, int ns, const double2* __r
 }
 
 // v = P p ; alpha = rho / <p, v>
-__global__ void k_dc_Ap(NodeGeo G, KState* pst, int ns, const double2* __restrict__ p, double2* __restrict__ v,
+static __global__ void k_dc_Ap(NodeGeo G, KState* pst, int ns, const double2* __restrict__ p, double2* __restrict__ v,
                         RedBuf rb) {
     extern __shared__ double2 smem[];
     const int s = threadIdx.x % ns;
@@ -174,7 +174,7 @@ __global__ void k_dc_Ap(NodeGeo G, KState* pst, int ns, const double2* __restric
 }
 
 // u += alpha p ; r -= alpha v ; rho_new = <r/m, r> ; err = |r|/|t| ; beta
-__global__ void k_dc_upd(NodeGeo G, KState* pst, int ns, const double2* __restrict__ p, const double2* __restrict__ v,
+static __global__ void k_dc_upd(NodeGeo G, KState* pst, int ns, const double2* __restrict__ p, const double2* __restrict__ v,
                          double2* __restrict__ u, double2* __restrict__ r, RedBuf rb, double tol, int maxit) {
     extern __shared__ double2 smem[];
     const int s = threadIdx.x % ns;
@@ -230,7 +230,7 @@ __global__ void k_dc_upd(NodeGeo G, KState* pst, int ns, const double2* __restri
 }
 
 // p = r/m + beta p
-__global__ void k_dc_p(NodeGeo G, const KState* pst, int ns, const double2* __restrict__ r, double2* __restrict__ p) {
+static __global__ void k_dc_p(NodeGeo G, const KState* pst, int ns, const double2* __restrict__ r, double2* __restrict__ p) {
     const int64_t W = G.np * ns;
     for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < W; g += (int64_t)gridDim.x * blockDim.x) {
         const int s = (int)(g % ns);
@@ -250,7 +250,7 @@ __global__ void k_dc_p(NodeGeo G, const KState* pst, int ns, const double2* __re
 }
 
 // x_e += (phi(end) - phi(start)) / len_e  unless both ends are boundary nodes
-__global__ void k_dc_grad(NodeGeo G, const KState* st, int ns, const double2* __restrict__ phi, double2* __restrict__ x) {
+static __global__ void k_dc_grad(NodeGeo G, const KState* st, int ns, const double2* __restrict__ phi, double2* __restrict__ x) {
     const int64_t nl = G.xnl + G.ynl + (int64_t)(G.nx + 1) * (G.ny + 1) * G.nz;
     const int64_t W = nl * ns;
     for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < W; g += (int64_t)gridDim.x * blockDim.x) {

@@ -17,7 +17,7 @@ namespace sfdx {
 // quirk: fine index ((m-1)asf+r)*..+((j-1)asf+s)*.. as in the reference (one
 // plane and one row too far; row overflow wraps into the next plane, a read
 // past the last plane is clamped back into it).
-__global__ void k_coarsen(int nx0, int ny0, int nz0, const double* __restrict__ a, const double* __restrict__ b,
+static __global__ void k_coarsen(int nx0, int ny0, int nz0, const double* __restrict__ a, const double* __restrict__ b,
                           const double* __restrict__ c, const double* __restrict__ a1, const double* __restrict__ b1,
                           const double* __restrict__ c1, int asf, int quirk, const double* __restrict__ sig0,
                           double* __restrict__ sig1) {
@@ -156,7 +156,7 @@ __global__ void k_extrapolate(int64_t n, const cplx<T>* __restrict__ u1, cplx<T>
 
 // Flags any non-zero off-diagonal conductivity (selects the anisotropic
 // cross terms of the operator).
-__global__ void k_any_offdiag(int64_t ncell, const double* __restrict__ sig, int* flag) {
+static __global__ void k_any_offdiag(int64_t ncell, const double* __restrict__ sig, int* flag) {
     for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < 3 * ncell; q += (int64_t)gridDim.x * blockDim.x)
         if (sig[3 * ncell + q] != 0.0) {
             *flag = 1;

@@ -117,7 +117,7 @@ __global__ void k_apply(Lev<T> L, const double* wms, int ns, const cplx<T>* __re
 
 // Right-hand side of dcfast: boundary rows carry the Dirichlet value, interior
 // rows -sum(K_ij p_j) over boundary columns.  FP64 only; written to b64.
-__global__ void k_build_rhs(Lev<double> L, const double* wms, const int* pols, const double2* edcs, int edc_stride,
+static __global__ void k_build_rhs(Lev<double> L, const double* wms, const int* pols, const double2* edcs, int edc_stride,
                             int ns, double2* __restrict__ b) {
     const int64_t W = L.nl * ns;
     for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < W; g += (int64_t)gridDim.x * blockDim.x) {
@@ -523,7 +523,7 @@ enum { ST_VCONV = 5 };
 
 // systems whose complex64 recurrence converged become active again until the
 // FP64 residual confirms it
-__global__ void k_reactivate(KState* st, int ns) {
+static __global__ void k_reactivate(KState* st, int ns) {
     int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s < ns && st[s].status == ST_CONV) {
         st[s].status = ST_RUN;
@@ -548,7 +548,7 @@ __global__ void k_flush(int64_t nl, const KState* st, int ns, double2* __restric
 }
 
 // x64 = xb for the systems whose last update was rejected (status ST_BREAK)
-__global__ void k_restore(int64_t nl, const KState* st, int ns, double2* __restrict__ x64, const double2* __restrict__ xb) {
+static __global__ void k_restore(int64_t nl, const KState* st, int ns, double2* __restrict__ x64, const double2* __restrict__ xb) {
     const int64_t W = nl * ns;
     for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < W; g += (int64_t)gridDim.x * blockDim.x) {
         const int s = (int)(g % ns);
@@ -665,7 +665,7 @@ __global__ void k_refine_add(int64_t nl, int ns, const double* scale, cplx<doubl
 }
 
 // r32 = r64 / scale_s  (normalised refinement right-hand side)
-__global__ void k_scale_to_f32(int64_t nl, int ns, const double* scale, const double2* __restrict__ src,
+static __global__ void k_scale_to_f32(int64_t nl, int ns, const double* scale, const double2* __restrict__ src,
                                float2* __restrict__ dst) {
     const int64_t W = nl * ns;
     for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < W; g += (int64_t)gridDim.x * blockDim.x) {
@@ -674,6 +674,13 @@ __global__ void k_scale_to_f32(int64_t nl, int ns, const double* scale, const do
         double2 v = src[g];
         dst[g] = sc > 0 ? make_float2((float)(v.x / sc), (float)(v.y / sc)) : make_float2(0.f, 0.f);
     }
+}
+
+// deterministic smooth input for kernel timing
+template <class T>
+__global__ void k_pattern(int64_t n, cplx<T>* __restrict__ v) {
+    for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < n; g += (int64_t)gridDim.x * blockDim.x)
+        v[g] = mk<T>((T)(1.0 + 1e-3 * (double)(g % 977)), (T)(0.5 - 1e-3 * (double)(g % 613)));
 }
 
 // interleave / de-interleave between [s][nl] (per-system) and [nl][ns] (batched)

@@ -1024,6 +1024,13 @@ extern "C" int sfdx_plan_solve(sfdx_plan* plan, const double* sigma, int sigma_o
     return rc;
 }
 
+extern "C" int sfdx_plan_load(sfdx_plan* plan, const double* sigma, int sigma_on_device) {
+    if (!plan || !sigma) return SFDX_ERR_ARG;
+    RC(set_conductivity(plan->P, sigma, sigma_on_device != 0));
+    CK(cudaStreamSynchronize(plan->P.st));
+    return SFDX_OK;
+}
+
 extern "C" const double* sfdx_plan_fields(sfdx_plan* plan) {
     if (!plan || !plan->P.have_solution) return nullptr;
     return plan->P.ex_out.as<double>();
@@ -1063,7 +1070,7 @@ extern "C" int sfdx_plan_set_stream(sfdx_plan* plan, void* stream) {
 extern "C" int sfdx_plan_kernel_time(sfdx_plan* plan, int kernel, int reps, double* ms, double* bytes) {
     if (!plan || !ms || reps < 1) return SFDX_ERR_ARG;
     Plan& P = plan->P;
-    if (!P.have_solution) return SFDX_ERR_ARG;
+    if (!P.lev[P.nlev - 1].sig64.p) return SFDX_ERR_ARG;  // conductivity not loaded yet
     const Level& F = P.lev[P.nlev - 1];
     const int ns = P.ns;
     const size_t n = (size_t)F.nl * ns;
@@ -1078,8 +1085,8 @@ extern "C" int sfdx_plan_kernel_time(sfdx_plan* plan, int kernel, int reps, doub
     }
     CK(cudaMemcpyAsync(P.d_state.p, init.data(), sizeof(KState) * ns, cudaMemcpyHostToDevice, P.st));
     // deterministic non-zero input
-    if (f32) KL(k_convert<double, float><<<grid_for(n, 256), 256, 0, P.st>>>(n, P.ex_out.as<double2>(), P.kv[0].as<float2>()));
-    else CK(cudaMemcpyAsync(P.kv[0].p, P.ex_out.p, n * 16, cudaMemcpyDeviceToDevice, P.st));
+    if (f32) KL(k_pattern<float><<<grid_for(n, 256), 256, 0, P.st>>>(n, P.kv[0].as<float2>()));
+    else KL(k_pattern<double><<<grid_for(n, 256), 256, 0, P.st>>>(n, P.kv[0].as<double2>()));
     const int B = block_for(ns);
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0));

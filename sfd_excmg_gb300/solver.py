@@ -90,6 +90,15 @@ class Plan:
         self.relres = rr.reshape(self.relres.shape)
         return ex
 
+    def load(self, sigma=None, sigma_device_ptr: int | None = None) -> None:
+        """Upload (and coarsen) the conductivity without solving."""
+        if sigma_device_ptr is not None:
+            sp, son = ctypes.c_void_p(sigma_device_ptr), 1
+        else:
+            self._sg = _d(self.model.sigma if sigma is None else sigma)
+            sp, son = ctypes.c_void_p(self._sg.ctypes.data), 0
+        capi.check(capi.lib().sfdx_plan_load(self._h, sp, son), "sfdx_plan_load")
+
     def impedance(self, recv=None, out_type: int = 1, tipper: bool = False):
         m = self.model
         rv = _d(np.asarray(m.recv if recv is None else recv).T)  # [3][nrec]
