@@ -78,6 +78,16 @@ def build(verbose: bool = False) -> str:
         if r.returncode != 0:
             raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
         os.replace(tmp, LIB)
+    # drop-in host executable `sfd3d <model> [level eps]`
+    host_src = os.path.join(HERE, "host", "sfd3d.cpp")
+    exe = os.path.join(LIBDIR, "sfd3d")
+    if not os.path.exists(exe) or os.path.getmtime(exe) < max(os.path.getmtime(LIB), os.path.getmtime(host_src)):
+        cmd = [os.environ.get("CXX", "g++")] + CXX_FLAGS + ["-I", INCLUDE, host_src, "-o", exe + ".tmp", "-L", LIBDIR,
+                                                            "-lsfdx", "-Wl,-rpath,$ORIGIN"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"host build failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+        os.replace(exe + ".tmp", exe)
     if verbose:
         print(f"built {LIB} ({len(jobs)} translation units recompiled)")
     return LIB

@@ -1,0 +1,74 @@
+// sfd3d.cpp -- drop-in host for `./sfd3d <model> [level eps]`
+// (sfd_excmg/src/sfd_excmg.f90:20-58): read <model>.fwd/.dat(/.topo), run the
+// forward solve on the GPU through the C ABI, write <model>.res.
+//
+// Options beyond the reference's argv come from the environment:
+//   SFDX_EXCMG=0|1 (fwd_acc, default 0 as in global_para.f90:19),
+//   SFDX_PRECISION=fp64|mixed, SFDX_VERBOSE=1.
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "sfdx.h"
+
+int main(int argc, char** argv) {
+    if (argc < 2) {
+        fprintf(stderr, "usage: %s <model> [level eps]\n", argv[0]);
+        return 2;
+    }
+    const char* name = argv[1];
+    int nx, ny, nz, nair, nf, nrec;
+    int rc = sfdx_read_sizes(name, &nx, &ny, &nz, &nair, &nf, &nrec);
+    if (rc) {
+        fprintf(stderr, "sfd3d: %s\n", sfdx_strerror(rc));
+        return 1;
+    }
+    sfdx_opts o;
+    sfdx_default_opts(&o);
+    const size_t ncell = (size_t)nx * ny * nz;
+    std::vector<double> a(nx), b(ny), c(nz), sigma(6 * ncell), freq(nf), recv(3 * (size_t)nrec);
+    int level, solver, out_type, abu[6];
+    double eps;
+    rc = sfdx_read_model(name, &o, &level, &eps, &solver, &out_type, a.data(), b.data(), c.data(), sigma.data(),
+                         freq.data(), recv.data(), abu);
+    if (rc) {
+        fprintf(stderr, "sfd3d: %s\n", sfdx_strerror(rc));
+        return 1;
+    }
+    if (argc > 3) {  // argv override of level and eps (sfd_excmg.f90:45-50)
+        level = atoi(argv[2]);
+        eps = atof(argv[3]);
+    }
+    o.level = level;
+    o.eps = eps;
+    o.solver = solver;
+    if (const char* e = getenv("SFDX_EXCMG")) o.excmg = atoi(e);
+    if (const char* p = getenv("SFDX_PRECISION")) o.precision = strcmp(p, "mixed") == 0 ? SFDX_MIXED : SFDX_FP64;
+    if (getenv("SFDX_VERBOSE")) o.verbose = 1;
+    const long long nl = (long long)nx * (ny + 1) * (nz + 1) + (long long)(nx + 1) * ny * (nz + 1) +
+                         (long long)(nx + 1) * (ny + 1) * nz;
+    std::vector<double> ex((size_t)nf * 2 * nl * 2);
+    std::vector<double> relres((size_t)nf * 2);
+    rc = sfdx_fwd_solve(&o, nx, ny, nz, nair, a.data(), b.data(), c.data(), sigma.data(), nf, freq.data(), ex.data(),
+                        nullptr, relres.data());
+    if (rc && rc != SFDX_ERR_NOCONV) {
+        fprintf(stderr, "sfd3d: %s\n", sfdx_strerror(rc));
+        return 1;
+    }
+    if (rc == SFDX_ERR_NOCONV) fprintf(stderr, "sfd3d: warning: %s\n", sfdx_strerror(rc));
+    std::vector<double> res((size_t)nf * nrec * 4);
+    rc = sfdx_impedance(nx, ny, nz, nair, a.data(), b.data(), c.data(), nf, freq.data(), ex.data(), nrec, recv.data(),
+                        out_type, o.quirks, res.data(), nullptr);
+    if (rc) {
+        fprintf(stderr, "sfd3d: %s\n", sfdx_strerror(rc));
+        return 1;
+    }
+    rc = sfdx_write_res(name, nf, freq.data(), nrec, recv.data(), res.data());
+    if (rc) {
+        fprintf(stderr, "sfd3d: %s\n", sfdx_strerror(rc));
+        return 1;
+    }
+    return 0;
+}
