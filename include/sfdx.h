@@ -203,6 +203,31 @@ int sfdx_div_correct(int nx, int ny, int nz, const double* a, const double* b, c
                      const double* sigma, int ns, double* x, double tol, int* pcg_iters);
 
 /* ------------------------------------------------------------------------
+ * Residual without any memory allocation.  No counterpart in the reference:
+ * it serves callers that cannot call cudaMalloc -- an application whose GPU
+ * memory is owned by its own pool or another runtime, or a loop that must not
+ * allocate -- and that already hold the model and the vectors on the device.
+ *
+ * r = rhs - K x for ns interleaved systems ([nl][ns] complex, DEVICE
+ * pointers d_sigma, d_rhs, d_x, d_r owned by the caller; a, b, c, freqs and
+ * the output relres[ns] = ||r|| / ||rhs|| are host arrays).  Work is issued
+ * on `stream` (a cudaStream_t, null = default stream) and the call returns
+ * after it completes.  Nothing is allocated: the tables, per-system state and
+ * reduction scratch live in one fixed device array of about 4.4 MB that every
+ * GPU loading the library holds until the process exits.  Limits: nx, ny, nz
+ * <= SFDX_NOALLOC_MAX_N and ns <= SFDX_NOALLOC_MAX_NS, otherwise
+ * SFDX_ERR_NOMEM.  The first call on a device looks up the array's device
+ * address (cudaGetSymbolAddress) and must come before any stream capture on
+ * that device.  All calls share the array and leave their data in it: calls
+ * that overlap on the GPU race and must be serialised by the caller.
+ * ------------------------------------------------------------------------ */
+#define SFDX_NOALLOC_MAX_N 1024
+#define SFDX_NOALLOC_MAX_NS 64
+int sfdx_residual_noalloc(int nx, int ny, int nz, const double* a, const double* b, const double* c,
+                          const double* d_sigma, int ns, const double* freqs, const double* d_rhs, const double* d_x,
+                          double* d_r, double* relres, void* stream);
+
+/* ------------------------------------------------------------------------
  * Reference file formats (file_opt.f90).  sfdx_read_model allocates nothing:
  * call with null arrays to get the sizes, then again with buffers.
  * ------------------------------------------------------------------------ */

@@ -112,6 +112,9 @@ _PROTO = {
                                          c_double_p, ctypes.c_double, ctypes.c_int, c_int_p, c_double_p, c_double_p]),
     "sfdx_div_correct": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, c_double_p, c_double_p,
                                         c_double_p, c_double_p, ctypes.c_int, c_double_p, ctypes.c_double, c_int_p]),
+    "sfdx_residual_noalloc": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, c_double_p, c_double_p,
+                                             c_double_p, ctypes.c_void_p, ctypes.c_int, c_double_p, ctypes.c_void_p,
+                                             ctypes.c_void_p, ctypes.c_void_p, c_double_p, ctypes.c_void_p]),
     "sfdx_read_sizes": (ctypes.c_int, [ctypes.c_char_p, c_int_p, c_int_p, c_int_p, c_int_p, c_int_p, c_int_p]),
     "sfdx_read_model": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_void_p, c_int_p, c_double_p, c_int_p, c_int_p,
                                        c_double_p, c_double_p, c_double_p, c_double_p, c_double_p, c_double_p,
