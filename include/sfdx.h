@@ -53,6 +53,10 @@ extern "C" {
 #define SFDX_SOLVER_BICG 4
 #define SFDX_SOLVER_COCR 6
 
+/* most systems (frequency x polarisation, or right-hand sides) in one batch;
+ * the reference solves one system at a time, so this has no counterpart there */
+#define SFDX_MAX_SYSTEMS 128
+
 /* precision */
 #define SFDX_FP64 0   /* complex128 everywhere                                    */
 #define SFDX_MIXED 1  /* complex64 operator/smoother/Krylov inside FP64 refinement */

@@ -103,18 +103,6 @@ __device__ __forceinline__ cplx<T> apply_row(const Lev<T>& L, int o, int i, int 
     return off + cmul<T>(mk<T>(rc.dre, -wm * rc.sbar), xe);
 }
 
-template <class T>
-__global__ void k_apply(Lev<T> L, const double* wms, int ns, const cplx<T>* __restrict__ x, cplx<T>* __restrict__ y) {
-    const int64_t W = L.nl * ns;
-    for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < W; g += (int64_t)gridDim.x * blockDim.x) {
-        int s = (int)(g % ns);
-        int64_t e = g / ns;
-        int o, i, j, k;
-        edecode(L, e, o, i, j, k);
-        y[g] = apply_row<T>(L, o, i, j, k, (T)wms[s], x, ns, s, x[g]);
-    }
-}
-
 // Right-hand side of dcfast: boundary rows carry the Dirichlet value, interior
 // rows -sum(K_ij p_j) over boundary columns.  FP64 only; written to b64.
 static __global__ void k_build_rhs(Lev<double> L, const double* wms, const int* pols, const double2* edcs, int edc_stride,
@@ -144,105 +132,8 @@ static __global__ void k_build_rhs(Lev<double> L, const double* wms, const int* 
     }
 }
 
-// ------------------------------------------------------------------ colours
-// Multi-colour ordering for the 13-point stencil: an edge only couples to
-// same-orientation edges across one of its two transverse directions, so
-// two colours per orientation suffice:
-//   Ex: (j+k)&1, Ey: (i+k)&1, Ez: (i+j)&1.
-// Colour order c = 2*orientation + parity.
-template <class T, int O>
-__device__ __forceinline__ bool colour_decode(const Lev<T>& L, int P, int64_t t, int& i, int& j, int& k) {
-    if (O == OX) {
-        int nj2 = (L.ny + 2) / 2;
-        i = (int)(t % L.nx);
-        int64_t r = t / L.nx;
-        int jj = (int)(r % nj2);
-        k = (int)(r / nj2);
-        j = 2 * jj + ((P + k) & 1);
-        return j <= L.ny && k <= L.nz;
-    } else if (O == OY) {
-        int ni2 = (L.nx + 2) / 2;
-        int ii = (int)(t % ni2);
-        int64_t r = t / ni2;
-        j = (int)(r % L.ny);
-        k = (int)(r / L.ny);
-        i = 2 * ii + ((P + k) & 1);
-        return i <= L.nx && k <= L.nz;
-    } else {
-        int ni2 = (L.nx + 2) / 2;
-        int ii = (int)(t % ni2);
-        int64_t r = t / ni2;
-        j = (int)(r % (L.ny + 1));
-        k = (int)(r / (L.ny + 1));
-        i = 2 * ii + ((P + j) & 1);
-        return i <= L.nx && k < L.nz;
-    }
-}
-template <class T> __host__ __device__ inline int64_t colour_count(const Lev<T>& L, int O) {
-    if (O == OX) return (int64_t)L.nx * ((L.ny + 2) / 2) * (L.nz + 1);
-    if (O == OY) return (int64_t)((L.nx + 2) / 2) * L.ny * (L.nz + 1);
-    return (int64_t)((L.nx + 2) / 2) * (L.ny + 1) * L.nz;
-}
-
 // Right-hand-side modes of the forward sweep.
 enum { RHS_VEC = 0, RHS_PUPD = 1, RHS_SUPD = 2 };
-
-// Forward sweep of colour (O,P):  w_e = (rhs_e - sum_{earlier colours} K_en w_n) / D_e.
-// RHS_PUPD: rhs = p = r + beta (p - omega v)   (stores p)
-// RHS_SUPD: rhs = s = r - alpha v             (stores s into q)
-// RHS_VEC : rhs = q
-template <class T, int O, int P, int MODE>
-__global__ void k_sweep_fwd(Lev<T> L, const KState* st, int ns, cplx<T>* __restrict__ w, cplx<T>* __restrict__ q,
-                            const cplx<T>* __restrict__ r, const cplx<T>* __restrict__ v) {
-    const int64_t W = colour_count(L, O) * ns;
-    for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < W; g += (int64_t)gridDim.x * blockDim.x) {
-        int s = (int)(g % ns);
-        if (!st[s].active) continue;
-        int i, j, k;
-        if (!colour_decode<T, O>(L, P, g / ns, i, j, k)) continue;
-        int64_t ge = eidx(L, O, i, j, k) * ns + s;
-        cplx<T> rhs;
-        if (MODE == RHS_PUPD) {
-            cplx<T> be = mk<T>((T)st[s].beta.x, (T)st[s].beta.y), om = mk<T>((T)st[s].omega.x, (T)st[s].omega.y);
-            rhs = r[ge] + cmul<T>(be, q[ge] - cmul<T>(om, v[ge]));
-            q[ge] = rhs;
-        } else if (MODE == RHS_SUPD) {
-            cplx<T> al = mk<T>((T)st[s].alpha.x, (T)st[s].alpha.y);
-            rhs = r[ge] - cmul<T>(al, v[ge]);
-            q[ge] = rhs;
-        } else {
-            rhs = q[ge];
-        }
-        if (is_bnd(L, O, i, j, k)) {
-            w[ge] = rhs;
-            continue;
-        }
-        T wm = (T)st[s].wm;
-        FetchInterior<T> f{&L, w, ns, s};
-        cplx<T> off = row_offdiag<T, O, P == 1, (O >= OY), (O == OZ)>(L, i, j, k, wm, f);
-        RowCoef<T> rc = row_diag<T, O>(L, i, j, k);
-        w[ge] = cdiv<T>(rhs - off, mk<T>(rc.dre, -wm * rc.sbar));
-    }
-}
-
-// Backward sweep of colour (O,P), in place:  x_e = w_e - D_e^{-1} sum_{later colours} K_en x_n.
-template <class T, int O, int P>
-__global__ void k_sweep_bwd(Lev<T> L, const KState* st, int ns, cplx<T>* __restrict__ x) {
-    const int64_t W = colour_count(L, O) * ns;
-    for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < W; g += (int64_t)gridDim.x * blockDim.x) {
-        int s = (int)(g % ns);
-        if (!st[s].active) continue;
-        int i, j, k;
-        if (!colour_decode<T, O>(L, P, g / ns, i, j, k)) continue;
-        if (is_bnd(L, O, i, j, k)) continue;
-        int64_t ge = eidx(L, O, i, j, k) * ns + s;
-        T wm = (T)st[s].wm;
-        FetchInterior<T> f{&L, x, ns, s};
-        cplx<T> off = row_offdiag<T, O, P == 0, (O == OX), (O <= OY)>(L, i, j, k, wm, f);
-        RowCoef<T> rc = row_diag<T, O>(L, i, j, k);
-        x[ge] = x[ge] - cdiv<T>(off, mk<T>(rc.dre, -wm * rc.sbar));
-    }
-}
 
 // Jacobi preconditioner (pre_type 'J'): y = D^{-1} rhs with the same fused
 // right-hand-side modes.
@@ -277,152 +168,6 @@ __global__ void k_jacobi(Lev<T> L, const KState* st, int ns, cplx<T>* __restrict
         else if (o == OY) rc = row_diag<T, OY>(L, i, j, k);
         else rc = row_diag<T, OZ>(L, i, j, k);
         w[g] = cdiv<T>(rhs, mk<T>(rc.dre, -wm * rc.sbar));
-    }
-}
-
-// ------------------------------------------------------------------ BiCGStab
-// (solvers.f90:522-719), right preconditioned, Hermitian inner products.
-//
-// k_bicg_v : v = A y ; alpha = rho / <rhat, v>
-template <class T>
-__global__ void k_bicg_v(Lev<T> L, KState* st, int ns, const cplx<T>* __restrict__ y, cplx<T>* __restrict__ v,
-                         const cplx<T>* __restrict__ rhat, RedBuf rb) {
-    extern __shared__ double2 smem[];
-    typedef typename AccOf<T>::type A;
-    const int s = threadIdx.x % ns;
-    const bool act = st[s].active;
-    const T wm = (T)st[s].wm;
-    A ar = 0, ai = 0;
-    const int64_t W = L.nl * ns;
-    if (act)
-        for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < W; g += (int64_t)gridDim.x * blockDim.x) {
-            int o, i, j, k;
-            edecode(L, g / ns, o, i, j, k);
-            cplx<T> val = apply_row<T>(L, o, i, j, k, wm, y, ns, s, y[g]);
-            v[g] = val;
-            cplx<T> d = cdot<T>(rhat[g], val);
-            ar += d.x;
-            ai += d.y;
-        }
-    double2 acc[1] = {make_double2(ar, ai)};
-    if (!block_reduce_and_last<1, A>(acc, ns, rb, smem)) return;
-    const int B = blockDim.x;
-    for (int ss = threadIdx.x; ss < ns; ss += B) {
-        if (!st[ss].active) continue;
-        double2 d = smem[B + ss];
-        double2 rho = st[ss].rho;
-        double den = d.x * d.x + d.y * d.y;
-        st[ss].alpha = make_double2((rho.x * d.x + rho.y * d.y) / den, (rho.y * d.x - rho.x * d.y) / den);
-        if (!isfinite(st[ss].alpha.x) || !isfinite(st[ss].alpha.y)) {  // breakdown: keep the last iterate
-            st[ss].active = 0;
-            st[ss].status = ST_BREAK;
-        }
-    }
-}
-
-// k_bicg_t : t = A z ; omega = <t,s>/<t,t>
-template <class T>
-__global__ void k_bicg_t(Lev<T> L, KState* st, int ns, const cplx<T>* __restrict__ z, cplx<T>* __restrict__ t,
-                         const cplx<T>* __restrict__ sv, RedBuf rb) {
-    extern __shared__ double2 smem[];
-    typedef typename AccOf<T>::type A;
-    const int s = threadIdx.x % ns;
-    const bool act = st[s].active;
-    const T wm = (T)st[s].wm;
-    A a0r = 0, a0i = 0, a1 = 0;
-    const int64_t W = L.nl * ns;
-    if (act)
-        for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < W; g += (int64_t)gridDim.x * blockDim.x) {
-            int o, i, j, k;
-            edecode(L, g / ns, o, i, j, k);
-            cplx<T> val = apply_row<T>(L, o, i, j, k, wm, z, ns, s, z[g]);
-            t[g] = val;
-            cplx<T> d = cdot<T>(val, sv[g]);
-            a0r += d.x;
-            a0i += d.y;
-            a1 += cabs2<T>(val);
-        }
-    double2 acc[2] = {make_double2(a0r, a0i), make_double2(a1, 0.0)};
-    if (!block_reduce_and_last<2, A>(acc, ns, rb, smem)) return;
-    const int B = blockDim.x;
-    for (int ss = threadIdx.x; ss < ns; ss += B) {
-        if (!st[ss].active) continue;
-        double2 ts = smem[B + ss];
-        double tt = smem[B + ns + ss].x;
-        st[ss].omega = make_double2(ts.x / tt, ts.y / tt);
-        if (!isfinite(st[ss].omega.x) || !isfinite(st[ss].omega.y) ||
-            (st[ss].omega.x == 0.0 && st[ss].omega.y == 0.0)) {  // breakdown: keep the last iterate
-            st[ss].active = 0;
-            st[ss].status = ST_BREAK;
-        }
-    }
-}
-
-// k_bicg_upd : x += alpha y + omega z ; r = s - omega t ; err = |r|/|b| ;
-// then the top-of-loop logic of the next iteration (convergence test, rho, beta).
-template <class T, class XT>
-__global__ void k_bicg_upd(Lev<T> L, KState* st, int ns, cplx<XT>* __restrict__ x, const cplx<T>* __restrict__ y,
-                           const cplx<T>* __restrict__ z, const cplx<T>* __restrict__ sv, const cplx<T>* __restrict__ t,
-                           cplx<T>* __restrict__ r, const cplx<T>* __restrict__ rhat, RedBuf rb, double* err_rec,
-                           int err_stride) {
-    extern __shared__ double2 smem[];
-    typedef typename AccOf<T>::type A;
-    const int s = threadIdx.x % ns;
-    const bool act = st[s].active;
-    const cplx<T> om = mk<T>((T)st[s].omega.x, (T)st[s].omega.y);
-    const cplx<XT> alx = mk<XT>((XT)st[s].alpha.x, (XT)st[s].alpha.y), omx = mk<XT>((XT)st[s].omega.x, (XT)st[s].omega.y);
-    A rr = 0, hr = 0, hi = 0;
-    const int64_t W = L.nl * ns;
-    if (act)
-        for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < W; g += (int64_t)gridDim.x * blockDim.x) {
-            cplx<T> yy = y[g], zz = z[g];
-            cplx<XT> y2 = mk<XT>((XT)yy.x, (XT)yy.y), z2 = mk<XT>((XT)zz.x, (XT)zz.y);
-            x[g] = x[g] + cmul<XT>(alx, y2) + cmul<XT>(omx, z2);
-            cplx<T> rn = sv[g] - cmul<T>(om, t[g]);
-            r[g] = rn;
-            rr += cabs2<T>(rn);
-            cplx<T> d = cdot<T>(rhat[g], rn);
-            hr += d.x;
-            hi += d.y;
-        }
-    double2 acc[2] = {make_double2(rr, 0.0), make_double2(hr, hi)};
-    if (!block_reduce_and_last<2, A>(acc, ns, rb, smem)) return;
-    const int B = blockDim.x;
-    for (int ss = threadIdx.x; ss < ns; ss += B) {
-        KState& S = st[ss];
-        if (!S.active) continue;
-        double nr = sqrt(smem[B + ss].x);
-        double2 rh = smem[B + ns + ss];
-        S.err = nr / S.babs;
-        S.it += 1;
-        if (err_rec && S.it <= S.itmax) err_rec[(size_t)ss * err_stride + S.it - 1] = S.err;
-        // scalars of the next iteration first: a system stopped below may be
-        // resumed (mixed precision re-check) and must continue consistently
-        S.rhoold = S.rho;
-        S.rho = rh;
-        double2 a = S.rho, b = S.rhoold, al2 = S.alpha, om2 = S.omega;
-        double bd = b.x * b.x + b.y * b.y, od = om2.x * om2.x + om2.y * om2.y;
-        double2 q1 = make_double2((a.x * b.x + a.y * b.y) / bd, (a.y * b.x - a.x * b.y) / bd);
-        double2 q2 = make_double2((al2.x * om2.x + al2.y * om2.y) / od, (al2.y * om2.x - al2.x * om2.y) / od);
-        S.beta = make_double2(q1.x * q2.x - q1.y * q2.y, q1.x * q2.y + q1.y * q2.x);
-        if (isnan(S.err)) {  // solvers.f90:683
-            S.status = ST_NAN;
-            S.active = 0;
-            S.iters = S.it - 1;
-            continue;
-        }
-        if (S.it > S.itmax) {
-            S.status = ST_MAXIT;
-            S.active = 0;
-            S.iters = S.itmax;
-            continue;
-        }
-        S.iters = S.it;
-        if (S.err < S.tol) {  // solvers.f90:625
-            S.status = ST_CONV;
-            S.active = 0;
-            continue;
-        }
     }
 }
 
@@ -531,22 +276,6 @@ static __global__ void k_reactivate(KState* st, int ns) {
     }
 }
 
-// x64 += x32 ; x32 = 0  (active systems)
-template <class T>
-__global__ void k_flush(int64_t nl, const KState* st, int ns, double2* __restrict__ x64, cplx<T>* __restrict__ x32,
-                        double2* __restrict__ xb) {
-    const int64_t W = nl * ns;
-    for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < W; g += (int64_t)gridDim.x * blockDim.x) {
-        const int s = (int)(g % ns);
-        if (!st[s].active) continue;
-        cplx<T> d = x32[g];
-        double2 v = x64[g];
-        if (xb) xb[g] = v;  // kept until the FP64 residual accepts the update
-        x64[g] = make_double2(v.x + (double)d.x, v.y + (double)d.y);
-        x32[g] = zero<T>();
-    }
-}
-
 // x64 = xb for the systems whose last update was rejected (status ST_BREAK)
 static __global__ void k_restore(int64_t nl, const KState* st, int ns, double2* __restrict__ x64, const double2* __restrict__ xb) {
     const int64_t W = nl * ns;
@@ -556,123 +285,12 @@ static __global__ void k_restore(int64_t nl, const KState* st, int ns, double2* 
     }
 }
 
-// r32 = b64 - A64 x64 ; FP64 convergence test ; re-synchronise the scalar
-// recurrences with the new residual.  solver: 1 BiCGStab (rho = <rhat, r>,
-// beta = rho/rhoold * alpha/omega), 3 GPBiCG (beta = alpha/omega *
-// <r0, r>/<r0, r_old>).
-template <class T>
-__global__ void k_reliable(Lev<double> L, KState* st, int ns, const double2* __restrict__ b, const double2* __restrict__ x,
-                           cplx<T>* __restrict__ r, const cplx<T>* __restrict__ rhat, int solver, RedBuf rb) {
-    extern __shared__ double2 smem[];
-    const int s = threadIdx.x % ns;
-    const bool act = st[s].active;
-    const double wm = st[s].wm;
-    double rr = 0, hr = 0, hi = 0;
-    const int64_t W = L.nl * ns;
-    if (act)
-        for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < W; g += (int64_t)gridDim.x * blockDim.x) {
-            int o, i, j, k;
-            edecode(L, g / ns, o, i, j, k);
-            double2 ax = apply_row<double>(L, o, i, j, k, wm, x, ns, s, x[g]);
-            double2 rv = b[g] - ax;
-            cplx<T> rt = mk<T>((T)rv.x, (T)rv.y);
-            r[g] = rt;
-            rr += rv.x * rv.x + rv.y * rv.y;
-            cplx<T> h = rhat[g];
-            hr += (double)h.x * rv.x + (double)h.y * rv.y;
-            hi += (double)h.x * rv.y - (double)h.y * rv.x;
-        }
-    double2 acc[2] = {make_double2(rr, 0.0), make_double2(hr, hi)};
-    if (!block_reduce_and_last<2, double>(acc, ns, rb, smem)) return;
-    const int B = blockDim.x;
-    for (int ss = threadIdx.x; ss < ns; ss += B) {
-        KState& S = st[ss];
-        if (!S.active) continue;
-        S.err = sqrt(smem[B + ss].x) / S.babs;
-        double2 h = smem[B + ns + ss];
-        if (isnan(S.err) || (S.errv > 0 && S.err > 10.0 * S.errv)) {
-            // the complex64 correction made the FP64 residual worse (kappa * eps32 > 1
-            // for this system): take it back (k_restore) and stop the mixed iteration
-            S.status = ST_BREAK;
-            S.active = 0;
-            S.pad[0] = 1;  // restore marker for k_restore
-            S.err = S.errv;
-            continue;
-        }
-        S.errv = S.err;
-        if (S.err < S.tol) {
-            S.status = ST_VCONV;
-            S.active = 0;
-            continue;
-        }
-        if (S.it > S.itmax) {
-            S.status = ST_MAXIT;
-            S.active = 0;
-            continue;
-        }
-        if (solver == 3) {
-            double2 a = S.alpha, o = S.omega, ro = S.rho;
-            double od = o.x * o.x + o.y * o.y, rd = ro.x * ro.x + ro.y * ro.y;
-            double2 q1 = make_double2((a.x * o.x + a.y * o.y) / od, (a.y * o.x - a.x * o.y) / od);
-            double2 q2 = make_double2((h.x * ro.x + h.y * ro.y) / rd, (h.y * ro.x - h.x * ro.y) / rd);
-            S.beta = make_double2(q1.x * q2.x - q1.y * q2.y, q1.x * q2.y + q1.y * q2.x);
-        } else {
-            S.rho = h;
-            double2 a = S.rho, bb = S.rhoold, al2 = S.alpha, om2 = S.omega;
-            double bd = bb.x * bb.x + bb.y * bb.y, od = om2.x * om2.x + om2.y * om2.y;
-            double2 q1 = make_double2((a.x * bb.x + a.y * bb.y) / bd, (a.y * bb.x - a.x * bb.y) / bd);
-            double2 q2 = make_double2((al2.x * om2.x + al2.y * om2.y) / od, (al2.y * om2.x - al2.x * om2.y) / od);
-            S.beta = make_double2(q1.x * q2.x - q1.y * q2.y, q1.x * q2.y + q1.y * q2.x);
-        }
-    }
-}
-
 // ------------------------------------------------------------------ misc vector kernels
-template <class T>
-__global__ void k_set_state(KState* st, int ns, const double* wms, double tol, int itmax) {
-    int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= ns) return;
-    KState S = {};
-    S.wm = wms[s];
-    S.tol = tol;
-    S.itmax = itmax;
-    S.active = 1;
-    S.status = ST_RUN;
-    st[s] = S;
-}
-
 template <class A, class B>
 __global__ void k_convert(int64_t n, const cplx<A>* __restrict__ src, cplx<B>* __restrict__ dst) {
     for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < n; g += (int64_t)gridDim.x * blockDim.x) {
         cplx<A> v = src[g];
         dst[g] = mk<B>((B)v.x, (B)v.y);
-    }
-}
-
-// x64 += scale_s * d32  (iterative refinement update)
-template <class T>
-__global__ void k_refine_add(int64_t nl, int ns, const double* scale, cplx<double>* __restrict__ x,
-                             const cplx<T>* __restrict__ d) {
-    const int64_t W = nl * ns;
-    for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < W; g += (int64_t)gridDim.x * blockDim.x) {
-        int s = (int)(g % ns);
-        double sc = scale[s];
-        if (sc == 0.0) continue;
-        cplx<T> v = d[g];
-        double2 xv = x[g];
-        x[g] = make_double2(xv.x + sc * (double)v.x, xv.y + sc * (double)v.y);
-    }
-}
-
-// r32 = r64 / scale_s  (normalised refinement right-hand side)
-static __global__ void k_scale_to_f32(int64_t nl, int ns, const double* scale, const double2* __restrict__ src,
-                               float2* __restrict__ dst) {
-    const int64_t W = nl * ns;
-    for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < W; g += (int64_t)gridDim.x * blockDim.x) {
-        int s = (int)(g % ns);
-        double sc = scale[s];
-        double2 v = src[g];
-        dst[g] = sc > 0 ? make_float2((float)(v.x / sc), (float)(v.y / sc)) : make_float2(0.f, 0.f);
     }
 }
 
@@ -683,16 +301,6 @@ __global__ void k_pattern(int64_t n, cplx<T>* __restrict__ v) {
         v[g] = mk<T>((T)(1.0 + 1e-3 * (double)(g % 977)), (T)(0.5 - 1e-3 * (double)(g % 613)));
 }
 
-// interleave / de-interleave between [s][nl] (per-system) and [nl][ns] (batched)
-template <class T>
-__global__ void k_gather_sys(int64_t nl, int ns, const cplx<T>* __restrict__ src_sys_major, cplx<T>* __restrict__ dst) {
-    const int64_t W = nl * ns;
-    for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < W; g += (int64_t)gridDim.x * blockDim.x) {
-        int s = (int)(g % ns);
-        int64_t e = g / ns;
-        dst[g] = src_sys_major[(size_t)s * nl + e];
-    }
-}
 template <class T>
 __global__ void k_scatter_sys(int64_t nl, int ns, const cplx<T>* __restrict__ src, cplx<T>* __restrict__ dst_sys_major) {
     const int64_t W = nl * ns;

@@ -1,0 +1,295 @@
+// sfdx_krylov.cuh -- host drivers of the Krylov solves of one level (all
+// systems of the batch at once): BiCGStab (Bicg_stab_p, solvers.f90:522-719),
+// GPBiCG (pgpbicg, solvers.f90:137-315), the multi-colour SSOR / Jacobi
+// preconditioner (lusol/ssorfac, diagcsr) and the reliable FP64 residual
+// updates of the mixed-precision solve.  Included by sfdx_krylov_f32.cu and
+// sfdx_krylov_f64.cu, which instantiate it per arithmetic type so that the
+// two compile in parallel.
+#pragma once
+#include "sfdx_plan.h"
+#include "sfdx_vkern.cuh"
+
+namespace sfdx {
+
+// ------------------------------------------------------------------ preconditioner
+template <class T, int VS, int O, int PP, int MODE>
+static void fwd_one(Plan& P, const Level& LV, const VCfg& c, cplx<T>* w, cplx<T>* q, const cplx<T>* r, const cplx<T>* v) {
+    const uint32_t W = mcolour_count(LV.mesh, O) * c.sg.G;
+    KL(k_fwd_v<T, VS, O, PP, MODE><<<grid_for(W, c.B, 16), c.B, 0, P.st>>>(LV.lev<T>(), LV.mesh, c.sg,
+                                                                           P.d_state.as<KState>(), w, q, r, v));
+}
+template <class T, int VS, int O, int PP>
+static void bwd_one(Plan& P, const Level& LV, const VCfg& c, cplx<T>* x) {
+    const uint32_t W = mcolour_count(LV.mesh, O) * c.sg.G;
+    KL(k_bwd_v<T, VS, O, PP><<<grid_for(W, c.B, 16), c.B, 0, P.st>>>(LV.lev<T>(), LV.mesh, c.sg, P.d_state.as<KState>(),
+                                                                     x));
+}
+
+// out = M^{-1} rhs where rhs is produced by MODE (see k_fwd_v).  Multi-colour
+// symmetric Gauss-Seidel: colours 0..5 forward, 4..0 backward (the backward
+// step of the last colour is the identity).
+template <class T, int VS, int MODE>
+static void precond(Plan& P, const Level& LV, cplx<T>* out, cplx<T>* q, const cplx<T>* r, const cplx<T>* v) {
+    if (P.o.precond == 'J') {
+        const int B = block_for(P.ns);
+        KL(k_jacobi<T, MODE><<<grid_for(LV.nl * P.ns, B, 16), B, 0, P.st>>>(LV.lev<T>(), P.d_state.as<KState>(), P.ns, out,
+                                                                            q, r, v));
+        return;
+    }
+    const VCfg c = vcfg(P, LV.nl, 0);
+    fwd_one<T, VS, OX, 0, MODE>(P, LV, c, out, q, r, v);
+    fwd_one<T, VS, OX, 1, MODE>(P, LV, c, out, q, r, v);
+    fwd_one<T, VS, OY, 0, MODE>(P, LV, c, out, q, r, v);
+    fwd_one<T, VS, OY, 1, MODE>(P, LV, c, out, q, r, v);
+    fwd_one<T, VS, OZ, 0, MODE>(P, LV, c, out, q, r, v);
+    fwd_one<T, VS, OZ, 1, MODE>(P, LV, c, out, q, r, v);
+    bwd_one<T, VS, OZ, 0>(P, LV, c, out);
+    bwd_one<T, VS, OY, 1>(P, LV, c, out);
+    bwd_one<T, VS, OY, 0>(P, LV, c, out);
+    bwd_one<T, VS, OX, 1>(P, LV, c, out);
+    bwd_one<T, VS, OX, 0>(P, LV, c, out);
+}
+
+static void init_states(Plan& P, const double* tols_host, double tol, int itmax, const int* mask_host,
+                        std::vector<KState>& init) {
+    init.resize(P.ns);
+    for (int q = 0; q < P.ns; q++) {
+        KState S;
+        memset(&S, 0, sizeof(S));
+        S.wm = P.wm[q];
+        S.tol = tols_host ? tols_host[q] : tol;
+        S.itmax = itmax;
+        S.active = mask_host ? mask_host[q] : 1;
+        S.status = S.active ? ST_RUN : ST_CONV;
+        init[q] = S;
+    }
+}
+
+// partial sums of the reducing kernels of one level (nq per system)
+static int reserve_partials(Plan& P, const VCfg& c, int nq) {
+    return P.d_part.alloc(std::max(P.d_part.bytes, (size_t)c.grid * nq * P.ns * sizeof(double2)));
+}
+
+// FP64 residual replacement for the systems still running or whose complex64
+// recurrence claims convergence; returns the number of systems left active.
+template <class T, int VS>
+static int reliable_update(Plan& P, const Level& LV, const Reliable& rel, cplx<T>* x32, cplx<T>* r, const cplx<T>* rhat,
+                           int solver, int& active) {
+    const int ns = P.ns;
+    const VCfg c = vcfg(P, LV.nl, 2);
+    RC(reserve_partials(P, c, 2));
+    KState* dst = P.d_state.as<KState>();
+    KL(k_reactivate<<<(ns + 127) / 128, 128, 0, P.st>>>(dst, ns));
+    KL(k_flush_v<T, VS><<<grid_for(LV.nl * c.sg.G, c.B, 16), c.B, 0, P.st>>>(LV.mesh, c.sg, dst, rel.x64, x32, rel.xb));
+    KL(k_reliable_v<T, VS><<<c.grid, c.B, c.smem, P.st>>>(LV.lev<double>(), LV.mesh, c.sg, dst, rel.b64, rel.x64, r, rhat,
+                                                           solver, redbuf(P)));
+    CK(cudaGetLastError());
+    RC(sync_state(P));
+    active = 0;
+    int rejected = 0;
+    for (int q = 0; q < ns; q++) {
+        active += P.hst[q].active;
+        rejected += P.hst[q].status == ST_BREAK && P.hst[q].pad[0] == 1;
+    }
+    if (rejected) {
+        const int B = block_for(ns);
+        KL(k_restore<<<grid_for(LV.nl * ns, B, 16), B, 0, P.st>>>(LV.nl, dst, ns, rel.x64, rel.xb));
+        CK(cudaGetLastError());
+    }
+    return SFDX_OK;
+}
+
+// Bicg_stab_p (solvers.f90:522-719) for the ns systems of level LV: A x = b.
+// Plain: x holds the initial guess (precision T).  With `rel` (mixed
+// precision) b/x are the complex64 work vectors and the FP64 b64/x64 of
+// `rel` define the system.
+template <class T, int VS>
+static int bicgstab_v(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, const double* tols_host, double tol,
+                      int itmax, const int* mask_host, const Reliable* rel) {
+    const Lev<T> L = LV.lev<T>();
+    const Mesh& M = LV.mesh;
+    const int ns = P.ns;
+    const size_t vb = (size_t)LV.nl * ns * sizeof(cplx<T>);
+    for (int q = 0; q < 8; q++) RC(P.kv[q].alloc(vb));
+    cplx<T>* r = P.kv[0].as<cplx<T>>();
+    cplx<T>* rhat = P.kv[1].as<cplx<T>>();
+    cplx<T>* p = P.kv[2].as<cplx<T>>();
+    cplx<T>* v = P.kv[3].as<cplx<T>>();
+    cplx<T>* y = P.kv[4].as<cplx<T>>();
+    cplx<T>* s = P.kv[5].as<cplx<T>>();
+    cplx<T>* z = P.kv[6].as<cplx<T>>();
+    cplx<T>* t = P.kv[7].as<cplx<T>>();
+    for (cplx<T>* q : {p, v, y, z}) CK(cudaMemsetAsync(q, 0, vb, P.st));
+    std::vector<KState> init;
+    init_states(P, tols_host, tol, itmax, mask_host, init);
+    CK(cudaMemcpyAsync(P.d_state.p, init.data(), sizeof(KState) * ns, cudaMemcpyHostToDevice, P.st));
+    const VCfg c = vcfg(P, LV.nl, 2);
+    RC(reserve_partials(P, c, 2));
+    KState* dst = P.d_state.as<KState>();
+    if (rel) {
+        CK(cudaMemsetAsync(x, 0, vb, P.st));
+        KL(k_residual_v<T, double, VS, 0><<<c.grid, c.B, c.smem, P.st>>>(LV.lev<double>(), M, c.sg, dst, rel->b64, rel->x64,
+                                                                          r, rhat, redbuf(P), P.hist, P.hist_stride));
+    } else {
+        KL(k_residual_v<T, T, VS, 0><<<c.grid, c.B, c.smem, P.st>>>(L, M, c.sg, dst, b, x, r, rhat, redbuf(P), P.hist,
+                                                                     P.hist_stride));
+    }
+    CK(cudaGetLastError());
+    const int check_every = 8;
+    int last_rel = 0;
+    for (int it = 1; it <= itmax; it++) {
+        // top of iteration `it` (solvers.f90:630-640): divergence correction and
+        // residual restart every corr_intv iterations (FP64 solves only)
+        if (!rel && std::is_same<T, double>::value && P.o.div_cor && it % P.o.corr_intv == 0) {
+            RC(div_correct(P, LV, reinterpret_cast<double2*>(x)));
+            KL(k_residual_v<T, T, VS, 1><<<c.grid, c.B, c.smem, P.st>>>(L, M, c.sg, dst, b, x, r, rhat, redbuf(P), nullptr,
+                                                                         0));
+        }
+        precond<T, VS, RHS_PUPD>(P, LV, y, p, r, v);
+        KL(k_bicg_v_v<T, VS><<<c.grid, c.B, c.smem, P.st>>>(L, M, c.sg, dst, y, v, rhat, redbuf(P)));
+        precond<T, VS, RHS_SUPD>(P, LV, z, s, r, v);
+        KL(k_bicg_t_v<T, VS><<<c.grid, c.B, c.smem, P.st>>>(L, M, c.sg, dst, z, t, s, redbuf(P)));
+        KL(k_bicg_upd_v<T, T, VS><<<c.grid, c.B, c.smem, P.st>>>(M, c.sg, dst, x, y, z, s, t, r, rhat, redbuf(P), P.hist,
+                                                                  P.hist_stride));
+        if (it % check_every == 0 || it == itmax) {
+            CK(cudaGetLastError());
+            RC(sync_state(P));
+            int act = 0, cand = 0;
+            for (int q = 0; q < ns; q++) {
+                act += P.hst[q].active;
+                cand += P.hst[q].status == ST_CONV;
+            }
+            if (rel && (cand || it - last_rel >= rel->every || it == itmax)) {
+                RC((reliable_update<T, VS>(P, LV, *rel, x, r, rhat, 1, act)));
+                last_rel = it;
+            }
+            if (!act) break;
+        }
+    }
+    if (rel)
+        KL(k_flush_v<T, VS><<<grid_for(LV.nl * c.sg.G, c.B, 16), c.B, 0, P.st>>>(M, c.sg, dst, rel->x64, x, nullptr));
+    RC(sync_state(P));
+    return SFDX_OK;
+}
+
+// pgpbicg (solvers.f90:137-315) for the ns systems of level LV (same calling
+// convention as bicgstab).
+template <class T, int VS>
+static int gpbicg_v(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, const double* tols_host, double tol,
+                    int itmax, const int* mask_host, const Reliable* rel) {
+    const Lev<T> L = LV.lev<T>();
+    const Mesh& M = LV.mesh;
+    const int ns = P.ns;
+    const size_t vb = (size_t)LV.nl * ns * sizeof(cplx<T>);
+    for (int q = 0; q < 14; q++) RC(P.kv[q].alloc(vb));
+    cplx<T>* V[14];
+    for (int q = 0; q < 14; q++) V[q] = P.kv[q].as<cplx<T>>();
+    cplx<T> *r = V[0], *r0 = V[1], *rp = V[2], *y = V[3], *p = V[4], *u = V[5], *w = V[6], *t = V[7];
+    cplx<T>* tp[2] = {V[8], V[9]};
+    cplx<T> *ap = V[10], *at = V[11], *z = V[12], *tmp = V[13];
+    for (cplx<T>* q : {u, w, t, tp[0], tp[1], z}) CK(cudaMemsetAsync(q, 0, vb, P.st));
+    std::vector<KState> init;
+    init_states(P, tols_host, tol, itmax, mask_host, init);
+    CK(cudaMemcpyAsync(P.d_state.p, init.data(), sizeof(KState) * ns, cudaMemcpyHostToDevice, P.st));
+    const VCfg c = vcfg(P, LV.nl, 4);
+    RC(reserve_partials(P, c, 4));
+    const int Ge = grid_for(LV.nl * c.sg.G, c.B, 16);
+    KState* dst = P.d_state.as<KState>();
+    if (rel) {
+        CK(cudaMemsetAsync(x, 0, vb, P.st));
+        KL(k_residual_v<T, double, VS, 3><<<c.grid, c.B, c.smem, P.st>>>(LV.lev<double>(), M, c.sg, dst, rel->b64, rel->x64,
+                                                                          r, r0, redbuf(P), nullptr, 0));
+    } else {
+        KL(k_residual_v<T, T, VS, 3><<<c.grid, c.B, c.smem, P.st>>>(L, M, c.sg, dst, b, x, r, r0, redbuf(P), nullptr, 0));
+    }
+    precond<T, VS, RHS_VEC>(P, LV, rp, r, nullptr, nullptr);
+    CK(cudaMemcpyAsync(p, rp, vb, cudaMemcpyDeviceToDevice, P.st));
+    int cur = 0, last_rel = 0;
+    for (int it = 1; it <= itmax; it++) {
+        if (!rel && std::is_same<T, double>::value && P.o.div_cor && it % P.o.corr_intv == 0) {
+            // solvers.f90:223-235: correct x, restart r and r0 (rp is kept)
+            RC(div_correct(P, LV, reinterpret_cast<double2*>(x)));
+            KL(k_residual_v<T, T, VS, 4><<<c.grid, c.B, c.smem, P.st>>>(L, M, c.sg, dst, b, x, r, r0, redbuf(P), nullptr,
+                                                                         0));
+        }
+        KL(k_gp_ap_v<T, VS><<<c.grid, c.B, c.smem, P.st>>>(L, M, c.sg, dst, p, ap, r0, r, redbuf(P)));
+        KL(k_gp_yt_v<T, VS><<<Ge, c.B, 0, P.st>>>(M, c.sg, dst, y, t, r, w, ap));
+        precond<T, VS, RHS_VEC>(P, LV, tmp, ap, nullptr, nullptr);
+        KL(k_gp_tp_v<T, VS><<<Ge, c.B, 0, P.st>>>(M, c.sg, dst, tp[cur], rp, tmp));
+        KL(k_gp_at_v<T, VS><<<c.grid, c.B, c.smem, P.st>>>(L, M, c.sg, dst, tp[cur], at, t, y, redbuf(P)));
+        KL(k_gp_upd_v<T, T, VS><<<c.grid, c.B, c.smem, P.st>>>(M, c.sg, dst, u, z, x, r, tmp, tp[cur ^ 1], rp, p, t, y, at,
+                                                                r0, redbuf(P), P.hist, P.hist_stride));
+        bool stop = false;
+        if (it % 8 == 0 || it == itmax) {
+            CK(cudaGetLastError());
+            RC(sync_state(P));
+            int act = 0, cand = 0;
+            for (int q = 0; q < ns; q++) {
+                act += P.hst[q].active;
+                cand += P.hst[q].status == ST_CONV;
+            }
+            if (rel && (cand || it - last_rel >= rel->every || it == itmax)) {
+                RC((reliable_update<T, VS>(P, LV, *rel, x, r, r0, 3, act)));
+                last_rel = it;
+            }
+            stop = !act;
+        }
+        if (stop) break;
+        precond<T, VS, RHS_VEC>(P, LV, rp, r, nullptr, nullptr);
+        KL(k_gp_pw_v<T, VS><<<Ge, c.B, 0, P.st>>>(M, c.sg, dst, w, p, at, ap, rp, u));
+        cur ^= 1;
+    }
+    if (rel) KL(k_flush_v<T, VS><<<Ge, c.B, 0, P.st>>>(M, c.sg, dst, rel->x64, x, nullptr));
+    RC(sync_state(P));
+    return SFDX_OK;
+}
+
+// ------------------------------------------------------------------ entry points (VS dispatch)
+template <class T>
+int bicgstab(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, const double* tols_host, double tol, int itmax,
+             const int* mask_host, const Reliable* rel) {
+    switch (vs_for(P.ns)) {
+        case 4: return bicgstab_v<T, 4>(P, LV, b, x, tols_host, tol, itmax, mask_host, rel);
+        case 2: return bicgstab_v<T, 2>(P, LV, b, x, tols_host, tol, itmax, mask_host, rel);
+        default: return bicgstab_v<T, 1>(P, LV, b, x, tols_host, tol, itmax, mask_host, rel);
+    }
+}
+template <class T>
+int gpbicg(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, const double* tols_host, double tol, int itmax,
+           const int* mask_host, const Reliable* rel) {
+    switch (vs_for(P.ns)) {
+        case 4: return gpbicg_v<T, 4>(P, LV, b, x, tols_host, tol, itmax, mask_host, rel);
+        case 2: return gpbicg_v<T, 2>(P, LV, b, x, tols_host, tol, itmax, mask_host, rel);
+        default: return gpbicg_v<T, 1>(P, LV, b, x, tols_host, tol, itmax, mask_host, rel);
+    }
+}
+template <class T> int precond_vec(Plan& P, const Level& LV, cplx<T>* out, cplx<T>* q) {
+    switch (vs_for(P.ns)) {
+        case 4: precond<T, 4, RHS_VEC>(P, LV, out, q, nullptr, nullptr); break;
+        case 2: precond<T, 2, RHS_VEC>(P, LV, out, q, nullptr, nullptr); break;
+        default: precond<T, 1, RHS_VEC>(P, LV, out, q, nullptr, nullptr); break;
+    }
+    CK(cudaGetLastError());
+    return SFDX_OK;
+}
+template <class T> int apply_op(Plan& P, const Level& LV, const cplx<T>* x, cplx<T>* y) {
+    const VCfg c = vcfg(P, LV.nl, 0, 16);
+    const double* wm = P.d_wm.as<double>();
+    switch (c.VS) {
+        case 4: KL(k_apply_v<T, 4><<<c.grid, c.B, 0, P.st>>>(LV.lev<T>(), LV.mesh, c.sg, wm, x, y)); break;
+        case 2: KL(k_apply_v<T, 2><<<c.grid, c.B, 0, P.st>>>(LV.lev<T>(), LV.mesh, c.sg, wm, x, y)); break;
+        default: KL(k_apply_v<T, 1><<<c.grid, c.B, 0, P.st>>>(LV.lev<T>(), LV.mesh, c.sg, wm, x, y)); break;
+    }
+    CK(cudaGetLastError());
+    return SFDX_OK;
+}
+
+#define SFDX_INSTANTIATE_KRYLOV(T)                                                                                      \
+    template int bicgstab<T>(Plan&, const Level&, const cplx<T>*, cplx<T>*, const double*, double, int, const int*,    \
+                             const Reliable*);                                                                          \
+    template int gpbicg<T>(Plan&, const Level&, const cplx<T>*, cplx<T>*, const double*, double, int, const int*,      \
+                           const Reliable*);                                                                            \
+    template int precond_vec<T>(Plan&, const Level&, cplx<T>*, cplx<T>*);                                               \
+    template int apply_op<T>(Plan&, const Level&, const cplx<T>*, cplx<T>*);
+
+}  // namespace sfdx

@@ -1,0 +1,237 @@
+// sfdx_plan.h -- host-side structures shared by the translation units of the
+// solver: device buffers, mesh levels, the plan (one mesh hierarchy + one
+// frequency list), launch sizing and the launch counter.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <type_traits>
+#include <vector>
+
+#include "sfdx.h"
+#include "sfdx_kernels.cuh"
+#include "sfdx_stencil.cuh"
+
+namespace sfdx {
+
+static const double kPi = 3.141592653589793238462643;
+static const double kMu = 4.0 * 3.141592653589793238462643 * 1e-7;
+
+#define CK(call)                                                        \
+    do {                                                                \
+        cudaError_t e_ = (call);                                        \
+        if (e_ != cudaSuccess) {                                        \
+            if (getenv("SFDX_DEBUG"))                                   \
+                fprintf(stderr, "sfdx: CUDA %s at %s:%d\n", cudaGetErrorString(e_), __FILE__, __LINE__); \
+            return SFDX_ERR_CUDA;                                       \
+        }                                                               \
+    } while (0)
+#define RC(call)                       \
+    do {                               \
+        int r_ = (call);               \
+        if (r_ != SFDX_OK) return r_;  \
+    } while (0)
+
+// kernel launches issued by this library (process-wide)
+extern std::atomic<long long> g_launches;
+#define KL(...) (g_launches.fetch_add(1, std::memory_order_relaxed), __VA_ARGS__)
+
+inline int device_sms() {
+    static int nsm = 0;
+    if (!nsm) {
+        int dev = 0, v = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+        nsm = v > 0 ? v : 1;
+    }
+    return nsm;
+}
+
+// block size: ns * 2^k in [128, 1024] and >= nq*ns (per-system reductions)
+inline int block_for(int ns, int nq = 2) {
+    int b = ns;
+    while (b < 128 || b < nq * ns) b *= 2;
+    return b;
+}
+inline int grid_for(int64_t work, int B, int per_sm = 8) {
+    int64_t g = (work + B - 1) / B;
+    int64_t cap = (int64_t)device_sms() * per_sm;
+    if (g > cap) g = cap;
+    if (g < 1) g = 1;
+    return (int)g;
+}
+// systems per thread of the hot kernels
+inline int vs_for(int ns) { return ns % 4 == 0 ? 4 : (ns % 2 == 0 ? 2 : 1); }
+// block of the system-group kernels: G * 2^k >= 128
+inline int vblock(int G) {
+    int b = G;
+    while (b < 128) b *= 2;
+    return b;
+}
+
+// ------------------------------------------------------------------ device buffers
+struct DBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    DBuf() = default;
+    DBuf(const DBuf&) = delete;
+    DBuf& operator=(const DBuf&) = delete;
+    DBuf(DBuf&& o) noexcept : p(o.p), bytes(o.bytes) {
+        o.p = nullptr;
+        o.bytes = 0;
+    }
+    ~DBuf() {
+        if (p) cudaFree(p);
+    }
+    int alloc(size_t n) {
+        if (n <= bytes) return SFDX_OK;
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+        if (cudaMalloc(&p, n) != cudaSuccess) return SFDX_ERR_NOMEM;
+        bytes = n;
+        return SFDX_OK;
+    }
+    template <class X> X* as() const { return reinterpret_cast<X*>(p); }
+};
+
+// ------------------------------------------------------------------ mesh level
+template <class T> AxisT<T> axis_ptrs(const T* base, int stride, int axis) {
+    const T* p = base + (size_t)axis * 6 * stride;
+    AxisT<T> a;
+    a.rh = p;
+    a.lo = p + stride;
+    a.hi = p + 2 * stride;
+    a.rs = p + 3 * stride;
+    a.wlo = p + 4 * stride;
+    a.whi = p + 5 * stride;
+    return a;
+}
+
+struct Level {
+    int nx = 0, ny = 0, nz = 0, nair = 0;
+    int64_t xnl = 0, ynl = 0, nl = 0, ncell = 0;
+    Mesh mesh;
+    std::vector<double> a, b, c;
+    int aniso = 0;
+    DBuf tab64, tab32;     // [3 axes][6 arrays][stride]
+    DBuf sig64, sig32;     // [6][ncell]
+    DBuf spac;             // a, b, c (device, FP64) for coarsening
+    DBuf crd_cubic;        // node coordinates used by cubic_interp on this level
+    DBuf crd_quad;         // node coordinates used by quad_interp_e (pairwise sums of a,b,c)
+    int stride = 0;
+
+    void set_dims(int X, int Y, int Z) {
+        nx = X; ny = Y; nz = Z;
+        xnl = (int64_t)nx * (ny + 1) * (nz + 1);
+        ynl = (int64_t)(nx + 1) * ny * (nz + 1);
+        nl = xnl + ynl + (int64_t)(nx + 1) * (ny + 1) * nz;
+        ncell = (int64_t)nx * ny * nz;
+        mesh = make_mesh(nx, ny, nz);
+    }
+    template <class T> Lev<T> lev() const {
+        Lev<T> L;
+        L.nx = nx; L.ny = ny; L.nz = nz;
+        L.xnl = xnl; L.ynl = ynl; L.nl = nl; L.ncell = ncell;
+        const T* base = std::is_same<T, double>::value ? (const T*)tab64.p : (const T*)tab32.p;
+        L.ax = axis_ptrs<T>(base, stride, 0);
+        L.ay = axis_ptrs<T>(base, stride, 1);
+        L.az = axis_ptrs<T>(base, stride, 2);
+        L.sig = std::is_same<T, double>::value ? (const T*)sig64.p : (const T*)sig32.p;
+        L.aniso = aniso;
+        return L;
+    }
+};
+
+// ------------------------------------------------------------------ plan
+struct Plan {
+    sfdx_opts o;
+    int nf = 0, ns = 0, nlev = 0;
+    std::vector<double> freq, wm;
+    std::vector<Level> lev;  // lev[0] coarsest ... lev[nlev-1] finest
+    cudaStream_t st = nullptr;      // stream all work of the plan is issued on
+    cudaStream_t own_st = nullptr;  // stream created by the plan (destroyed with it)
+    // per-system device data
+    DBuf d_state, d_wm, d_pol, d_edc, d_part, d_counter, d_tol, d_mask, d_scale, d_flag;
+    // FP64 vectors (finest-level size)
+    DBuf x64, b64, r64, u0, u1, ut, ex_out;
+    // Krylov vectors (precision of the active solve)
+    DBuf kv[14];
+    // divergence correction: t, r, p, v, phi (nodes) and the PCG state
+    DBuf dcv[5], d_pst;
+    int dc_calls = 0, dc_last_iters = 0;
+    DBuf errrec;
+    int edc_stride = 0;
+    double* hist = nullptr;  // optional device residual history [ns][hist_stride]
+    int hist_stride = 0;
+    std::vector<int> iters;        // [nf][2][nlev]
+    std::vector<double> level_ms;  // wall time per level of the last solve
+    std::vector<double> relres;    // [nf][2]
+    std::vector<KState> hst;
+    bool have_solution = false;
+    Plan() = default;
+    Plan(const Plan&) = delete;
+    ~Plan() {
+        if (own_st) cudaStreamDestroy(own_st);
+    }
+};
+
+inline int sync_state(Plan& P) {
+    P.hst.resize(P.ns);
+    CK(cudaMemcpyAsync(P.hst.data(), P.d_state.p, sizeof(KState) * P.ns, cudaMemcpyDeviceToHost, P.st));
+    CK(cudaStreamSynchronize(P.st));
+    return SFDX_OK;
+}
+
+inline RedBuf redbuf(Plan& P) {
+    RedBuf r;
+    r.part = P.d_part.as<double2>();
+    r.counter = P.d_counter.as<unsigned int>();
+    return r;
+}
+
+// Launch shape of a system-group kernel over the edges of a level (W = nl * G
+// work items); `nq` complex partial sums per system for reducing kernels.
+struct VCfg {
+    int VS, B, grid;
+    size_t smem;
+    SysG sg;
+};
+inline VCfg vcfg(const Plan& P, int64_t nl, int nq, int per_sm = 8) {
+    VCfg c;
+    c.VS = vs_for(P.ns);
+    c.sg = make_sysg(P.ns, c.VS);
+    c.B = vblock(c.sg.G);
+    c.grid = grid_for(nl * c.sg.G, c.B, per_sm);
+    c.smem = nq > 0 ? vred_smem_bytes(c.B, nq, P.ns) : 0;
+    return c;
+}
+
+// Reliable-update context of a mixed-precision solve: the FP64 right-hand
+// side and solution; the complex64 iteration works on a partial solution.
+struct Reliable {
+    const double2* b64;
+    double2* x64;
+    int every;    // iterations between FP64 residual replacements
+    double2* xb;  // copy of x64 before the last update (restored on rejection)
+};
+
+// ------------------------------------------------------------------ drivers (sfdx_krylov*.cu)
+template <class T>
+int bicgstab(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, const double* tols_host, double tol, int itmax,
+             const int* mask_host, const Reliable* rel = nullptr);
+template <class T>
+int gpbicg(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, const double* tols_host, double tol, int itmax,
+           const int* mask_host, const Reliable* rel = nullptr);
+// out = M^{-1} q (multi-colour SSOR or Jacobi) for all active systems
+template <class T> int precond_vec(Plan& P, const Level& LV, cplx<T>* out, cplx<T>* q);
+// y = A x for all systems (per-system frequencies in P.d_wm)
+template <class T> int apply_op(Plan& P, const Level& LV, const cplx<T>* x, cplx<T>* y);
+
+// ------------------------------------------------------------------ sfdx_solver.cu
+int div_correct(Plan& P, const Level& LV, double2* x);
+
+}  // namespace sfdx

@@ -10,8 +10,9 @@
 //    doublemode_acc (:1258, fwd_acc = 1)      -> solve_cascade
 //      u1u2 + pardiso_spd (:1228, :765)       -> coarse levels: FP64 Krylov to coarse_tol
 //      extint_v (excmg.f90:9)                 -> prolongate (k_interp, k_extrapolate)
-//    Bicg_stab_p (solvers.f90:522)            -> bicgstab<T>
-//    lusol/ssorfac (multi-colour)             -> precond<T>
+//    Bicg_stab_p (solvers.f90:522)            -> bicgstab<T>   (sfdx_krylov.cuh)
+//    pgpbicg (solvers.f90:137)                -> gpbicg<T>     (sfdx_krylov.cuh)
+//    lusol/ssorfac (multi-colour)             -> precond       (sfdx_krylov.cuh)
 //  mixed precision                            -> solve_level_mixed (FP64 residual,
 //                                                complex64 inner BiCGStab)
 #include <cuda_runtime.h>
@@ -31,101 +32,15 @@
 #include "sfdx.h"
 #include "sfdx_divcorr.cuh"
 #include "sfdx_excmg.cuh"
-#include "sfdx_gpbicg.cuh"
 #include "sfdx_host.h"
 #include "sfdx_kernels.cuh"
+#include "sfdx_plan.h"
 
 using namespace sfdx;
 
 namespace sfdx {
 
-static const double kPi = 3.141592653589793238462643;
-static const double kMu = 4.0 * 3.141592653589793238462643 * 1e-7;
-
-#define CK(call)                                                        \
-    do {                                                                \
-        cudaError_t e_ = (call);                                        \
-        if (e_ != cudaSuccess) {                                        \
-            if (getenv("SFDX_DEBUG"))                                   \
-                fprintf(stderr, "sfdx: CUDA %s at %s:%d\n", cudaGetErrorString(e_), __FILE__, __LINE__); \
-            return SFDX_ERR_CUDA;                                       \
-        }                                                               \
-    } while (0)
-#define RC(call)                       \
-    do {                               \
-        int r_ = (call);               \
-        if (r_ != SFDX_OK) return r_;  \
-    } while (0)
-
-static int g_nsm = 0;
-// kernel launches issued by this library (process-wide)
-static std::atomic<long long> g_launches{0};
-#define KL(...) (g_launches.fetch_add(1, std::memory_order_relaxed), __VA_ARGS__)
-static int device_sms() {
-    if (!g_nsm) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&g_nsm, cudaDevAttrMultiProcessorCount, dev);
-        if (g_nsm <= 0) g_nsm = 1;
-    }
-    return g_nsm;
-}
-
-// block size: ns * 2^k in [128, 1024] and >= 2*ns (reductions need NQ*ns <= B)
-static int block_for(int ns, int nq = 2) {
-    int b = ns;
-    while (b < 128 || b < nq * ns) b *= 2;
-    return b;
-}
-static int grid_for(int64_t work, int B, int per_sm = 8) {
-    int64_t g = (work + B - 1) / B;
-    int64_t cap = (int64_t)device_sms() * per_sm;
-    if (g > cap) g = cap;
-    if (g < 1) g = 1;
-    return (int)g;
-}
-
-// ------------------------------------------------------------------ device buffers
-struct DBuf {
-    void* p = nullptr;
-    size_t bytes = 0;
-    ~DBuf() {
-        if (p) cudaFree(p);
-    }
-    int alloc(size_t n) {
-        if (n <= bytes) return SFDX_OK;
-        if (p) cudaFree(p);
-        p = nullptr;
-        bytes = 0;
-        if (cudaMalloc(&p, n) != cudaSuccess) return SFDX_ERR_NOMEM;
-        bytes = n;
-        return SFDX_OK;
-    }
-    template <class X> X* as() const { return reinterpret_cast<X*>(p); }
-};
-
-// ------------------------------------------------------------------ mesh level
-struct Level {
-    int nx = 0, ny = 0, nz = 0, nair = 0;
-    int64_t xnl = 0, ynl = 0, nl = 0, ncell = 0;
-    std::vector<double> a, b, c;
-    int aniso = 0;
-    DBuf tab64, tab32;     // [3 axes][6 arrays][stride]
-    DBuf sig64, sig32;     // [6][ncell]
-    DBuf spac;             // a, b, c (device, FP64) for coarsening
-    DBuf crd_cubic;        // node coordinates used by cubic_interp on this level
-    DBuf crd_quad;         // node coordinates used by quad_interp_e (pairwise sums of a,b,c)
-    int stride = 0;
-
-    void set_dims(int X, int Y, int Z) {
-        nx = X; ny = Y; nz = Z;
-        xnl = (int64_t)nx * (ny + 1) * (nz + 1);
-        ynl = (int64_t)(nx + 1) * ny * (nz + 1);
-        nl = xnl + ynl + (int64_t)(nx + 1) * (ny + 1) * nz;
-        ncell = (int64_t)nx * ny * nz;
-    }
-    template <class T> Lev<T> lev() const;
-};
+std::atomic<long long> g_launches{0};
 
 static void axis_tables(const std::vector<double>& h, int stride, double* out) {
     const int n = (int)h.size();
@@ -145,30 +60,6 @@ static void axis_tables(const std::vector<double>& h, int stride, double* out) {
         wl[m] = h[m - 1] / s;
         wh[m] = h[m] / s;
     }
-}
-
-template <class T> static AxisT<T> axis_ptrs(const T* base, int stride, int axis) {
-    const T* p = base + (size_t)axis * 6 * stride;
-    AxisT<T> a;
-    a.rh = p;
-    a.lo = p + stride;
-    a.hi = p + 2 * stride;
-    a.rs = p + 3 * stride;
-    a.wlo = p + 4 * stride;
-    a.whi = p + 5 * stride;
-    return a;
-}
-template <class T> Lev<T> Level::lev() const {
-    Lev<T> L;
-    L.nx = nx; L.ny = ny; L.nz = nz;
-    L.xnl = xnl; L.ynl = ynl; L.nl = nl; L.ncell = ncell;
-    const T* base = std::is_same<T, double>::value ? (const T*)tab64.p : (const T*)tab32.p;
-    L.ax = axis_ptrs<T>(base, stride, 0);
-    L.ay = axis_ptrs<T>(base, stride, 1);
-    L.az = axis_ptrs<T>(base, stride, 2);
-    L.sig = std::is_same<T, double>::value ? (const T*)sig64.p : (const T*)sig32.p;
-    L.aniso = aniso;
-    return L;
 }
 
 static std::vector<double> node_coords(const std::vector<double>& h, int nair, bool is_z) {
@@ -227,86 +118,6 @@ static int upload_level_tables(Level& L, cudaStream_t st) {
     return SFDX_OK;
 }
 
-// ------------------------------------------------------------------ plan
-struct Plan {
-    sfdx_opts o;
-    int nf = 0, ns = 0, nlev = 0;
-    std::vector<double> freq, wm;
-    std::vector<Level> lev;  // lev[0] coarsest ... lev[nlev-1] finest
-    cudaStream_t st = nullptr;      // stream all work of the plan is issued on
-    cudaStream_t own_st = nullptr;  // stream created by the plan (destroyed with it)
-    // per-system device data
-    DBuf d_state, d_wm, d_pol, d_edc, d_part, d_counter, d_tol, d_mask, d_scale, d_flag;
-    // FP64 vectors (finest-level size)
-    DBuf x64, b64, r64, u0, u1, ut, ex_out;
-    // Krylov vectors (precision of the active solve)
-    DBuf kv[14];
-    // divergence correction: t, r, p, v, phi (nodes) and the PCG state
-    DBuf dcv[5], d_pst;
-    int dc_calls = 0, dc_last_iters = 0;
-    DBuf errrec;
-    int edc_stride = 0;
-    double* hist = nullptr;  // optional device residual history [ns][hist_stride]
-    int hist_stride = 0;
-    std::vector<int> iters;        // [nf][2][nlev]
-    std::vector<double> level_ms;  // wall time per level of the last solve
-    std::vector<double> relres;    // [nf][2]
-    std::vector<KState> hst;
-    bool have_solution = false;
-    ~Plan() {
-        if (own_st) cudaStreamDestroy(own_st);
-    }
-};
-
-static int sync_state(Plan& P) {
-    P.hst.resize(P.ns);
-    CK(cudaMemcpyAsync(P.hst.data(), P.d_state.p, sizeof(KState) * P.ns, cudaMemcpyDeviceToHost, P.st));
-    CK(cudaStreamSynchronize(P.st));
-    return SFDX_OK;
-}
-
-static RedBuf redbuf(Plan& P) {
-    RedBuf r;
-    r.part = P.d_part.as<double2>();
-    r.counter = P.d_counter.as<unsigned int>();
-    return r;
-}
-
-// ------------------------------------------------------------------ preconditioner
-template <class T, int O, int PP, int MODE>
-static void fwd_one(Plan& P, const Lev<T>& L, cplx<T>* w, cplx<T>* q, const cplx<T>* r, const cplx<T>* v) {
-    const int B = block_for(P.ns);
-    const int64_t W = colour_count(L, O) * P.ns;
-    KL(k_sweep_fwd<T, O, PP, MODE><<<grid_for(W, B, 16), B, 0, P.st>>>(L, P.d_state.as<KState>(), P.ns, w, q, r, v));
-}
-template <class T, int O, int PP>
-static void bwd_one(Plan& P, const Lev<T>& L, cplx<T>* x) {
-    const int B = block_for(P.ns);
-    const int64_t W = colour_count(L, O) * P.ns;
-    KL(k_sweep_bwd<T, O, PP><<<grid_for(W, B, 16), B, 0, P.st>>>(L, P.d_state.as<KState>(), P.ns, x));
-}
-
-// out = M^{-1} rhs where rhs is produced by MODE (see k_sweep_fwd)
-template <class T, int MODE>
-static void precond(Plan& P, const Lev<T>& L, cplx<T>* out, cplx<T>* q, const cplx<T>* r, const cplx<T>* v) {
-    if (P.o.precond == 'J') {
-        const int B = block_for(P.ns);
-        KL(k_jacobi<T, MODE><<<grid_for(L.nl * P.ns, B, 16), B, 0, P.st>>>(L, P.d_state.as<KState>(), P.ns, out, q, r, v));
-        return;
-    }
-    fwd_one<T, OX, 0, MODE>(P, L, out, q, r, v);
-    fwd_one<T, OX, 1, MODE>(P, L, out, q, r, v);
-    fwd_one<T, OY, 0, MODE>(P, L, out, q, r, v);
-    fwd_one<T, OY, 1, MODE>(P, L, out, q, r, v);
-    fwd_one<T, OZ, 0, MODE>(P, L, out, q, r, v);
-    fwd_one<T, OZ, 1, MODE>(P, L, out, q, r, v);
-    bwd_one<T, OZ, 0>(P, L, out);
-    bwd_one<T, OY, 1>(P, L, out);
-    bwd_one<T, OY, 0>(P, L, out);
-    bwd_one<T, OX, 1>(P, L, out);
-    bwd_one<T, OX, 0>(P, L, out);
-}
-
 // ------------------------------------------------------------------ divergence correction
 static NodeGeo node_geo(const Level& LV) {
     NodeGeo G;
@@ -320,7 +131,7 @@ static NodeGeo node_geo(const Level& LV) {
 }
 
 // x += grad(phi), P phi = T x  for the systems active in P.d_state
-static int div_correct(Plan& P, const Level& LV, double2* x) {
+int div_correct(Plan& P, const Level& LV, double2* x) {
     const int ns = P.ns;
     const NodeGeo G = node_geo(LV);
     const size_t nb = (size_t)G.np * ns * sizeof(double2);
@@ -355,200 +166,6 @@ static int div_correct(Plan& P, const Level& LV, double2* x) {
     CK(cudaStreamSynchronize(P.st));
     P.dc_calls++;
     P.dc_last_iters = h[0].iters;
-    return SFDX_OK;
-}
-
-// ------------------------------------------------------------------ Krylov drivers
-// Reliable-update context of a mixed-precision solve: the FP64 right-hand
-// side and solution; the complex64 iteration works on a partial solution.
-struct Reliable {
-    const double2* b64;
-    double2* x64;
-    int every;    // iterations between FP64 residual replacements
-    double2* xb;  // copy of x64 before the last update (restored on rejection)
-};
-
-static void init_states(Plan& P, const double* tols_host, double tol, int itmax, const int* mask_host,
-                        std::vector<KState>& init) {
-    init.resize(P.ns);
-    for (int q = 0; q < P.ns; q++) {
-        KState S;
-        memset(&S, 0, sizeof(S));
-        S.wm = P.wm[q];
-        S.tol = tols_host ? tols_host[q] : tol;
-        S.itmax = itmax;
-        S.active = mask_host ? mask_host[q] : 1;
-        S.status = S.active ? ST_RUN : ST_CONV;
-        init[q] = S;
-    }
-}
-
-// FP64 residual replacement for the systems still running or whose complex64
-// recurrence claims convergence; returns the number of systems left active.
-template <class T>
-static int reliable_update(Plan& P, const Level& LV, const Reliable& rel, cplx<T>* x32, cplx<T>* r, const cplx<T>* rhat,
-                           int solver, int& active) {
-    const int ns = P.ns;
-    const int B = block_for(ns, 4);
-    KState* dst = P.d_state.as<KState>();
-    KL(k_reactivate<<<(ns + 127) / 128, 128, 0, P.st>>>(dst, ns));
-    KL(k_flush<T><<<grid_for(LV.nl * ns, B, 16), B, 0, P.st>>>(LV.nl, dst, ns, rel.x64, x32, rel.xb));
-    KL(k_reliable<T><<<grid_for(LV.nl * ns, B, 8), B, 4 * B * sizeof(double2), P.st>>>(
-        LV.lev<double>(), dst, ns, rel.b64, rel.x64, r, rhat, solver, redbuf(P)));
-    CK(cudaGetLastError());
-    RC(sync_state(P));
-    active = 0;
-    int rejected = 0;
-    for (int q = 0; q < ns; q++) {
-        active += P.hst[q].active;
-        rejected += P.hst[q].status == ST_BREAK && P.hst[q].pad[0] == 1;
-    }
-    if (rejected) {
-        KL(k_restore<<<grid_for(LV.nl * ns, B, 16), B, 0, P.st>>>(LV.nl, dst, ns, rel.x64, rel.xb));
-        CK(cudaGetLastError());
-    }
-    return SFDX_OK;
-}
-
-// Bicg_stab_p (solvers.f90:522-719) for the ns systems of level L: A x = b.
-// Plain: x holds the initial guess (precision T).  With `rel` (mixed
-// precision) b/x are the complex64 work vectors and the FP64 b64/x64 of
-// `rel` define the system.
-template <class T>
-static int bicgstab(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, const double* tols_host, double tol,
-                    int itmax, const int* mask_host, const Reliable* rel = nullptr) {
-    const Lev<T> L = LV.lev<T>();
-    const int ns = P.ns;
-    const size_t vb = (size_t)LV.nl * ns * sizeof(cplx<T>);
-    for (int q = 0; q < 8; q++) RC(P.kv[q].alloc(vb));
-    cplx<T>* r = P.kv[0].as<cplx<T>>();
-    cplx<T>* rhat = P.kv[1].as<cplx<T>>();
-    cplx<T>* p = P.kv[2].as<cplx<T>>();
-    cplx<T>* v = P.kv[3].as<cplx<T>>();
-    cplx<T>* y = P.kv[4].as<cplx<T>>();
-    cplx<T>* s = P.kv[5].as<cplx<T>>();
-    cplx<T>* z = P.kv[6].as<cplx<T>>();
-    cplx<T>* t = P.kv[7].as<cplx<T>>();
-    for (cplx<T>* q : {p, v, y, z}) CK(cudaMemsetAsync(q, 0, vb, P.st));
-    std::vector<KState> init;
-    init_states(P, tols_host, tol, itmax, mask_host, init);
-    CK(cudaMemcpyAsync(P.d_state.p, init.data(), sizeof(KState) * ns, cudaMemcpyHostToDevice, P.st));
-    const int B = block_for(ns, 4);
-    const size_t smem = 4 * B * sizeof(double2);
-    const int G = grid_for(LV.nl * ns, B, 8);
-    RC(P.d_part.alloc(std::max(P.d_part.bytes, (size_t)G * 4 * ns * sizeof(double2))));
-    KState* dst = P.d_state.as<KState>();
-    if (rel) {
-        CK(cudaMemsetAsync(x, 0, vb, P.st));
-        KL(k_residual<T, double, 0><<<G, B, smem, P.st>>>(LV.lev<double>(), dst, ns, rel->b64, rel->x64, r, rhat,
-                                                            redbuf(P), P.hist, P.hist_stride));
-    } else {
-        KL(k_residual<T, T, 0><<<G, B, smem, P.st>>>(L, dst, ns, b, x, r, rhat, redbuf(P), P.hist, P.hist_stride));
-    }
-    CK(cudaGetLastError());
-    const int check_every = 8;
-    int last_rel = 0;
-    for (int it = 1; it <= itmax; it++) {
-        // top of iteration `it` (solvers.f90:630-640): divergence correction and
-        // residual restart every corr_intv iterations (FP64 solves only)
-        if (!rel && std::is_same<T, double>::value && P.o.div_cor && it % P.o.corr_intv == 0) {
-            RC(div_correct(P, LV, reinterpret_cast<double2*>(x)));
-            KL(k_residual<T, T, 1><<<G, B, smem, P.st>>>(L, dst, ns, b, x, r, rhat, redbuf(P), nullptr, 0));
-        }
-        precond<T, RHS_PUPD>(P, L, y, p, r, v);
-        KL(k_bicg_v<T><<<G, B, smem, P.st>>>(L, dst, ns, y, v, rhat, redbuf(P)));
-        precond<T, RHS_SUPD>(P, L, z, s, r, v);
-        KL(k_bicg_t<T><<<G, B, smem, P.st>>>(L, dst, ns, z, t, s, redbuf(P)));
-        KL(k_bicg_upd<T, T><<<G, B, smem, P.st>>>(L, dst, ns, x, y, z, s, t, r, rhat, redbuf(P), P.hist, P.hist_stride));
-        if (it % check_every == 0 || it == itmax) {
-            CK(cudaGetLastError());
-            RC(sync_state(P));
-            int act = 0, cand = 0;
-            for (int q = 0; q < ns; q++) {
-                act += P.hst[q].active;
-                cand += P.hst[q].status == ST_CONV;
-            }
-            if (rel && (cand || it - last_rel >= rel->every || it == itmax)) {
-                RC(reliable_update<T>(P, LV, *rel, x, r, rhat, 1, act));
-                last_rel = it;
-            }
-            if (!act) break;
-        }
-    }
-    if (rel) KL(k_flush<T><<<grid_for(LV.nl * ns, B, 16), B, 0, P.st>>>(LV.nl, dst, ns, rel->x64, x, nullptr));
-    RC(sync_state(P));
-    return SFDX_OK;
-}
-
-// pgpbicg (solvers.f90:137-315) for the ns systems of level L (same calling
-// convention as bicgstab).
-template <class T>
-static int gpbicg(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, const double* tols_host, double tol,
-                  int itmax, const int* mask_host, const Reliable* rel = nullptr) {
-    const Lev<T> L = LV.lev<T>();
-    const int ns = P.ns;
-    const size_t vb = (size_t)LV.nl * ns * sizeof(cplx<T>);
-    for (int q = 0; q < 14; q++) RC(P.kv[q].alloc(vb));
-    cplx<T>* V[14];
-    for (int q = 0; q < 14; q++) V[q] = P.kv[q].as<cplx<T>>();
-    cplx<T> *r = V[0], *r0 = V[1], *rp = V[2], *y = V[3], *p = V[4], *u = V[5], *w = V[6], *t = V[7];
-    cplx<T>* tp[2] = {V[8], V[9]};
-    cplx<T> *ap = V[10], *at = V[11], *z = V[12], *tmp = V[13];
-    for (cplx<T>* q : {u, w, t, tp[0], tp[1], z}) CK(cudaMemsetAsync(q, 0, vb, P.st));
-    std::vector<KState> init;
-    init_states(P, tols_host, tol, itmax, mask_host, init);
-    CK(cudaMemcpyAsync(P.d_state.p, init.data(), sizeof(KState) * ns, cudaMemcpyHostToDevice, P.st));
-    const int B = block_for(ns, 4);
-    const size_t smem = 4 * B * sizeof(double2);
-    const int G = grid_for(LV.nl * ns, B, 8);
-    RC(P.d_part.alloc(std::max(P.d_part.bytes, (size_t)G * 4 * ns * sizeof(double2))));
-    KState* dst = P.d_state.as<KState>();
-    if (rel) {
-        CK(cudaMemsetAsync(x, 0, vb, P.st));
-        KL(k_residual<T, double, 3><<<G, B, smem, P.st>>>(LV.lev<double>(), dst, ns, rel->b64, rel->x64, r, r0,
-                                                            redbuf(P), nullptr, 0));
-    } else {
-        KL(k_residual<T, T, 3><<<G, B, smem, P.st>>>(L, dst, ns, b, x, r, r0, redbuf(P), nullptr, 0));
-    }
-    precond<T, RHS_VEC>(P, L, rp, r, nullptr, nullptr);
-    CK(cudaMemcpyAsync(p, rp, vb, cudaMemcpyDeviceToDevice, P.st));
-    const int Ge = grid_for(LV.nl * ns, B, 16);
-    int cur = 0, last_rel = 0;
-    for (int it = 1; it <= itmax; it++) {
-        if (!rel && std::is_same<T, double>::value && P.o.div_cor && it % P.o.corr_intv == 0) {
-            // solvers.f90:223-235: correct x, restart r and r0 (rp is kept)
-            RC(div_correct(P, LV, reinterpret_cast<double2*>(x)));
-            KL(k_residual<T, T, 4><<<G, B, smem, P.st>>>(L, dst, ns, b, x, r, r0, redbuf(P), nullptr, 0));
-        }
-        KL(k_gp_ap<T><<<G, B, smem, P.st>>>(L, dst, ns, p, ap, r0, r, redbuf(P)));
-        KL(k_gp_yt<T><<<Ge, B, 0, P.st>>>(LV.nl, dst, ns, y, t, r, w, ap));
-        precond<T, RHS_VEC>(P, L, tmp, ap, nullptr, nullptr);
-        KL(k_gp_tp<T><<<Ge, B, 0, P.st>>>(LV.nl, dst, ns, tp[cur], rp, tmp));
-        KL(k_gp_at<T><<<G, B, smem, P.st>>>(L, dst, ns, tp[cur], at, t, y, redbuf(P)));
-        KL(k_gp_upd<T, T><<<G, B, smem, P.st>>>(LV.nl, dst, ns, u, z, x, r, tmp, tp[cur ^ 1], rp, p, t, y, at, r0,
-                                                 redbuf(P), P.hist, P.hist_stride));
-        bool stop = false;
-        if (it % 8 == 0 || it == itmax) {
-            CK(cudaGetLastError());
-            RC(sync_state(P));
-            int act = 0, cand = 0;
-            for (int q = 0; q < ns; q++) {
-                act += P.hst[q].active;
-                cand += P.hst[q].status == ST_CONV;
-            }
-            if (rel && (cand || it - last_rel >= rel->every || it == itmax)) {
-                RC(reliable_update<T>(P, LV, *rel, x, r, r0, 3, act));
-                last_rel = it;
-            }
-            stop = !act;
-        }
-        if (stop) break;
-        precond<T, RHS_VEC>(P, L, rp, r, nullptr, nullptr);
-        KL(k_gp_pw<T><<<Ge, B, 0, P.st>>>(LV.nl, dst, ns, w, p, at, ap, rp, u));
-        cur ^= 1;
-    }
-    if (rel) KL(k_flush<T><<<grid_for(LV.nl * ns, B, 16), B, 0, P.st>>>(LV.nl, dst, ns, rel->x64, x, nullptr));
-    RC(sync_state(P));
     return SFDX_OK;
 }
 
@@ -965,7 +582,7 @@ extern "C" int sfdx_plan_create(sfdx_plan** out, const sfdx_opts* opts, int nx, 
     P.o = o;
     P.nf = nf;
     P.ns = 2 * nf;
-    if (P.ns > 512) return SFDX_ERR_UNSUPPORTED;
+    if (P.ns > SFDX_MAX_SYSTEMS) return SFDX_ERR_UNSUPPORTED;
     P.freq.assign(freq, freq + nf);
     P.wm.resize(P.ns);
     for (int f = 0; f < nf; f++) {
@@ -973,6 +590,11 @@ extern "C" int sfdx_plan_create(sfdx_plan** out, const sfdx_opts* opts, int nx, 
         P.wm[2 * f] = P.wm[2 * f + 1] = 2 * kPi * freq[f] * kMu;
     }
     P.nlev = o.excmg ? o.level : 1;
+    {  // the hot kernels index edge x system work items in 32 bits
+        const int64_t nl = (int64_t)nx * (ny + 1) * (nz + 1) + (int64_t)(nx + 1) * ny * (nz + 1) +
+                           (int64_t)(nx + 1) * (ny + 1) * nz;
+        if (nl * P.ns >= (1LL << 31)) return SFDX_ERR_UNSUPPORTED;
+    }
     if (o.excmg) {
         const int f = 1 << o.level;  // cubic_interp tiles 8 fine cells on level 3 and up
         if (nx % f || ny % f || nz % f) return SFDX_ERR_MESH;
@@ -1093,10 +715,10 @@ extern "C" int sfdx_plan_kernel_time(sfdx_plan* plan, int kernel, int reps, doub
     CK(cudaEventCreate(&e1));
     auto launch = [&]() {
         switch (kernel) {
-            case 0: KL(k_apply<float><<<grid_for(n, B, 16), B, 0, P.st>>>(F.lev<float>(), P.d_wm.as<double>(), ns, P.kv[0].as<float2>(), P.kv[1].as<float2>())); break;
-            case 1: KL(k_apply<double><<<grid_for(n, B, 16), B, 0, P.st>>>(F.lev<double>(), P.d_wm.as<double>(), ns, P.kv[0].as<double2>(), P.kv[1].as<double2>())); break;
-            case 2: precond<float, RHS_VEC>(P, F.lev<float>(), P.kv[1].as<float2>(), P.kv[0].as<float2>(), nullptr, nullptr); break;
-            case 3: precond<double, RHS_VEC>(P, F.lev<double>(), P.kv[1].as<double2>(), P.kv[0].as<double2>(), nullptr, nullptr); break;
+            case 0: apply_op<float>(P, F, P.kv[0].as<float2>(), P.kv[1].as<float2>()); break;
+            case 1: apply_op<double>(P, F, P.kv[0].as<double2>(), P.kv[1].as<double2>()); break;
+            case 2: precond_vec<float>(P, F, P.kv[1].as<float2>(), P.kv[0].as<float2>()); break;
+            case 3: precond_vec<double>(P, F, P.kv[1].as<double2>(), P.kv[0].as<double2>()); break;
             default: break;
         }
     };
@@ -1199,7 +821,7 @@ namespace {
 // A one-level plan over host inputs, ns systems at the given frequencies.
 int component_plan(sfdx_plan** h, const sfdx_opts* o, int nx, int ny, int nz, const double* a, const double* b,
                    const double* c, const double* sigma, int ns, const double* freqs) {
-    if (ns < 1 || ns > 512 || !freqs) return SFDX_ERR_ARG;
+    if (ns < 1 || ns > SFDX_MAX_SYSTEMS || !freqs) return SFDX_ERR_ARG;
     sfdx_opts oo;
     if (o) oo = *o;
     else sfdx_default_opts(&oo);
@@ -1210,6 +832,7 @@ int component_plan(sfdx_plan** h, const sfdx_opts* o, int nx, int ny, int nz, co
     RC(sfdx_plan_create(h, &oo, nx, ny, nz, 0, a, b, c, (int)fr.size(), fr.data()));
     Plan& P = (*h)->P;
     P.ns = ns;
+    if (P.lev[0].nl * ns >= (1LL << 31)) return SFDX_ERR_UNSUPPORTED;
     P.wm.resize(ns);
     for (int s = 0; s < ns; s++) P.wm[s] = 2 * kPi * freqs[s] * kMu;
     RC(P.d_wm.alloc(sizeof(double) * ns));
@@ -1239,15 +862,13 @@ extern "C" int sfdx_apply_operator(int nx, int ny, int nz, const double* a, cons
     CK(cudaMemcpyAsync(dx.p, x, n * 16, cudaMemcpyHostToDevice, P.st));
     const int B = block_for(ns);
     if (precision == SFDX_FP64) {
-        KL(k_apply<double><<<grid_for(n, B, 16), B, 0, P.st>>>(L.lev<double>(), P.d_wm.as<double>(), ns, dx.as<double2>(),
-                                                              dy.as<double2>()));
+        RC(apply_op<double>(P, L, dx.as<double2>(), dy.as<double2>()));
     } else {
         DBuf fx, fy;
         RC(fx.alloc(n * 8));
         RC(fy.alloc(n * 8));
         KL(k_convert<double, float><<<grid_for(n, 256), 256, 0, P.st>>>(n, dx.as<double2>(), fx.as<float2>()));
-        KL(k_apply<float><<<grid_for(n, B, 16), B, 0, P.st>>>(L.lev<float>(), P.d_wm.as<double>(), ns, fx.as<float2>(),
-                                                             fy.as<float2>()));
+        RC(apply_op<float>(P, L, fx.as<float2>(), fy.as<float2>()));
         KL(k_convert<float, double><<<grid_for(n, 256), 256, 0, P.st>>>(n, fy.as<float2>(), dy.as<double2>()));
         CK(cudaStreamSynchronize(P.st));
     }
@@ -1310,13 +931,13 @@ extern "C" int sfdx_precond_apply(int nx, int ny, int nz, const double* a, const
     RC(dx.alloc(n * 16));
     CK(cudaMemcpyAsync(dy.p, y, n * 16, cudaMemcpyHostToDevice, P.st));
     if (precision == SFDX_FP64) {
-        precond<double, RHS_VEC>(P, L.lev<double>(), dx.as<double2>(), dy.as<double2>(), nullptr, nullptr);
+        RC(precond_vec<double>(P, L, dx.as<double2>(), dy.as<double2>()));
     } else {
         DBuf fy, fx;
         RC(fy.alloc(n * 8));
         RC(fx.alloc(n * 8));
         KL(k_convert<double, float><<<grid_for(n, 256), 256, 0, P.st>>>(n, dy.as<double2>(), fy.as<float2>()));
-        precond<float, RHS_VEC>(P, L.lev<float>(), fx.as<float2>(), fy.as<float2>(), nullptr, nullptr);
+        RC(precond_vec<float>(P, L, fx.as<float2>(), fy.as<float2>()));
         KL(k_convert<float, double><<<grid_for(n, 256), 256, 0, P.st>>>(n, fx.as<float2>(), dx.as<double2>()));
         CK(cudaStreamSynchronize(P.st));
     }
@@ -1367,7 +988,7 @@ extern "C" int sfdx_mesh_coarsen(int nx, int ny, int nz, const double* a, const 
 
 extern "C" int sfdx_prolongate(int nx, int ny, int nz, const double* a1, const double* b1, const double* c1, int nair,
                                int ns, const double* u0, const double* u1, double* u, int quirks) {
-    if (!a1 || !b1 || !c1 || !u0 || !u1 || !u || ns < 1 || ns > 512) return SFDX_ERR_ARG;
+    if (!a1 || !b1 || !c1 || !u0 || !u1 || !u || ns < 1 || ns > SFDX_MAX_SYSTEMS) return SFDX_ERR_ARG;
     if (nx % 8 || ny % 8 || nz % 8) return SFDX_ERR_MESH;
     // a 3-level hierarchy whose finest level is this mesh
     sfdx_opts o;
