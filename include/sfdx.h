@@ -71,7 +71,11 @@ typedef struct sfdx_opts {
     int solver;         /* SFDX_SOLVER_*                                               */
     int excmg;          /* fwd_acc: 0 single solve from zero guess, 1 EXCMG cascade    */
     int precond;        /* 'S' multi-colour SSOR, 'J' Jacobi (pre_type)                */
-    int div_cor;        /* divergence correction on/off (div_cor)                      */
+    int div_cor;        /* divergence correction (div_cor): 0 off, 1 the reference's
+                           (div_correc every corr_intv iterations), 2 consistent
+                           gradient-space correction between restart cycles of
+                           corr_intv iterations and after the last (no counterpart
+                           in the reference: sfdx_grad_correct below)              */
     int corr_intv;      /* iterations between corrections (corr_intv = 200)            */
     double corr_tol;    /* nodal-Poisson PCG tolerance (corr_tol = 1e-3)               */
     double ssor_omega;  /* SSOR relaxation (ssor_omg = 1)                              */
@@ -136,6 +140,12 @@ int sfdx_plan_set_stream(sfdx_plan* plan, void* stream);
 /* CUDA-event time (ms per launch) of one kernel family on the finest level and its
  * algorithmic HBM bytes: 0 operator c64, 1 operator c128, 2 MC-SSOR c64, 3 MC-SSOR c128. */
 int sfdx_plan_kernel_time(sfdx_plan* plan, int kernel, int reps, double* ms, double* bytes);
+/* Pick the number of systems each thread of the hot kernels handles (4, 2
+ * or 1 consecutive systems, complex64 and complex128 separately) by timing an
+ * operator plus a multi-colour SSOR application per candidate, `reps` times
+ * each, on the finest level (conductivity must be loaded).  No counterpart in
+ * the reference.  The choices are returned in *vs32, *vs64 (optional). */
+int sfdx_plan_autotune(sfdx_plan* plan, int reps, int* vs32, int* vs64);
 /* Wall time (ms) of each level of the last solve, coarsest first (n >= levels). */
 int sfdx_plan_level_times(const sfdx_plan* plan, double* ms, int n);
 void sfdx_plan_destroy(sfdx_plan* plan);
@@ -205,6 +215,19 @@ int sfdx_krylov_solve(const sfdx_opts* o, int nx, int ny, int nz, const double* 
  * interleaved systems.  Returns PCG iterations of system 0 in *pcg_iters. */
 int sfdx_div_correct(int nx, int ny, int nz, const double* a, const double* b, const double* c,
                      const double* sigma, int ns, double* x, double tol, int* pcg_iters);
+
+/* Consistent gradient-space correction.  No counterpart in the reference; it
+ * replaces the divergence correction above where the field must stay a
+ * solution of the discrete system: x += G phi with
+ * (G^T V Ms G) phi = G^T V (rhs - K x) / (-i w mu), G the nodal gradient
+ * (interior nodes), V the edge dual volumes, Ms the mass (conductivity) part
+ * of K.  The exact solution is a fixed point; the error's gradient component
+ * is removed.  Nodal PCG (Jacobi) to relative tolerance tol, at most maxit
+ * iterations (*pcg_iters: the most any system took).  rhs, x: [nl][ns]
+ * complex, host. */
+int sfdx_grad_correct(int nx, int ny, int nz, const double* a, const double* b, const double* c,
+                      const double* sigma, int ns, const double* freqs, const double* rhs, double* x, double tol,
+                      int maxit, int* pcg_iters);
 
 /* ------------------------------------------------------------------------
  * Residual without any memory allocation.  No counterpart in the reference:

@@ -112,6 +112,10 @@ _PROTO = {
                                          c_double_p, ctypes.c_double, ctypes.c_int, c_int_p, c_double_p, c_double_p]),
     "sfdx_div_correct": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, c_double_p, c_double_p,
                                         c_double_p, c_double_p, ctypes.c_int, c_double_p, ctypes.c_double, c_int_p]),
+    "sfdx_plan_autotune": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, c_int_p, c_int_p]),
+    "sfdx_grad_correct": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, c_double_p, c_double_p,
+                                         c_double_p, c_double_p, ctypes.c_int, c_double_p, c_double_p, c_double_p,
+                                         ctypes.c_double, ctypes.c_int, c_int_p]),
     "sfdx_residual_noalloc": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, c_double_p, c_double_p,
                                              c_double_p, ctypes.c_void_p, ctypes.c_int, c_double_p, ctypes.c_void_p,
                                              ctypes.c_void_p, ctypes.c_void_p, c_double_p, ctypes.c_void_p]),

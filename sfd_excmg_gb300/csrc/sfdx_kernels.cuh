@@ -265,6 +265,9 @@ __global__ void k_residual(Lev<XT> L, KState* st, int ns, const cplx<XT>* __rest
 // residuals, Sleijpen & van der Vorst 1996).  Convergence is decided on the
 // FP64 residual only.
 enum { ST_VCONV = 5 };
+// a system masked out of this solve (already finished, or handed elsewhere):
+// never reactivated, never updated
+enum { ST_SKIP = 6 };
 
 // systems whose complex64 recurrence converged become active again until the
 // FP64 residual confirms it

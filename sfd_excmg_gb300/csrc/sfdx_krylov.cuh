@@ -15,14 +15,12 @@ namespace sfdx {
 template <class T, int VS, int O, int PP, int MODE>
 static void fwd_one(Plan& P, const Level& LV, const VCfg& c, cplx<T>* w, cplx<T>* q, const cplx<T>* r, const cplx<T>* v) {
     const uint32_t W = mcolour_count(LV.mesh, O) * c.sg.G;
-    KL(k_fwd_v<T, VS, O, PP, MODE><<<grid_for(W, c.B, 16), c.B, 0, P.st>>>(LV.lev<T>(), LV.mesh, c.sg,
-                                                                           P.d_state.as<KState>(), w, q, r, v));
+    vlaunch(k_fwd_v<T, VS, O, PP, MODE>, W, c.B, 0, P.st, LV.lev<T>(), LV.mesh, c.sg, P.d_state.as<KState>(), w, q, r, v);
 }
 template <class T, int VS, int O, int PP>
 static void bwd_one(Plan& P, const Level& LV, const VCfg& c, cplx<T>* x) {
     const uint32_t W = mcolour_count(LV.mesh, O) * c.sg.G;
-    KL(k_bwd_v<T, VS, O, PP><<<grid_for(W, c.B, 16), c.B, 0, P.st>>>(LV.lev<T>(), LV.mesh, c.sg, P.d_state.as<KState>(),
-                                                                     x));
+    vlaunch(k_bwd_v<T, VS, O, PP>, W, c.B, 0, P.st, LV.lev<T>(), LV.mesh, c.sg, P.d_state.as<KState>(), x);
 }
 
 // out = M^{-1} rhs where rhs is produced by MODE (see k_fwd_v).  Multi-colour
@@ -36,7 +34,7 @@ static void precond(Plan& P, const Level& LV, cplx<T>* out, cplx<T>* q, const cp
                                                                             q, r, v));
         return;
     }
-    const VCfg c = vcfg(P, LV.nl, 0);
+    const VCfg c = vcfg(P, LV.nl, 0, VS);
     fwd_one<T, VS, OX, 0, MODE>(P, LV, c, out, q, r, v);
     fwd_one<T, VS, OX, 1, MODE>(P, LV, c, out, q, r, v);
     fwd_one<T, VS, OY, 0, MODE>(P, LV, c, out, q, r, v);
@@ -60,14 +58,14 @@ static void init_states(Plan& P, const double* tols_host, double tol, int itmax,
         S.tol = tols_host ? tols_host[q] : tol;
         S.itmax = itmax;
         S.active = mask_host ? mask_host[q] : 1;
-        S.status = S.active ? ST_RUN : ST_CONV;
+        S.status = S.active ? ST_RUN : ST_SKIP;
         init[q] = S;
     }
 }
 
 // partial sums of the reducing kernels of one level (nq per system)
-static int reserve_partials(Plan& P, const VCfg& c, int nq) {
-    return P.d_part.alloc(std::max(P.d_part.bytes, (size_t)c.grid * nq * P.ns * sizeof(double2)));
+static int reserve_partials(Plan& P, const VCfg&, int nq) {
+    return P.d_part.alloc(std::max(P.d_part.bytes, (size_t)max_resident_blocks() * nq * P.ns * sizeof(double2)));
 }
 
 // FP64 residual replacement for the systems still running or whose complex64
@@ -75,14 +73,15 @@ static int reserve_partials(Plan& P, const VCfg& c, int nq) {
 template <class T, int VS>
 static int reliable_update(Plan& P, const Level& LV, const Reliable& rel, cplx<T>* x32, cplx<T>* r, const cplx<T>* rhat,
                            int solver, int& active) {
+    constexpr int VSD = VS > 2 ? 2 : VS;  // systems per thread of the FP64 residual
     const int ns = P.ns;
-    const VCfg c = vcfg(P, LV.nl, 2);
-    RC(reserve_partials(P, c, 2));
+    const VCfg c = vcfg(P, LV.nl, 2, VS);
+    const VCfg cd = vcfg(P, LV.nl, 2, VSD);
+    RC(reserve_partials(P, cd, 2));
     KState* dst = P.d_state.as<KState>();
     KL(k_reactivate<<<(ns + 127) / 128, 128, 0, P.st>>>(dst, ns));
-    KL(k_flush_v<T, VS><<<grid_for(LV.nl * c.sg.G, c.B, 16), c.B, 0, P.st>>>(LV.mesh, c.sg, dst, rel.x64, x32, rel.xb));
-    KL(k_reliable_v<T, VS><<<c.grid, c.B, c.smem, P.st>>>(LV.lev<double>(), LV.mesh, c.sg, dst, rel.b64, rel.x64, r, rhat,
-                                                           solver, redbuf(P)));
+    vlaunch(k_flush_v<T, VS, false>, LV.nl * c.sg.G, c.B, 0, P.st, LV.mesh, c.sg, dst, rel.x64, x32, rel.xb);
+    vlaunch(k_reliable_v<T, VSD>, LV.nl * cd.sg.G, cd.B, cd.smem, P.st, LV.lev<double>(), LV.mesh, cd.sg, dst, rel.b64, rel.x64, r, rhat, solver, redbuf(P));
     CK(cudaGetLastError());
     RC(sync_state(P));
     active = 0;
@@ -123,16 +122,17 @@ static int bicgstab_v(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, co
     std::vector<KState> init;
     init_states(P, tols_host, tol, itmax, mask_host, init);
     CK(cudaMemcpyAsync(P.d_state.p, init.data(), sizeof(KState) * ns, cudaMemcpyHostToDevice, P.st));
-    const VCfg c = vcfg(P, LV.nl, 2);
+    constexpr int VSD = VS > 2 ? 2 : VS;  // systems per thread of FP64 residuals
+    const VCfg c = vcfg(P, LV.nl, 2, VS);
+    const VCfg cd = vcfg(P, LV.nl, 2, VSD);
     RC(reserve_partials(P, c, 2));
+    RC(reserve_partials(P, cd, 2));
     KState* dst = P.d_state.as<KState>();
     if (rel) {
         CK(cudaMemsetAsync(x, 0, vb, P.st));
-        KL(k_residual_v<T, double, VS, 0><<<c.grid, c.B, c.smem, P.st>>>(LV.lev<double>(), M, c.sg, dst, rel->b64, rel->x64,
-                                                                          r, rhat, redbuf(P), P.hist, P.hist_stride));
+        vlaunch(k_residual_v<T, double, VSD, 0>, LV.nl * cd.sg.G, cd.B, cd.smem, P.st, LV.lev<double>(), M, cd.sg, dst, rel->b64, rel->x64, r, rhat, redbuf(P), P.hist, P.hist_stride);
     } else {
-        KL(k_residual_v<T, T, VS, 0><<<c.grid, c.B, c.smem, P.st>>>(L, M, c.sg, dst, b, x, r, rhat, redbuf(P), P.hist,
-                                                                     P.hist_stride));
+        vlaunch(k_residual_v<T, T, VS, 0>, LV.nl * c.sg.G, c.B, c.smem, P.st, L, M, c.sg, dst, b, x, r, rhat, redbuf(P), P.hist, P.hist_stride);
     }
     CK(cudaGetLastError());
     const int check_every = 8;
@@ -140,17 +140,15 @@ static int bicgstab_v(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, co
     for (int it = 1; it <= itmax; it++) {
         // top of iteration `it` (solvers.f90:630-640): divergence correction and
         // residual restart every corr_intv iterations (FP64 solves only)
-        if (!rel && std::is_same<T, double>::value && P.o.div_cor && it % P.o.corr_intv == 0) {
+        if (!rel && std::is_same<T, double>::value && P.o.div_cor == 1 && it % P.o.corr_intv == 0) {
             RC(div_correct(P, LV, reinterpret_cast<double2*>(x)));
-            KL(k_residual_v<T, T, VS, 1><<<c.grid, c.B, c.smem, P.st>>>(L, M, c.sg, dst, b, x, r, rhat, redbuf(P), nullptr,
-                                                                         0));
+            vlaunch(k_residual_v<T, T, VS, 1>, LV.nl * c.sg.G, c.B, c.smem, P.st, L, M, c.sg, dst, b, x, r, rhat, redbuf(P), nullptr, 0);
         }
         precond<T, VS, RHS_PUPD>(P, LV, y, p, r, v);
-        KL(k_bicg_v_v<T, VS><<<c.grid, c.B, c.smem, P.st>>>(L, M, c.sg, dst, y, v, rhat, redbuf(P)));
+        vlaunch(k_bicg_v_v<T, VS>, LV.nl * c.sg.G, c.B, c.smem, P.st, L, M, c.sg, dst, y, v, rhat, redbuf(P));
         precond<T, VS, RHS_SUPD>(P, LV, z, s, r, v);
-        KL(k_bicg_t_v<T, VS><<<c.grid, c.B, c.smem, P.st>>>(L, M, c.sg, dst, z, t, s, redbuf(P)));
-        KL(k_bicg_upd_v<T, T, VS><<<c.grid, c.B, c.smem, P.st>>>(M, c.sg, dst, x, y, z, s, t, r, rhat, redbuf(P), P.hist,
-                                                                  P.hist_stride));
+        vlaunch(k_bicg_t_v<T, VS>, LV.nl * c.sg.G, c.B, c.smem, P.st, L, M, c.sg, dst, z, t, s, redbuf(P));
+        vlaunch(k_bicg_upd_v<T, T, VS>, LV.nl * c.sg.G, c.B, c.smem, P.st, M, c.sg, dst, x, y, z, s, t, r, rhat, redbuf(P), P.hist, P.hist_stride);
         if (it % check_every == 0 || it == itmax) {
             CK(cudaGetLastError());
             RC(sync_state(P));
@@ -159,7 +157,7 @@ static int bicgstab_v(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, co
                 act += P.hst[q].active;
                 cand += P.hst[q].status == ST_CONV;
             }
-            if (rel && (cand || it - last_rel >= rel->every || it == itmax)) {
+            if (rel && (cand || (act && (it - last_rel >= rel->every || it == itmax)))) {
                 RC((reliable_update<T, VS>(P, LV, *rel, x, r, rhat, 1, act)));
                 last_rel = it;
             }
@@ -167,7 +165,7 @@ static int bicgstab_v(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, co
         }
     }
     if (rel)
-        KL(k_flush_v<T, VS><<<grid_for(LV.nl * c.sg.G, c.B, 16), c.B, 0, P.st>>>(M, c.sg, dst, rel->x64, x, nullptr));
+        vlaunch(k_flush_v<T, VS, true>, LV.nl * c.sg.G, c.B, 0, P.st, M, c.sg, dst, rel->x64, x, nullptr);
     RC(sync_state(P));
     return SFDX_OK;
 }
@@ -191,34 +189,34 @@ static int gpbicg_v(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, cons
     std::vector<KState> init;
     init_states(P, tols_host, tol, itmax, mask_host, init);
     CK(cudaMemcpyAsync(P.d_state.p, init.data(), sizeof(KState) * ns, cudaMemcpyHostToDevice, P.st));
-    const VCfg c = vcfg(P, LV.nl, 4);
+    constexpr int VSD = VS > 2 ? 2 : VS;  // systems per thread of FP64 residuals
+    const VCfg c = vcfg(P, LV.nl, 4, VS);
+    const VCfg cd = vcfg(P, LV.nl, 2, VSD);
     RC(reserve_partials(P, c, 4));
+    RC(reserve_partials(P, cd, 2));
     const int Ge = grid_for(LV.nl * c.sg.G, c.B, 16);
     KState* dst = P.d_state.as<KState>();
     if (rel) {
         CK(cudaMemsetAsync(x, 0, vb, P.st));
-        KL(k_residual_v<T, double, VS, 3><<<c.grid, c.B, c.smem, P.st>>>(LV.lev<double>(), M, c.sg, dst, rel->b64, rel->x64,
-                                                                          r, r0, redbuf(P), nullptr, 0));
+        vlaunch(k_residual_v<T, double, VSD, 3>, LV.nl * cd.sg.G, cd.B, cd.smem, P.st, LV.lev<double>(), M, cd.sg, dst, rel->b64, rel->x64, r, r0, redbuf(P), nullptr, 0);
     } else {
-        KL(k_residual_v<T, T, VS, 3><<<c.grid, c.B, c.smem, P.st>>>(L, M, c.sg, dst, b, x, r, r0, redbuf(P), nullptr, 0));
+        vlaunch(k_residual_v<T, T, VS, 3>, LV.nl * c.sg.G, c.B, c.smem, P.st, L, M, c.sg, dst, b, x, r, r0, redbuf(P), nullptr, 0);
     }
     precond<T, VS, RHS_VEC>(P, LV, rp, r, nullptr, nullptr);
     CK(cudaMemcpyAsync(p, rp, vb, cudaMemcpyDeviceToDevice, P.st));
     int cur = 0, last_rel = 0;
     for (int it = 1; it <= itmax; it++) {
-        if (!rel && std::is_same<T, double>::value && P.o.div_cor && it % P.o.corr_intv == 0) {
+        if (!rel && std::is_same<T, double>::value && P.o.div_cor == 1 && it % P.o.corr_intv == 0) {
             // solvers.f90:223-235: correct x, restart r and r0 (rp is kept)
             RC(div_correct(P, LV, reinterpret_cast<double2*>(x)));
-            KL(k_residual_v<T, T, VS, 4><<<c.grid, c.B, c.smem, P.st>>>(L, M, c.sg, dst, b, x, r, r0, redbuf(P), nullptr,
-                                                                         0));
+            vlaunch(k_residual_v<T, T, VS, 4>, LV.nl * c.sg.G, c.B, c.smem, P.st, L, M, c.sg, dst, b, x, r, r0, redbuf(P), nullptr, 0);
         }
-        KL(k_gp_ap_v<T, VS><<<c.grid, c.B, c.smem, P.st>>>(L, M, c.sg, dst, p, ap, r0, r, redbuf(P)));
-        KL(k_gp_yt_v<T, VS><<<Ge, c.B, 0, P.st>>>(M, c.sg, dst, y, t, r, w, ap));
+        vlaunch(k_gp_ap_v<T, VS>, LV.nl * c.sg.G, c.B, c.smem, P.st, L, M, c.sg, dst, p, ap, r0, r, redbuf(P));
+        vlaunch(k_gp_yt_v<T, VS>, LV.nl * c.sg.G, c.B, 0, P.st, M, c.sg, dst, y, t, r, w, ap);
         precond<T, VS, RHS_VEC>(P, LV, tmp, ap, nullptr, nullptr);
-        KL(k_gp_tp_v<T, VS><<<Ge, c.B, 0, P.st>>>(M, c.sg, dst, tp[cur], rp, tmp));
-        KL(k_gp_at_v<T, VS><<<c.grid, c.B, c.smem, P.st>>>(L, M, c.sg, dst, tp[cur], at, t, y, redbuf(P)));
-        KL(k_gp_upd_v<T, T, VS><<<c.grid, c.B, c.smem, P.st>>>(M, c.sg, dst, u, z, x, r, tmp, tp[cur ^ 1], rp, p, t, y, at,
-                                                                r0, redbuf(P), P.hist, P.hist_stride));
+        vlaunch(k_gp_tp_v<T, VS>, LV.nl * c.sg.G, c.B, 0, P.st, M, c.sg, dst, tp[cur], rp, tmp);
+        vlaunch(k_gp_at_v<T, VS>, LV.nl * c.sg.G, c.B, c.smem, P.st, L, M, c.sg, dst, tp[cur], at, t, y, redbuf(P));
+        vlaunch(k_gp_upd_v<T, T, VS>, LV.nl * c.sg.G, c.B, c.smem, P.st, M, c.sg, dst, u, z, x, r, tmp, tp[cur ^ 1], rp, p, t, y, at, r0, redbuf(P), P.hist, P.hist_stride);
         bool stop = false;
         if (it % 8 == 0 || it == itmax) {
             CK(cudaGetLastError());
@@ -228,7 +226,7 @@ static int gpbicg_v(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, cons
                 act += P.hst[q].active;
                 cand += P.hst[q].status == ST_CONV;
             }
-            if (rel && (cand || it - last_rel >= rel->every || it == itmax)) {
+            if (rel && (cand || (act && (it - last_rel >= rel->every || it == itmax)))) {
                 RC((reliable_update<T, VS>(P, LV, *rel, x, r, r0, 3, act)));
                 last_rel = it;
             }
@@ -236,11 +234,79 @@ static int gpbicg_v(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, cons
         }
         if (stop) break;
         precond<T, VS, RHS_VEC>(P, LV, rp, r, nullptr, nullptr);
-        KL(k_gp_pw_v<T, VS><<<Ge, c.B, 0, P.st>>>(M, c.sg, dst, w, p, at, ap, rp, u));
+        vlaunch(k_gp_pw_v<T, VS>, LV.nl * c.sg.G, c.B, 0, P.st, M, c.sg, dst, w, p, at, ap, rp, u);
         cur ^= 1;
     }
-    if (rel) KL(k_flush_v<T, VS><<<Ge, c.B, 0, P.st>>>(M, c.sg, dst, rel->x64, x, nullptr));
+    if (rel) vlaunch(k_flush_v<T, VS, true>, LV.nl * c.sg.G, c.B, 0, P.st, M, c.sg, dst, rel->x64, x, nullptr);
     RC(sync_state(P));
+    return SFDX_OK;
+}
+
+// ------------------------------------------------------------------ corrected restart cycles
+// div_cor = 2: the Krylov solve runs in cycles of corr_intv iterations; before
+// every cycle and after the last one the FP64 iterate gets the consistent
+// gradient-space correction (sfdx_gradcorr.cuh), and each cycle restarts the
+// Krylov recurrences from the corrected iterate.  `run(itmax_cycle, mask)` is
+// one Krylov solve from the current iterate; per-system iteration counts
+// and statuses over all cycles are left in P.hst.
+template <class T, class F>
+static int corrected_cycles(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, int itmax, const int* mask_host,
+                            const Reliable* rel, F run) {
+    const int ns = P.ns;
+    const double2* b64 = rel ? rel->b64 : reinterpret_cast<const double2*>(b);
+    double2* x64 = rel ? rel->x64 : reinterpret_cast<double2*>(x);
+    std::vector<int> mask(ns), part(ns), used(ns, 0), fin(ns, ST_CONV);
+    for (int q = 0; q < ns; q++) part[q] = mask[q] = mask_host ? (mask_host[q] != 0) : 1;
+    const int cyc = P.o.corr_intv > 0 ? P.o.corr_intv : 25;
+    const int gc_maxit = 2000;  // pcg itmax (div_correc.f90:57)
+    for (;;) {
+        int gc_its = 0;
+        RC(grad_correct(P, LV, b64, x64, mask.data(), P.o.corr_tol, gc_maxit, &gc_its));
+        int room = 0;
+        for (int q = 0; q < ns; q++)
+            if (mask[q]) room = std::max(room, itmax - used[q]);
+        RC(run(std::min(cyc, room), mask.data()));
+        if (P.o.verbose || getenv("SFDX_VERBOSE")) {
+            double emin = 1e300, emax = 0;
+            int cnt[6] = {0, 0, 0, 0, 0, 0};
+            for (int q = 0; q < ns; q++) {
+                if (!mask[q]) continue;
+                emin = std::min(emin, P.hst[q].err);
+                emax = std::max(emax, P.hst[q].err);
+                if (P.hst[q].status >= 0 && P.hst[q].status < 6) cnt[P.hst[q].status]++;
+            }
+            fprintf(stderr,
+                    "sfdx:   cycle (%s, %d its, nodal pcg %d): err %.2e..%.2e  run %d conv %d maxit %d nan %d break %d "
+                    "vconv %d\n",
+                    rel ? "mixed" : "fp64", std::min(cyc, room), gc_its, emin, emax, cnt[0], cnt[1], cnt[2], cnt[3],
+                    cnt[4], cnt[5]);
+        }
+        int left = 0;
+        for (int q = 0; q < ns; q++) {
+            if (!mask[q]) continue;
+            const int st = P.hst[q].status;
+            used[q] += std::max(1, P.hst[q].iters);
+            if (st == ST_CONV || st == ST_VCONV || st == ST_NAN || (st == ST_BREAK && rel)) {
+                mask[q] = 0;  // converged, failed, or handed to the caller's FP64 finish
+                fin[q] = st;
+            } else if (used[q] >= itmax) {
+                mask[q] = 0;
+                fin[q] = ST_MAXIT;
+            } else {
+                left++;  // cycle limit reached (or an FP64 breakdown): restart
+            }
+        }
+        if (!left) break;
+    }
+    std::vector<int> last(ns);
+    for (int q = 0; q < ns; q++) last[q] = part[q] && fin[q] != ST_NAN && !(fin[q] == ST_BREAK && rel);
+    RC(grad_correct(P, LV, b64, x64, last.data(), P.o.corr_tol, gc_maxit, nullptr));
+    P.hst.resize(ns);
+    for (int q = 0; q < ns; q++) {
+        if (!part[q]) continue;
+        P.hst[q].iters = used[q];
+        P.hst[q].status = fin[q];
+    }
     return SFDX_OK;
 }
 
@@ -248,23 +314,33 @@ static int gpbicg_v(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, cons
 template <class T>
 int bicgstab(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, const double* tols_host, double tol, int itmax,
              const int* mask_host, const Reliable* rel) {
-    switch (vs_for(P.ns)) {
-        case 4: return bicgstab_v<T, 4>(P, LV, b, x, tols_host, tol, itmax, mask_host, rel);
-        case 2: return bicgstab_v<T, 2>(P, LV, b, x, tols_host, tol, itmax, mask_host, rel);
-        default: return bicgstab_v<T, 1>(P, LV, b, x, tols_host, tol, itmax, mask_host, rel);
-    }
+    auto run = [&](int itc, const int* m) -> int {
+        switch (plan_vs<T>(P)) {
+            case 4: return bicgstab_v<T, 4>(P, LV, b, x, tols_host, tol, itc, m, rel);
+            case 2: return bicgstab_v<T, 2>(P, LV, b, x, tols_host, tol, itc, m, rel);
+            default: return bicgstab_v<T, 1>(P, LV, b, x, tols_host, tol, itc, m, rel);
+        }
+    };
+    if (P.o.div_cor == 2 && (rel || std::is_same<T, double>::value))
+        return corrected_cycles<T>(P, LV, b, x, itmax, mask_host, rel, run);
+    return run(itmax, mask_host);
 }
 template <class T>
 int gpbicg(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, const double* tols_host, double tol, int itmax,
            const int* mask_host, const Reliable* rel) {
-    switch (vs_for(P.ns)) {
-        case 4: return gpbicg_v<T, 4>(P, LV, b, x, tols_host, tol, itmax, mask_host, rel);
-        case 2: return gpbicg_v<T, 2>(P, LV, b, x, tols_host, tol, itmax, mask_host, rel);
-        default: return gpbicg_v<T, 1>(P, LV, b, x, tols_host, tol, itmax, mask_host, rel);
-    }
+    auto run = [&](int itc, const int* m) -> int {
+        switch (plan_vs<T>(P)) {
+            case 4: return gpbicg_v<T, 4>(P, LV, b, x, tols_host, tol, itc, m, rel);
+            case 2: return gpbicg_v<T, 2>(P, LV, b, x, tols_host, tol, itc, m, rel);
+            default: return gpbicg_v<T, 1>(P, LV, b, x, tols_host, tol, itc, m, rel);
+        }
+    };
+    if (P.o.div_cor == 2 && (rel || std::is_same<T, double>::value))
+        return corrected_cycles<T>(P, LV, b, x, itmax, mask_host, rel, run);
+    return run(itmax, mask_host);
 }
 template <class T> int precond_vec(Plan& P, const Level& LV, cplx<T>* out, cplx<T>* q) {
-    switch (vs_for(P.ns)) {
+    switch (plan_vs<T>(P)) {
         case 4: precond<T, 4, RHS_VEC>(P, LV, out, q, nullptr, nullptr); break;
         case 2: precond<T, 2, RHS_VEC>(P, LV, out, q, nullptr, nullptr); break;
         default: precond<T, 1, RHS_VEC>(P, LV, out, q, nullptr, nullptr); break;
@@ -273,12 +349,12 @@ template <class T> int precond_vec(Plan& P, const Level& LV, cplx<T>* out, cplx<
     return SFDX_OK;
 }
 template <class T> int apply_op(Plan& P, const Level& LV, const cplx<T>* x, cplx<T>* y) {
-    const VCfg c = vcfg(P, LV.nl, 0, 16);
+    const VCfg c = vcfg(P, LV.nl, 0, plan_vs<T>(P), 16);
     const double* wm = P.d_wm.as<double>();
     switch (c.VS) {
-        case 4: KL(k_apply_v<T, 4><<<c.grid, c.B, 0, P.st>>>(LV.lev<T>(), LV.mesh, c.sg, wm, x, y)); break;
-        case 2: KL(k_apply_v<T, 2><<<c.grid, c.B, 0, P.st>>>(LV.lev<T>(), LV.mesh, c.sg, wm, x, y)); break;
-        default: KL(k_apply_v<T, 1><<<c.grid, c.B, 0, P.st>>>(LV.lev<T>(), LV.mesh, c.sg, wm, x, y)); break;
+        case 4: vlaunch(k_apply_v<T, 4>, LV.nl * c.sg.G, c.B, 0, P.st, LV.lev<T>(), LV.mesh, c.sg, wm, x, y); break;
+        case 2: vlaunch(k_apply_v<T, 2>, LV.nl * c.sg.G, c.B, 0, P.st, LV.lev<T>(), LV.mesh, c.sg, wm, x, y); break;
+        default: vlaunch(k_apply_v<T, 1>, LV.nl * c.sg.G, c.B, 0, P.st, LV.lev<T>(), LV.mesh, c.sg, wm, x, y); break;
     }
     CK(cudaGetLastError());
     return SFDX_OK;

@@ -6,6 +6,9 @@
 
 #include <atomic>
 #include <cstdio>
+#include <map>
+#include <mutex>
+#include <tuple>
 #include <cstdlib>
 #include <cstring>
 #include <type_traits>
@@ -63,8 +66,48 @@ inline int grid_for(int64_t work, int B, int per_sm = 8) {
     if (g < 1) g = 1;
     return (int)g;
 }
-// systems per thread of the hot kernels
-inline int vs_for(int ns) { return ns % 4 == 0 ? 4 : (ns % 2 == 0 ? 2 : 1); }
+// Grid of a grid-stride kernel: the blocks that can be resident at once (one
+// wave), capped by the work.  With one wave every block walks the domain in
+// step with the others, so the neighbour data of a plane is fetched from DRAM
+// about once; a second wave of blocks would sweep the domain again.
+inline int resident_grid(const void* fn, int B, size_t smem, int64_t work) {
+    static std::mutex mu;
+    static std::map<std::tuple<const void*, int, size_t>, int> cache;
+    int per = 0;
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        auto key = std::make_tuple(fn, B, smem);
+        auto it = cache.find(key);
+        if (it != cache.end()) {
+            per = it->second;
+        } else {
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, B, smem) != cudaSuccess || per < 1) per = 1;
+            cache[key] = per;
+        }
+    }
+    int64_t g = (work + B - 1) / B;
+    const int64_t cap = (int64_t)per * device_sms();
+    if (g > cap) g = cap;
+    if (g < 1) g = 1;
+    return (int)g;
+}
+// most blocks resident_grid() returns (sizes the per-block partial sums)
+inline int64_t max_resident_blocks() { return (int64_t)device_sms() * 32; }
+
+template <class... KA, class... A>
+inline void vlaunch(void (*k)(KA...), int64_t work, int B, size_t smem, cudaStream_t st, A... args) {
+    const int g = resident_grid((const void*)k, B, smem, work);
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+    k<<<g, B, smem, st>>>(args...);
+}
+
+// systems per thread of the hot kernels: the largest of 4, 2, 1 that is at
+// most `want` and divides ns
+inline int vs_pick(int ns, int want) {
+    if (want >= 4 && ns % 4 == 0) return 4;
+    if (want >= 2 && ns % 2 == 0) return 2;
+    return 1;
+}
 // block of the system-group kernels: G * 2^k >= 128
 inline int vblock(int G) {
     int b = G;
@@ -123,6 +166,11 @@ struct Level {
     DBuf crd_cubic;        // node coordinates used by cubic_interp on this level
     DBuf crd_quad;         // node coordinates used by quad_interp_e (pairwise sums of a,b,c)
     int stride = 0;
+    // assembled nodal operator of the gradient-space correction (27-point
+    // stencil, float) and its inverse diagonal; rebuilt after the conductivity
+    // of the level changes
+    mutable DBuf gc_coef, gc_dinv;
+    mutable bool gc_ok = false;
 
     void set_dims(int X, int Y, int Z) {
         nx = X; ny = Y; nz = Z;
@@ -163,6 +211,10 @@ struct Plan {
     // divergence correction: t, r, p, v, phi (nodes) and the PCG state
     DBuf dcv[5], d_pst;
     int dc_calls = 0, dc_last_iters = 0;
+    // consistent gradient correction: node vectors phi, r, z, p, q of the
+    // nodal PCG; edge vectors of the probing that assembles the nodal operator
+    DBuf gcn[5], gce[2];
+    long long gc_calls = 0, gc_iters = 0;
     DBuf errrec;
     int edc_stride = 0;
     double* hist = nullptr;  // optional device residual history [ns][hist_stride]
@@ -172,6 +224,9 @@ struct Plan {
     std::vector<double> relres;    // [nf][2]
     std::vector<KState> hst;
     bool have_solution = false;
+    // systems per thread of the complex64 / complex128 hot kernels (upper
+    // bounds; sfdx_plan_autotune measures and sets them)
+    int vs32 = 4, vs64 = 2;
     Plan() = default;
     Plan(const Plan&) = delete;
     ~Plan() {
@@ -200,9 +255,10 @@ struct VCfg {
     size_t smem;
     SysG sg;
 };
-inline VCfg vcfg(const Plan& P, int64_t nl, int nq, int per_sm = 8) {
+template <class T> inline int plan_vs(const Plan& P) { return vs_pick(P.ns, sizeof(T) == 4 ? P.vs32 : P.vs64); }
+inline VCfg vcfg(const Plan& P, int64_t nl, int nq, int VS, int per_sm = 8) {
     VCfg c;
-    c.VS = vs_for(P.ns);
+    c.VS = VS;
     c.sg = make_sysg(P.ns, c.VS);
     c.B = vblock(c.sg.G);
     c.grid = grid_for(nl * c.sg.G, c.B, per_sm);
@@ -233,5 +289,12 @@ template <class T> int apply_op(Plan& P, const Level& LV, const cplx<T>* x, cplx
 
 // ------------------------------------------------------------------ sfdx_solver.cu
 int div_correct(Plan& P, const Level& LV, double2* x);
+
+// ------------------------------------------------------------------ sfdx_gradcorr.cu
+// x += G phi with (G^T V Ms G) phi = G^T V (b - A x) / (-i w mu) for the systems
+// with mask[s] != 0 (all when mask is null); nodal PCG to relative tolerance
+// `tol`, at most `maxit` iterations (*iters: the most any system took).
+int grad_correct(Plan& P, const Level& LV, const double2* b, double2* x, const int* mask, double tol, int maxit,
+                 int* iters);
 
 }  // namespace sfdx

@@ -251,7 +251,7 @@ static int solve_level_mixed(Plan& P, const Level& LV, double tol, int itmax, st
     if (nleft) {
         std::vector<int> its64, st64;
         const int save = P.o.div_cor;
-        P.o.div_cor = 0;  // the FP64 finish is a continuation, not a reference restart
+        if (save == 1) P.o.div_cor = 0;  // the FP64 finish is a continuation, not a reference restart
         int rc;
         if (P.o.solver == SFDX_SOLVER_GPBICG)
             rc = gpbicg<double>(P, LV, P.b64.as<double2>(), P.x64.as<double2>(), nullptr, tol, itmax - used_max,
@@ -355,6 +355,7 @@ static int set_conductivity(Plan& P, const double* sigma, bool on_device) {
     }
     for (int l = 0; l < P.nlev; l++) {
         Level& L = P.lev[l];
+        L.gc_ok = false;
         RC(L.sig32.alloc((size_t)6 * L.ncell * sizeof(float)));
         // sigma is real: convert pairs as if complex (6*ncell is even)
         int64_t n2 = 3 * L.ncell;
@@ -506,6 +507,8 @@ static int validate_opts(const sfdx_opts& o) {
     if (o.excmg && o.level < 3) return SFDX_ERR_ARG;
     if (o.precond != 'S' && o.precond != 'J') return SFDX_ERR_ARG;
     if (o.precision != SFDX_FP64 && o.precision != SFDX_MIXED) return SFDX_ERR_ARG;
+    if (o.div_cor < 0 || o.div_cor > 2) return SFDX_ERR_ARG;
+    if (o.div_cor == 2 && (o.corr_intv < 1 || !(o.corr_tol > 0))) return SFDX_ERR_ARG;
     if (o.solver != SFDX_SOLVER_BICGSTAB && o.solver != SFDX_SOLVER_GPBICG && o.solver != SFDX_SOLVER_TFQMR &&
         o.solver != SFDX_SOLVER_BICG && o.solver != SFDX_SOLVER_COCR)
         return SFDX_ERR_ARG;
@@ -739,6 +742,66 @@ extern "C" int sfdx_plan_kernel_time(sfdx_plan* plan, int kernel, int reps, doub
     double b1 = (double)F.nl * ns * 4 * p + (double)F.ncell * 6 * p;
     if (kernel == 2 || kernel == 3) b1 *= 2;  // forward + backward sweep
     if (bytes) *bytes = b1;
+    return SFDX_OK;
+}
+
+// Pick the systems-per-thread grouping of the complex64 and complex128 hot
+// kernels by timing one operator application plus one multi-colour SSOR
+// application per candidate on the finest level.
+extern "C" int sfdx_plan_autotune(sfdx_plan* plan, int reps, int* vs32, int* vs64) {
+    if (!plan || reps < 1) return SFDX_ERR_ARG;
+    Plan& P = plan->P;
+    const Level& F = P.lev[P.nlev - 1];
+    if (!F.sig64.p) return SFDX_ERR_ARG;  // conductivity not loaded yet
+    const int ns = P.ns;
+    const size_t n = (size_t)F.nl * ns;
+    for (int q = 0; q < 3; q++) RC(P.kv[q].alloc(n * 16));
+    std::vector<KState> init(ns);
+    for (int q = 0; q < ns; q++) {
+        memset(&init[q], 0, sizeof(KState));
+        init[q].wm = P.wm[q];
+        init[q].active = 1;
+    }
+    CK(cudaMemcpyAsync(P.d_state.p, init.data(), sizeof(KState) * ns, cudaMemcpyHostToDevice, P.st));
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    int best[2] = {P.vs32, P.vs64};
+    for (int prec = 0; prec < 2; prec++) {
+        double tbest = 1e300;
+        for (int cand : {4, 2, 1}) {
+            if (vs_pick(ns, cand) != cand) continue;
+            int& slot = prec == 0 ? P.vs32 : P.vs64;
+            slot = cand;
+            float t = 0;
+            for (int r = 0; r <= reps; r++) {  // first pass warms up
+                if (r == 1) CK(cudaEventRecord(e0, P.st));
+                if (prec == 0) {
+                    RC(apply_op<float>(P, F, P.kv[0].as<float2>(), P.kv[1].as<float2>()));
+                    RC(precond_vec<float>(P, F, P.kv[2].as<float2>(), P.kv[1].as<float2>()));
+                } else {
+                    RC(apply_op<double>(P, F, P.kv[0].as<double2>(), P.kv[1].as<double2>()));
+                    RC(precond_vec<double>(P, F, P.kv[2].as<double2>(), P.kv[1].as<double2>()));
+                }
+            }
+            CK(cudaEventRecord(e1, P.st));
+            CK(cudaEventSynchronize(e1));
+            CK(cudaEventElapsedTime(&t, e0, e1));
+            if (t < tbest) {
+                tbest = t;
+                best[prec] = cand;
+            }
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    P.vs32 = best[0];
+    P.vs64 = best[1];
+    if (vs32) *vs32 = vs_pick(ns, P.vs32);
+    if (vs64) *vs64 = vs_pick(ns, P.vs64);
+    if (P.o.verbose || getenv("SFDX_VERBOSE"))
+        fprintf(stderr, "sfdx: autotune: %d systems per thread (complex64), %d (complex128)\n", vs_pick(ns, P.vs32),
+                vs_pick(ns, P.vs64));
     return SFDX_OK;
 }
 
@@ -1076,5 +1139,26 @@ extern "C" int sfdx_div_correct(int nx, int ny, int nz, const double* a, const d
     CK(cudaMemcpyAsync(x, P.x64.p, n * 16, cudaMemcpyDeviceToHost, P.st));
     CK(cudaStreamSynchronize(P.st));
     if (pcg_iters) *pcg_iters = P.dc_last_iters;
+    return SFDX_OK;
+}
+
+extern "C" int sfdx_grad_correct(int nx, int ny, int nz, const double* a, const double* b, const double* c,
+                                 const double* sigma, int ns, const double* freqs, const double* rhs, double* x,
+                                 double tol, int maxit, int* pcg_iters) {
+    if (!sigma || !rhs || !x || !(tol > 0) || maxit < 1) return SFDX_ERR_ARG;
+    PlanGuard g;
+    RC(component_plan(&g.p, nullptr, nx, ny, nz, a, b, c, sigma, ns, freqs));
+    Plan& P = g.p->P;
+    const Level& L = P.lev[0];
+    const size_t n = (size_t)L.nl * ns;
+    RC(P.x64.alloc(n * 16));
+    RC(P.b64.alloc(n * 16));
+    CK(cudaMemcpyAsync(P.b64.p, rhs, n * 16, cudaMemcpyHostToDevice, P.st));
+    CK(cudaMemcpyAsync(P.x64.p, x, n * 16, cudaMemcpyHostToDevice, P.st));
+    int it = 0;
+    RC(grad_correct(P, L, P.b64.as<double2>(), P.x64.as<double2>(), nullptr, tol, maxit, &it));
+    CK(cudaMemcpyAsync(x, P.x64.p, n * 16, cudaMemcpyDeviceToHost, P.st));
+    CK(cudaStreamSynchronize(P.st));
+    if (pcg_iters) *pcg_iters = it;
     return SFDX_OK;
 }

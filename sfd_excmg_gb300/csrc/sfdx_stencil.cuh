@@ -43,7 +43,8 @@ __device__ __forceinline__ uint32_t fdiv(const FastDiv& f, uint32_t n) { return 
 struct Mesh {
     int nx, ny, nz;
     uint32_t xnl, ynl, nl;
-    FastDiv fnx, fnx1, fny, fny1, fni2, fnj2;
+    uint32_t sx, sy, sz;  // edges per z-plane: Ex nx(ny+1), Ey (nx+1)ny, Ez (nx+1)(ny+1)
+    FastDiv fnx, fnx1, fny, fny1, fni2, fnj2, fsp;
 };
 inline Mesh make_mesh(int nx, int ny, int nz) {
     Mesh M;
@@ -57,7 +58,42 @@ inline Mesh make_mesh(int nx, int ny, int nz) {
     M.fny1 = make_fastdiv(ny + 1);
     M.fni2 = make_fastdiv((nx + 2) / 2);
     M.fnj2 = make_fastdiv((ny + 2) / 2);
+    M.sx = (uint32_t)nx * (ny + 1);
+    M.sy = (uint32_t)(nx + 1) * ny;
+    M.sz = (uint32_t)(nx + 1) * (ny + 1);
+    M.fsp = make_fastdiv(M.sx + M.sy + M.sz);
     return M;
+}
+
+// Work item w (0 <= w < nl) of the operator-type kernels in plane order:
+// plane k holds Ex(.,.,k), Ey(.,.,k) and Ez(.,.,k) (no Ez on the last plane),
+// so that the neighbours a row reads (planes k-1..k+1, all orientations) were
+// touched moments earlier and are still in L2.  Returns the orientation and
+// sets the edge index e of the reference ordering and (i, j, k).
+__device__ __forceinline__ int mdecode_plane(const Mesh& M, uint32_t w, uint32_t& e, int& i, int& j, int& k) {
+    const uint32_t kk = fdiv(M.fsp, w);
+    uint32_t r = w - kk * M.fsp.d;
+    k = (int)kk;
+    if (r < M.sx) {
+        const uint32_t jj = fdiv(M.fnx, r);
+        i = (int)(r - jj * (uint32_t)M.nx);
+        j = (int)jj;
+        e = kk * M.sx + r;
+        return OX;
+    }
+    r -= M.sx;
+    const uint32_t jj = fdiv(M.fnx1, r < M.sy ? r : r - M.sy);
+    if (r < M.sy) {
+        i = (int)(r - jj * (uint32_t)(M.nx + 1));
+        j = (int)jj;
+        e = M.xnl + kk * M.sy + r;
+        return OY;
+    }
+    r -= M.sy;
+    i = (int)(r - jj * (uint32_t)(M.nx + 1));
+    j = (int)jj;
+    e = M.xnl + M.ynl + kk * M.sz + r;
+    return OZ;
 }
 
 // edge index -> orientation and (i, j, k)
@@ -406,10 +442,9 @@ __device__ __forceinline__ void row_apply_o(const Lev<T>& L, const Mesh& M, uint
     }
 }
 template <class T, int VS>
-__device__ __forceinline__ void row_apply(const Lev<T>& L, const Mesh& M, uint32_t e, const cplx<T>* x, int ns, int s0,
-                                          const T (&wm)[VS], const CV<T, VS>& xe, CV<T, VS>& y) {
-    int i, j, k;
-    const int o = mdecode(M, e, i, j, k);
+__device__ __forceinline__ void row_apply(const Lev<T>& L, const Mesh& M, int o, uint32_t e, int i, int j, int k,
+                                          const cplx<T>* x, int ns, int s0, const T (&wm)[VS], const CV<T, VS>& xe,
+                                          CV<T, VS>& y) {
     if (o == OX)
         row_apply_o<T, VS, OX>(L, M, e, i, j, k, x, ns, s0, wm, xe, y);
     else if (o == OY)

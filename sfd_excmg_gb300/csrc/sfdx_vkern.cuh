@@ -121,11 +121,13 @@ __global__ void k_apply_v(Lev<T> L, Mesh M, SysG sgp, const double* wms, const c
 #pragma unroll
     for (int v = 0; v < VS; v++) wm[v] = (T)wms[s0 + v];
     SFDX_GRID_LOOP(t, M.nl * sgp.G) {
-        const uint32_t e = fdiv(sgp.fG, t);
+        uint32_t e;
+        int i, j, k;
+        const int o = mdecode_plane(M, fdiv(sgp.fG, t), e, i, j, k);
         const size_t g = (size_t)e * ns + s0;
         CV<T, VS> xe, val;
         cvld<T, VS>(xe, x + g);
-        row_apply<T, VS>(L, M, e, x, ns, s0, wm, xe, val);
+        row_apply<T, VS>(L, M, o, e, i, j, k, x, ns, s0, wm, xe, val);
         cvst<T, VS>(y + g, val);
     }
 }
@@ -229,11 +231,13 @@ __global__ void k_residual_v(Lev<XT> L, Mesh M, SysG sgp, KState* st, const cplx
     for (int u = 0; u < VS; u++) acc[0][u] = make_double2(0.0, 0.0);
     if (S.act)
         SFDX_GRID_LOOP(t, M.nl * sgp.G) {
-            const uint32_t e = fdiv(sgp.fG, t);
+            uint32_t e;
+            int i, j, k;
+            const int o = mdecode_plane(M, fdiv(sgp.fG, t), e, i, j, k);
             const size_t g = (size_t)e * ns + s0;
             CV<XT, VS> xe, ax, bv;
             cvld<XT, VS>(xe, x + g);
-            row_apply<XT, VS>(L, M, e, x, ns, s0, S.wm, xe, ax);
+            row_apply<XT, VS>(L, M, o, e, i, j, k, x, ns, s0, S.wm, xe, ax);
             cvld<XT, VS>(bv, bvec + g);
             CV<T, VS> rt;
 #pragma unroll
@@ -316,11 +320,13 @@ __global__ void k_bicg_v_v(Lev<T> L, Mesh M, SysG sgp, KState* st, const cplx<T>
     for (int u = 0; u < VS; u++) ar[u] = ai[u] = 0;
     if (S.act)
         SFDX_GRID_LOOP(t, M.nl * sgp.G) {
-            const uint32_t e = fdiv(sgp.fG, t);
+            uint32_t e;
+            int i, j, k;
+            const int o = mdecode_plane(M, fdiv(sgp.fG, t), e, i, j, k);
             const size_t g = (size_t)e * ns + s0;
             CV<T, VS> ye, val, h;
             cvld<T, VS>(ye, y + g);
-            row_apply<T, VS>(L, M, e, y, ns, s0, S.wm, ye, val);
+            row_apply<T, VS>(L, M, o, e, i, j, k, y, ns, s0, S.wm, ye, val);
             cvst_m<T, VS>(v + g, val, S.act);
             cvld<T, VS>(h, rhat + g);
 #pragma unroll
@@ -361,11 +367,13 @@ __global__ void k_bicg_t_v(Lev<T> L, Mesh M, SysG sgp, KState* st, const cplx<T>
     for (int u = 0; u < VS; u++) a0r[u] = a0i[u] = a1[u] = 0;
     if (S.act)
         SFDX_GRID_LOOP(t, M.nl * sgp.G) {
-            const uint32_t e = fdiv(sgp.fG, t);
+            uint32_t e;
+            int i, j, k;
+            const int o = mdecode_plane(M, fdiv(sgp.fG, t), e, i, j, k);
             const size_t g = (size_t)e * ns + s0;
             CV<T, VS> ze, val, ss;
             cvld<T, VS>(ze, z + g);
-            row_apply<T, VS>(L, M, e, z, ns, s0, S.wm, ze, val);
+            row_apply<T, VS>(L, M, o, e, i, j, k, z, ns, s0, S.wm, ze, val);
             cvst_m<T, VS>(tv + g, val, S.act);
             cvld<T, VS>(ss, sv + g);
 #pragma unroll
@@ -502,11 +510,13 @@ __global__ void k_gp_ap_v(Lev<T> L, Mesh M, SysG sgp, KState* st, const cplx<T>*
     for (int u = 0; u < VS; u++) a0r[u] = a0i[u] = a1r[u] = a1i[u] = 0;
     if (S.act)
         SFDX_GRID_LOOP(t, M.nl * sgp.G) {
-            const uint32_t e = fdiv(sgp.fG, t);
+            uint32_t e;
+            int i, j, k;
+            const int o = mdecode_plane(M, fdiv(sgp.fG, t), e, i, j, k);
             const size_t g = (size_t)e * ns + s0;
             CV<T, VS> pe, val, q0, rr;
             cvld<T, VS>(pe, p + g);
-            row_apply<T, VS>(L, M, e, p, ns, s0, S.wm, pe, val);
+            row_apply<T, VS>(L, M, o, e, i, j, k, p, ns, s0, S.wm, pe, val);
             cvst_m<T, VS>(ap + g, val, S.act);
             cvld<T, VS>(q0, r0 + g);
             cvld<T, VS>(rr, r + g);
@@ -600,11 +610,13 @@ __global__ void k_gp_at_v(Lev<T> L, Mesh M, SysG sgp, KState* st, const cplx<T>*
     for (int u = 0; u < VS; u++) c0r[u] = c0i[u] = c1[u] = c2[u] = c3r[u] = c3i[u] = c4r[u] = c4i[u] = 0;
     if (S.act)
         SFDX_GRID_LOOP(t, M.nl * sgp.G) {
-            const uint32_t e = fdiv(sgp.fG, t);
+            uint32_t e;
+            int i, j, k;
+            const int o = mdecode_plane(M, fdiv(sgp.fG, t), e, i, j, k);
             const size_t g = (size_t)e * ns + s0;
             CV<T, VS> pe, val, tt, yy;
             cvld<T, VS>(pe, tp + g);
-            row_apply<T, VS>(L, M, e, tp, ns, s0, S.wm, pe, val);
+            row_apply<T, VS>(L, M, o, e, i, j, k, tp, ns, s0, S.wm, pe, val);
             cvst_m<T, VS>(at + g, val, S.act);
             cvld<T, VS>(tt, tv + g);
             cvld<T, VS>(yy, y + g);
@@ -794,12 +806,21 @@ __global__ void k_gp_pw_v(Mesh M, SysG sgp, const KState* st, cplx<T>* __restric
 }
 
 // ------------------------------------------------------------------ reliable updates
-// x64 += x32 ; x32 = 0 (active systems; xb keeps x64 before the update)
-template <class T, int VS>
+// x64 += x32 ; x32 = 0 (xb keeps x64 before the update).  ALL = false: the
+// active systems (a reliable update in the middle of a solve); ALL = true:
+// every system without a NaN (the end of a solve, including systems stopped by
+// the iteration limit or a breakdown, whose partial solution would otherwise
+// be lost; systems already flushed hold x32 = 0)
+template <class T, int VS, bool ALL>
 __global__ void k_flush_v(Mesh M, SysG sgp, const KState* st, double2* __restrict__ x64, cplx<T>* __restrict__ x32,
                           double2* __restrict__ xb) {
     const int ns = sgp.ns, s0 = (threadIdx.x % sgp.G) * VS;
-    const SysV<T, VS> S = load_sys<T, VS>(st, s0);
+    SysV<T, VS> S = load_sys<T, VS>(st, s0);
+    if (ALL) {
+        S.act = 0;
+#pragma unroll
+        for (int v = 0; v < VS; v++) S.act |= (st[s0 + v].status != ST_NAN ? 1u : 0u) << v;
+    }
     if (!S.act) return;
     SFDX_GRID_LOOP(t, M.nl * sgp.G) {
         const size_t g = (size_t)fdiv(sgp.fG, t) * ns + s0;
@@ -832,11 +853,13 @@ __global__ void k_reliable_v(Lev<double> L, Mesh M, SysG sgp, KState* st, const 
     for (int q = 0; q < VS; q++) acc[0][q] = acc[1][q] = make_double2(0.0, 0.0);
     if (S.act)
         SFDX_GRID_LOOP(t, M.nl * sgp.G) {
-            const uint32_t e = fdiv(sgp.fG, t);
+            uint32_t e;
+            int i, j, k;
+            const int o = mdecode_plane(M, fdiv(sgp.fG, t), e, i, j, k);
             const size_t g = (size_t)e * ns + s0;
             CV<double, VS> xe, ax, bv;
             cvld<double, VS>(xe, x + g);
-            row_apply<double, VS>(L, M, e, x, ns, s0, S.wm, xe, ax);
+            row_apply<double, VS>(L, M, o, e, i, j, k, x, ns, s0, S.wm, xe, ax);
             cvld<double, VS>(bv, b + g);
             CV<T, VS> rt, h;
             cvld<T, VS>(h, rhat + g);

@@ -129,6 +129,14 @@ class Plan:
                    "sfdx_plan_kernel_time")
         return ms.value, b.value
 
+    def autotune(self, reps: int = 3):
+        """Measure and set the systems-per-thread grouping of the hot kernels
+        (sfdx_plan_autotune); returns (complex64, complex128) choices."""
+        a, b = ctypes.c_int(), ctypes.c_int()
+        capi.check(capi.lib().sfdx_plan_autotune(self._h, reps, ctypes.byref(a), ctypes.byref(b)),
+                   "sfdx_plan_autotune")
+        return a.value, b.value
+
     def device_bytes(self) -> int:
         return int(capi.lib().sfdx_plan_device_bytes(self._h))
 
@@ -248,3 +256,17 @@ def krylov_solve(nx, ny, nz, a, b, c, sigma, freqs, rhs, x0=None, tol=1e-8, itma
         capi.check(rc, "sfdx_krylov_solve")
     out = (x.reshape(np.shape(rhs)), it, rr, rc)
     return out + (hist,) if history else out
+
+
+def grad_correct(nx, ny, nz, a, b, c, sigma, freqs, rhs, x, tol=1e-8, maxit=2000):
+    """Consistent gradient-space correction of x (sfdx_grad_correct): returns
+    (x + G phi, nodal PCG iterations)."""
+    freqs = _d(np.atleast_1d(freqs))
+    ns = len(freqs)
+    r = _z(rhs).reshape(-1, ns)
+    xx = _z(x).reshape(-1, ns).copy()
+    it = np.zeros(1, np.int32)
+    capi.check(capi.lib().sfdx_grad_correct(nx, ny, nz, capi.dptr(_d(a)), capi.dptr(_d(b)), capi.dptr(_d(c)),
+                                            capi.dptr(_d(sigma)), ns, capi.dptr(freqs), capi.zptr(r), capi.zptr(xx),
+                                            tol, maxit, capi.iptr(it)), "sfdx_grad_correct")
+    return xx.reshape(np.shape(x)), int(it[0])

@@ -221,3 +221,38 @@ def small_aniso(n: int = 16, nair: int = 8, nz_earth: int = 24, seed: int = 0, f
     yc = _centres(b)
     recv = np.array([[xc[n // 2], yc[n // 2], 0.0], [xc[n // 2 - 2], yc[n // 2 + 1], 0.0]])
     return Model(n, n, nz, nair, a, b, c, sig, np.asarray(freqs, float), recv)
+
+
+def dtm1(sigma_air: float = SIGMA_AIR) -> Model:
+    """The reference's own example model DTM1.0 (generator sfd_excmg/input.py:6-95,
+    receivers :97-117), restated: 128x128 cells laterally, 128 earth layers under 64
+    air layers (nz = 192, ~9.6 M edges); 16 blocks of 8 equal cells per axis with
+    block widths 29.2, 16.2, 9, 5 km towards the 8 central 5 km blocks, vertical
+    blocks 10 x 5 km then 5 km * 1.8^n; 100 ohm-m half-space with three isotropic
+    bodies (10, 1 and 10^4 ohm-m); air layers mirror the deepest earth layers;
+    frequencies 0.001-1 Hz; 4 receiver lines of 17 sites; 4 levels, tol 1e-10,
+    BiCGStab."""
+    edge = [2.92e4, 1.62e4, 9e3, 5e3]
+    a0 = np.array(edge + [5e3] * 8 + edge[::-1])
+    c0 = np.array([5e3] * 10 + [5e3 * 1.8 ** (i + 1) for i in range(6)])
+    a = np.repeat(a0 / 8, 8)
+    b = a.copy()
+    ce = np.repeat(c0 / 8, 8)
+    nair = 64
+    c = np.concatenate([ce[::-1][:nair], ce])
+    nx, ny, nze = 128, 128, 128
+    nz = nze + nair
+    s3 = np.zeros((6, nz, ny, nx))
+    s3[0:3, nair:] = 1e-2
+    bodies = (((32, 96), (60, 68), (8, 32), 0.1), ((40, 64), (60, 100), (32, 40), 1.0),
+              ((64, 88), (28, 68), (32, 80), 1e-4))
+    for (x0, x1), (y0, y1), (z0, z1), s in bodies:
+        s3[0:3, nair + z0:nair + z1, y0:y1, x0:x1] = s
+    s3[0:3, :nair] = sigma_air
+    sites = np.array([-37.5, -32.5, -27.5, -22.5, -17.5, -12.5, -7.5, -2.5, 0.0, 2.5, 7.5, 12.5, 17.5, 22.5, 27.5,
+                      32.5, 37.5]) * 1e3
+    z = np.zeros_like(sites)
+    recv = np.concatenate([np.stack([sites, z, z], 1), np.stack([z - 15e3, sites, z], 1),
+                           np.stack([z, sites, z], 1), np.stack([z + 15e3, sites, z], 1)])
+    freq = np.array([0.001, 0.01, 0.1, 1.0])
+    return Model(nx, ny, nz, nair, a, b, c, s3.reshape(6, -1), freq, recv, level=4, eps=1e-10, solver=1, out_type=1)

@@ -241,6 +241,37 @@ def test_krylov_batched_systems_non_power_of_two(solver):
         assert np.linalg.norm(r) <= 1.01e-9 * np.linalg.norm(rhs[:, s])
 
 
+def test_grad_correct_matches_oracle():
+    """Consistent gradient-space correction: the GPU result equals the oracle's exact
+    Galerkin projection, and the corrected residual has no nodal component left."""
+    m = _model(9)
+    freqs = [0.05, 0.05, 30.0, 30.0]
+    rng = np.random.default_rng(4)
+    x = rng.standard_normal((m.nl, 4)) + 1j * rng.standard_normal((m.nl, 4))
+    rhs = np.empty_like(x)
+    Ks = []
+    for q in range(2):
+        K, p1, p2, _ = _csr(m, freqs[2 * q])
+        rhs[:, 2 * q], rhs[:, 2 * q + 1] = p1, p2
+        Ks += [K, K]
+    # the nodal PCG runs in complex64 (its job is a loose projection), so it is
+    # asked for 1e-5 here
+    got, its = S.grad_correct(m.nx, m.ny, m.nz, m.a, m.b, m.c, m.sigma, freqs, rhs, x, tol=1e-5, maxit=5000)
+    assert 0 < its < 5000
+    G = O.node_gradient(m.nx, m.ny, m.nz, m.a, m.b, m.c)
+    V = O.edge_dual_volumes(m.nx, m.ny, m.nz, m.a, m.b, m.c)
+    for s in range(4):
+        # the corrected residual has no nodal (gradient-space) component left
+        n0 = np.linalg.norm(G.T @ (V * (rhs[:, s] - Ks[s] @ x[:, s])))
+        n1 = np.linalg.norm(G.T @ (V * (rhs[:, s] - Ks[s] @ got[:, s])))
+        assert n1 <= 1e-4 * n0
+        # and equals the oracle's exact projection to the PCG tolerance times the
+        # conditioning of the nodal system (air 1e-9 S/m against earth)
+        ref = O.grad_correct(m.nx, m.ny, m.nz, m.a, m.b, m.c, m.sigma, freqs[s], rhs[:, s], x[:, s])
+        dref = ref - x[:, s]
+        assert np.linalg.norm(got[:, s] - ref) <= 1e-2 * np.linalg.norm(dref)
+
+
 def test_divergence_correction_matches_div_correc():
     m = _model(5)
     rng = np.random.default_rng(9)

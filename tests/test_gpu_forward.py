@@ -42,39 +42,64 @@ def test_halfspace_known_answer():
     assert np.all(np.abs(res[..., 2:4] - 45.0) < 2.0), res
 
 
-def _z_tolerance(freq):
-    """Attainable impedance agreement between an iterative solve to relative residual
-    1e-10 and the exact (direct) discrete solution.  Below ~1 Hz the fields vary over
-    skin depths of tens of km, so H (a difference quotient over 50-100 m cells) loses
-    2-3 digits, and the field components the w*mu*sigma term barely controls are only
-    determined to residual/(w*mu*sigma*h^2); both limits are properties of the
-    discretisation, shared by the reference's own iterative solves."""
-    return np.where(np.asarray(freq) >= 1.0, 1e-4, 3e-2)[:, None, None]
+# Impedance agreement with the exact (direct) discrete solution.  An iterative
+# solve to relative residual eps leaves errors of order eps * kappa in the
+# near-null space of the operator (discrete gradients in air and at low
+# frequency), and the impedance evaluation is sensitive to them; the consistent
+# gradient-space correction (div_cor = 2) removes that component, so what is
+# left is the residual-bound error of the remaining (static air) modes.
+def z_tol_corrected(freq):
+    """Remaining error after the correction: eps times the conditioning of the
+    non-gradient modes, which grows as the skin depth outgrows the domain."""
+    return np.where(np.asarray(freq) < 0.1, 5e-4, 1e-4)[:, None, None]
 
 
 @pytest.mark.parametrize("excmg", [0, 1])
 def test_forward_fp64_matches_direct(excmg):
     m = syn.small_aniso(n=16, seed=1, freqs=(0.05, 20.0))
-    ex, it, rr = S.fwd_solve(m, eps=1e-10, excmg=excmg, level=3, div_cor=0, solver=3)
-    assert np.all(rr < 1e-9), rr
+    ex, it, rr = S.fwd_solve(m, eps=1e-10, excmg=excmg, level=3, div_cor=2, corr_intv=25, corr_tol=1e-2, solver=3)
+    assert np.all(rr < 1.5e-10), rr
     _, zref = _direct_Z(m)
     z = S.impedance(m, ex)
     err = np.abs(_zc(z) - _zc(zref)) / np.abs(_zc(zref))
-    assert np.all(err < _z_tolerance(m.freq)), err
+    assert np.all(err < z_tol_corrected(m.freq)), err
 
 
 def test_forward_mixed_matches_fp64():
     m = syn.small_aniso(n=16, seed=2, freqs=(0.01, 1.0, 100.0))
-    ex64, _, rr64 = S.fwd_solve(m, eps=1e-10, excmg=1, level=3, div_cor=0, solver=3)
-    exm, _, rrm = S.fwd_solve(m, eps=1e-10, excmg=1, level=3, precision=S.MIXED, solver=3)
-    assert np.all(rrm < 1e-10), rrm
+    opts = dict(eps=1e-10, excmg=1, level=3, div_cor=2, corr_intv=25, corr_tol=1e-2, solver=3)
+    ex64, _, rr64 = S.fwd_solve(m, **opts)
+    exm, _, rrm = S.fwd_solve(m, precision=S.MIXED, **opts)
+    assert np.all(rrm < 1.5e-10), rrm
     z64 = _zc(S.impedance(m, ex64))
     zm = _zc(S.impedance(m, exm))
     _, zref = _direct_Z(m)
     zr = _zc(zref)
     e64 = np.abs(z64 - zr) / np.abs(zr)
     em = np.abs(zm - zr) / np.abs(zr)
-    assert np.all(em < _z_tolerance(m.freq)), (em, e64)
+    assert np.all(em < z_tol_corrected(m.freq)), (em, e64)
+    assert np.all(e64 < z_tol_corrected(m.freq)), (em, e64)
+
+
+def test_uncorrected_error_lies_in_gradient_space():
+    """Without the correction the field error of a converged iterative solve is (almost)
+    entirely a discrete gradient: one correction step brings the impedances to the
+    corrected accuracy."""
+    m = syn.small_aniso(n=16, seed=1, freqs=(0.05,))
+    ex, it, rr = S.fwd_solve(m, eps=1e-10, excmg=1, level=3, div_cor=0, solver=3)
+    _, zref = _direct_Z(m)
+    zr = _zc(zref)
+    e0 = np.abs(_zc(S.impedance(m, ex)) - zr) / np.abs(zr)
+    ff = m.freq[0]
+    conv = O.column_conv(m.sigma, m.nx, m.ny, m.nz)
+    edc, _, _ = O.mt1d_anl(ff, conv, m.c)
+    _, p1, p2 = O.assemble(m.nx, m.ny, m.nz, m.a, m.b, m.c, m.sigma, ff, edc)
+    rhs = np.stack([p1, p2], axis=1)
+    xc, _ = S.grad_correct(m.nx, m.ny, m.nz, m.a, m.b, m.c, m.sigma, [ff, ff], rhs, ex[0].T.copy(), tol=1e-6)
+    exc = ex.copy()
+    exc[0] = xc.T
+    e1 = np.abs(_zc(S.impedance(m, exc)) - zr) / np.abs(zr)
+    assert e1.max() < 0.05 * e0.max(), (e0.max(), e1.max())
 
 
 def test_plan_reuse_and_device_impedance():

@@ -1,0 +1,174 @@
+"""Known-answer tests that pin the oracle (CPU, no GPU needed).
+
+The reference ships no golden vectors and cannot be compiled here (ifort +
+MKL), so the oracle's restatement is pinned by answers known independently:
+the analytic homogeneous and layered 1-D responses, the half-space apparent
+resistivity and phase of the 3-D discretisation, a 3-D solve of a 1-D model,
+exact reproduction of constant fields by the EXCMG prolongation, and the
+algebraic identities the gradient-space correction relies on.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from sfd_excmg_gb300 import synthetic as syn
+
+MU = 4e-7 * np.pi
+
+
+def _layered_column(thick, sig, nz_per, h):
+    """conv (nz,6) and c (nz) for layers of given conductivity; the last layer is the basement."""
+    c, conv = [], []
+    for t, s in zip(thick, sig):
+        n = int(round(t / h)) if t is not None else nz_per
+        c += [h] * n
+        conv += [[s, s, s, 0, 0, 0]] * n
+    return np.array(conv, float), np.array(c, float)
+
+
+@pytest.mark.parametrize("f", [0.01, 1.0, 100.0])
+def test_mt1d_homogeneous_halfspace_is_analytic(f):
+    nz, h, sig = 40, 50.0, 0.01
+    conv = np.zeros((nz, 6))
+    conv[:, :3] = sig
+    e, _, imp = O.mt1d_anl(f, conv, np.full(nz, h))
+    z = np.arange(nz + 1) * h
+    delta = np.sqrt(2 / (2 * np.pi * f * MU * sig))
+    np.testing.assert_allclose(e[:nz + 1], np.exp(-(1 - 1j) * z / delta), rtol=0, atol=1e-13)
+    w = 2 * np.pi * f
+    np.testing.assert_allclose(np.abs(imp[1]) ** 2 / (w * MU), 1 / sig, rtol=1e-12)
+    np.testing.assert_allclose(abs(np.degrees(np.angle(imp[1]))), 45.0, atol=1e-9)
+
+
+def _wait_impedance(f, thick, sig):
+    """Layered-earth impedance by Wait's recursion (isotropic layers, last = half-space)."""
+    w = 2 * np.pi * f
+    k = np.sqrt(-1j * w * MU * np.asarray(sig, complex))
+    zeta = w * MU / k
+    Z = zeta[-1]
+    for n in range(len(sig) - 2, -1, -1):
+        t = np.tanh(1j * k[n] * thick[n])
+        Z = zeta[n] * (Z + zeta[n] * t) / (zeta[n] + Z * t)
+    return Z
+
+
+@pytest.mark.parametrize("f", [0.1, 3.0])
+def test_mt1d_layered_impedance_matches_recursion(f):
+    h = 25.0
+    thick = [500.0, 750.0, None]
+    sig = [0.01, 0.5, 0.002]
+    conv, c = _layered_column(thick, sig, 60, h)
+    e, hfield, imp = O.mt1d_anl(f, conv, c)
+    Z = _wait_impedance(f, [500.0, 750.0], sig)
+    # the surface impedance E/H of the propagated xy-mode fields (magnitude and
+    # phase of Zxy, the sign convention of the time factor aside)
+    zs = e[0] / hfield[0]
+    np.testing.assert_allclose(abs(zs), abs(Z), rtol=1e-10)
+    np.testing.assert_allclose(abs(np.angle(zs)), abs(np.angle(Z)), rtol=1e-9)
+    # mt1d_anl's own impedance output is taken at the bottom node (model_selec.f90,
+    # i = nz+1), i.e. the basement half-space
+    zb = _wait_impedance(f, [], sig[-1:])
+    np.testing.assert_allclose(abs(imp[1]), abs(zb), rtol=1e-10)
+
+
+def _direct_res(m, out_type=2):
+    om = O.OracleModel(m.nx, m.ny, m.nz, m.nair, m.a, m.b, m.c, m.sigma, m.freq, m.recv)
+    ex = np.zeros((m.nf, 2, m.nl), np.complex128)
+    for k, ff in enumerate(m.freq):
+        u1, u2, _, _, _ = O.direct_solve(om, ff)
+        ex[k, 0], ex[k, 1] = u1, u2
+    return ex, O.impedances(om, ex, out_type=out_type, rd=2)
+
+
+def test_direct_halfspace_apparent_resistivity_and_phase():
+    m = syn.halfspace(n=16, freqs=(1.0, 10.0))
+    _, res = _direct_res(m)
+    # 16^3 cells: discretisation error within 5 % and 2 degrees
+    assert np.all(np.abs(res[..., 0:2] / 100.0 - 1) < 0.05), res
+    assert np.all(np.abs(np.abs(res[..., 2:4]) - 45.0) < 2.0), res
+
+
+def test_direct_solve_of_1d_model_is_laterally_uniform_and_matches_1d():
+    """A laterally uniform model: the 3-D solution equals the 1-D background on every
+    column (the Dirichlet data is the 1-D solution, and the 3-D rows of a 1-D model
+    reduce to the same second difference)."""
+    m = syn.halfspace(n=16, freqs=(2.0,))
+    ex, _ = _direct_res(m)
+    nx, ny, nz = m.nx, m.ny, m.nz
+    conv = O.column_conv(m.sigma, nx, ny, nz)
+    edc, _, _ = O.mt1d_anl(2.0, conv, m.c)
+    exs = ex[0, 0, :nx * (ny + 1) * (nz + 1)].reshape(nz + 1, ny + 1, nx)
+    col = exs[:, ny // 2, nx // 2]
+    np.testing.assert_allclose(col, edc[:nz + 1], rtol=0, atol=2e-3 * np.abs(edc[:nz + 1]).max())
+    # laterally uniform
+    assert np.abs(exs[:, 1:-1, :] - col[:, None, None]).max() < 2e-3 * np.abs(col).max()
+
+
+@pytest.mark.parametrize("quirk", [False, True])
+def test_prolongation_reproduces_constant_fields(quirk):
+    m = syn.small_aniso(n=16, seed=4)
+    nx, ny, nz = m.nx, m.ny, m.nz
+    sizes = [(nx // 4, ny // 4, nz // 4), (nx // 2, ny // 2, nz // 2)]
+    vals = (1.5 - 0.5j, -0.25 + 2j, 0.75 + 0.1j)
+    def field(x, y, z):
+        nxl = x * (y + 1) * (z + 1)
+        nyl = (x + 1) * y * (z + 1)
+        nzl = (x + 1) * (y + 1) * z
+        return np.concatenate([np.full(nxl, vals[0]), np.full(nyl, vals[1]), np.full(nzl, vals[2])])
+    u0 = field(*sizes[0])
+    u1 = field(*sizes[1])
+    u, _ = O.extint_v(nx, ny, nz, m.a, m.b, m.c, m.nair, u0, u1, midpoint_quirk=quirk)
+    np.testing.assert_allclose(u, field(nx, ny, nz), rtol=0, atol=1e-12)
+
+
+def _ms(m, ff):
+    conv = O.column_conv(m.sigma, m.nx, m.ny, m.nz)
+    edc, _, _ = O.mt1d_anl(ff, conv, m.c)
+    K1, p1, _ = O.assemble(m.nx, m.ny, m.nz, m.a, m.b, m.c, m.sigma, ff, edc)
+    K2, _, _ = O.assemble(m.nx, m.ny, m.nz, m.a, m.b, m.c, m.sigma, 2 * ff, edc)
+    w1, w2 = 2 * np.pi * ff * MU, 4 * np.pi * ff * MU
+    Ms = ((K1 - K2) / (-1j * (w1 - w2))).real
+    return K1, p1, Ms, w1
+
+
+def test_gradient_space_identities():
+    """C G = 0 (curl-curl part of the assembled rows annihilates discrete gradients), the
+    dual-volume-weighted curl-curl is symmetric, and G^T V Ms G is symmetric positive
+    definite -- the facts behind the consistent gradient-space correction."""
+    m = syn.small_aniso(n=12, seed=2)
+    K, _, Ms, w = _ms(m, 0.5)
+    C = (K + 1j * w * Ms).real
+    G = O.node_gradient(m.nx, m.ny, m.nz, m.a, m.b, m.c)
+    V = O.edge_dual_volumes(m.nx, m.ny, m.nz, m.a, m.b, m.c)
+    interior = V > 0
+    CG = (C @ G).tocsr()[interior]
+    assert abs(CG).max() <= 1e-12 * abs(C).max() * abs(G).max()
+    VC = (C.multiply(V[:, None])).tocsr()[interior][:, interior]
+    assert abs(VC - VC.T).max() <= 1e-12 * abs(VC).max()
+    N = (G.T @ (Ms.multiply(V[:, None])) @ G).toarray()
+    assert np.abs(N - N.T).max() <= 1e-12 * np.abs(N).max()
+    assert np.linalg.eigvalsh((N + N.T) / 2).min() > 0
+
+
+def test_oracle_grad_correct_is_a_projection():
+    m = syn.small_aniso(n=12, seed=5)
+    ff = 0.2
+    K, p1, _, _ = _ms(m, ff)
+    rng = np.random.default_rng(1)
+    x = rng.standard_normal(m.nl) + 1j * rng.standard_normal(m.nl)
+    x1 = O.grad_correct(m.nx, m.ny, m.nz, m.a, m.b, m.c, m.sigma, ff, p1, x)
+    x2 = O.grad_correct(m.nx, m.ny, m.nz, m.a, m.b, m.c, m.sigma, ff, p1, x1)
+    # idempotent up to the conditioning of N (air conductivity 1e-9 against
+    # earth 1e-2..1 makes the nodal system span ~8 orders of magnitude)
+    assert np.linalg.norm(x2 - x1) <= 1e-4 * np.linalg.norm(x1 - x)
+    G = O.node_gradient(m.nx, m.ny, m.nz, m.a, m.b, m.c)
+    V = O.edge_dual_volumes(m.nx, m.ny, m.nz, m.a, m.b, m.c)
+    n0 = np.linalg.norm(G.T @ (V * (p1 - K @ x)))
+    n1 = np.linalg.norm(G.T @ (V * (p1 - K @ x1)))
+    assert n1 <= 1e-10 * n0
+    # the exact discrete solution is a fixed point (both sides carry rounding
+    # amplified by the near-singular gradient modes of K)
+    from scipy.sparse.linalg import splu
+    xs = splu(K.tocsc()).solve(p1)
+    xs1 = O.grad_correct(m.nx, m.ny, m.nz, m.a, m.b, m.c, m.sigma, ff, p1, xs)
+    assert np.linalg.norm(xs1 - xs) <= 1e-4 * np.linalg.norm(xs)
