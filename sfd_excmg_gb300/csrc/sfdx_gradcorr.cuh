@@ -30,7 +30,7 @@
 // products), to a loose relative tolerance; residual, right-hand side and the
 // update of the FP64 field stay FP64.
 #pragma once
-#include "sfdx_vkern.cuh"
+#include "sfdx_nodemg.cuh"
 
 namespace sfdx {
 
@@ -186,30 +186,10 @@ static __global__ void k_gc_probe(Mesh M, uint32_t np, double2* __restrict__ pr)
         pr[t] = make_double2(!node_bnd(M, i, j, k) && node_colour27(i, j, k) == c ? 1.0 : 0.0, 0.0);
     }
 }
-// stencil entry d = (di+1) + 3 (dj+1) + 9 (dk+1) of interior node n is the
-// probe response of the colour of node n + (di, dj, dk); boundary nodes get the
-// identity row.  dinv = 1 / diagonal.
-static __global__ void k_gc_assemble(Mesh M, uint32_t np, const double2* __restrict__ Q, float* __restrict__ coef,
-                                     float* __restrict__ dinv) {
-    for (uint32_t n = blockIdx.x * blockDim.x + threadIdx.x; n < np; n += gridDim.x * blockDim.x) {
-        int i, j, k;
-        node_ijk(M, n, i, j, k);
-        const bool bnd = node_bnd(M, i, j, k);
-        for (int d = 0; d < 27; d++) {
-            const int di = d % 3 - 1, dj = (d / 3) % 3 - 1, dk = d / 9 - 1;
-            float v;
-            if (bnd) v = d == 13 ? 1.f : 0.f;
-            else v = (float)Q[(size_t)n * 27 + node_colour27(i + di, j + dj, k + dk)].x;
-            coef[(size_t)d * np + n] = v;
-        }
-        const float dg = bnd ? 1.f : (float)Q[(size_t)n * 27 + node_colour27(i, j, k)].x;
-        dinv[n] = dg > 0.f ? 1.f / dg : 1.f;
-    }
-}
-
 // Start of the nodal PCG: t = i/(w mu) G^T V r (interior nodes; r the FP64
-// edge residual), r_n = t, z = dinv r, p = z, phi = 0; sums |t|^2 and <r, z>.
-template <class T, int VS>
+// edge residual), r_n = t, phi = 0, |t|^2; with JAC also z = dinv r, p = z and
+// <r, z> (Jacobi preconditioner; otherwise the multigrid V-cycle makes z).
+template <class T, int VS, bool JAC>
 __global__ void k_gc_rhs(Lev<double> L, Mesh M, SysG sgp, uint32_t np, KState* pst, const double2* __restrict__ redge,
                          const float* __restrict__ dinv, cplx<T>* __restrict__ rn, cplx<T>* __restrict__ z,
                          cplx<T>* __restrict__ p, cplx<T>* __restrict__ phi, RedBuf rb) {
@@ -254,8 +234,10 @@ __global__ void k_gc_rhs(Lev<double> L, Mesh M, SysG sgp, uint32_t np, KState* p
                 acc[1][u].x += di * (tv.v[u].x * tv.v[u].x + tv.v[u].y * tv.v[u].y);
             }
             cvst_m<T, VS>(rn + g, tt, S.act);
-            cvst_m<T, VS>(z + g, zz, S.act);
-            cvst_m<T, VS>(p + g, zz, S.act);
+            if (JAC) {
+                cvst_m<T, VS>(z + g, zz, S.act);
+                cvst_m<T, VS>(p + g, zz, S.act);
+            }
             cvst_m<T, VS>(phi + g, zero, S.act);
         }
     if (!vreduce_last<2, VS>(acc, sgp, rb, smem)) return;
@@ -333,8 +315,9 @@ __global__ void k_gc_Ap(Mesh M, SysG sgp, uint32_t np, KState* pst, const float*
     }
 }
 
-// phi += alpha p ; r -= alpha q ; z = dinv r ; <r,z>, |r|^2 ; beta, stopping test
-template <class T, int VS>
+// phi += alpha p ; r -= alpha q ; |r|^2 and the stopping test; with JAC also
+// z = dinv r, <r,z> and beta (otherwise k_gc_rz after the V-cycle)
+template <class T, int VS, bool JAC>
 __global__ void k_gc_upd(SysG sgp, uint32_t np, KState* pst, const float* __restrict__ dinv,
                          const cplx<T>* __restrict__ p, const cplx<T>* __restrict__ q, cplx<T>* __restrict__ phi,
                          cplx<T>* __restrict__ rn, cplx<T>* __restrict__ z, RedBuf rb) {
@@ -369,17 +352,19 @@ __global__ void k_gc_upd(SysG sgp, uint32_t np, KState* pst, const float* __rest
             }
             cvst_m<T, VS>(phi + g, fv, S.act);
             cvst_m<T, VS>(rn + g, rv, S.act);
-            cvst_m<T, VS>(z + g, zv, S.act);
+            if (JAC) cvst_m<T, VS>(z + g, zv, S.act);
         }
     if (!vreduce_last<2, VS>(acc, sgp, rb, smem)) return;
     const int B = blockDim.x;
     for (int ss = threadIdx.x; ss < ns; ss += B) {
         KState& Q = pst[ss];
         if (!Q.active) continue;
-        const double2 rz = smem[B + ss], ro = Q.rho;
-        const double rd = ro.x * ro.x + ro.y * ro.y;
-        Q.beta = make_double2((rz.x * ro.x + rz.y * ro.y) / rd, (rz.y * ro.x - rz.x * ro.y) / rd);
-        Q.rho = rz;
+        if (JAC) {
+            const double2 rz = smem[B + ss], ro = Q.rho;
+            const double rd = ro.x * ro.x + ro.y * ro.y;
+            Q.beta = make_double2((rz.x * ro.x + rz.y * ro.y) / rd, (rz.y * ro.x - rz.x * ro.y) / rd);
+            Q.rho = rz;
+        }
         Q.err = sqrt(smem[B + ns + ss].x) / Q.babs;
         Q.it += 1;
         Q.iters = Q.it;
@@ -396,8 +381,49 @@ __global__ void k_gc_upd(SysG sgp, uint32_t np, KState* pst, const float* __rest
     }
 }
 
-// p = z + beta p
-template <class T, int VS>
+// <r, z> after the preconditioner: rho, and beta = rho_new / rho_old unless FIRST
+template <class T, int VS, bool FIRST>
+__global__ void k_gc_rz(SysG sgp, uint32_t np, KState* pst, const cplx<T>* __restrict__ rn, const cplx<T>* __restrict__ z,
+                        RedBuf rb) {
+    extern __shared__ double2 smem[];
+    const int ns = sgp.ns, s0 = (threadIdx.x % sgp.G) * VS;
+    const SysV<T, VS> S = load_sys<T, VS>(pst, s0);
+    double2 acc[1][VS];
+#pragma unroll
+    for (int u = 0; u < VS; u++) acc[0][u] = make_double2(0.0, 0.0);
+    if (S.act)
+        SFDX_GRID_LOOP(t, np * sgp.G) {
+            const size_t g = (size_t)fdiv(sgp.fG, t) * ns + s0;
+            CV<T, VS> rv, zv;
+            cvld<T, VS>(rv, rn + g);
+            cvld<T, VS>(zv, z + g);
+#pragma unroll
+            for (int u = 0; u < VS; u++) {
+                acc[0][u].x += (double)rv.v[u].x * zv.v[u].x + (double)rv.v[u].y * zv.v[u].y;
+                acc[0][u].y += (double)rv.v[u].x * zv.v[u].y - (double)rv.v[u].y * zv.v[u].x;
+            }
+        }
+    if (!vreduce_last<1, VS>(acc, sgp, rb, smem)) return;
+    const int B = blockDim.x;
+    for (int ss = threadIdx.x; ss < ns; ss += B) {
+        KState& Q = pst[ss];
+        if (!Q.active) continue;
+        const double2 rz = smem[B + ss];
+        if (!FIRST) {
+            const double2 ro = Q.rho;
+            const double rd = ro.x * ro.x + ro.y * ro.y;
+            Q.beta = make_double2((rz.x * ro.x + rz.y * ro.y) / rd, (rz.y * ro.x - rz.x * ro.y) / rd);
+        }
+        Q.rho = rz;
+        if (!isfinite(rz.x) || !isfinite(rz.y)) {
+            Q.active = 0;
+            Q.status = ST_BREAK;
+        }
+    }
+}
+
+// p = z + beta p  (FIRST: p = z)
+template <class T, int VS, bool FIRST>
 __global__ void k_gc_p(SysG sgp, uint32_t np, const KState* pst, const cplx<T>* __restrict__ z, cplx<T>* __restrict__ p) {
     const int ns = sgp.ns, s0 = (threadIdx.x % sgp.G) * VS;
     const SysV<T, VS> S = load_sys<T, VS>(pst, s0);
@@ -409,9 +435,13 @@ __global__ void k_gc_p(SysG sgp, uint32_t np, const KState* pst, const cplx<T>* 
         const size_t g = (size_t)fdiv(sgp.fG, t) * ns + s0;
         CV<T, VS> zv, pv;
         cvld<T, VS>(zv, z + g);
-        cvldw<T, VS>(pv, p + g);
+        if (FIRST) {
+            pv = zv;
+        } else {
+            cvldw<T, VS>(pv, p + g);
 #pragma unroll
-        for (int u = 0; u < VS; u++) pv.v[u] = zv.v[u] + cmul<T>(be[u], pv.v[u]);
+            for (int u = 0; u < VS; u++) pv.v[u] = zv.v[u] + cmul<T>(be[u], pv.v[u]);
+        }
         cvst_m<T, VS>(p + g, pv, S.act);
     }
 }

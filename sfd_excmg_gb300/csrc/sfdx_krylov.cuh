@@ -6,6 +6,8 @@
 // sfdx_krylov_f64.cu, which instantiate it per arithmetic type so that the
 // two compile in parallel.
 #pragma once
+#include <chrono>
+
 #include "sfdx_plan.h"
 #include "sfdx_vkern.cuh"
 
@@ -243,12 +245,35 @@ static int gpbicg_v(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, cons
 }
 
 // ------------------------------------------------------------------ corrected restart cycles
+// dst[e][i] = src[e][idx[i]] (i < nd)  /  dst[e][idx[i]] = src[e][i]
+static __global__ void k_gather_cols(int64_t nl, int ns, int nd, const int* __restrict__ idx,
+                                     const double2* __restrict__ src, double2* __restrict__ dst) {
+    for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < nl * nd; g += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t e = g / nd;
+        const int i = (int)(g - e * nd);
+        dst[g] = src[e * ns + __ldg(idx + i)];
+    }
+}
+static __global__ void k_scatter_cols(int64_t nl, int ns, int nd, const int* __restrict__ idx,
+                                      const double2* __restrict__ src, double2* __restrict__ dst) {
+    for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < nl * nd; g += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t e = g / nd;
+        const int i = (int)(g - e * nd);
+        dst[e * ns + __ldg(idx + i)] = src[g];
+    }
+}
+
 // div_cor = 2: the Krylov solve runs in cycles of corr_intv iterations; before
 // every cycle and after the last one the FP64 iterate gets the consistent
 // gradient-space correction (sfdx_gradcorr.cuh), and each cycle restarts the
-// Krylov recurrences from the corrected iterate.  `run(itmax_cycle, mask)` is
-// one Krylov solve from the current iterate; per-system iteration counts
-// and statuses over all cycles are left in P.hst.
+// Krylov recurrences from the corrected iterate.  Because a cycle starts from
+// the FP64 iterate alone, the systems still running are packed into a
+// smaller batch for the cycle (FP64 right-hand side and iterate gathered,
+// iterate scattered back): finished systems cost nothing, and the kernels'
+// threads all work on running systems.  `run(itmax_cycle, b, x, rel)` is one
+// Krylov solve from the current iterate of every system of the (possibly
+// packed) batch; per-system iteration counts and statuses over all cycles are
+// left in P.hst.
 template <class T, class F>
 static int corrected_cycles(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, int itmax, const int* mask_host,
                             const Reliable* rel, F run) {
@@ -259,33 +284,84 @@ static int corrected_cycles(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>*
     for (int q = 0; q < ns; q++) part[q] = mask[q] = mask_host ? (mask_host[q] != 0) : 1;
     const int cyc = P.o.corr_intv > 0 ? P.o.corr_intv : 25;
     const int gc_maxit = 2000;  // pcg itmax (div_correc.f90:57)
+    const std::vector<double> wm_all = P.wm;
+    const bool can_pack = P.hist == nullptr;  // residual histories are indexed by the full batch
+    std::vector<KState> hs(ns);
     for (;;) {
-        int gc_its = 0;
-        RC(grad_correct(P, LV, b64, x64, mask.data(), P.o.corr_tol, gc_maxit, &gc_its));
+        std::vector<int> idx;
+        for (int q = 0; q < ns; q++)
+            if (mask[q]) idx.push_back(q);
+        const int nd = (int)idx.size();
+        const bool pack = can_pack && nd < ns;
+        const double2* bc = b64;
+        double2* xc = x64;
+        if (pack) {  // the running systems become a batch of nd
+            const size_t nb = (size_t)LV.nl * nd * sizeof(double2);
+            RC(P.cb64.alloc(nb));
+            RC(P.cx64.alloc(nb));
+            RC(P.d_idx.alloc(sizeof(int) * ns));
+            CK(cudaMemcpyAsync(P.d_idx.p, idx.data(), sizeof(int) * nd, cudaMemcpyHostToDevice, P.st));
+            KL(k_gather_cols<<<grid_for(LV.nl * nd, 256, 16), 256, 0, P.st>>>(LV.nl, ns, nd, P.d_idx.as<int>(), b64,
+                                                                              P.cb64.as<double2>()));
+            KL(k_gather_cols<<<grid_for(LV.nl * nd, 256, 16), 256, 0, P.st>>>(LV.nl, ns, nd, P.d_idx.as<int>(), x64,
+                                                                              P.cx64.as<double2>()));
+            bc = P.cb64.as<double2>();
+            xc = P.cx64.as<double2>();
+            P.ns = nd;
+            P.wm.resize(nd);
+            for (int i = 0; i < nd; i++) P.wm[i] = wm_all[idx[i]];
+        }
         int room = 0;
         for (int q = 0; q < ns; q++)
             if (mask[q]) room = std::max(room, itmax - used[q]);
-        RC(run(std::min(cyc, room), mask.data()));
+        const int* m = pack ? nullptr : mask.data();
+        int gc_its = 0;
+        const auto t0 = std::chrono::steady_clock::now();
+        int rc = grad_correct(P, LV, bc, xc, m, P.o.corr_tol, gc_maxit, &gc_its);
+        const auto t1 = std::chrono::steady_clock::now();
+        if (rc == SFDX_OK) {
+            if (rel) {
+                Reliable rc_rel = *rel;
+                rc_rel.b64 = bc;
+                rc_rel.x64 = xc;
+                rc = run(std::min(cyc, room), m, b, x, &rc_rel);
+            } else {
+                rc = run(std::min(cyc, room), m, reinterpret_cast<const cplx<T>*>(bc), reinterpret_cast<cplx<T>*>(xc),
+                         nullptr);
+            }
+        }
+        const auto t2 = std::chrono::steady_clock::now();
+        if (pack) {  // back to the full batch
+            KL(k_scatter_cols<<<grid_for(LV.nl * nd, 256, 16), 256, 0, P.st>>>(LV.nl, ns, nd, P.d_idx.as<int>(),
+                                                                               P.cx64.as<double2>(), x64));
+            P.ns = ns;
+            P.wm = wm_all;
+            if (rc == SFDX_OK)
+                for (int i = 0; i < nd; i++) hs[idx[i]] = P.hst[i];
+        } else if (rc == SFDX_OK) {
+            for (int q = 0; q < ns; q++) hs[q] = P.hst[q];
+        }
+        RC(rc);
         if (P.o.verbose || getenv("SFDX_VERBOSE")) {
             double emin = 1e300, emax = 0;
             int cnt[6] = {0, 0, 0, 0, 0, 0};
-            for (int q = 0; q < ns; q++) {
-                if (!mask[q]) continue;
-                emin = std::min(emin, P.hst[q].err);
-                emax = std::max(emax, P.hst[q].err);
-                if (P.hst[q].status >= 0 && P.hst[q].status < 6) cnt[P.hst[q].status]++;
+            for (int q : idx) {
+                emin = std::min(emin, hs[q].err);
+                emax = std::max(emax, hs[q].err);
+                if (hs[q].status >= 0 && hs[q].status < 6) cnt[hs[q].status]++;
             }
+            const double ms_gc = std::chrono::duration<double, std::milli>(t1 - t0).count();
+            const double ms_kr = std::chrono::duration<double, std::milli>(t2 - t1).count();
             fprintf(stderr,
-                    "sfdx:   cycle (%s, %d its, nodal pcg %d): err %.2e..%.2e  run %d conv %d maxit %d nan %d break %d "
-                    "vconv %d\n",
-                    rel ? "mixed" : "fp64", std::min(cyc, room), gc_its, emin, emax, cnt[0], cnt[1], cnt[2], cnt[3],
-                    cnt[4], cnt[5]);
+                    "sfdx:   cycle (%s, %d of %d systems, %d its %.1f ms, nodal pcg %d its %.1f ms): err %.2e..%.2e  run %d "
+                    "conv %d maxit %d nan %d break %d vconv %d\n",
+                    rel ? "mixed" : "fp64", nd, ns, std::min(cyc, room), ms_kr, gc_its, ms_gc, emin, emax, cnt[0],
+                    cnt[1], cnt[2], cnt[3], cnt[4], cnt[5]);
         }
         int left = 0;
-        for (int q = 0; q < ns; q++) {
-            if (!mask[q]) continue;
-            const int st = P.hst[q].status;
-            used[q] += std::max(1, P.hst[q].iters);
+        for (int q : idx) {
+            const int st = hs[q].status;
+            used[q] += std::max(1, hs[q].iters);
             if (st == ST_CONV || st == ST_VCONV || st == ST_NAN || (st == ST_BREAK && rel)) {
                 mask[q] = 0;  // converged, failed, or handed to the caller's FP64 finish
                 fin[q] = st;
@@ -303,6 +379,7 @@ static int corrected_cycles(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>*
     RC(grad_correct(P, LV, b64, x64, last.data(), P.o.corr_tol, gc_maxit, nullptr));
     P.hst.resize(ns);
     for (int q = 0; q < ns; q++) {
+        P.hst[q] = hs[q];
         if (!part[q]) continue;
         P.hst[q].iters = used[q];
         P.hst[q].status = fin[q];
@@ -314,30 +391,30 @@ static int corrected_cycles(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>*
 template <class T>
 int bicgstab(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, const double* tols_host, double tol, int itmax,
              const int* mask_host, const Reliable* rel) {
-    auto run = [&](int itc, const int* m) -> int {
+    auto run = [&](int itc, const int* m, const cplx<T>* bb, cplx<T>* xx, const Reliable* rr) -> int {
         switch (plan_vs<T>(P)) {
-            case 4: return bicgstab_v<T, 4>(P, LV, b, x, tols_host, tol, itc, m, rel);
-            case 2: return bicgstab_v<T, 2>(P, LV, b, x, tols_host, tol, itc, m, rel);
-            default: return bicgstab_v<T, 1>(P, LV, b, x, tols_host, tol, itc, m, rel);
+            case 4: return bicgstab_v<T, 4>(P, LV, bb, xx, tols_host, tol, itc, m, rr);
+            case 2: return bicgstab_v<T, 2>(P, LV, bb, xx, tols_host, tol, itc, m, rr);
+            default: return bicgstab_v<T, 1>(P, LV, bb, xx, tols_host, tol, itc, m, rr);
         }
     };
     if (P.o.div_cor == 2 && (rel || std::is_same<T, double>::value))
         return corrected_cycles<T>(P, LV, b, x, itmax, mask_host, rel, run);
-    return run(itmax, mask_host);
+    return run(itmax, mask_host, b, x, rel);
 }
 template <class T>
 int gpbicg(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, const double* tols_host, double tol, int itmax,
            const int* mask_host, const Reliable* rel) {
-    auto run = [&](int itc, const int* m) -> int {
+    auto run = [&](int itc, const int* m, const cplx<T>* bb, cplx<T>* xx, const Reliable* rr) -> int {
         switch (plan_vs<T>(P)) {
-            case 4: return gpbicg_v<T, 4>(P, LV, b, x, tols_host, tol, itc, m, rel);
-            case 2: return gpbicg_v<T, 2>(P, LV, b, x, tols_host, tol, itc, m, rel);
-            default: return gpbicg_v<T, 1>(P, LV, b, x, tols_host, tol, itc, m, rel);
+            case 4: return gpbicg_v<T, 4>(P, LV, bb, xx, tols_host, tol, itc, m, rr);
+            case 2: return gpbicg_v<T, 2>(P, LV, bb, xx, tols_host, tol, itc, m, rr);
+            default: return gpbicg_v<T, 1>(P, LV, bb, xx, tols_host, tol, itc, m, rr);
         }
     };
     if (P.o.div_cor == 2 && (rel || std::is_same<T, double>::value))
         return corrected_cycles<T>(P, LV, b, x, itmax, mask_host, rel, run);
-    return run(itmax, mask_host);
+    return run(itmax, mask_host, b, x, rel);
 }
 template <class T> int precond_vec(Plan& P, const Level& LV, cplx<T>* out, cplx<T>* q) {
     switch (plan_vs<T>(P)) {

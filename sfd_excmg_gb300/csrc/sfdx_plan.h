@@ -16,6 +16,7 @@
 
 #include "sfdx.h"
 #include "sfdx_kernels.cuh"
+#include "sfdx_nodemg.cuh"
 #include "sfdx_stencil.cuh"
 
 namespace sfdx {
@@ -154,6 +155,17 @@ template <class T> AxisT<T> axis_ptrs(const T* base, int stride, int axis) {
     return a;
 }
 
+// One level of the nodal multigrid of the gradient-space correction: the
+// 27-point stencil (float) with its inverse diagonal, and the V-cycle work
+// vectors (complex64, ns systems) of that grid.
+struct NodeMG {
+    NGrid g;
+    DBuf coef, dinv;
+    DBuf x, b, t, r;
+    NodeMG() = default;
+    NodeMG(NodeMG&&) = default;
+};
+
 struct Level {
     int nx = 0, ny = 0, nz = 0, nair = 0;
     int64_t xnl = 0, ynl = 0, nl = 0, ncell = 0;
@@ -166,10 +178,9 @@ struct Level {
     DBuf crd_cubic;        // node coordinates used by cubic_interp on this level
     DBuf crd_quad;         // node coordinates used by quad_interp_e (pairwise sums of a,b,c)
     int stride = 0;
-    // assembled nodal operator of the gradient-space correction (27-point
-    // stencil, float) and its inverse diagonal; rebuilt after the conductivity
-    // of the level changes
-    mutable DBuf gc_coef, gc_dinv;
+    // nodal multigrid hierarchy of the gradient-space correction (mg[0]: this
+    // level's node grid); rebuilt after the conductivity of the level changes
+    mutable std::vector<NodeMG> mg;
     mutable bool gc_ok = false;
 
     void set_dims(int X, int Y, int Z) {
@@ -214,6 +225,9 @@ struct Plan {
     // consistent gradient correction: node vectors phi, r, z, p, q of the
     // nodal PCG; edge vectors of the probing that assembles the nodal operator
     DBuf gcn[5], gce[2];
+    // FP64 right-hand side and iterate of the running systems packed into a
+    // smaller batch (restart cycles), and their indices in the full batch
+    DBuf cb64, cx64, d_idx;
     long long gc_calls = 0, gc_iters = 0;
     DBuf errrec;
     int edc_stride = 0;
