@@ -30,6 +30,21 @@ template <class T> __device__ __forceinline__ cplx<T> cst(const double2 z) { ret
 // acc[q][v] of each thread (systems s0+v) -> per-block partials part[block][q][ns];
 // the last block sums the partials of every slot in a fixed order and leaves the
 // totals at sm[blockDim + q*ns + s].  Shared memory: vred_smem_bytes() bytes.
+// sum of p[b * pitch] for b = b0, b0 + step, ... < nb, in a fixed order with
+// eight independent accumulators, so that eight L2 loads are in flight
+__device__ __forceinline__ double2 sum_partials(const double2* p, size_t pitch, int b0, int step, int nb) {
+    double2 a[8];
+#pragma unroll
+    for (int j = 0; j < 8; j++) a[j] = make_double2(0.0, 0.0);
+    int b = b0;
+    for (; b + 7 * step < nb; b += 8 * step) {
+#pragma unroll
+        for (int j = 0; j < 8; j++) a[j] = a[j] + __ldcg(p + (size_t)(b + j * step) * pitch);
+    }
+    for (int j = 0; b < nb; b += step, j++) a[j] = a[j] + __ldcg(p + (size_t)b * pitch);
+    return ((a[0] + a[1]) + (a[2] + a[3])) + ((a[4] + a[5]) + (a[6] + a[7]));
+}
+
 template <int NQ, int VS>
 __device__ __forceinline__ bool vreduce_last(double2 (&acc)[NQ][VS], const SysG& sgp, RedBuf rb, double2* sm) {
     const int t = threadIdx.x, B = blockDim.x, G = sgp.G, ns = sgp.ns;
@@ -83,9 +98,7 @@ __device__ __forceinline__ bool vreduce_last(double2 (&acc)[NQ][VS], const SysG&
         __syncthreads();
         for (int slot = t; slot < slots; slot += B) {
             const int q = slot / ns, s = slot - q * ns;
-            double2 a = make_double2(0.0, 0.0);
-            for (int b = 0; b < (int)gridDim.x; b++) a = a + __ldcg(rb.part + ((size_t)b * NQ + q) * ns + s);
-            sm[B + slot] = a;
+            sm[B + slot] = sum_partials(rb.part + (size_t)q * ns + s, (size_t)NQ * ns, 0, 1, (int)gridDim.x);
         }
     } else {  // `per` threads per slot, each a fixed stride of blocks
         const int per = B / slots;
@@ -93,7 +106,7 @@ __device__ __forceinline__ bool vreduce_last(double2 (&acc)[NQ][VS], const SysG&
         double2 a = make_double2(0.0, 0.0);
         if (slot < slots) {
             const int q = slot / ns, s = slot - q * ns;
-            for (int b = ln; b < (int)gridDim.x; b += per) a = a + __ldcg(rb.part + ((size_t)b * NQ + q) * ns + s);
+            a = sum_partials(rb.part + (size_t)q * ns + s, (size_t)NQ * ns, ln, per, (int)gridDim.x);
         }
         __syncthreads();
         sm[t] = a;
