@@ -124,7 +124,7 @@ def max_over_ranks(x, world):
     return float(t.item())
 
 
-SOLVER = {"bicgstab": 1, "gpbicg": 3}
+SOLVER = {"bicgstab": 1, "gpbicg": 3, "cocr": 6}
 
 
 # Divergence handling of the benchmark solves: the consistent gradient-space
@@ -132,14 +132,40 @@ SOLVER = {"bicgstab": 1, "gpbicg": 3}
 GC_OPTS = dict(div_cor=2, corr_intv=40, corr_tol=1e-2)
 
 
-def solve_opts(precision, solver="bicgstab", div_cor=2, eps=1e-10, corr_intv=None):
+def solve_opts(precision, solver="bicgstab", div_cor=2, eps=1e-10, corr_intv=None, level=3):
     import sfd_excmg_gb300 as S
-    o = dict(excmg=1, level=3, eps=eps, precision=S.MIXED if precision == "mixed" else S.FP64,
+    o = dict(excmg=1, level=level, eps=eps, precision=S.MIXED if precision == "mixed" else S.FP64,
              solver=SOLVER[solver])
     o.update(GC_OPTS if div_cor == 2 else dict(div_cor=div_cor))
     if corr_intv:
         o["corr_intv"] = corr_intv
     return o
+
+
+# Workloads: the default anisotropic topography model, the large single model
+# (128x128x96 core cells, 4 levels, tol 1e-7) and the reference's own DTM1
+# example (4 levels, tol 1e-10) whose CPU times the reference publishes.
+WORKLOADS = {
+    "cfg2": ("cfg2: anisotropic 20-block model with Gaussian hills, 64x64x48 core cells of 50 m (80x80x80, "
+             "1,574,640 edges), 8 freqs 1e-3..1e3 Hz x 2 pols, EXCMG 3 levels, tol {eps:g}, 32x32 receivers", 1e-10),
+    "cfg4": ("cfg4: 128x128x96 core cells of 25 m + 16 padding per side, 12 bottom, 36 air (160x160x144, "
+             "11,203,024 edges), 3 layers + 10 anisotropic boxes, 6 freqs 0.01..100 Hz x 2 pols, EXCMG 4 levels, "
+             "tol {eps:g}", 1e-7),
+    "dtm1": ("dtm1: the reference's DTM1.0 example (input.py), 128x128x192 cells incl. 64 air layers "
+             "(9,568,704 edges), 4 freqs 0.001..1 Hz x 2 pols, EXCMG 4 levels, tol {eps:g}, 68 receivers", 1e-10),
+}
+# Reference CPU time for DTM1 (EXCMG, 4 levels, tol 1e-10; Xeon Gold 6248R, serial):
+# 93.62 + 76.84 + 45.95 + 63.31 s for the four frequencies x two polarisations.
+PUBLISHED_SOLVES_PER_S = {"dtm1": 8.0 / (93.62 + 76.84 + 45.95 + 63.31)}
+
+
+def make_workload(name):
+    from sfd_excmg_gb300 import synthetic as syn
+    if name == "cfg4":
+        return syn.config4(seed=0)
+    if name == "dtm1":
+        return syn.dtm1()
+    return syn.config2(seed=0)
 
 
 def cpu_sample(model, freqs_idx, threads, iters=REF_SAMPLE_ITERS):
@@ -242,9 +268,10 @@ def run_ours(args, rank, world, local):
     from sfd_excmg_gb300 import capi
     from sfd_excmg_gb300 import synthetic as syn
 
-    m = syn.config2(seed=0)
+    m = make_workload(args.workload)
+    eps = args.eps if args.eps else WORKLOADS[args.workload][1]
     ns = 2 * m.nf
-    opts = solve_opts(args.precision, args.solver, args.div_cor, args.eps, args.corr_intv)
+    opts = solve_opts(args.precision, args.solver, args.div_cor, eps, args.corr_intv, m.level)
     plan = S.Plan(m, **opts)
     stream = torch.cuda.Stream()
     plan.set_stream(stream.cuda_stream)
@@ -304,7 +331,7 @@ def run_ours(args, rank, world, local):
 
     extra = {}
     if args.compare_fp64 and rank == 0:
-        p64 = S.Plan(m, **solve_opts("fp64", args.solver, args.div_cor, args.eps, args.corr_intv))
+        p64 = S.Plan(m, **solve_opts("fp64", args.solver, args.div_cor, eps, args.corr_intv, m.level))
         t = time.perf_counter()
         p64.solve(allow_noconv=True)
         t64 = time.perf_counter() - t
@@ -322,7 +349,7 @@ def run_ours(args, rank, world, local):
         return
     dom = kern["mc_ssor_c64"]
     cpu = None
-    if args.cpu_baseline:
+    if args.cpu_baseline and args.workload == "cfg2":  # the iteration counts of the reference are measured on cfg2
         its = reference_iterations()
         wall, t_it, t_setup = cpu_sample(m, [0], 1)
         n_it = float(np.mean(its)) if its else float("nan")
@@ -332,10 +359,9 @@ def run_ours(args, rank, world, local):
     line = {
         "metric": "MT solves/s", "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "c64+c128" if args.precision == "mixed" else "c128", "data": "synthetic",
-        "config": {"workload": "cfg2: anisotropic 20-block model with Gaussian hills, 64x64x48 core cells of 50 m "
-                               "(80x80x80, 1,574,640 edges), 8 freqs 1e-3..1e3 Hz x 2 pols, EXCMG 3 levels, "
-                               f"tol {args.eps:g}, 32x32 receivers",
+        "vs_baseline": (value / PUBLISHED_SOLVES_PER_S[args.workload]) if args.workload in PUBLISHED_SOLVES_PER_S else None,
+        "dtype": "c64+c128" if args.precision == "mixed" else "c128", "data": "synthetic",
+        "config": {"workload": WORKLOADS[args.workload][0].format(eps=eps),
                    "precision": args.precision, "solver": args.solver, "div_cor": args.div_cor,
                    "systems_per_thread": {"c64": vs[0], "c128": vs[1]},
                    "systems_per_step": ns, "l2": "working set > L2 (no flush)"},
@@ -358,9 +384,10 @@ def run_profile(args):
     """Kernel families on the finest level of the workload, CUDA-event timed (few launches)."""
     import sfd_excmg_gb300 as S
     from sfd_excmg_gb300 import synthetic as syn
-    m = syn.config2(seed=0)
+    m = make_workload(args.workload)
+    eps = args.eps if args.eps else WORKLOADS[args.workload][1]
     hbm, src = peaks()
-    with S.Plan(m, **solve_opts(args.precision, args.solver, args.div_cor, args.eps, args.corr_intv)) as p:
+    with S.Plan(m, **solve_opts(args.precision, args.solver, args.div_cor, eps, args.corr_intv, m.level)) as p:
         p.load()
         out = {}
         for kid, name in ((2, "mc_ssor_c64"), (0, "operator_c64"), (1, "operator_c128")):
@@ -383,9 +410,10 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--solver", default="gpbicg", choices=list(SOLVER))
-    ap.add_argument("--eps", type=float, default=1e-10,
-                    help="finest-level relative residual tolerance (1e-10: the accuracy at which the mixed-precision "
-                         "impedances agree with the FP64 ones to ~1e-5)")
+    ap.add_argument("--workload", default="cfg2", choices=list(WORKLOADS))
+    ap.add_argument("--eps", type=float, default=None,
+                    help="finest-level relative residual tolerance (default per workload; cfg2: 1e-10, the accuracy "
+                         "at which the mixed-precision impedances agree with the FP64 ones to ~1e-5)")
     ap.add_argument("--corr-intv", dest="corr_intv", type=int, default=None,
                     help="Krylov iterations per restart cycle of the gradient correction (default 25)")
     ap.add_argument("--div-cor", dest="div_cor", type=int, default=2, choices=[0, 1, 2],

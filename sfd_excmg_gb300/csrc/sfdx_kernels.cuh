@@ -133,7 +133,7 @@ static __global__ void k_build_rhs(Lev<double> L, const double* wms, const int* 
 }
 
 // Right-hand-side modes of the forward sweep.
-enum { RHS_VEC = 0, RHS_PUPD = 1, RHS_SUPD = 2 };
+enum { RHS_VEC = 0, RHS_PUPD = 1, RHS_SUPD = 2, RHS_COCR = 3 };
 
 // Jacobi preconditioner (pre_type 'J'): y = D^{-1} rhs with the same fused
 // right-hand-side modes.

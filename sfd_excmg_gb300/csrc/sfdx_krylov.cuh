@@ -15,9 +15,11 @@ namespace sfdx {
 
 // ------------------------------------------------------------------ preconditioner
 template <class T, int VS, int O, int PP, int MODE>
-static void fwd_one(Plan& P, const Level& LV, const VCfg& c, cplx<T>* w, cplx<T>* q, const cplx<T>* r, const cplx<T>* v) {
+static void fwd_one(Plan& P, const Level& LV, const VCfg& c, cplx<T>* w, cplx<T>* q, const cplx<T>* r, const cplx<T>* v,
+                    cplx<T>* aux) {
     const uint32_t W = mcolour_count(LV.mesh, O) * c.sg.G;
-    vlaunch(k_fwd_v<T, VS, O, PP, MODE>, W, c.B, 0, P.st, LV.lev<T>(), LV.mesh, c.sg, P.d_state.as<KState>(), w, q, r, v);
+    vlaunch(k_fwd_v<T, VS, O, PP, MODE>, W, c.B, 0, P.st, LV.lev<T>(), LV.mesh, c.sg, P.d_state.as<KState>(), w, q, r, v,
+            aux);
 }
 template <class T, int VS, int O, int PP>
 static void bwd_one(Plan& P, const Level& LV, const VCfg& c, cplx<T>* x) {
@@ -29,7 +31,8 @@ static void bwd_one(Plan& P, const Level& LV, const VCfg& c, cplx<T>* x) {
 // symmetric Gauss-Seidel: colours 0..5 forward, 4..0 backward (the backward
 // step of the last colour is the identity).
 template <class T, int VS, int MODE>
-static void precond(Plan& P, const Level& LV, cplx<T>* out, cplx<T>* q, const cplx<T>* r, const cplx<T>* v) {
+static void precond(Plan& P, const Level& LV, cplx<T>* out, cplx<T>* q, const cplx<T>* r, const cplx<T>* v,
+                    cplx<T>* aux = nullptr) {
     if (P.o.precond == 'J') {
         const int B = block_for(P.ns);
         KL(k_jacobi<T, MODE><<<grid_for(LV.nl * P.ns, B, 16), B, 0, P.st>>>(LV.lev<T>(), P.d_state.as<KState>(), P.ns, out,
@@ -37,12 +40,12 @@ static void precond(Plan& P, const Level& LV, cplx<T>* out, cplx<T>* q, const cp
         return;
     }
     const VCfg c = vcfg(P, LV.nl, 0, VS);
-    fwd_one<T, VS, OX, 0, MODE>(P, LV, c, out, q, r, v);
-    fwd_one<T, VS, OX, 1, MODE>(P, LV, c, out, q, r, v);
-    fwd_one<T, VS, OY, 0, MODE>(P, LV, c, out, q, r, v);
-    fwd_one<T, VS, OY, 1, MODE>(P, LV, c, out, q, r, v);
-    fwd_one<T, VS, OZ, 0, MODE>(P, LV, c, out, q, r, v);
-    fwd_one<T, VS, OZ, 1, MODE>(P, LV, c, out, q, r, v);
+    fwd_one<T, VS, OX, 0, MODE>(P, LV, c, out, q, r, v, aux);
+    fwd_one<T, VS, OX, 1, MODE>(P, LV, c, out, q, r, v, aux);
+    fwd_one<T, VS, OY, 0, MODE>(P, LV, c, out, q, r, v, aux);
+    fwd_one<T, VS, OY, 1, MODE>(P, LV, c, out, q, r, v, aux);
+    fwd_one<T, VS, OZ, 0, MODE>(P, LV, c, out, q, r, v, aux);
+    fwd_one<T, VS, OZ, 1, MODE>(P, LV, c, out, q, r, v, aux);
     bwd_one<T, VS, OZ, 0>(P, LV, c, out);
     bwd_one<T, VS, OY, 1>(P, LV, c, out);
     bwd_one<T, VS, OY, 0>(P, LV, c, out);
@@ -244,6 +247,89 @@ static int gpbicg_v(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, cons
     return SFDX_OK;
 }
 
+// Preconditioned COCR (SFDX_SOLVER_COCR; no working counterpart: pcocr,
+// solvers.f90:58-135, divides by an unset m_j and is unreachable) for the ns
+// systems of level LV, same calling convention as bicgstab.  The bilinear
+// form and the kernels are in sfdx_vkern.cuh.  With `rel` the recurrence is
+// restarted from the FP64 residual after every reliable update.
+template <class T, int VS>
+static int cocr_v(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, const double* tols_host, double tol, int itmax,
+                  const int* mask_host, const Reliable* rel) {
+    constexpr int VSD = VS > 2 ? 2 : VS;
+    const Lev<T> L = LV.lev<T>();
+    const Mesh& M = LV.mesh;
+    const int ns = P.ns;
+    const size_t vb = (size_t)LV.nl * ns * sizeof(cplx<T>);
+    for (int k = 0; k < 6; k++) RC(P.kv[k].alloc(vb));
+    cplx<T> *r = P.kv[0].as<cplx<T>>(), *z = P.kv[1].as<cplx<T>>(), *u = P.kv[2].as<cplx<T>>();
+    cplx<T> *w = P.kv[3].as<cplx<T>>(), *p = P.kv[4].as<cplx<T>>(), *q = P.kv[5].as<cplx<T>>();
+    std::vector<KState> init;
+    init_states(P, tols_host, tol, itmax, mask_host, init);
+    CK(cudaMemcpyAsync(P.d_state.p, init.data(), sizeof(KState) * ns, cudaMemcpyHostToDevice, P.st));
+    const VCfg c = vcfg(P, LV.nl, 1, VS);
+    const VCfg cd = vcfg(P, LV.nl, 2, VSD);
+    RC(reserve_partials(P, c, 2));
+    KState* dst = P.d_state.as<KState>();
+    const int64_t W = LV.nl * c.sg.G, WD = LV.nl * cd.sg.G;
+    if (rel) {
+        vlaunch(k_fix_bnd<double, VSD>, WD, cd.B, 0, P.st, M, cd.sg, dst, rel->b64, rel->x64);
+        CK(cudaMemsetAsync(x, 0, vb, P.st));
+        vlaunch(k_residual_v<T, double, VSD, 3>, WD, cd.B, cd.smem, P.st, LV.lev<double>(), M, cd.sg, dst, rel->b64,
+                rel->x64, r, (cplx<T>*)nullptr, redbuf(P), (double*)nullptr, 0);
+    } else {
+        vlaunch(k_fix_bnd<T, VS>, W, c.B, 0, P.st, M, c.sg, dst, b, x);
+        vlaunch(k_residual_v<T, T, VS, 3>, W, c.B, c.smem, P.st, L, M, c.sg, dst, b, x, r, (cplx<T>*)nullptr, redbuf(P),
+                (double*)nullptr, 0);
+    }
+    auto restart = [&]() -> int {  // z = M^-1 r ; p = w = 0 ; next beta = 0
+        CK(cudaMemsetAsync(p, 0, vb, P.st));
+        CK(cudaMemsetAsync(w, 0, vb, P.st));
+        precond<T, VS, RHS_VEC>(P, LV, z, r, nullptr, nullptr);
+        return SFDX_OK;
+    };
+    RC(restart());
+    bool first = true;
+    int last_rel = 0;
+    for (int it = 1; it <= itmax; it++) {
+        if (first)
+            vlaunch(k_cocr_u<T, VS, true>, W, c.B, c.smem, P.st, L, M, c.sg, dst, (const cplx<T>*)z, u, redbuf(P));
+        else
+            vlaunch(k_cocr_u<T, VS, false>, W, c.B, c.smem, P.st, L, M, c.sg, dst, (const cplx<T>*)z, u, redbuf(P));
+        first = false;
+        if (P.o.precond == 'J') {
+            vlaunch(k_cocr_dir<T, VS>, W, c.B, 0, P.st, M, c.sg, dst, (const cplx<T>*)u, w, (const cplx<T>*)z, p);
+            precond<T, VS, RHS_VEC>(P, LV, q, w, nullptr, nullptr);
+        } else {
+            precond<T, VS, RHS_COCR>(P, LV, q, w, u, z, p);
+        }
+        vlaunch(k_cocr_alpha<T, VS>, W, c.B, c.smem, P.st, L, M, c.sg, dst, (const cplx<T>*)w, (const cplx<T>*)q,
+                redbuf(P));
+        vlaunch(k_cocr_upd<T, T, VS>, W, c.B, c.smem, P.st, M, c.sg, dst, x, r, z, (const cplx<T>*)p, (const cplx<T>*)w,
+                (const cplx<T>*)q, redbuf(P), P.hist, P.hist_stride);
+        if (it % 8 == 0 || it == itmax) {
+            CK(cudaGetLastError());
+            RC(sync_state(P));
+            int act = 0, cand = 0;
+            for (int k = 0; k < ns; k++) {
+                act += P.hst[k].active;
+                cand += P.hst[k].status == ST_CONV;
+            }
+            if (rel && (cand || (act && (it - last_rel >= rel->every || it == itmax)))) {
+                RC((reliable_update<T, VS>(P, LV, *rel, x, r, r, 6, act)));
+                last_rel = it;
+                if (act && it < itmax) {
+                    RC(restart());
+                    first = true;
+                }
+            }
+            if (!act) break;
+        }
+    }
+    if (rel) vlaunch(k_flush_v<T, VS, true>, W, c.B, 0, P.st, M, c.sg, dst, rel->x64, x, (double2*)nullptr);
+    RC(sync_state(P));
+    return SFDX_OK;
+}
+
 // ------------------------------------------------------------------ corrected restart cycles
 // dst[e][i] = src[e][idx[i]] (i < nd)  /  dst[e][idx[i]] = src[e][i]
 static __global__ void k_gather_cols(int64_t nl, int ns, int nd, const int* __restrict__ idx,
@@ -416,6 +502,20 @@ int gpbicg(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, const double*
         return corrected_cycles<T>(P, LV, b, x, itmax, mask_host, rel, run);
     return run(itmax, mask_host, b, x, rel);
 }
+template <class T>
+int cocr(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, const double* tols_host, double tol, int itmax,
+         const int* mask_host, const Reliable* rel) {
+    auto run = [&](int itc, const int* m, const cplx<T>* bb, cplx<T>* xx, const Reliable* rr) -> int {
+        switch (plan_vs<T>(P)) {
+            case 4: return cocr_v<T, 4>(P, LV, bb, xx, tols_host, tol, itc, m, rr);
+            case 2: return cocr_v<T, 2>(P, LV, bb, xx, tols_host, tol, itc, m, rr);
+            default: return cocr_v<T, 1>(P, LV, bb, xx, tols_host, tol, itc, m, rr);
+        }
+    };
+    if (P.o.div_cor == 2 && (rel || std::is_same<T, double>::value))
+        return corrected_cycles<T>(P, LV, b, x, itmax, mask_host, rel, run);
+    return run(itmax, mask_host, b, x, rel);
+}
 template <class T> int precond_vec(Plan& P, const Level& LV, cplx<T>* out, cplx<T>* q) {
     switch (plan_vs<T>(P)) {
         case 4: precond<T, 4, RHS_VEC>(P, LV, out, q, nullptr, nullptr); break;
@@ -442,6 +542,8 @@ template <class T> int apply_op(Plan& P, const Level& LV, const cplx<T>* x, cplx
                              const Reliable*);                                                                          \
     template int gpbicg<T>(Plan&, const Level&, const cplx<T>*, cplx<T>*, const double*, double, int, const int*,      \
                            const Reliable*);                                                                            \
+    template int cocr<T>(Plan&, const Level&, const cplx<T>*, cplx<T>*, const double*, double, int, const int*,        \
+                         const Reliable*);                                                                              \
     template int precond_vec<T>(Plan&, const Level&, cplx<T>*, cplx<T>*);                                               \
     template int apply_op<T>(Plan&, const Level&, const cplx<T>*, cplx<T>*);
 

@@ -296,6 +296,9 @@ int bicgstab(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, const doubl
 template <class T>
 int gpbicg(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, const double* tols_host, double tol, int itmax,
            const int* mask_host, const Reliable* rel = nullptr);
+template <class T>
+int cocr(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, const double* tols_host, double tol, int itmax,
+         const int* mask_host, const Reliable* rel = nullptr);
 // out = M^{-1} q (multi-colour SSOR or Jacobi) for all active systems
 template <class T> int precond_vec(Plan& P, const Level& LV, cplx<T>* out, cplx<T>* q);
 // y = A x for all systems (per-system frequencies in P.d_wm)

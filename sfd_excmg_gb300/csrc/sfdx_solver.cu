@@ -204,6 +204,8 @@ static int solve_level_fp64(Plan& P, const Level& LV, double tol, int itmax, std
         RC(bicgstab<double>(P, LV, P.b64.as<double2>(), P.x64.as<double2>(), nullptr, tol, itmax, nullptr));
     else if (P.o.solver == SFDX_SOLVER_GPBICG)
         RC(gpbicg<double>(P, LV, P.b64.as<double2>(), P.x64.as<double2>(), nullptr, tol, itmax, nullptr));
+    else if (P.o.solver == SFDX_SOLVER_COCR)
+        RC(cocr<double>(P, LV, P.b64.as<double2>(), P.x64.as<double2>(), nullptr, tol, itmax, nullptr));
     else
         return SFDX_ERR_UNSUPPORTED;
     its.resize(P.ns);
@@ -230,6 +232,8 @@ static int solve_level_mixed(Plan& P, const Level& LV, double tol, int itmax, st
         RC(gpbicg<float>(P, LV, nullptr, x32.as<float2>(), nullptr, tol, itmax, nullptr, &rel));
     else if (P.o.solver == SFDX_SOLVER_BICGSTAB)
         RC(bicgstab<float>(P, LV, nullptr, x32.as<float2>(), nullptr, tol, itmax, nullptr, &rel));
+    else if (P.o.solver == SFDX_SOLVER_COCR)
+        RC(cocr<float>(P, LV, nullptr, x32.as<float2>(), nullptr, tol, itmax, nullptr, &rel));
     else
         return SFDX_ERR_UNSUPPORTED;
     its.resize(ns);
@@ -256,6 +260,9 @@ static int solve_level_mixed(Plan& P, const Level& LV, double tol, int itmax, st
         if (P.o.solver == SFDX_SOLVER_GPBICG)
             rc = gpbicg<double>(P, LV, P.b64.as<double2>(), P.x64.as<double2>(), nullptr, tol, itmax - used_max,
                                 left.data());
+        else if (P.o.solver == SFDX_SOLVER_COCR)
+            rc = cocr<double>(P, LV, P.b64.as<double2>(), P.x64.as<double2>(), nullptr, tol, itmax - used_max,
+                              left.data());
         else
             rc = bicgstab<double>(P, LV, P.b64.as<double2>(), P.x64.as<double2>(), nullptr, tol, itmax - used_max,
                                   left.data());

@@ -453,6 +453,17 @@ __device__ __forceinline__ void row_apply(const Lev<T>& L, const Mesh& M, int o,
         row_apply_o<T, VS, OZ>(L, M, e, i, j, k, x, ns, s0, wm, xe, y);
 }
 
+// Dual volume of edge (o,i,j,k): length x the two transverse half-spacing
+// sums -- the row weight that makes the operator complex symmetric (V K = K^T V
+// on the interior rows).  Boundary (identity) rows get weight 1.
+template <class T>
+__device__ __forceinline__ T edge_vol(const Lev<T>& L, const Mesh& M, int o, int i, int j, int k) {
+    if (mbnd(M, o, i, j, k)) return T(1);
+    if (o == OX) return T(0.25) / (__ldg(L.ax.rh + i) * __ldg(L.ay.rs + j) * __ldg(L.az.rs + k));
+    if (o == OY) return T(0.25) / (__ldg(L.ay.rh + j) * __ldg(L.ax.rs + i) * __ldg(L.az.rs + k));
+    return T(0.25) / (__ldg(L.az.rh + k) * __ldg(L.ax.rs + i) * __ldg(L.ay.rs + j));
+}
+
 // ---------------------------------------------------------------- system groups
 // A thread's systems are s0 .. s0+VS-1 with s0 = (threadIdx.x % G) * VS;
 // blockDim and the grid stride are multiples of G.

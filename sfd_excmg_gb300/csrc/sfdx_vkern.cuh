@@ -148,10 +148,12 @@ __global__ void k_apply_v(Lev<T> L, Mesh M, SysG sgp, const double* wms, const c
 // ------------------------------------------------------------------ multi-colour SSOR
 // Forward sweep of colour (O,P):  w_e = (rhs_e - sum_{earlier colours} K_en w_n) / D_e,
 // rhs from MODE (RHS_PUPD: p = r + beta (p - omega v) stored in q; RHS_SUPD:
-// s = r - alpha v stored in q; RHS_VEC: q).
+// s = r - alpha v stored in q; RHS_VEC: q; RHS_COCR: q = r + beta q stored in
+// q (the operator image of the new search direction) and aux = v + beta aux
+// (the search direction itself), rhs = q).
 template <class T, int VS, int O, int P, int MODE>
 __global__ void k_fwd_v(Lev<T> L, Mesh M, SysG sgp, const KState* st, cplx<T>* __restrict__ w, cplx<T>* __restrict__ q,
-                        const cplx<T>* __restrict__ r, const cplx<T>* __restrict__ v) {
+                        const cplx<T>* __restrict__ r, const cplx<T>* __restrict__ v, cplx<T>* __restrict__ aux) {
     const int ns = sgp.ns, s0 = (threadIdx.x % sgp.G) * VS;
     const SysV<T, VS> S = load_sys<T, VS>(st, s0);
     if (!S.act) return;
@@ -163,6 +165,8 @@ __global__ void k_fwd_v(Lev<T> L, Mesh M, SysG sgp, const KState* st, cplx<T>* _
             c2[u] = cst<T>(st[s0 + u].omega);
         } else if (MODE == RHS_SUPD) {
             c1[u] = cst<T>(st[s0 + u].alpha);
+        } else if (MODE == RHS_COCR) {
+            c1[u] = cst<T>(st[s0 + u].beta);
         }
     }
     SFDX_GRID_LOOP(t, mcolour_count(M, O) * sgp.G) {
@@ -186,6 +190,19 @@ __global__ void k_fwd_v(Lev<T> L, Mesh M, SysG sgp, const KState* st, cplx<T>* _
 #pragma unroll
             for (int u = 0; u < VS; u++) rhs.v[u] = rr.v[u] - cmul<T>(c1[u], vv.v[u]);
             cvst_m<T, VS>(q + g, rhs, S.act);
+        } else if (MODE == RHS_COCR) {
+            CV<T, VS> uu, qq, zz, pp;
+            cvld<T, VS>(uu, r + g);
+            cvldw<T, VS>(qq, q + g);
+            cvld<T, VS>(zz, v + g);
+            cvldw<T, VS>(pp, aux + g);
+#pragma unroll
+            for (int u = 0; u < VS; u++) {
+                rhs.v[u] = uu.v[u] + cmul<T>(c1[u], qq.v[u]);
+                pp.v[u] = zz.v[u] + cmul<T>(c1[u], pp.v[u]);
+            }
+            cvst_m<T, VS>(q + g, rhs, S.act);
+            cvst_m<T, VS>(aux + g, pp, S.act);
         } else {
             cvld<T, VS>(rhs, q + g);
         }
@@ -913,7 +930,9 @@ __global__ void k_reliable_v(Lev<double> L, Mesh M, SysG sgp, KState* st, const 
             Q.active = 0;
             continue;
         }
-        if (solver == 3) {
+        if (solver == 6) {
+            // COCR: the driver restarts the recurrence from the new residual
+        } else if (solver == 3) {
             double2 a = Q.alpha, o = Q.omega, ro = Q.rho;
             double od = o.x * o.x + o.y * o.y, rd = ro.x * ro.x + ro.y * ro.y;
             double2 q1 = make_double2((a.x * o.x + a.y * o.y) / od, (a.y * o.x - a.x * o.y) / od);
@@ -926,6 +945,225 @@ __global__ void k_reliable_v(Lev<double> L, Mesh M, SysG sgp, KState* st, const 
             double2 q1 = make_double2((a.x * bb.x + a.y * bb.y) / bd, (a.y * bb.x - a.x * bb.y) / bd);
             double2 q2 = make_double2((al2.x * om2.x + al2.y * om2.y) / od, (al2.y * om2.x - al2.x * om2.y) / od);
             Q.beta = make_double2(q1.x * q2.x - q1.y * q2.y, q1.x * q2.y + q1.y * q2.x);
+        }
+    }
+}
+
+// ------------------------------------------------------------------ COCR
+// Preconditioned COCR (Sogabe & Zhang 2007) in the bilinear form
+// B(u, v) = sum_e u_e V_e v_e (no conjugation): V K and V M are complex
+// symmetric for the operator K of fd_assemb/dcfast and its multi-colour SSOR M
+// (V the edge dual volumes), so the short recurrence of COCR applies.  Per
+// iteration one operator application (u = K z) and one preconditioner
+// application (q = M^-1 w); the direction updates p = z + beta p and
+// w = u + beta w ride on the first sweep (RHS_COCR).
+
+// x_b = b_b on the boundary edges (identity rows), so that the boundary
+// residual is zero before the recurrence starts and stays zero
+template <class XT, int VS>
+__global__ void k_fix_bnd(Mesh M, SysG sgp, const KState* st, const cplx<XT>* __restrict__ b, cplx<XT>* __restrict__ x) {
+    const int ns = sgp.ns, s0 = (threadIdx.x % sgp.G) * VS;
+    const SysV<XT, VS> S = load_sys<XT, VS>(st, s0);
+    if (!S.act) return;
+    SFDX_GRID_LOOP(t, M.nl * sgp.G) {
+        const uint32_t e = fdiv(sgp.fG, t);
+        int i, j, k;
+        const int o = mdecode(M, e, i, j, k);
+        if (!mbnd(M, o, i, j, k)) continue;
+        const size_t g = (size_t)e * ns + s0;
+        CV<XT, VS> bv;
+        cvld<XT, VS>(bv, b + g);
+        cvst_m<XT, VS>(x + g, bv, S.act);
+    }
+}
+
+// u = K z ; rho_new = B(z, u) ; beta = rho_new / rho (FIRST: 0) ; rho = rho_new
+template <class T, int VS, bool FIRST>
+__global__ void k_cocr_u(Lev<T> L, Mesh M, SysG sgp, KState* st, const cplx<T>* __restrict__ z, cplx<T>* __restrict__ u,
+                         RedBuf rb) {
+    extern __shared__ double2 smem[];
+    typedef double A;  // the dual volumes span many orders of magnitude
+    const int ns = sgp.ns, s0 = (threadIdx.x % sgp.G) * VS;
+    const SysV<T, VS> S = load_sys<T, VS>(st, s0);
+    A ar[VS], ai[VS];
+#pragma unroll
+    for (int q = 0; q < VS; q++) ar[q] = ai[q] = 0;
+    if (S.act)
+        SFDX_GRID_LOOP(t, M.nl * sgp.G) {
+            uint32_t e;
+            int i, j, k;
+            const int o = mdecode_plane(M, fdiv(sgp.fG, t), e, i, j, k);
+            const size_t g = (size_t)e * ns + s0;
+            CV<T, VS> ze, val;
+            cvld<T, VS>(ze, z + g);
+            row_apply<T, VS>(L, M, o, e, i, j, k, z, ns, s0, S.wm, ze, val);
+            cvst_m<T, VS>(u + g, val, S.act);
+            const A vol = (A)edge_vol<T>(L, M, o, i, j, k);
+#pragma unroll
+            for (int q = 0; q < VS; q++) {
+                ar[q] += vol * ((A)ze.v[q].x * val.v[q].x - (A)ze.v[q].y * val.v[q].y);
+                ai[q] += vol * ((A)ze.v[q].x * val.v[q].y + (A)ze.v[q].y * val.v[q].x);
+            }
+        }
+    double2 acc[1][VS];
+#pragma unroll
+    for (int q = 0; q < VS; q++) acc[0][q] = make_double2(ar[q], ai[q]);
+    if (!vreduce_last<1, VS>(acc, sgp, rb, smem)) return;
+    const int B = blockDim.x;
+    for (int ss = threadIdx.x; ss < ns; ss += B) {
+        KState& Q = st[ss];
+        if (!Q.active) continue;
+        const double2 rn = smem[B + ss], ro = Q.rho;
+        if (FIRST) {
+            Q.beta = make_double2(0.0, 0.0);
+        } else {
+            const double rd = ro.x * ro.x + ro.y * ro.y;
+            Q.beta = make_double2((rn.x * ro.x + rn.y * ro.y) / rd, (rn.y * ro.x - rn.x * ro.y) / rd);
+        }
+        Q.rho = rn;
+        if (!isfinite(Q.beta.x) || !isfinite(Q.beta.y) || (rn.x == 0.0 && rn.y == 0.0)) {
+            Q.active = 0;
+            Q.status = ST_BREAK;
+        }
+    }
+}
+
+// w = u + beta w ; p = z + beta p  (the direction update when the
+// preconditioner is not the SSOR sweep that fuses it)
+template <class T, int VS>
+__global__ void k_cocr_dir(Mesh M, SysG sgp, const KState* st, const cplx<T>* __restrict__ u, cplx<T>* __restrict__ w,
+                           const cplx<T>* __restrict__ z, cplx<T>* __restrict__ p) {
+    const int ns = sgp.ns, s0 = (threadIdx.x % sgp.G) * VS;
+    const SysV<T, VS> S = load_sys<T, VS>(st, s0);
+    if (!S.act) return;
+    cplx<T> be[VS];
+#pragma unroll
+    for (int q = 0; q < VS; q++) be[q] = cst<T>(st[s0 + q].beta);
+    SFDX_GRID_LOOP(t, M.nl * sgp.G) {
+        const size_t g = (size_t)fdiv(sgp.fG, t) * ns + s0;
+        CV<T, VS> uu, ww, zz, pp;
+        cvld<T, VS>(uu, u + g);
+        cvldw<T, VS>(ww, w + g);
+        cvld<T, VS>(zz, z + g);
+        cvldw<T, VS>(pp, p + g);
+#pragma unroll
+        for (int q = 0; q < VS; q++) {
+            ww.v[q] = uu.v[q] + cmul<T>(be[q], ww.v[q]);
+            pp.v[q] = zz.v[q] + cmul<T>(be[q], pp.v[q]);
+        }
+        cvst_m<T, VS>(w + g, ww, S.act);
+        cvst_m<T, VS>(p + g, pp, S.act);
+    }
+}
+
+// alpha = rho / B(w, q)
+template <class T, int VS>
+__global__ void k_cocr_alpha(Lev<T> L, Mesh M, SysG sgp, KState* st, const cplx<T>* __restrict__ w,
+                             const cplx<T>* __restrict__ q, RedBuf rb) {
+    extern __shared__ double2 smem[];
+    typedef double A;  // the dual volumes span many orders of magnitude
+    const int ns = sgp.ns, s0 = (threadIdx.x % sgp.G) * VS;
+    const SysV<T, VS> S = load_sys<T, VS>(st, s0);
+    A ar[VS], ai[VS];
+#pragma unroll
+    for (int u = 0; u < VS; u++) ar[u] = ai[u] = 0;
+    if (S.act)
+        SFDX_GRID_LOOP(t, M.nl * sgp.G) {
+            const uint32_t e = fdiv(sgp.fG, t);
+            int i, j, k;
+            const int o = mdecode(M, e, i, j, k);
+            const size_t g = (size_t)e * ns + s0;
+            CV<T, VS> wv, qv;
+            cvld<T, VS>(wv, w + g);
+            cvld<T, VS>(qv, q + g);
+            const A vol = (A)edge_vol<T>(L, M, o, i, j, k);
+#pragma unroll
+            for (int u = 0; u < VS; u++) {
+                ar[u] += vol * ((A)wv.v[u].x * qv.v[u].x - (A)wv.v[u].y * qv.v[u].y);
+                ai[u] += vol * ((A)wv.v[u].x * qv.v[u].y + (A)wv.v[u].y * qv.v[u].x);
+            }
+        }
+    double2 acc[1][VS];
+#pragma unroll
+    for (int u = 0; u < VS; u++) acc[0][u] = make_double2(ar[u], ai[u]);
+    if (!vreduce_last<1, VS>(acc, sgp, rb, smem)) return;
+    const int B = blockDim.x;
+    for (int ss = threadIdx.x; ss < ns; ss += B) {
+        KState& Q = st[ss];
+        if (!Q.active) continue;
+        const double2 d = smem[B + ss], n = Q.rho;
+        const double den = d.x * d.x + d.y * d.y;
+        Q.alpha = make_double2((n.x * d.x + n.y * d.y) / den, (n.y * d.x - n.x * d.y) / den);
+        if (!isfinite(Q.alpha.x) || !isfinite(Q.alpha.y)) {
+            Q.active = 0;
+            Q.status = ST_BREAK;
+        }
+    }
+}
+
+// x += alpha p ; r -= alpha w ; z -= alpha q ; err = |r| / |b| and the
+// stopping tests (as GPBiCG: solvers.f90:272 semantics)
+template <class T, class XT, int VS>
+__global__ void k_cocr_upd(Mesh M, SysG sgp, KState* st, cplx<XT>* __restrict__ x, cplx<T>* __restrict__ r,
+                           cplx<T>* __restrict__ z, const cplx<T>* __restrict__ p, const cplx<T>* __restrict__ w,
+                           const cplx<T>* __restrict__ q, RedBuf rb, double* err_rec, int err_stride) {
+    extern __shared__ double2 smem[];
+    typedef typename AccOf<T>::type A;
+    const int ns = sgp.ns, s0 = (threadIdx.x % sgp.G) * VS;
+    const SysV<T, VS> S = load_sys<T, VS>(st, s0);
+    cplx<T> al[VS];
+    cplx<XT> alx[VS];
+    A rr[VS];
+#pragma unroll
+    for (int u = 0; u < VS; u++) {
+        al[u] = cst<T>(st[s0 + u].alpha);
+        alx[u] = cst<XT>(st[s0 + u].alpha);
+        rr[u] = 0;
+    }
+    if (S.act)
+        SFDX_GRID_LOOP(t, M.nl * sgp.G) {
+            const size_t g = (size_t)fdiv(sgp.fG, t) * ns + s0;
+            CV<T, VS> rv, zv, pv, wv, qv;
+            CV<XT, VS> xv;
+            cvldw<T, VS>(rv, r + g);
+            cvldw<T, VS>(zv, z + g);
+            cvld<T, VS>(pv, p + g);
+            cvld<T, VS>(wv, w + g);
+            cvld<T, VS>(qv, q + g);
+            cvldw<XT, VS>(xv, x + g);
+#pragma unroll
+            for (int u = 0; u < VS; u++) {
+                const cplx<XT> p2 = mk<XT>((XT)pv.v[u].x, (XT)pv.v[u].y);
+                xv.v[u] = xv.v[u] + cmul<XT>(alx[u], p2);
+                rv.v[u] = rv.v[u] - cmul<T>(al[u], wv.v[u]);
+                zv.v[u] = zv.v[u] - cmul<T>(al[u], qv.v[u]);
+                rr[u] += cabs2<T>(rv.v[u]);
+            }
+            cvst_m<XT, VS>(x + g, xv, S.act);
+            cvst_m<T, VS>(r + g, rv, S.act);
+            cvst_m<T, VS>(z + g, zv, S.act);
+        }
+    double2 acc[1][VS];
+#pragma unroll
+    for (int u = 0; u < VS; u++) acc[0][u] = make_double2(rr[u], 0.0);
+    if (!vreduce_last<1, VS>(acc, sgp, rb, smem)) return;
+    const int B = blockDim.x;
+    for (int ss = threadIdx.x; ss < ns; ss += B) {
+        KState& Q = st[ss];
+        if (!Q.active) continue;
+        Q.err = sqrt(smem[B + ss].x) / Q.babs;
+        if (err_rec && Q.it <= Q.itmax) err_rec[(size_t)ss * err_stride + Q.it - 1] = Q.err;
+        Q.iters = Q.it;
+        Q.it += 1;
+        if (isnan(Q.err)) {
+            Q.status = ST_NAN;
+            Q.active = 0;
+        } else if (Q.err <= Q.tol) {
+            Q.status = ST_CONV;
+            Q.active = 0;
+        } else if (Q.iters >= Q.itmax) {
+            Q.status = ST_MAXIT;
+            Q.active = 0;
         }
     }
 }

@@ -185,7 +185,7 @@ def _earth_edges(m):
     return np.concatenate([kx >= na, ky >= na, kz >= na])
 
 
-@pytest.mark.parametrize("solver", [1, 3])
+@pytest.mark.parametrize("solver", [1, 3, 6])
 def test_krylov_fp64_converges_to_direct_solution(solver):
     m = _model(0)
     ff = 1.0
@@ -207,7 +207,7 @@ def test_krylov_fp64_converges_to_direct_solution(solver):
         assert np.linalg.norm(K @ (x[:, s] - xd)) <= 1e-9 * np.linalg.norm(p)
 
 
-@pytest.mark.parametrize("solver", [1, 3])
+@pytest.mark.parametrize("solver", [1, 3, 6])
 def test_krylov_mixed_precision_reaches_fp64_tolerance(solver):
     m = _model(3)
     ff = 0.1
@@ -221,7 +221,7 @@ def test_krylov_mixed_precision_reaches_fp64_tolerance(solver):
         assert np.linalg.norm(r) < 1e-10 * np.linalg.norm(p)
 
 
-@pytest.mark.parametrize("solver", [1, 3])
+@pytest.mark.parametrize("solver", [1, 3, 6])
 def test_krylov_batched_systems_non_power_of_two(solver):
     """Six systems (three frequencies x two right-hand sides): two systems per thread,
     three thread groups, so the per-system reductions take the shared-memory tree."""
@@ -239,6 +239,27 @@ def test_krylov_batched_systems_non_power_of_two(solver):
     for s in range(6):
         r = rhs[:, s] - Ks[s] @ x[:, s]
         assert np.linalg.norm(r) <= 1.01e-9 * np.linalg.norm(rhs[:, s])
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_cocr_with_gradient_correction_converges(precision):
+    """COCR (solver 6) in restart cycles with the gradient-space correction reaches the
+    tolerance on the true FP64 residual, for complex128 and for complex64 iterations."""
+    m = _model(10)
+    freqs = [0.02, 0.02, 8.0, 8.0]
+    rhs, Ks = [], []
+    for q in range(2):
+        K, p1, p2, _ = _csr(m, freqs[2 * q])
+        Ks += [K, K]
+        rhs += [p1, p2]
+    rhs = np.stack(rhs, axis=1)
+    x, it, rr, rc = S.krylov_solve(m.nx, m.ny, m.nz, m.a, m.b, m.c, m.sigma, freqs, rhs, tol=1e-9, itmax=3000,
+                                   solver=6, div_cor=2, corr_intv=40, corr_tol=1e-2,
+                                   precision=S.MIXED if precision == "mixed" else S.FP64)
+    assert rc == 0, (it, rr)
+    for s in range(4):
+        r = rhs[:, s] - Ks[s] @ x[:, s]
+        assert np.linalg.norm(r) <= 1.05e-9 * np.linalg.norm(rhs[:, s])
 
 
 def test_grad_correct_matches_oracle():

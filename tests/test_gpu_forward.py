@@ -86,7 +86,8 @@ def test_uncorrected_error_lies_in_gradient_space():
     entirely a discrete gradient: one correction step brings the impedances to the
     corrected accuracy."""
     m = syn.small_aniso(n=16, seed=1, freqs=(0.05,))
-    ex, it, rr = S.fwd_solve(m, eps=1e-10, excmg=1, level=3, div_cor=0, solver=3)
+    # (without the correction FP64 GPBiCG can stall near 1e-10 on this model)
+    ex, it, rr = S.fwd_solve(m, eps=1e-9, excmg=1, level=3, div_cor=0, solver=3)
     _, zref = _direct_Z(m)
     zr = _zc(zref)
     e0 = np.abs(_zc(S.impedance(m, ex)) - zr) / np.abs(zr)
