@@ -151,6 +151,9 @@ WORKLOADS = {
     "cfg4": ("cfg4: 128x128x96 core cells of 25 m + 16 padding per side, 12 bottom, 36 air (160x160x144, "
              "11,203,024 edges), 3 layers + 10 anisotropic boxes, 6 freqs 0.01..100 Hz x 2 pols, EXCMG 4 levels, "
              "tol {eps:g}", 1e-7),
+    "cfg3": ("cfg3: 8 models per batch, cells per axis drawn from {{48,...,96}} (padding and air included), isotropic "
+             "log10 rho GRF (mean 2, std 0.5, corr 5 cells), 16 freqs 1e-3..1e3 Hz x 2 pols = 256 systems, EXCMG 3 "
+             "levels, tol {eps:g}, one host thread + stream per model", 1e-10),
     "dtm1": ("dtm1: the reference's DTM1.0 example (input.py), 128x128x192 cells incl. 64 air layers "
              "(9,568,704 edges), 4 freqs 0.001..1 Hz x 2 pols, EXCMG 4 levels, tol {eps:g}, 68 receivers", 1e-10),
 }
@@ -344,6 +347,9 @@ def run_ours(args, rank, world, local):
                  "fp64_fine_iters": p64.iters[:, :, -1].ravel().tolist()}
         p64.close()
 
+    if rank == 0 and args.adjoint:
+        extra["adjoint"] = adjoint_measure(S, syn, torch, stream, args.solver, 1e-10, fd_cells=args.fd_cells)
+
     if rank != 0:
         plan.close()
         return
@@ -378,6 +384,193 @@ def run_ours(args, rank, world, local):
     line.update(extra)
     print(json.dumps(line), flush=True)
     plan.close()
+
+
+def adjoint_measure(S, syn, torch, stream, solver, eps, fd_cells=0, reps=2, seed=0):
+    """cfg5: least-squares impedance misfit of an isotropic GRF model against data from a
+    perturbed model (+2 % Gaussian noise, weights 1/(0.02|Z|)^2) and its gradient
+    d misfit / d log sigma by one adjoint solve per frequency and polarisation.  Times the
+    forward solve (+ misfit) and the adjoint (+ per-cell contraction) with CUDA events on
+    the plan's stream, compares the mixed-precision gradient with the FP64 GPU adjoint and,
+    with fd_cells > 0, both with central differences (h = 1e-4 in log sigma) of FP64 GPU
+    forward solves at that many random core cells (each perturbed solve starts from the base
+    fields and solves the correction equation to a 1e-9 reduction, sfdx_plan_resolve)."""
+    m, mt = syn.config5(seed), syn.config5_true(seed)
+    opts = solve_opts("mixed", solver, 2, eps, None, m.level)
+    opts64 = solve_opts("fp64", solver, 2, eps, None, m.level)
+    with S.Plan(mt, **opts) as pt:
+        pt.solve(fetch=False, allow_noconv=True)
+        z = pt.impedance()
+    rng = np.random.default_rng(seed + 7)
+    zc = z[..., 0::2] + 1j * z[..., 1::2]
+    sd = 0.02 * np.abs(zc)
+    zn = zc + sd * (rng.standard_normal(zc.shape) + 1j * rng.standard_normal(zc.shape)) / np.sqrt(2)
+    zobs = np.stack([zn.real[..., 0], zn.imag[..., 0], zn.real[..., 1], zn.imag[..., 1]], -1)
+    wts = 1.0 / sd ** 2
+    plan = S.Plan(m, **opts)
+    plan.set_stream(stream.cuda_stream)
+    sig = torch.from_numpy(np.ascontiguousarray(m.sigma)).to("cuda")
+    g = torch.empty((6, m.ncell), dtype=torch.float64, device="cuda")
+
+    def fwd():
+        plan.solve(sigma_device_ptr=sig.data_ptr(), fetch=False, allow_noconv=True)
+        return plan.misfit_grad(zobs, wts, with_grad=False)[0]
+
+    def adj():
+        return plan.misfit_grad(zobs, wts, grad_device_ptr=g.data_ptr(), allow_noconv=True)
+
+    fwd()
+    adj()
+    tf, ta = [], []
+    for _ in range(reps):
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        ev[0].record(stream)
+        mis = fwd()
+        ev[1].record(stream)
+        res = adj()
+        ev[2].record(stream)
+        ev[2].synchronize()
+        tf.append(ev[0].elapsed_time(ev[1]))
+        ta.append(ev[1].elapsed_time(ev[2]))
+    fwd_iters = plan.iters[:, :, -1].ravel().tolist()
+    adj_iters, adj_rr = res[3].ravel().tolist(), float(res[4].max())
+    sg3 = m.sigma[0]
+    dlog = sg3 * g[0:3].sum(0).cpu().numpy()
+    plan.close()
+    p64 = S.Plan(m, **opts64)
+    p64.solve(fetch=False, allow_noconv=True)
+    mis64, g64, _, it64, _ = p64.misfit_grad(zobs, wts, allow_noconv=True)
+    dlog64 = sg3 * g64[0:3].sum(0)
+    out = {"workload": ("cfg5: cfg2 mesh without hills (80x80x80, 1,574,640 edges), isotropic log10 rho GRF "
+                        "(mean 2, std 0.5, corr 5 cells), 6 freqs 1e-3..1e3 Hz x 2 pols, 32x32 receivers, data "
+                        "from a perturbed GRF model + 2 % noise, EXCMG 3 levels, tol " + f"{eps:g}"),
+           "precision": "mixed", "fwd_ms": float(np.median(tf)), "adjoint_ms": float(np.median(ta)),
+           "grad_over_fwd": float(np.median(ta) / np.median(tf)),
+           "fwd_plus_grad_over_fwd": float((np.median(tf) + np.median(ta)) / np.median(tf)),
+           "misfit": mis, "misfit_fp64": mis64,
+           "grad_rel_err_vs_fp64_adjoint": float(np.linalg.norm(dlog - dlog64) / np.linalg.norm(dlog64)),
+           "fwd_fine_iters": fwd_iters, "adjoint_iters": adj_iters, "adjoint_relres_max": adj_rr,
+           "adjoint_iters_fp64": it64.ravel().tolist()}
+    if fd_cells:
+        rs = np.random.default_rng(seed + 11)
+        npad, nc, ncz = 8, 64, 48
+        cells, fd = [], []
+        for _ in range(fd_cells):
+            i = rs.integers(npad, npad + nc)
+            j = rs.integers(npad, npad + nc)
+            k = rs.integers(m.nair, m.nair + ncz // 3)
+            cells.append(int((k * m.ny + j) * m.nx + i))
+        h = 1e-4
+        for c in cells:
+            f = []
+            for sgn in (1, -1):
+                s2 = m.sigma.copy()
+                s2[0:3, c] *= np.exp(sgn * h)
+                p64.resolve(sigma=s2, tol=-1e-9, allow_noconv=True)
+                f.append(p64.misfit_grad(zobs, wts, with_grad=False)[0])
+            fd.append((f[0] - f[1]) / (2 * h))
+        fd = np.array(fd)
+        a64 = dlog64[cells]
+        am = dlog[cells]
+        out["fd_check"] = {"cells": len(cells), "h_log_sigma": h, "forward": "fp64 GPU, correction equation from the base fields",
+                           "max_rel_err_fp64_adjoint": float(np.max(np.abs(a64 - fd) / np.abs(fd))),
+                           "median_rel_err_fp64_adjoint": float(np.median(np.abs(a64 - fd) / np.abs(fd))),
+                           "max_rel_err_mixed_adjoint": float(np.max(np.abs(am - fd) / np.abs(fd))),
+                           "median_rel_err_mixed_adjoint": float(np.median(np.abs(am - fd) / np.abs(fd))),
+                           "fd": fd.tolist(), "adjoint_fp64": a64.tolist(), "adjoint_mixed": am.tolist()}
+    p64.close()
+    return out
+
+
+def run_batch(args, rank, world, local):
+    """cfg3: the 8 models solved together (sfdx_plan_solve_batch: one host thread and
+    stream per model) -- value; the same plans one after another -- sequential_solves_per_s."""
+    import torch
+    torch.cuda.set_device(local)
+    import sfd_excmg_gb300 as S
+    from sfd_excmg_gb300 import capi
+    from sfd_excmg_gb300 import synthetic as syn
+    eps = args.eps if args.eps else WORKLOADS["cfg3"][1]
+    models = syn.config3(seed=rank)
+    opts = solve_opts(args.precision, args.solver, args.div_cor, eps, args.corr_intv, 3)
+    plans = [S.Plan(m, **opts) for m in models]
+    sig = [torch.from_numpy(np.ascontiguousarray(m.sigma)).to("cuda") for m in models]
+    ptrs = [t.data_ptr() for t in sig]
+    ns = sum(2 * m.nf for m in models)
+    L = capi.lib()
+
+    def step():
+        S.solve_batch(plans, sigma_device_ptrs=ptrs, allow_noconv=True)
+        return [p.impedance() for p in plans]
+
+    step()
+    vs = [p.autotune() for p in plans]
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    barrier(world)
+    clocks = Clocks(local)
+    clocks.start()
+    l0 = L.sfdx_launch_count()
+    t = time.perf_counter()
+    for _ in range(args.steps):
+        z = step()
+    torch.cuda.synchronize()
+    sec = (time.perf_counter() - t) / args.steps
+    launches = (L.sfdx_launch_count() - l0) / args.steps
+    clk = clocks.stop()
+    sec = max_over_ranks(sec, world)
+    # the same plans one after another
+    t = time.perf_counter()
+    for p, ptr in zip(plans, ptrs):
+        p.solve(sigma_device_ptr=ptr, fetch=False, allow_noconv=True)
+        p.impedance()
+    torch.cuda.synchronize()
+    seq = time.perf_counter() - t
+    # end to end: host conductivities in, impedances out
+    t = time.perf_counter()
+    S.solve_batch(plans, sigmas=[m.sigma for m in models], allow_noconv=True)
+    zz = [p.impedance() for p in plans]
+    e2e = time.perf_counter() - t
+    h2d = sum(m.sigma.nbytes for m in models)
+    d2h = sum(z_.nbytes for z_ in zz)
+    status = [int(p.status) for p in plans]
+    iters = [p.iters[:, :, -1].ravel().tolist() for p in plans]
+    for p in plans:
+        p.close()
+    extra = {}
+    if args.compare_fp64 and rank == 0:
+        p64 = [S.Plan(m, **solve_opts("fp64", args.solver, args.div_cor, eps, args.corr_intv, 3)) for m in models]
+        t = time.perf_counter()
+        S.solve_batch(p64, sigma_device_ptrs=ptrs, allow_noconv=True)
+        t64 = time.perf_counter() - t
+        rel = []
+        for p, zm in zip(p64, z):
+            z64 = p.impedance()
+            a = zm[..., 0::2] + 1j * zm[..., 1::2]
+            b = z64[..., 0::2] + 1j * z64[..., 1::2]
+            rel.append((np.abs(a - b) / np.abs(b)).ravel())
+            p.close()
+        rel = np.concatenate(rel)
+        extra = {"z_rel_err_vs_fp64": float(rel.max()), "z_rel_err_vs_fp64_median": float(np.median(rel)),
+                 "fp64_solves_per_s": ns / t64}
+    if rank != 0:
+        return
+    value = ns * world / sec
+    line = {
+        "metric": "MT solves/s", "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "c64+c128" if args.precision == "mixed" else "c128", "data": "synthetic",
+        "config": {"workload": WORKLOADS["cfg3"][0].format(eps=eps),
+                   "meshes": [[m.nx, m.ny, m.nz] for m in models], "edges": [int(m.nl) for m in models],
+                   "precision": args.precision, "solver": args.solver, "div_cor": args.div_cor,
+                   "systems_per_thread": vs, "systems_per_step": ns, "l2": "working set > L2 (no flush)"},
+        "e2e": {"value": ns / e2e, "unit": "solves/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": int(launches), "sequential_solves_per_s": ns / seq, "clocks": clk,
+        "solve": {"status": status, "fine_iters": iters},
+    }
+    line.update(extra)
+    print(json.dumps(line), flush=True)
 
 
 def run_profile(args):
@@ -419,6 +612,11 @@ def main():
     ap.add_argument("--div-cor", dest="div_cor", type=int, default=2, choices=[0, 1, 2],
                     help="0 none, 1 the reference's divergence correction, 2 consistent gradient-space correction")
     ap.add_argument("--no-compare-fp64", dest="compare_fp64", action="store_false")
+    ap.add_argument("--no-adjoint", dest="adjoint", action="store_false",
+                    help="skip the misfit-gradient measurement (cfg5 workload: forward vs adjoint time, FP64 check)")
+    ap.add_argument("--fd-cells", dest="fd_cells", type=int, default=0,
+                    help="also check the gradient against central differences of FP64 forward solves at this many "
+                         "random cells (cfg5 asks for 20)")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     ap.add_argument("--e2e-strict", dest="e2e_allow_noconv", action="store_false")
     ap.add_argument("--profile", action="store_true",
@@ -430,6 +628,8 @@ def main():
         run_profile(args)
     elif args.impl == "reference":
         run_reference(args, rank, world)
+    elif args.workload == "cfg3":
+        run_batch(args, rank, world, local)
     else:
         run_ours(args, rank, world, local)
 

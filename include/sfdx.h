@@ -127,10 +127,48 @@ int sfdx_plan_create(sfdx_plan** plan, const sfdx_opts* o, int nx, int ny, int n
                      const double* b, const double* c, int nf, const double* freq);
 int sfdx_plan_solve(sfdx_plan* plan, const double* sigma, int sigma_on_device, double* ex, int ex_on_device,
                     int* iters, double* relres);
+/* Solve several plans at once (models of different meshes and frequency lists):
+ * each plan runs on its own host thread and its own stream (plans must be
+ * distinct and should not share a stream), so the GPU overlaps the models.
+ * Per plan q: sigma[q], ex[q] (array or entries may be null), iters[q],
+ * relres[q] (optional) as sfdx_plan_solve; status[q] its return code.
+ * Returns the first error of any plan (SFDX_ERR_NOCONV only if nothing
+ * worse).  No counterpart in the reference (it solves one system at a time). */
+int sfdx_plan_solve_batch(int nplans, sfdx_plan* const* plans, const double* const* sigma, int sigma_on_device,
+                          double* const* ex, int ex_on_device, int* const* iters, double* const* relres, int* status);
+/* Re-solve the finest level for a changed conductivity, starting from the
+ * fields of the plan's last full solve (no EXCMG cascade): perturbation and
+ * continuation studies (finite-difference checks of the misfit gradient), where
+ * those fields are a close initial guess and their error cancels in a central
+ * difference.  tol > 0: relative residual of A x = b from those fields;
+ * tol <= 0: solve the correction equation A d = b - A x0 from zero to a relative
+ * reduction |tol| (0: the plan's eps) and return x0 + d.  Outputs as
+ * sfdx_plan_solve (iters: the finest-level slot).  No counterpart in the
+ * reference. */
+int sfdx_plan_resolve(sfdx_plan* plan, const double* sigma, int sigma_on_device, double tol, int* iters,
+                      double* relres);
 /* Load (and coarsen) the conductivity without solving. */
 int sfdx_plan_load(sfdx_plan* plan, const double* sigma, int sigma_on_device);
 /* Impedances from the plan's last solution (device resident), see sfdx_impedance. */
 int sfdx_plan_impedance(sfdx_plan* plan, int nrec, const double* recv, int out_type, double* out, double* tipper);
+/* Gradient of the impedance misfit of the plan's last solution with respect to
+ * the cell conductivities, by one adjoint solve per frequency and polarisation
+ * (the forward operator with a right-hand side on the receiver planes, solved
+ * with the plan's solver, precision and corrections from a zero guess).  No
+ * counterpart in the reference (it has no inversion path).
+ *   zobs [nf][nrec][4] observed (Re Zxy, Im Zxy, Re Zyx, Im Zyx); wts
+ *   [nf][nrec][2] data weights (null: 1); misfit = sum wxy |Zxy - dxy|^2 +
+ *   wyx |Zyx - dyx|^2 over frequencies and receivers; zpred (optional)
+ *   [nf][nrec][4] the predicted impedances; grad [6][ncell] = d misfit /
+ *   d sigma(cell, component) with the Dirichlet data (the 1-D background of
+ *   cell column (1,1)) held fixed, on the device if grad_on_device (null:
+ *   misfit and zpred only, no adjoint solve); tol the
+ *   adjoint solve's relative residual (<= 0: the plan's eps); adj_iters /
+ *   adj_relres (optional, [nf][2]) its iterations and FP64 relative residuals.
+ * The forward fields stay valid (sfdx_plan_fields, sfdx_plan_impedance). */
+int sfdx_plan_misfit_grad(sfdx_plan* plan, int nrec, const double* recv, const double* zobs, const double* wts,
+                          double tol, double* misfit, double* zpred, double* grad, int grad_on_device,
+                          int* adj_iters, double* adj_relres);
 /* Device pointer of the plan's last solution, layout [nf][2][nl] complex (valid until the next solve). */
 const double* sfdx_plan_fields(sfdx_plan* plan);
 /* Bytes of device memory held by the plan. */

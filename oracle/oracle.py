@@ -441,3 +441,153 @@ def grad_correct(nx, ny, nz, a, b, c, sigma, ff, rhs, x):
     lu = splu(N)
     phi = lu.solve(t.real) + 1j * lu.solve(t.imag)
     return _z(x) + G @ phi
+
+
+# --------------------------------------------------------------------------- adjoint gradient
+# No counterpart in the reference (it has no inversion path).  The checker of the
+# library's misfit gradient, computed independently of the library's route: the
+# transposed system is solved directly (no use of the dual-volume symmetry), the
+# operator derivative comes from re-assembling fd_assemb + dcfast with one cell
+# perturbed (the rows are linear in sigma), and the derivative of the impedances
+# with respect to the edge values from probing post_process (linear in the
+# fields) and a fourth-order difference of Z(E, H) (holomorphic).
+def _zfun(f):
+    """(Zxy, Zyx) from the receiver fields f[10] = (Ex, Ey, Hx, Hy, Hz) x 2 polarisations."""
+    ex1, ey1, hx1, hy1 = f[0], f[1], f[2], f[3]
+    ex2, ey2, hx2, hy2 = f[5], f[6], f[7], f[8]
+    det = hx1 * hy2 - hx2 * hy1
+    return np.array([(ex2 * hx1 - ex1 * hx2) / det, (ey1 * hy2 - ey2 * hy1) / det])
+
+
+def _dz_dfields(f):
+    """d(Zxy, Zyx)/d f (2 x 10, holomorphic derivative) by a fourth-order central difference."""
+    out = np.zeros((2, 10), np.complex128)
+    for q in range(10):
+        h = 1e-4 * max(abs(f[q]), np.abs(f).max() * 1e-3)
+        e = np.zeros(10, np.complex128)
+        e[q] = h
+        out[:, q] = (-_zfun(f + 2 * e) + 8 * _zfun(f + e) - 8 * _zfun(f - e) + _zfun(f - 2 * e)) / (12 * h)
+    return out
+
+
+def _surface_edges(nx, ny, nz, nair):
+    """Edge indices post_process reads: Ex and Ey on node planes nair, nair+1, Ez of layer nair."""
+    xnl = nx * (ny + 1) * (nz + 1)
+    ynl = (nx + 1) * ny * (nz + 1)
+    pex, pey, pez = nx * (ny + 1), (nx + 1) * ny, (nx + 1) * (ny + 1)
+    return np.concatenate([nair * pex + np.arange(2 * pex), xnl + nair * pey + np.arange(2 * pey),
+                           xnl + ynl + nair * pez + np.arange(pez)])
+
+
+def receiver_jacobian(model: OracleModel, ff, rd=2):
+    """J[nrec, 5, n_surface] with fields(pol) = J x_pol on the surface edges, and those edge indices."""
+    idx = _surface_edges(model.nx, model.ny, model.nz, model.nair)
+    nl = nedges(model.nx, model.ny, model.nz)
+    nrec = model.recv.shape[0]
+    J = np.zeros((nrec, 5, idx.size), np.complex128)
+    x = np.zeros(nl, np.complex128)
+    zero = np.zeros(nl, np.complex128)
+    for t, e in enumerate(idx):
+        x[e] = 1.0
+        _, _, fld = post_process(model, x, zero, ff, 1, rd)
+        J[:, :, t] = fld[:, 0:5]
+        x[e] = 0.0
+    return J, idx
+
+
+def misfit(model: OracleModel, zobs, wts=None, rd=2):
+    """sum_f,r wxy |Zxy - dxy|^2 + wyx |Zyx - dyx|^2 of the exact discrete solution."""
+    ex = np.zeros((model.freq.size, 2, nedges(model.nx, model.ny, model.nz)), np.complex128)
+    for k, ff in enumerate(model.freq):
+        u1, u2, _, _, _ = direct_solve(model, ff)
+        ex[k, 0], ex[k, 1] = u1, u2
+    z = impedances(model, ex, out_type=1, rd=rd)
+    zc = z[..., 0::2] + 1j * z[..., 1::2]
+    dc = zobs[..., 0::2] + 1j * zobs[..., 1::2]
+    w = np.ones(zc.shape) if wts is None else wts
+    return float((w * np.abs(zc - dc) ** 2).sum())
+
+
+def misfit_grad_cells(model: OracleModel, zobs, cells, comps, wts=None, rd=2):
+    """(misfit, d misfit / d sigma[comp, cell] for the listed (cell, comp) pairs, and per
+    frequency the exact forward fields x[2, nl] and adjoint fields mu[2, nl] with
+    K_II mu = V^-1 g_I, mu = 0 on the Dirichlet edges -- the quantities the library's
+    per-cell contraction uses)."""
+    nx, ny, nz = model.nx, model.ny, model.nz
+    nrec = model.recv.shape[0]
+    V = edge_dual_volumes(nx, ny, nz, model.a, model.b, model.c)
+    grad = np.zeros(len(cells))
+    phi = 0.0
+    xs, mus = [], []
+    conv = column_conv(model.sigma, nx, ny, nz)
+    for k, ff in enumerate(model.freq):
+        edc, _, _ = mt1d_anl(ff, conv, model.c)
+        K, p1, p2 = assemble(nx, ny, nz, model.a, model.b, model.c, model.sigma, ff, edc)
+        lu = splu(K.tocsc())
+        x = np.stack([lu.solve(p1), lu.solve(p2)])
+        _, _, fld = post_process(model, x[0], x[1], ff, 1, rd)
+        J, idx = receiver_jacobian(model, ff, rd)
+        g = np.zeros((2, x.shape[1]), np.complex128)
+        for r in range(nrec):
+            z = _zfun(fld[r])
+            d = zobs[k, r, 0::2] + 1j * zobs[k, r, 1::2]
+            w = np.ones(2) if wts is None else wts[k, r]
+            phi += float((w * np.abs(z - d) ** 2).sum())
+            cf = (w * np.conj(z - d)) @ _dz_dfields(fld[r])  # d phi / d fields[10]
+            for p in range(2):
+                g[p, idx] += cf[5 * p:5 * p + 5] @ J[r]
+        luT = splu(K.T.tocsc())
+        lam = np.stack([luT.solve(g[0]), luT.solve(g[1])])
+        interior = V > 0
+        mu = np.zeros_like(lam)
+        mu[:, interior] = lam[:, interior] / V[interior]
+        xs.append(x)
+        mus.append(mu)
+        for t, (cell, q) in enumerate(zip(cells, comps)):
+            sg = model.sigma.copy()
+            dl = max(abs(sg[q, cell]), 1e-3)
+            sg[q, cell] += dl
+            K2, q1, q2 = assemble(nx, ny, nz, model.a, model.b, model.c, sg, ff, edc)
+            dK = (K2 - K) / dl
+            dp = (np.stack([q1, q2]) - np.stack([p1, p2])) / dl
+            for p in range(2):
+                grad[t] += -2.0 * np.real(lam[p] @ (dK @ x[p] - dp[p]))
+    return phi, grad, xs, mus
+
+
+def sigma_grad_local(nx, ny, nz, a, b, c, wm, xs, mus):
+    """Per-cell contraction restated in numpy: d misfit / d sigma[6, ncell] from forward
+    fields xs[s] and adjoint fields mus[s] (zero on the Dirichlet edges) of systems with
+    w mu0 = wm[s]: -2 sum_s wm_s Im(sum_ee' (V dM/dsigma)_ee' mu_e x_e'), where V dM/dsigma
+    is vol/4 between an edge and itself for the diagonal components and vol/8 between the
+    differently oriented edges of one face level for the off-diagonal ones."""
+    a, b, c = _d(a), _d(b), _d(c)
+    xnl = nx * (ny + 1) * (nz + 1)
+    ynl = (nx + 1) * ny * (nz + 1)
+    k, j, i = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+    i, j, k = i.ravel(), j.ravel(), k.ravel()
+    vol = a[i] * b[j] * c[k]
+    EX = lambda dj, dk: ((k + dk) * (ny + 1) + j + dj) * nx + i  # noqa: E731
+    EY = lambda di, dk: xnl + ((k + dk) * ny + j) * (nx + 1) + i + di  # noqa: E731
+    EZ = lambda di, dj: xnl + ynl + (k * (ny + 1) + j + dj) * (nx + 1) + i + di  # noqa: E731
+    out = np.zeros((6, nx * ny * nz))
+    for s in range(len(wm)):
+        x, mu = xs[s], mus[s]
+        S = np.zeros((6, i.size), np.complex128)
+        for u in (0, 1):
+            for v in (0, 1):
+                S[0] += mu[EX(u, v)] * x[EX(u, v)]
+                S[1] += mu[EY(u, v)] * x[EY(u, v)]
+                S[2] += mu[EZ(u, v)] * x[EZ(u, v)]
+        for v in (0, 1):
+            S[3] += (mu[EX(0, v)] + mu[EX(1, v)]) * (x[EY(0, v)] + x[EY(1, v)]) + \
+                    (mu[EY(0, v)] + mu[EY(1, v)]) * (x[EX(0, v)] + x[EX(1, v)])
+        for u in (0, 1):
+            S[4] += (mu[EX(u, 0)] + mu[EX(u, 1)]) * (x[EZ(0, u)] + x[EZ(1, u)]) + \
+                    (mu[EZ(0, u)] + mu[EZ(1, u)]) * (x[EX(u, 0)] + x[EX(u, 1)])
+            S[5] += (mu[EY(u, 0)] + mu[EY(u, 1)]) * (x[EZ(u, 0)] + x[EZ(u, 1)]) + \
+                    (mu[EZ(u, 0)] + mu[EZ(u, 1)]) * (x[EY(u, 0)] + x[EY(u, 1)])
+        out += -2.0 * wm[s] * S.imag
+    out[:3] *= vol / 4
+    out[3:] *= vol / 8
+    return out

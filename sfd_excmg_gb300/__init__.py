@@ -8,13 +8,21 @@ from . import capi
 from .capi import FP64, MIXED, QUIRKS_REFERENCE, Opts, SfdxError
 from .model import Model
 from .solver import (Plan, apply_operator, build_rhs, fwd_solve, grad_correct, impedance, krylov_solve, mesh_coarsen,
-                     mt1d, precond_apply, prolongate)
+                     mt1d, precond_apply, prolongate, solve_batch)
 
 __all__ = [
     "capi", "Opts", "SfdxError", "FP64", "MIXED", "QUIRKS_REFERENCE", "Model", "Plan", "fwd_solve", "impedance",
     "mt1d", "apply_operator", "build_rhs", "precond_apply", "mesh_coarsen", "prolongate", "krylov_solve",
-    "grad_correct",
+    "grad_correct", "solve_batch", "sigma_misfit", "log_sigma_misfit",
 ]
+
+
+def __getattr__(name):
+    # the autograd functions import torch; load them on first use
+    if name in ("sigma_misfit", "log_sigma_misfit"):
+        from . import adjoint
+        return getattr(adjoint, name)
+    raise AttributeError(name)
 
 
 def build(verbose: bool = False) -> str:

@@ -81,7 +81,16 @@ _PROTO = {
                                        ctypes.c_int, c_int_p, c_double_p]),
     "sfdx_plan_impedance": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, c_double_p, ctypes.c_int, c_double_p,
                                            c_double_p]),
+    "sfdx_plan_misfit_grad": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, c_double_p, c_double_p, c_double_p,
+                                             ctypes.c_double, c_double_p, c_double_p, c_double_p, ctypes.c_int,
+                                             c_int_p, c_double_p]),
     "sfdx_plan_fields": (ctypes.c_void_p, [ctypes.c_void_p]),
+    "sfdx_plan_solve_batch": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_void_p),
+                                             ctypes.POINTER(ctypes.c_void_p), ctypes.c_int,
+                                             ctypes.POINTER(ctypes.c_void_p), ctypes.c_int,
+                                             ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_void_p), c_int_p]),
+    "sfdx_plan_resolve": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_double, c_int_p,
+                                         c_double_p]),
     "sfdx_plan_load": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]),
     "sfdx_plan_device_bytes": (ctypes.c_longlong, [ctypes.c_void_p]),
     "sfdx_plan_destroy": (None, [ctypes.c_void_p]),

@@ -21,6 +21,11 @@ namespace sfdx {
 typedef std::complex<double> zd;
 static const double kPi = 3.141592653589793238462643;
 static const double kMu = 4.0 * 3.141592653589793238462643 * 1e-7;
+#define HRC(x)                   \
+    do {                         \
+        int rc_ = (x);           \
+        if (rc_) return rc_;     \
+    } while (0)
 
 // -------------------------------------------------------------------- mt1d
 // Propagator form of Pek & Santos (2002) for a stack of anisotropic layers:
@@ -137,37 +142,79 @@ static double qcoef(double x, const double* x0, int q) {
     return (x - x0[0]) * (x - x0[1]) / (x0[2] - x0[0]) / (x0[2] - x0[1]);
 }
 
-int impedance_from_surface(const SurfaceView& sv, const double* a, const double* b, const double* c, double ff,
-                           int nrec, const double* recv, int out_type, int transpose, double* out, double* tip) {
-    const int nx = sv.nx, ny = sv.ny, nair = sv.nair;
-    const size_t nxy = (size_t)nx * ny;
-    std::vector<zd> E[2][2], H[2][3];  // E[pol][x|y], H[pol][x|y|z] at (i,j)
-    for (int p = 0; p < 2; p++) {
-        for (int q = 0; q < 2; q++) E[p][q].assign(nxy, 0);
-        for (int q = 0; q < 3; q++) H[p][q].assign(nxy, 0);
+// E (x, y) and H (x, y, z) of one polarisation at the cell centres (i, j) of
+// the surface, [j*nx + i]: E is the mean of the two surface edges, H = curl E
+// / (i w mu) from one-sided differences into the first earth layer.
+struct SurfFields {
+    std::vector<zd> E[2], H[3];
+    void init(size_t n) {
+        for (auto& v : E) v.assign(n, 0);
+        for (auto& v : H) v.assign(n, 0);
     }
-    const zd iwm = zd(0, 1) * 2.0 * kPi * ff * kMu;
-    const double cz = c[nair];
-    for (int p = 0; p < 2; p++)
-        for (int j = 0; j < ny; j++)
-            for (int i = 0; i < nx; i++) {
-                // Ex at plane m (=nair) and m+1, rows j, j+1; Ey at columns i, i+1; Ez layer m+1
-                zd ex0 = (sv.ex(p, 0, i, j) + sv.ex(p, 0, i, j + 1)) / 2.0;
-                zd ey0 = (sv.ey(p, 0, i, j) + sv.ey(p, 0, i + 1, j)) / 2.0;
-                E[p][0][(size_t)j * nx + i] = ex0;
-                E[p][1][(size_t)j * nx + i] = ey0;
-                zd exz = ((sv.ex(p, 1, i, j) + sv.ex(p, 1, i, j + 1)) / 2.0 - ex0) / cz;
-                zd ezx = ((sv.ez(p, i + 1, j) + sv.ez(p, i + 1, j + 1)) / 2.0 - (sv.ez(p, i, j + 1) + sv.ez(p, i, j)) / 2.0) / a[i];
-                zd eyz = ((sv.ey(p, 1, i, j) + sv.ey(p, 1, i + 1, j)) / 2.0 - ey0) / cz;
-                zd ezy = (-(sv.ez(p, i, j) + sv.ez(p, i + 1, j)) / 2.0 + (sv.ez(p, i, j + 1) + sv.ez(p, i + 1, j + 1)) / 2.0) / b[j];
-                zd exy = (sv.ex(p, 0, i, j + 1) - sv.ex(p, 0, i, j)) / b[j];
-                zd eyx = (sv.ey(p, 0, i + 1, j) - sv.ey(p, 0, i, j)) / a[i];
-                H[p][1][(size_t)j * nx + i] = (exz - ezx) / iwm;
-                H[p][0][(size_t)j * nx + i] = (ezy - eyz) / iwm;
-                H[p][2][(size_t)j * nx + i] = (exy - eyx) / iwm;
-            }
-    // cell-centre coordinates (arho_interp2 :729-735)
-    std::vector<double> aax(nx), bby(ny);
+};
+static void surface_fields(const SurfaceView& sv, int p, const double* a, const double* b, double cz, zd iwm,
+                           SurfFields& F) {
+    const int nx = sv.nx, ny = sv.ny;
+    F.init((size_t)nx * ny);
+    for (int j = 0; j < ny; j++)
+        for (int i = 0; i < nx; i++) {
+            const size_t id = (size_t)j * nx + i;
+            zd ex0 = (sv.ex(p, 0, i, j) + sv.ex(p, 0, i, j + 1)) / 2.0;
+            zd ey0 = (sv.ey(p, 0, i, j) + sv.ey(p, 0, i + 1, j)) / 2.0;
+            F.E[0][id] = ex0;
+            F.E[1][id] = ey0;
+            zd exz = ((sv.ex(p, 1, i, j) + sv.ex(p, 1, i, j + 1)) / 2.0 - ex0) / cz;
+            zd ezx = ((sv.ez(p, i + 1, j) + sv.ez(p, i + 1, j + 1)) / 2.0 - (sv.ez(p, i, j + 1) + sv.ez(p, i, j)) / 2.0) / a[i];
+            zd eyz = ((sv.ey(p, 1, i, j) + sv.ey(p, 1, i + 1, j)) / 2.0 - ey0) / cz;
+            zd ezy = (-(sv.ez(p, i, j) + sv.ez(p, i + 1, j)) / 2.0 + (sv.ez(p, i, j + 1) + sv.ez(p, i + 1, j + 1)) / 2.0) / b[j];
+            zd exy = (sv.ex(p, 0, i, j + 1) - sv.ex(p, 0, i, j)) / b[j];
+            zd eyx = (sv.ey(p, 0, i + 1, j) - sv.ey(p, 0, i, j)) / a[i];
+            F.H[1][id] = (exz - ezx) / iwm;
+            F.H[0][id] = (ezy - eyz) / iwm;
+            F.H[2][id] = (exy - eyx) / iwm;
+        }
+}
+// Transpose of surface_fields: cotangents dF at the cell centres are
+// accumulated onto the edge planes of polarisation p in g (the linear map is
+// holomorphic, so no conjugation).
+static void surface_fields_adjoint(SurfaceGrad& g, int p, const double* a, const double* b, double cz, zd iwm,
+                                   const SurfFields& dF) {
+    const int nx = g.nx, ny = g.ny;
+    for (int j = 0; j < ny; j++)
+        for (int i = 0; i < nx; i++) {
+            const size_t id = (size_t)j * nx + i;
+            const zd hx = dF.H[0][id] / iwm, hy = dF.H[1][id] / iwm, hz = dF.H[2][id] / iwm;
+            // H_y = (exz - ezx), H_x = (ezy - eyz), H_z = (exy - eyx)
+            const zd dexz = hy, dezx = -hy, dezy = hx, deyz = -hx, dexy = hz, deyx = -hz;
+            const zd dex0 = dF.E[0][id] - dexz / cz, dey0 = dF.E[1][id] - deyz / cz;
+            g.ex(p, 1, i, j) += dexz / cz / 2.0;
+            g.ex(p, 1, i, j + 1) += dexz / cz / 2.0;
+            g.ey(p, 1, i, j) += deyz / cz / 2.0;
+            g.ey(p, 1, i + 1, j) += deyz / cz / 2.0;
+            g.ez(p, i + 1, j) += dezx / a[i] / 2.0;
+            g.ez(p, i + 1, j + 1) += dezx / a[i] / 2.0;
+            g.ez(p, i, j) -= dezx / a[i] / 2.0;
+            g.ez(p, i, j + 1) -= dezx / a[i] / 2.0;
+            g.ez(p, i, j + 1) += dezy / b[j] / 2.0;
+            g.ez(p, i + 1, j + 1) += dezy / b[j] / 2.0;
+            g.ez(p, i, j) -= dezy / b[j] / 2.0;
+            g.ez(p, i + 1, j) -= dezy / b[j] / 2.0;
+            g.ex(p, 0, i, j + 1) += dexy / b[j];
+            g.ex(p, 0, i, j) -= dexy / b[j];
+            g.ey(p, 0, i + 1, j) += deyx / a[i];
+            g.ey(p, 0, i, j) -= deyx / a[i];
+            g.ex(p, 0, i, j) += dex0 / 2.0;
+            g.ex(p, 0, i, j + 1) += dex0 / 2.0;
+            g.ey(p, 0, i, j) += dey0 / 2.0;
+            g.ey(p, 0, i + 1, j) += dey0 / 2.0;
+        }
+}
+
+// cell-centre coordinates (arho_interp2 :729-735)
+static void cell_centres(int nx, int ny, const double* a, const double* b, std::vector<double>& aax,
+                         std::vector<double>& bby) {
+    aax.assign(nx, 0.0);
+    bby.assign(ny, 0.0);
     double sa = 0, sb = 0;
     for (int i = 0; i < nx; i++) sa += a[i];
     for (int i = 0; i < ny; i++) sb += b[i];
@@ -183,36 +230,66 @@ int impedance_from_surface(const SurfaceView& sv, const double* a, const double*
         for (int q = 0; q < i - 1; q++) s += b[q];
         bby[i - 1] = -sb / 2 + s + b[i - 1] / 2;
     }
-    for (int r = 0; r < nrec; r++) {
-        double xr = recv[r], yr = recv[(size_t)nrec + r];
-        int irec = -1, jrec = -1;
-        for (int j = 1; j <= nx - 1; j++)
-            if (xr >= aax[j - 1] && xr <= aax[j]) { irec = j; break; }
-        for (int j = 1; j <= ny - 1; j++)
-            if (yr >= bby[j - 1] && yr <= bby[j]) { jrec = j; break; }
-        if (irec < 2 || jrec < 2 || irec + 1 > nx || jrec + 1 > ny) return SFDX_ERR_RECEIVER;
-        if (transpose && (jrec + 1 > nx || irec + 1 > ny)) return SFDX_ERR_RECEIVER;
-        double c1[3], c2[3];
-        for (int q = 0; q < 3; q++) c1[q] = qcoef(xr, &aax[irec - 2], q);
-        for (int q = 0; q < 3; q++) c2[q] = qcoef(yr, &bby[jrec - 2], q);
-        zd f[2][5];
-        for (int p = 0; p < 2; p++) {
-            for (int q = 0; q < 5; q++) f[p][q] = 0;
-            for (int mm = 1; mm <= 3; mm++)
-                for (int nn = 1; nn <= 3; nn++) {
-                    double w = c1[mm - 1] * c2[nn - 1];
-                    // 1-based (I,J) of the field array; transposed stencil as rd=2
-                    int I = transpose ? mm + jrec - 2 : mm + irec - 2;
-                    int J = transpose ? nn + irec - 2 : nn + jrec - 2;
-                    size_t id = (size_t)(J - 1) * nx + (I - 1);
-                    size_t idz = (size_t)(nn + jrec - 3) * nx + (mm + irec - 3);
-                    f[p][0] += w * E[p][0][id];
-                    f[p][1] += w * E[p][1][id];
-                    f[p][2] += w * H[p][0][id];
-                    f[p][3] += w * H[p][1][id];
-                    f[p][4] += w * H[p][2][idz];
-                }
+}
+
+// The 9 cell centres and weights that interpolate a receiver: id[] for E, Hx
+// and Hy (transposed stencil with rd=2), idz[] for Hz.
+struct RecvStencil {
+    size_t id[9], idz[9];
+    double w[9];
+};
+static int receiver_stencil(int nx, int ny, const std::vector<double>& aax, const std::vector<double>& bby, double xr,
+                            double yr, int transpose, RecvStencil& S) {
+    int irec = -1, jrec = -1;
+    for (int j = 1; j <= nx - 1; j++)
+        if (xr >= aax[j - 1] && xr <= aax[j]) { irec = j; break; }
+    for (int j = 1; j <= ny - 1; j++)
+        if (yr >= bby[j - 1] && yr <= bby[j]) { jrec = j; break; }
+    if (irec < 2 || jrec < 2 || irec + 1 > nx || jrec + 1 > ny) return SFDX_ERR_RECEIVER;
+    if (transpose && (jrec + 1 > nx || irec + 1 > ny)) return SFDX_ERR_RECEIVER;
+    double c1[3], c2[3];
+    for (int q = 0; q < 3; q++) c1[q] = qcoef(xr, &aax[irec - 2], q);
+    for (int q = 0; q < 3; q++) c2[q] = qcoef(yr, &bby[jrec - 2], q);
+    int t = 0;
+    for (int mm = 1; mm <= 3; mm++)
+        for (int nn = 1; nn <= 3; nn++, t++) {
+            S.w[t] = c1[mm - 1] * c2[nn - 1];
+            // 1-based (I,J) of the field array
+            int I = transpose ? mm + jrec - 2 : mm + irec - 2;
+            int J = transpose ? nn + irec - 2 : nn + jrec - 2;
+            S.id[t] = (size_t)(J - 1) * nx + (I - 1);
+            S.idz[t] = (size_t)(nn + jrec - 3) * nx + (mm + irec - 3);
         }
+    return SFDX_OK;
+}
+
+// f[p][0..4] = (Ex, Ey, Hx, Hy, Hz) of polarisation p at the receiver
+static void receiver_fields(const SurfFields* F, const RecvStencil& S, zd f[2][5]) {
+    for (int p = 0; p < 2; p++) {
+        for (int q = 0; q < 5; q++) f[p][q] = 0;
+        for (int t = 0; t < 9; t++) {
+            f[p][0] += S.w[t] * F[p].E[0][S.id[t]];
+            f[p][1] += S.w[t] * F[p].E[1][S.id[t]];
+            f[p][2] += S.w[t] * F[p].H[0][S.id[t]];
+            f[p][3] += S.w[t] * F[p].H[1][S.id[t]];
+            f[p][4] += S.w[t] * F[p].H[2][S.idz[t]];
+        }
+    }
+}
+
+int impedance_from_surface(const SurfaceView& sv, const double* a, const double* b, const double* c, double ff,
+                           int nrec, const double* recv, int out_type, int transpose, double* out, double* tip) {
+    const int nx = sv.nx, ny = sv.ny;
+    const zd iwm = zd(0, 1) * 2.0 * kPi * ff * kMu;
+    SurfFields F[2];
+    for (int p = 0; p < 2; p++) surface_fields(sv, p, a, b, c[sv.nair], iwm, F[p]);
+    std::vector<double> aax, bby;
+    cell_centres(nx, ny, a, b, aax, bby);
+    for (int r = 0; r < nrec; r++) {
+        RecvStencil S;
+        HRC(receiver_stencil(nx, ny, aax, bby, recv[r], recv[(size_t)nrec + r], transpose, S));
+        zd f[2][5];
+        receiver_fields(F, S, f);
         zd det = f[0][2] * f[1][3] - f[1][2] * f[0][3];
         zd zxy = (f[1][0] * f[0][2] - f[0][0] * f[1][2]) / det;
         zd zyx = (f[0][1] * f[1][3] - f[1][1] * f[0][3]) / det;
@@ -239,6 +316,67 @@ int impedance_from_surface(const SurfaceView& sv, const double* a, const double*
             t[3] = ty.imag();
         }
     }
+    return SFDX_OK;
+}
+
+// Least-squares impedance misfit of one frequency and its derivative with
+// respect to the surface edge values (reverse mode through Z, the receiver
+// interpolation and surface_fields).  phi = sum_r wxy |Zxy - dxy|^2 + wyx |Zyx
+// - dyx|^2; g = d phi / d x in the holomorphic (Wirtinger) sense, so that
+// d phi = 2 Re(g^T dx).
+int impedance_misfit_adjoint(const SurfaceView& sv, const double* a, const double* b, const double* c, double ff,
+                             int nrec, const double* recv, int transpose, const double* zobs, const double* wts,
+                             double* misfit, double* zpred, SurfaceGrad& g) {
+    const int nx = sv.nx, ny = sv.ny;
+    const size_t n = (size_t)nx * ny;
+    const zd iwm = zd(0, 1) * 2.0 * kPi * ff * kMu;
+    SurfFields F[2], dF[2];
+    for (int p = 0; p < 2; p++) {
+        surface_fields(sv, p, a, b, c[sv.nair], iwm, F[p]);
+        dF[p].init(n);
+    }
+    std::vector<double> aax, bby;
+    cell_centres(nx, ny, a, b, aax, bby);
+    double phi = 0;
+    for (int r = 0; r < nrec; r++) {
+        RecvStencil S;
+        HRC(receiver_stencil(nx, ny, aax, bby, recv[r], recv[(size_t)nrec + r], transpose, S));
+        zd f[2][5];
+        receiver_fields(F, S, f);
+        const zd Ex1 = f[0][0], Ex2 = f[1][0], Ey1 = f[0][1], Ey2 = f[1][1];
+        const zd Hx1 = f[0][2], Hy1 = f[0][3], Hx2 = f[1][2], Hy2 = f[1][3];
+        const zd det = Hx1 * Hy2 - Hx2 * Hy1;
+        const zd zxy = (Ex2 * Hx1 - Ex1 * Hx2) / det;
+        const zd zyx = (Ey1 * Hy2 - Ey2 * Hy1) / det;
+        const double* d = zobs + (size_t)r * 4;
+        const double wxy = wts ? wts[(size_t)r * 2] : 1.0, wyx = wts ? wts[(size_t)r * 2 + 1] : 1.0;
+        const zd rxy = zxy - zd(d[0], d[1]), ryx = zyx - zd(d[2], d[3]);
+        phi += wxy * std::norm(rxy) + wyx * std::norm(ryx);
+        if (zpred) {
+            double* o = zpred + (size_t)r * 4;
+            o[0] = zxy.real(); o[1] = zxy.imag(); o[2] = zyx.real(); o[3] = zyx.imag();
+        }
+        // d phi / dZ, then through Z(E, H)
+        const zd cxy = wxy * std::conj(rxy), cyx = wyx * std::conj(ryx);
+        zd cf[2][4];
+        cf[0][0] = cxy * (-Hx2 / det);                                              // Ex1
+        cf[1][0] = cxy * (Hx1 / det);                                               // Ex2
+        cf[0][1] = cyx * (Hy2 / det);                                               // Ey1
+        cf[1][1] = cyx * (-Hy1 / det);                                              // Ey2
+        cf[0][2] = cxy * ((Ex2 - zxy * Hy2) / det) + cyx * (-zyx * Hy2 / det);      // Hx1
+        cf[1][2] = cxy * ((-Ex1 + zxy * Hy1) / det) + cyx * (zyx * Hy1 / det);      // Hx2
+        cf[0][3] = cxy * (zxy * Hx2 / det) + cyx * ((-Ey2 + zyx * Hx2) / det);      // Hy1
+        cf[1][3] = cxy * (-zxy * Hx1 / det) + cyx * ((Ey1 - zyx * Hx1) / det);      // Hy2
+        for (int p = 0; p < 2; p++)
+            for (int t = 0; t < 9; t++) {
+                dF[p].E[0][S.id[t]] += S.w[t] * cf[p][0];
+                dF[p].E[1][S.id[t]] += S.w[t] * cf[p][1];
+                dF[p].H[0][S.id[t]] += S.w[t] * cf[p][2];
+                dF[p].H[1][S.id[t]] += S.w[t] * cf[p][3];
+            }
+    }
+    for (int p = 0; p < 2; p++) surface_fields_adjoint(g, p, a, b, c[sv.nair], iwm, dF[p]);
+    *misfit += phi;
     return SFDX_OK;
 }
 

@@ -26,7 +26,26 @@ struct SurfaceView {
     std::complex<double> ez(int p, int i, int j) const { return ezs[p][(size_t)j * (nx + 1) + i]; }
 };
 
+// Writable edge planes of the same shape (adjoint sources), both polarisations.
+struct SurfaceGrad {
+    int nx, ny;
+    std::complex<double>* exs[2];
+    std::complex<double>* eys[2];
+    std::complex<double>* ezs[2];
+    std::complex<double>& ex(int p, int plane, int i, int j) { return exs[p][((size_t)plane * (ny + 1) + j) * nx + i]; }
+    std::complex<double>& ey(int p, int plane, int i, int j) { return eys[p][((size_t)plane * ny + j) * (nx + 1) + i]; }
+    std::complex<double>& ez(int p, int i, int j) { return ezs[p][(size_t)j * (nx + 1) + i]; }
+};
+
 int impedance_from_surface(const SurfaceView& sv, const double* a, const double* b, const double* c, double ff,
                            int nrec, const double* recv, int out_type, int transpose, double* out, double* tip);
+
+// Impedance misfit of one frequency (added to *misfit), the predicted Z
+// (optional, [nrec][4]) and its derivative with respect to the surface edge
+// values, accumulated into g.  zobs [nrec][4] = (Re, Im Zxy, Re, Im Zyx);
+// wts [nrec][2] (null: 1).
+int impedance_misfit_adjoint(const SurfaceView& sv, const double* a, const double* b, const double* c, double ff,
+                             int nrec, const double* recv, int transpose, const double* zobs, const double* wts,
+                             double* misfit, double* zpred, SurfaceGrad& g);
 
 }  // namespace sfdx

@@ -73,6 +73,28 @@ static int reserve_partials(Plan& P, const VCfg&, int nq) {
     return P.d_part.alloc(std::max(P.d_part.bytes, (size_t)max_resident_blocks() * nq * P.ns * sizeof(double2)));
 }
 
+// Graph key of one check interval (8 iterations): everything the captured
+// launches bake in besides the caller's vectors in `extra`.
+template <class T>
+static std::vector<uintptr_t> interval_key(const Plan& P, const Level& LV, int solver, int VS,
+                                           std::initializer_list<uintptr_t> extra) {
+    std::vector<uintptr_t> k = {(uintptr_t)solver, sizeof(T), (uintptr_t)VS, (uintptr_t)&LV, (uintptr_t)P.ns,
+                                (uintptr_t)LV.aniso, (uintptr_t)P.o.precond, (uintptr_t)P.d_state.p,
+                                (uintptr_t)P.d_part.p, (uintptr_t)P.d_counter.p, (uintptr_t)P.hist,
+                                (uintptr_t)P.hist_stride, (uintptr_t)LV.sig32.p, (uintptr_t)LV.sig64.p,
+                                (uintptr_t)LV.tab32.p, (uintptr_t)LV.tab64.p};
+    for (const DBuf& b : P.kv) k.push_back((uintptr_t)b.p);
+    k.insert(k.end(), extra);
+    return k;
+}
+// whether iterations it .. it+7 run as one captured graph: graphs enabled,
+// a whole check interval, not the first one (it runs eagerly and fills the
+// launch-shape cache), and no host work inside (the reference's divergence
+// correction runs on the host every corr_intv iterations)
+static bool graph_interval(const Plan& P, int it, int itmax, bool host_work) {
+    return P.o.use_graphs && !host_work && it > 8 && (it - 1) % 8 == 0 && it + 7 <= itmax;
+}
+
 // FP64 residual replacement for the systems still running or whose complex64
 // recurrence claims convergence; returns the number of systems left active.
 template <class T, int VS>
@@ -142,18 +164,29 @@ static int bicgstab_v(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, co
     CK(cudaGetLastError());
     const int check_every = 8;
     int last_rel = 0;
-    for (int it = 1; it <= itmax; it++) {
-        // top of iteration `it` (solvers.f90:630-640): divergence correction and
-        // residual restart every corr_intv iterations (FP64 solves only)
-        if (!rel && std::is_same<T, double>::value && P.o.div_cor == 1 && it % P.o.corr_intv == 0) {
-            RC(div_correct(P, LV, reinterpret_cast<double2*>(x)));
-            vlaunch(k_residual_v<T, T, VS, 1>, LV.nl * c.sg.G, c.B, c.smem, P.st, L, M, c.sg, dst, b, x, r, rhat, redbuf(P), nullptr, 0);
-        }
+    const bool div1 = !rel && std::is_same<T, double>::value && P.o.div_cor == 1;
+    auto body = [&]() {
         precond<T, VS, RHS_PUPD>(P, LV, y, p, r, v);
         vlaunch(k_bicg_v_v<T, VS>, LV.nl * c.sg.G, c.B, c.smem, P.st, L, M, c.sg, dst, y, v, rhat, redbuf(P));
         precond<T, VS, RHS_SUPD>(P, LV, z, s, r, v);
         vlaunch(k_bicg_t_v<T, VS>, LV.nl * c.sg.G, c.B, c.smem, P.st, L, M, c.sg, dst, z, t, s, redbuf(P));
         vlaunch(k_bicg_upd_v<T, T, VS>, LV.nl * c.sg.G, c.B, c.smem, P.st, M, c.sg, dst, x, y, z, s, t, r, rhat, redbuf(P), P.hist, P.hist_stride);
+    };
+    for (int it = 1; it <= itmax; it++) {
+        // top of iteration `it` (solvers.f90:630-640): divergence correction and
+        // residual restart every corr_intv iterations (FP64 solves only)
+        if (div1 && it % P.o.corr_intv == 0) {
+            RC(div_correct(P, LV, reinterpret_cast<double2*>(x)));
+            vlaunch(k_residual_v<T, T, VS, 1>, LV.nl * c.sg.G, c.B, c.smem, P.st, L, M, c.sg, dst, b, x, r, rhat, redbuf(P), nullptr, 0);
+        }
+        if (graph_interval(P, it, itmax, div1)) {
+            RC(graph_run(P, interval_key<T>(P, LV, 1, VS, {(uintptr_t)x, (uintptr_t)b}), [&] {
+                for (int q = 0; q < check_every; q++) body();
+            }));
+            it += check_every - 1;
+        } else {
+            body();
+        }
         if (it % check_every == 0 || it == itmax) {
             CK(cudaGetLastError());
             RC(sync_state(P));
@@ -210,18 +243,44 @@ static int gpbicg_v(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, cons
     precond<T, VS, RHS_VEC>(P, LV, rp, r, nullptr, nullptr);
     CK(cudaMemcpyAsync(p, rp, vb, cudaMemcpyDeviceToDevice, P.st));
     int cur = 0, last_rel = 0;
+    const bool div1 = !rel && std::is_same<T, double>::value && P.o.div_cor == 1;
+    // one iteration up to the convergence check, with t' in tp[cc]
+    auto body = [&](int cc) {
+        vlaunch(k_gp_ap_v<T, VS>, LV.nl * c.sg.G, c.B, c.smem, P.st, L, M, c.sg, dst, p, ap, r0, r, redbuf(P));
+        vlaunch(k_gp_yt_v<T, VS>, LV.nl * c.sg.G, c.B, 0, P.st, M, c.sg, dst, y, t, r, w, ap);
+        precond<T, VS, RHS_VEC>(P, LV, tmp, ap, nullptr, nullptr);
+        vlaunch(k_gp_tp_v<T, VS>, LV.nl * c.sg.G, c.B, 0, P.st, M, c.sg, dst, tp[cc], rp, tmp);
+        vlaunch(k_gp_at_v<T, VS>, LV.nl * c.sg.G, c.B, c.smem, P.st, L, M, c.sg, dst, tp[cc], at, t, y, redbuf(P));
+        vlaunch(k_gp_upd_v<T, T, VS>, LV.nl * c.sg.G, c.B, c.smem, P.st, M, c.sg, dst, u, z, x, r, tmp, tp[cc ^ 1], rp, p, t, y, at, r0, redbuf(P), P.hist, P.hist_stride);
+    };
+    // the rest of the iteration after the check
+    auto tail = [&]() {
+        precond<T, VS, RHS_VEC>(P, LV, rp, r, nullptr, nullptr);
+        vlaunch(k_gp_pw_v<T, VS>, LV.nl * c.sg.G, c.B, 0, P.st, M, c.sg, dst, w, p, at, ap, rp, u);
+    };
     for (int it = 1; it <= itmax; it++) {
-        if (!rel && std::is_same<T, double>::value && P.o.div_cor == 1 && it % P.o.corr_intv == 0) {
+        if (div1 && it % P.o.corr_intv == 0) {
             // solvers.f90:223-235: correct x, restart r and r0 (rp is kept)
             RC(div_correct(P, LV, reinterpret_cast<double2*>(x)));
             vlaunch(k_residual_v<T, T, VS, 4>, LV.nl * c.sg.G, c.B, c.smem, P.st, L, M, c.sg, dst, b, x, r, r0, redbuf(P), nullptr, 0);
         }
-        vlaunch(k_gp_ap_v<T, VS>, LV.nl * c.sg.G, c.B, c.smem, P.st, L, M, c.sg, dst, p, ap, r0, r, redbuf(P));
-        vlaunch(k_gp_yt_v<T, VS>, LV.nl * c.sg.G, c.B, 0, P.st, M, c.sg, dst, y, t, r, w, ap);
-        precond<T, VS, RHS_VEC>(P, LV, tmp, ap, nullptr, nullptr);
-        vlaunch(k_gp_tp_v<T, VS>, LV.nl * c.sg.G, c.B, 0, P.st, M, c.sg, dst, tp[cur], rp, tmp);
-        vlaunch(k_gp_at_v<T, VS>, LV.nl * c.sg.G, c.B, c.smem, P.st, L, M, c.sg, dst, tp[cur], at, t, y, redbuf(P));
-        vlaunch(k_gp_upd_v<T, T, VS>, LV.nl * c.sg.G, c.B, c.smem, P.st, M, c.sg, dst, u, z, x, r, tmp, tp[cur ^ 1], rp, p, t, y, at, r0, redbuf(P), P.hist, P.hist_stride);
+        if (graph_interval(P, it, itmax, div1)) {
+            const int c0 = cur;
+            RC(graph_run(P, interval_key<T>(P, LV, 3, VS, {(uintptr_t)x, (uintptr_t)b, (uintptr_t)c0}), [&] {
+                int cc = c0;
+                for (int q = 0; q < 8; q++) {
+                    if (q) {
+                        tail();
+                        cc ^= 1;
+                    }
+                    body(cc);
+                }
+            }));
+            it += 7;
+            cur = c0 ^ 1;
+        } else {
+            body(cur);
+        }
         bool stop = false;
         if (it % 8 == 0 || it == itmax) {
             CK(cudaGetLastError());
@@ -238,8 +297,7 @@ static int gpbicg_v(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, cons
             stop = !act;
         }
         if (stop) break;
-        precond<T, VS, RHS_VEC>(P, LV, rp, r, nullptr, nullptr);
-        vlaunch(k_gp_pw_v<T, VS>, LV.nl * c.sg.G, c.B, 0, P.st, M, c.sg, dst, w, p, at, ap, rp, u);
+        tail();
         cur ^= 1;
     }
     if (rel) vlaunch(k_flush_v<T, VS, true>, LV.nl * c.sg.G, c.B, 0, P.st, M, c.sg, dst, rel->x64, x, nullptr);
@@ -290,12 +348,11 @@ static int cocr_v(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, const 
     RC(restart());
     bool first = true;
     int last_rel = 0;
-    for (int it = 1; it <= itmax; it++) {
-        if (first)
+    auto body = [&](bool fst) {
+        if (fst)
             vlaunch(k_cocr_u<T, VS, true>, W, c.B, c.smem, P.st, L, M, c.sg, dst, (const cplx<T>*)z, u, redbuf(P));
         else
             vlaunch(k_cocr_u<T, VS, false>, W, c.B, c.smem, P.st, L, M, c.sg, dst, (const cplx<T>*)z, u, redbuf(P));
-        first = false;
         if (P.o.precond == 'J') {
             vlaunch(k_cocr_dir<T, VS>, W, c.B, 0, P.st, M, c.sg, dst, (const cplx<T>*)u, w, (const cplx<T>*)z, p);
             precond<T, VS, RHS_VEC>(P, LV, q, w, nullptr, nullptr);
@@ -306,6 +363,18 @@ static int cocr_v(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, const 
                 redbuf(P));
         vlaunch(k_cocr_upd<T, T, VS>, W, c.B, c.smem, P.st, M, c.sg, dst, x, r, z, (const cplx<T>*)p, (const cplx<T>*)w,
                 (const cplx<T>*)q, redbuf(P), P.hist, P.hist_stride);
+    };
+    for (int it = 1; it <= itmax; it++) {
+        if (graph_interval(P, it, itmax, false)) {
+            const bool f0 = first;
+            RC(graph_run(P, interval_key<T>(P, LV, 6, VS, {(uintptr_t)x, (uintptr_t)b, (uintptr_t)f0}), [&] {
+                for (int k = 0; k < 8; k++) body(f0 && k == 0);
+            }));
+            it += 7;
+        } else {
+            body(first);
+        }
+        first = false;
         if (it % 8 == 0 || it == itmax) {
             CK(cudaGetLastError());
             RC(sync_state(P));

@@ -44,13 +44,12 @@ extern std::atomic<long long> g_launches;
 #define KL(...) (g_launches.fetch_add(1, std::memory_order_relaxed), __VA_ARGS__)
 
 inline int device_sms() {
-    static int nsm = 0;
-    if (!nsm) {
+    static const int nsm = [] {
         int dev = 0, v = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
-        nsm = v > 0 ? v : 1;
-    }
+        return v > 0 ? v : 1;
+    }();
     return nsm;
 }
 
@@ -205,6 +204,24 @@ struct Level {
     }
 };
 
+// ------------------------------------------------------------------ CUDA graphs
+// Launch sequences that run between two host checks (a check interval of
+// Krylov iterations) are captured once per key -- level, batch size,
+// buffers, scalar kernel arguments -- and replayed as one graph launch.
+struct GraphEntry {
+    cudaGraphExec_t exec = nullptr;
+    long long nodes = 0;
+};
+struct GraphCache {
+    std::map<std::vector<uintptr_t>, GraphEntry> m;
+    GraphCache() = default;
+    GraphCache(const GraphCache&) = delete;
+    ~GraphCache() {
+        for (auto& kv : m)
+            if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+    }
+};
+
 // ------------------------------------------------------------------ plan
 struct Plan {
     sfdx_opts o;
@@ -217,6 +234,17 @@ struct Plan {
     DBuf d_state, d_wm, d_pol, d_edc, d_part, d_counter, d_tol, d_mask, d_scale, d_flag;
     // FP64 vectors (finest-level size)
     DBuf x64, b64, r64, u0, u1, ut, ex_out;
+    // forward fields of the last solve, interleaved like x64, kept while
+    // x64 holds adjoint solutions (xf_valid: xf matches the last solve)
+    DBuf xf;
+    bool xf_valid = false;
+    // fields of the last full (cascade) solve, the initial guess of
+    // sfdx_plan_resolve (base_valid: xbase matches that solve)
+    DBuf xbase;
+    bool base_valid = false;
+    // mixed precision: complex64 partial solution and the FP64 iterate saved
+    // before each reliable update
+    DBuf x32, xb;
     // Krylov vectors (precision of the active solve)
     DBuf kv[14];
     // divergence correction: t, r, p, v, phi (nodes) and the PCG state
@@ -241,12 +269,45 @@ struct Plan {
     // systems per thread of the complex64 / complex128 hot kernels (upper
     // bounds; sfdx_plan_autotune measures and sets them)
     int vs32 = 4, vs64 = 2;
+    GraphCache graphs;  // captured check intervals (o.use_graphs)
     Plan() = default;
     Plan(const Plan&) = delete;
     ~Plan() {
         if (own_st) cudaStreamDestroy(own_st);
     }
 };
+
+// Run `seq` (kernel launches on P.st only, no host synchronisation) through
+// the plan's graph cache under `key`: captured and instantiated on first use,
+// replayed afterwards.  The launch counter advances by the graph's node count
+// on every replay (the capture itself counted the launches it recorded).
+template <class F> int graph_run(Plan& P, const std::vector<uintptr_t>& key, F&& seq) {
+    auto it = P.graphs.m.find(key);
+    if (it != P.graphs.m.end()) {
+        g_launches.fetch_add(it->second.nodes, std::memory_order_relaxed);
+        CK(cudaGraphLaunch(it->second.exec, P.st));
+        return SFDX_OK;
+    }
+    cudaGraph_t g = nullptr;
+    CK(cudaStreamBeginCapture(P.st, cudaStreamCaptureModeThreadLocal));
+    seq();
+    const cudaError_t e = cudaStreamEndCapture(P.st, &g);
+    if (e != cudaSuccess || !g) {
+        if (g) cudaGraphDestroy(g);
+        cudaGetLastError();
+        return SFDX_ERR_CUDA;
+    }
+    GraphEntry ge;
+    size_t n = 0;
+    cudaGraphGetNodes(g, nullptr, &n);
+    ge.nodes = (long long)n;
+    const cudaError_t ei = cudaGraphInstantiate(&ge.exec, g, 0);
+    cudaGraphDestroy(g);
+    CK(ei);
+    P.graphs.m.emplace(key, ge);
+    CK(cudaGraphLaunch(ge.exec, P.st));
+    return SFDX_OK;
+}
 
 inline int sync_state(Plan& P) {
     P.hst.resize(P.ns);
@@ -306,6 +367,19 @@ template <class T> int apply_op(Plan& P, const Level& LV, const cplx<T>* x, cplx
 
 // ------------------------------------------------------------------ sfdx_solver.cu
 int div_correct(Plan& P, const Level& LV, double2* x);
+// FP64 (coarse or FP64 plans) or mixed-precision solve of all systems of level
+// LV from the iterate in P.x64 with right-hand side P.b64 (its[], status[]
+// per system)
+int solve_level(Plan& P, const Level& LV, double tol, int itmax, bool coarse, std::vector<int>& its,
+                std::vector<int>& status);
+// ||b - A x|| / ||b|| per system in FP64
+int true_residual(Plan& P, const Level& LV, const double2* b, const double2* x, double* rel, const int* mask);
+
+// ------------------------------------------------------------------ sfdx_adjoint.cu
+// Impedance misfit of the last solution and its gradient with respect to the
+// conductivity of every cell and component ([6][ncell], host or device).
+int misfit_grad(Plan& P, int nrec, const double* recv, const double* zobs, const double* wts, double tol,
+                double* misfit, double* zpred, double* grad, bool grad_on_device, int* adj_iters, double* adj_relres);
 
 // ------------------------------------------------------------------ sfdx_gradcorr.cu
 // x += G phi with (G^T V Ms G) phi = G^T V (b - A x) / (-i w mu) for the systems

@@ -26,6 +26,7 @@
 #include <cstring>
 #include <ctime>
 #include <memory>
+#include <thread>
 #include <type_traits>
 #include <vector>
 
@@ -170,7 +171,7 @@ int div_correct(Plan& P, const Level& LV, double2* x) {
 }
 
 // true relative residual ||b - A x|| / ||b|| per system (FP64)
-static int true_residual(Plan& P, const Level& LV, const double2* b, const double2* x, double* rel, const int* mask) {
+int true_residual(Plan& P, const Level& LV, const double2* b, const double2* x, double* rel, const int* mask) {
     const int ns = P.ns;
     std::vector<KState> init(ns);
     for (int q = 0; q < ns; q++) {
@@ -223,11 +224,11 @@ static int solve_level_mixed(Plan& P, const Level& LV, double tol, int itmax, st
                              std::vector<int>& status) {
     const int ns = P.ns;
     const size_t n = (size_t)LV.nl * ns;
-    DBuf x32, xb;
+    DBuf& x32 = P.x32;
     RC(x32.alloc(n * sizeof(float2)));
-    RC(xb.alloc(n * sizeof(double2)));
+    RC(P.xb.alloc(n * sizeof(double2)));
     Reliable rel{P.b64.as<double2>(), P.x64.as<double2>(), P.o.reliable_every > 0 ? P.o.reliable_every : 40,
-                 xb.as<double2>()};
+                 P.xb.as<double2>()};
     if (P.o.solver == SFDX_SOLVER_GPBICG)
         RC(gpbicg<float>(P, LV, nullptr, x32.as<float2>(), nullptr, tol, itmax, nullptr, &rel));
     else if (P.o.solver == SFDX_SOLVER_BICGSTAB)
@@ -278,8 +279,8 @@ static int solve_level_mixed(Plan& P, const Level& LV, double tol, int itmax, st
     return SFDX_OK;
 }
 
-static int solve_level(Plan& P, const Level& LV, double tol, int itmax, bool coarse, std::vector<int>& its,
-                       std::vector<int>& status) {
+int solve_level(Plan& P, const Level& LV, double tol, int itmax, bool coarse, std::vector<int>& its,
+                std::vector<int>& status) {
     if (coarse || P.o.precision == SFDX_FP64) return solve_level_fp64(P, LV, tol, itmax, its, status);
     return solve_level_mixed(P, LV, tol, itmax, its, status);
 }
@@ -344,15 +345,8 @@ static int set_conductivity(Plan& P, const double* sigma, bool on_device) {
         Level& C = P.lev[l];
         const int k = P.nlev - 1 - l;
         RC(C.sig64.alloc((size_t)6 * C.ncell * sizeof(double)));
-        DBuf c1;
-        RC(c1.alloc((C.nx + C.ny + C.nz) * sizeof(double)));
-        std::vector<double> cs;
-        cs.insert(cs.end(), C.a.begin(), C.a.end());
-        cs.insert(cs.end(), C.b.begin(), C.b.end());
-        cs.insert(cs.end(), C.c.begin(), C.c.end());
-        CK(cudaMemcpyAsync(c1.p, cs.data(), cs.size() * 8, cudaMemcpyHostToDevice, P.st));
         const double* fs = F.spac.as<double>();
-        const double* cp = c1.as<double>();
+        const double* cp = C.spac.as<double>();  // this level's a, b, c
         KL(k_coarsen<<<grid_for(C.ncell, 128, 32), 128, 0, P.st>>>(F.nx, F.ny, F.nz, fs, fs + F.nx, fs + F.nx + F.ny, cp,
                                                                 cp + C.nx, cp + C.nx + C.ny, 1 << k,
                                                                 (P.o.quirks & SFDX_QUIRK_COARSEN_SHIFT) ? 1 : 0,
@@ -444,6 +438,8 @@ static int plan_solve(Plan& P) {
     const size_t nfine = (size_t)F.nl * ns * sizeof(double2);
     RC(P.x64.alloc(nfine));
     RC(P.b64.alloc(nfine));
+    P.xf_valid = false;
+    P.base_valid = false;
     std::vector<double> col;
     P.level_ms.assign(P.nlev, 0.0);
     if (!P.o.excmg) {
@@ -508,6 +504,61 @@ static int plan_solve(Plan& P) {
     CK(cudaStreamSynchronize(P.st));
     P.have_solution = true;
     return rc_conv;
+}
+
+// x += a over n complex128 values
+static __global__ void k_add_to(int64_t n, const double2* __restrict__ a, double2* __restrict__ x) {
+    for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < n; g += (int64_t)gridDim.x * blockDim.x) {
+        const double2 v = x[g], w = a[g];
+        x[g] = make_double2(v.x + w.x, v.y + w.y);
+    }
+}
+
+// Finest level only, for a changed conductivity, from the fields x0 of the last
+// full solve.  tol > 0: solve A x = b from x0 to relative residual tol.
+// tol <= 0: solve the correction equation A d = b - A x0 from zero to a
+// relative reduction |tol| (or eps) of that residual, then x = x0 + d -- the
+// residual's own scale sets the tolerance, so a small perturbation of the
+// model is resolved to the same relative accuracy as a full solve.
+static int plan_resolve(Plan& P, double tol) {
+    const int ns = P.ns;
+    const Level& F = P.lev[P.nlev - 1];
+    const int64_t n = F.nl * ns;
+    const size_t nfine = (size_t)n * sizeof(double2);
+    if (!P.base_valid) {
+        RC(P.xbase.alloc(nfine));
+        CK(cudaMemcpyAsync(P.xbase.p, (P.xf_valid ? P.xf : P.x64).p, nfine, cudaMemcpyDeviceToDevice, P.st));
+        P.base_valid = true;
+    }
+    CK(cudaMemcpyAsync(P.x64.p, P.xbase.p, nfine, cudaMemcpyDeviceToDevice, P.st));
+    P.xf_valid = false;
+    std::vector<double> col;
+    RC(level_column(P, F, col));
+    RC(level_rhs(P, F, col));
+    std::vector<int> its, status;
+    const double t0 = now_ms();
+    if (tol > 0) {
+        RC(solve_level(P, F, tol, P.o.maxit_plain, false, its, status));
+    } else {
+        std::vector<double> r0(ns);
+        RC(true_residual(P, F, P.b64.as<double2>(), P.x64.as<double2>(), r0.data(), nullptr));  // r64 = b - A x0
+        CK(cudaMemcpyAsync(P.b64.p, P.r64.p, nfine, cudaMemcpyDeviceToDevice, P.st));
+        CK(cudaMemsetAsync(P.x64.p, 0, nfine, P.st));
+        RC(solve_level(P, F, tol < 0 ? -tol : P.o.eps, P.o.maxit_plain, false, its, status));
+        KL(k_add_to<<<grid_for(n, 256, 16), 256, 0, P.st>>>(n, P.xbase.as<double2>(), P.x64.as<double2>()));
+        CK(cudaGetLastError());
+        RC(level_rhs(P, F, col));  // b again, for the reported residual
+    }
+    record_iters(P, P.nlev - 1, its);
+    RC(true_residual(P, F, P.b64.as<double2>(), P.x64.as<double2>(), P.relres.data(), nullptr));
+    const int B = block_for(ns);
+    KL(k_scatter_sys<double><<<grid_for(F.nl * ns, B, 16), B, 0, P.st>>>(F.nl, ns, P.x64.as<double2>(), P.ex_out.as<double2>()));
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(P.st));
+    P.level_ms.assign(P.nlev, 0.0);
+    P.level_ms[P.nlev - 1] = now_ms() - t0;
+    P.have_solution = true;
+    return status_to_rc(status);
 }
 
 static int validate_opts(const sfdx_opts& o) {
@@ -656,6 +707,59 @@ extern "C" int sfdx_plan_solve(sfdx_plan* plan, const double* sigma, int sigma_o
     return rc;
 }
 
+// Several plans at once: each plan's solve runs on its own host thread and
+// its own stream, so the GPU overlaps the models' kernels and one model's
+// host synchronisations (convergence checks, restart cycles) do not stall
+// the others.
+extern "C" int sfdx_plan_solve_batch(int nplans, sfdx_plan* const* plans, const double* const* sigma,
+                                     int sigma_on_device, double* const* ex, int ex_on_device, int* const* iters,
+                                     double* const* relres, int* status) {
+    if (nplans < 1 || !plans || !sigma) return SFDX_ERR_ARG;
+    for (int q = 0; q < nplans; q++) {
+        if (!plans[q] || !sigma[q]) return SFDX_ERR_ARG;
+        for (int r = 0; r < q; r++)
+            if (plans[r] == plans[q]) return SFDX_ERR_ARG;
+    }
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
+    std::vector<int> rc(nplans, SFDX_OK);
+    std::vector<std::thread> th;
+    th.reserve(nplans);
+    for (int q = 0; q < nplans; q++)
+        th.emplace_back([&, q] {
+            try {
+                if (cudaSetDevice(dev) != cudaSuccess) {
+                    rc[q] = SFDX_ERR_CUDA;
+                    return;
+                }
+                rc[q] = sfdx_plan_solve(plans[q], sigma[q], sigma_on_device, ex ? ex[q] : nullptr, ex_on_device,
+                                        iters ? iters[q] : nullptr, relres ? relres[q] : nullptr);
+            } catch (...) {
+                rc[q] = SFDX_ERR_NOMEM;
+            }
+        });
+    for (auto& t : th) t.join();
+    int out = SFDX_OK;
+    for (int q = 0; q < nplans; q++) {
+        if (status) status[q] = rc[q];
+        if (rc[q] != SFDX_OK && (out == SFDX_OK || out == SFDX_ERR_NOCONV)) out = rc[q];
+    }
+    return out;
+}
+
+extern "C" int sfdx_plan_resolve(sfdx_plan* plan, const double* sigma, int sigma_on_device, double tol, int* iters,
+                                 double* relres) {
+    if (!plan || !sigma) return SFDX_ERR_ARG;
+    Plan& P = plan->P;
+    if (!P.have_solution) return SFDX_ERR_ARG;
+    RC(set_conductivity(P, sigma, sigma_on_device != 0));
+    const int rc = plan_resolve(P, tol);
+    if (rc != SFDX_OK && rc != SFDX_ERR_NOCONV) return rc;
+    if (iters) memcpy(iters, P.iters.data(), P.iters.size() * sizeof(int));
+    if (relres) memcpy(relres, P.relres.data(), P.relres.size() * sizeof(double));
+    return rc;
+}
+
 extern "C" int sfdx_plan_load(sfdx_plan* plan, const double* sigma, int sigma_on_device) {
     if (!plan || !sigma) return SFDX_ERR_ARG;
     RC(set_conductivity(plan->P, sigma, sigma_on_device != 0));
@@ -673,12 +777,19 @@ extern "C" long long sfdx_plan_device_bytes(const sfdx_plan* plan) {
     const Plan& P = plan->P;
     long long s = 0;
     const DBuf* bufs[] = {&P.d_state, &P.d_wm, &P.d_pol, &P.d_edc, &P.d_part, &P.d_counter, &P.d_tol, &P.d_mask,
-                          &P.d_scale, &P.d_flag, &P.x64, &P.b64, &P.r64, &P.u0, &P.u1, &P.ut, &P.ex_out, &P.errrec};
+                          &P.d_scale, &P.d_flag, &P.x64, &P.b64, &P.r64, &P.u0, &P.u1, &P.ut, &P.ex_out, &P.errrec,
+                          &P.xf, &P.x32, &P.xb, &P.cb64, &P.cx64, &P.d_idx, &P.d_pst};
     for (auto* b : bufs) s += (long long)b->bytes;
     for (auto& b : P.kv) s += (long long)b.bytes;
-    for (auto& L : P.lev)
+    for (auto& b : P.dcv) s += (long long)b.bytes;
+    for (auto& b : P.gcn) s += (long long)b.bytes;
+    for (auto& b : P.gce) s += (long long)b.bytes;
+    for (auto& L : P.lev) {
         s += (long long)(L.tab64.bytes + L.tab32.bytes + L.sig64.bytes + L.sig32.bytes + L.spac.bytes +
                          L.crd_cubic.bytes + L.crd_quad.bytes);
+        for (auto& g : L.mg)
+            s += (long long)(g.coef.bytes + g.dinv.bytes + g.x.bytes + g.b.bytes + g.t.bytes + g.r.bytes);
+    }
     return s;
 }
 
@@ -851,6 +962,14 @@ extern "C" int sfdx_plan_impedance(sfdx_plan* plan, int nrec, const double* recv
                                   tipper ? tipper + (size_t)f * nrec * 4 : nullptr));
     }
     return SFDX_OK;
+}
+
+extern "C" int sfdx_plan_misfit_grad(sfdx_plan* plan, int nrec, const double* recv, const double* zobs,
+                                     const double* wts, double tol, double* misfit, double* zpred, double* grad,
+                                     int grad_on_device, int* adj_iters, double* adj_relres) {
+    if (!plan || !recv || !zobs || !misfit || nrec < 1) return SFDX_ERR_ARG;
+    return misfit_grad(plan->P, nrec, recv, zobs, wts, tol, misfit, zpred, grad, grad_on_device != 0, adj_iters,
+                       adj_relres);
 }
 
 extern "C" int sfdx_fwd_solve(const sfdx_opts* o, int nx, int ny, int nz, int nair, const double* a, const double* b,

@@ -63,8 +63,9 @@ class Plan:
         self.close()
 
     def solve(self, sigma=None, out=None, sigma_device_ptr: int | None = None, out_device_ptr: int | None = None,
-              allow_noconv: bool = False):
-        """Solve all frequencies x polarisations.  Returns ex[nf, 2, nl] (host) unless a device output is given."""
+              allow_noconv: bool = False, fetch: bool = True):
+        """Solve all frequencies x polarisations.  Returns ex[nf, 2, nl] (host) unless a device output is
+        given or ``fetch`` is False (fields left in the plan's device memory only)."""
         L = capi.lib()
         m = self.model
         if sigma_device_ptr is not None:
@@ -77,6 +78,8 @@ class Plan:
         ex = None
         if out_device_ptr is not None:
             op, oon = ctypes.c_void_p(out_device_ptr), 1
+        elif not fetch:
+            op, oon = ctypes.c_void_p(0), 0
         else:
             ex = out if out is not None else np.zeros((m.nf, 2, m.nl), np.complex128)
             op, oon = ctypes.c_void_p(ex.ctypes.data), 0
@@ -89,6 +92,25 @@ class Plan:
         self.iters = it.reshape(self.iters.shape)
         self.relres = rr.reshape(self.relres.shape)
         return ex
+
+    def resolve(self, sigma=None, sigma_device_ptr: int | None = None, tol: float = 0.0,
+                allow_noconv: bool = False) -> None:
+        """Finest-level re-solve for a changed conductivity from the last full solve's fields x0
+        (sfdx_plan_resolve).  tol > 0: relative residual; tol <= 0: correction equation
+        A d = b - A x0 reduced by |tol| (0: the plan's eps), x = x0 + d."""
+        if sigma_device_ptr is not None:
+            sp, son = ctypes.c_void_p(sigma_device_ptr), 1
+        else:
+            self._sg = _d(self.model.sigma if sigma is None else sigma)
+            sp, son = ctypes.c_void_p(self._sg.ctypes.data), 0
+        it = np.zeros(self.iters.size, np.int32)
+        rr = np.zeros(self.relres.size)
+        rc = capi.lib().sfdx_plan_resolve(self._h, sp, son, tol, capi.iptr(it), capi.dptr(rr))
+        self.status = rc
+        if rc != 0 and not (allow_noconv and rc == 4):
+            raise capi.SfdxError(rc, "sfdx_plan_resolve")
+        self.iters = it.reshape(self.iters.shape)
+        self.relres = rr.reshape(self.relres.shape)
 
     def load(self, sigma=None, sigma_device_ptr: int | None = None) -> None:
         """Upload (and coarsen) the conductivity without solving."""
@@ -109,6 +131,37 @@ class Plan:
                                                    capi.dptr(tip) if tip is not None else None),
                    "sfdx_plan_impedance")
         return (out, tip) if tipper else out
+
+    def misfit_grad(self, zobs, wts=None, recv=None, tol: float = 0.0, grad_device_ptr: int | None = None,
+                    allow_noconv: bool = False, with_grad: bool = True):
+        """Impedance misfit of the last solution and d misfit / d sigma (sfdx_plan_misfit_grad).
+
+        zobs[nf, nrec, 4] = (Re Zxy, Im Zxy, Re Zyx, Im Zyx); wts[nf, nrec, 2] (None: 1).
+        Returns (misfit, grad[6, ncell] or None when written to ``grad_device_ptr`` or not
+        asked for (``with_grad=False``: no adjoint solve), zpred[nf, nrec, 4], adjoint
+        iterations[nf, 2], adjoint relative residuals[nf, 2])."""
+        m = self.model
+        rv = _d(np.asarray(m.recv if recv is None else recv).T)
+        nrec = rv.shape[1]
+        zo = _d(zobs).reshape(m.nf, nrec, 4)
+        wt = None if wts is None else _d(wts).reshape(m.nf, nrec, 2)
+        zp = np.zeros((m.nf, nrec, 4))
+        mis = ctypes.c_double()
+        it = np.zeros(2 * m.nf, np.int32)
+        rr = np.zeros(2 * m.nf)
+        if not with_grad:
+            g, gp, gon = None, None, 0
+        elif grad_device_ptr is not None:
+            g, gp, gon = None, ctypes.cast(ctypes.c_void_p(grad_device_ptr), capi.c_double_p), 1
+        else:
+            g = np.zeros((6, m.ncell))
+            gp, gon = capi.dptr(g), 0
+        rc = capi.lib().sfdx_plan_misfit_grad(self._h, nrec, capi.dptr(rv), capi.dptr(zo),
+                                               capi.dptr(wt) if wt is not None else None, tol, ctypes.byref(mis),
+                                               capi.dptr(zp), gp, gon, capi.iptr(it), capi.dptr(rr))
+        if rc != 0 and not (allow_noconv and rc == 4):
+            raise capi.SfdxError(rc, "sfdx_plan_misfit_grad")
+        return mis.value, g, zp, it.reshape(m.nf, 2), rr.reshape(m.nf, 2)
 
     def fields_device_ptr(self) -> int:
         return capi.lib().sfdx_plan_fields(self._h) or 0
@@ -139,6 +192,34 @@ class Plan:
 
     def device_bytes(self) -> int:
         return int(capi.lib().sfdx_plan_device_bytes(self._h))
+
+
+def solve_batch(plans, sigmas=None, sigma_device_ptrs=None, allow_noconv: bool = False):
+    """Solve several plans at once (sfdx_plan_solve_batch): one host thread and one stream per
+    plan.  Fields stay in each plan's device memory (``Plan.impedance``, ``Plan.fields_device_ptr``);
+    each plan's ``iters``/``relres``/``status`` are updated.  Returns the per-plan status codes."""
+    n = len(plans)
+    arr = lambda vals: (ctypes.c_void_p * n)(*vals)  # noqa: E731
+    keep = []
+    if sigma_device_ptrs is not None:
+        sp, son = arr(sigma_device_ptrs), 1
+    else:
+        for q, p in enumerate(plans):
+            keep.append(_d(p.model.sigma if sigmas is None else sigmas[q]))
+        sp, son = arr([k.ctypes.data for k in keep]), 0
+    its = [np.zeros(p.iters.size, np.int32) for p in plans]
+    rrs = [np.zeros(p.relres.size) for p in plans]
+    st = np.zeros(n, np.int32)
+    rc = capi.lib().sfdx_plan_solve_batch(n, arr([p._h.value for p in plans]), sp, son, None, 0,
+                                          arr([a.ctypes.data for a in its]), arr([a.ctypes.data for a in rrs]),
+                                          capi.iptr(st))
+    for q, p in enumerate(plans):
+        p.status = int(st[q])
+        p.iters = its[q].reshape(p.iters.shape)
+        p.relres = rrs[q].reshape(p.relres.shape)
+    if rc != 0 and not (allow_noconv and rc == 4):
+        raise capi.SfdxError(rc, "sfdx_plan_solve_batch")
+    return st
 
 
 def fwd_solve(model: Model, **opts):

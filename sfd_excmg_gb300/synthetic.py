@@ -155,6 +155,32 @@ def grf(shape, corr_len, rng) -> np.ndarray:
     return (f - f.mean()) / (f.std() + 1e-30)
 
 
+def config3(seed: int = 0, nmodels: int = 8, nf: int = 16) -> list:
+    """Batched multi-model case: `nmodels` models whose cell counts per axis
+    (padding and air included) are drawn uniformly from {48, 56, ..., 96}
+    (multiples of 8, 3 levels): 50 m core cells, 4 lateral padding cells per
+    side (x1.3), 4 bottom padding cells, 8 air layers; isotropic log10(rho)
+    Gaussian random field (mean 2, std 0.5, correlation 5 cells); nf
+    frequencies over 0.001-1000 Hz; 8x8 receivers over the core."""
+    rng = np.random.default_rng(seed)
+    sizes = np.arange(48, 97, 8)
+    models = []
+    for _ in range(nmodels):
+        nx, ny, nz = (int(v) for v in rng.choice(sizes, 3))
+        npad, nair, nbot = 4, 8, 4
+        ncx, ncy, ncz = nx - 2 * npad, ny - 2 * npad, nz - nair - nbot
+        a, b, c = _mesh(ncx, ncy, ncz, 50.0, npad, 1.3, nbot, 1.3, nair)
+        sig = np.zeros((6, nx * ny * nz))
+        s3 = sig.reshape(6, nz, ny, nx)
+        f = 2.0 + 0.5 * grf((nz - nair, ny, nx), 5.0, rng)
+        s3[0:3, nair:] = (10.0 ** -f)[None]
+        s3[0:3, :nair] = SIGMA_AIR
+        freq = np.logspace(-3, 3, nf)
+        recv = _core_receivers(a, b, npad, ncx, ncy, 8, 8)
+        models.append(Model(nx, ny, nz, nair, a, b, c, sig, freq, recv, level=3, eps=1e-8, solver=1, out_type=1))
+    return models
+
+
 def config4(seed: int = 0) -> Model:
     """Large single model: 128x128x96 core cells of 25 m, 16 lateral padding
     cells per side, 12 bottom padding, 36 air layers (160x160x144, 11.2 M edges);
@@ -196,6 +222,18 @@ def config5(seed: int = 0) -> Model:
     s3[0:3, m.nair:] = (10.0 ** -f)[None]
     s3[0:3, : m.nair] = SIGMA_AIR
     m.freq = np.logspace(-3, 3, 6)
+    return m
+
+
+def config5_true(seed: int = 0) -> Model:
+    """The model that generates the config-5 data: config5(seed) with log10(rho)
+    of the earth perturbed by 0.25 x a second Gaussian random field
+    (correlation 5 cells)."""
+    m = config5(seed)
+    rng = np.random.default_rng(seed + 1000)
+    nze = m.nz - m.nair
+    s3 = m.sigma.reshape(6, m.nz, m.ny, m.nx)
+    s3[0:3, m.nair:] *= (10.0 ** (-0.25 * grf((nze, m.ny, m.nx), 5.0, rng)))[None]
     return m
 
 

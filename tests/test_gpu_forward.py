@@ -114,3 +114,24 @@ def test_plan_reuse_and_device_impedance():
     np.testing.assert_array_equal(z1, z2)
     zh = S.impedance(m, ex1)
     np.testing.assert_allclose(z1, zh, rtol=0, atol=1e-14 * np.abs(zh).max())
+
+
+def test_solve_batch_matches_single_solves():
+    """Models of different meshes solved together (one host thread and stream per plan)
+    give exactly the fields of the same plans solved one at a time."""
+    models = [syn.small_aniso(n=16, seed=5, freqs=(0.2, 5.0)), syn.small_aniso(n=24, seed=6, freqs=(1.0,)),
+              syn.halfspace(n=16, freqs=(3.0, 30.0, 300.0))]
+    opts = dict(eps=1e-9, excmg=1, level=3, div_cor=2, corr_intv=25, corr_tol=1e-2, solver=3, precision=S.MIXED)
+    plans = [S.Plan(m, **opts) for m in models]
+    try:
+        st = S.solve_batch(plans)
+        assert np.all(st == 0), st
+        zb = [p.impedance() for p in plans]
+        its = [p.iters.copy() for p in plans]
+        for p, z, it in zip(plans, zb, its):
+            p.solve(fetch=False)
+            np.testing.assert_array_equal(p.impedance(), z)
+            np.testing.assert_array_equal(p.iters, it)
+    finally:
+        for p in plans:
+            p.close()
