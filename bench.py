@@ -124,7 +124,7 @@ def max_over_ranks(x, world):
     return float(t.item())
 
 
-SOLVER = {"bicgstab": 1, "gpbicg": 3, "cocr": 6}
+SOLVER = {"bicgstab": 1, "tfqmr": 2, "gpbicg": 3, "bicg": 4, "cocr": 6}
 
 
 # Divergence handling of the benchmark solves: the consistent gradient-space
@@ -132,10 +132,13 @@ SOLVER = {"bicgstab": 1, "gpbicg": 3, "cocr": 6}
 GC_OPTS = dict(div_cor=2, corr_intv=40, corr_tol=1e-2)
 
 
+USE_GRAPHS = 1  # CUDA-graph capture of the Krylov check intervals (--no-graphs: 0)
+
+
 def solve_opts(precision, solver="bicgstab", div_cor=2, eps=1e-10, corr_intv=None, level=3):
     import sfd_excmg_gb300 as S
     o = dict(excmg=1, level=level, eps=eps, precision=S.MIXED if precision == "mixed" else S.FP64,
-             solver=SOLVER[solver])
+             solver=SOLVER[solver], use_graphs=USE_GRAPHS)
     o.update(GC_OPTS if div_cor == 2 else dict(div_cor=div_cor))
     if corr_intv:
         o["corr_intv"] = corr_intv
@@ -370,7 +373,8 @@ def run_ours(args, rank, world, local):
         "config": {"workload": WORKLOADS[args.workload][0].format(eps=eps),
                    "precision": args.precision, "solver": args.solver, "div_cor": args.div_cor,
                    "systems_per_thread": {"c64": vs[0], "c128": vs[1]},
-                   "systems_per_step": ns, "l2": "working set > L2 (no flush)"},
+                   "systems_per_step": ns, "cuda_graphs": bool(USE_GRAPHS),
+                   "l2": "working set > L2 (no flush)"},
         "e2e": {"value": ns / e2e_s, "unit": "solves/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "achieved": dom["gbs"], "peak": hbm, "unit": "GB/s", "frac": dom["gbs"] / hbm,
@@ -386,12 +390,13 @@ def run_ours(args, rank, world, local):
     plan.close()
 
 
-def adjoint_measure(S, syn, torch, stream, solver, eps, fd_cells=0, reps=2, seed=0):
+def adjoint_measure(S, syn, torch, stream, solver, eps, fd_cells=0, reps=2, seed=0, adj_tol=1e-9):
     """cfg5: least-squares impedance misfit of an isotropic GRF model against data from a
     perturbed model (+2 % Gaussian noise, weights 1/(0.02|Z|)^2) and its gradient
     d misfit / d log sigma by one adjoint solve per frequency and polarisation.  Times the
-    forward solve (+ misfit) and the adjoint (+ per-cell contraction) with CUDA events on
-    the plan's stream, compares the mixed-precision gradient with the FP64 GPU adjoint and,
+    forward solve (+ misfit, tolerance eps) and the adjoint (+ per-cell contraction,
+    tolerance adj_tol, and once more at eps) with CUDA events on the plan's stream,
+    compares the mixed-precision gradients with the FP64 GPU adjoint at eps and,
     with fd_cells > 0, both with central differences (h = 1e-4 in log sigma) of FP64 GPU
     forward solves at that many random core cells (each perturbed solve starts from the base
     fields and solves the correction equation to a 1e-9 reduction, sfdx_plan_resolve)."""
@@ -416,26 +421,31 @@ def adjoint_measure(S, syn, torch, stream, solver, eps, fd_cells=0, reps=2, seed
         plan.solve(sigma_device_ptr=sig.data_ptr(), fetch=False, allow_noconv=True)
         return plan.misfit_grad(zobs, wts, with_grad=False)[0]
 
-    def adj():
-        return plan.misfit_grad(zobs, wts, grad_device_ptr=g.data_ptr(), allow_noconv=True)
+    def adj(tol):
+        return plan.misfit_grad(zobs, wts, tol=tol, grad_device_ptr=g.data_ptr(), allow_noconv=True)
+
+    def timed(fn):
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        ev[0].record(stream)
+        out = fn()
+        ev[1].record(stream)
+        ev[1].synchronize()
+        return out, ev[0].elapsed_time(ev[1])
 
     fwd()
-    adj()
+    adj(adj_tol)
     tf, ta = [], []
     for _ in range(reps):
-        ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
-        ev[0].record(stream)
-        mis = fwd()
-        ev[1].record(stream)
-        res = adj()
-        ev[2].record(stream)
-        ev[2].synchronize()
-        tf.append(ev[0].elapsed_time(ev[1]))
-        ta.append(ev[1].elapsed_time(ev[2]))
+        mis, t = timed(fwd)
+        tf.append(t)
+        res, t = timed(lambda: adj(adj_tol))
+        ta.append(t)
     fwd_iters = plan.iters[:, :, -1].ravel().tolist()
     adj_iters, adj_rr = res[3].ravel().tolist(), float(res[4].max())
     sg3 = m.sigma[0]
     dlog = sg3 * g[0:3].sum(0).cpu().numpy()
+    res_e, t_e = timed(lambda: adj(eps))  # the adjoint at the forward tolerance
+    dlog_e = sg3 * g[0:3].sum(0).cpu().numpy()
     plan.close()
     p64 = S.Plan(m, **opts64)
     p64.solve(fetch=False, allow_noconv=True)
@@ -444,13 +454,18 @@ def adjoint_measure(S, syn, torch, stream, solver, eps, fd_cells=0, reps=2, seed
     out = {"workload": ("cfg5: cfg2 mesh without hills (80x80x80, 1,574,640 edges), isotropic log10 rho GRF "
                         "(mean 2, std 0.5, corr 5 cells), 6 freqs 1e-3..1e3 Hz x 2 pols, 32x32 receivers, data "
                         "from a perturbed GRF model + 2 % noise, EXCMG 3 levels, tol " + f"{eps:g}"),
-           "precision": "mixed", "fwd_ms": float(np.median(tf)), "adjoint_ms": float(np.median(ta)),
+           "precision": "mixed", "fwd_tol": eps, "adjoint_tol": adj_tol,
+           "fwd_ms": float(np.median(tf)), "adjoint_ms": float(np.median(ta)),
            "grad_over_fwd": float(np.median(ta) / np.median(tf)),
            "fwd_plus_grad_over_fwd": float((np.median(tf) + np.median(ta)) / np.median(tf)),
            "misfit": mis, "misfit_fp64": mis64,
            "grad_rel_err_vs_fp64_adjoint": float(np.linalg.norm(dlog - dlog64) / np.linalg.norm(dlog64)),
            "fwd_fine_iters": fwd_iters, "adjoint_iters": adj_iters, "adjoint_relres_max": adj_rr,
-           "adjoint_iters_fp64": it64.ravel().tolist()}
+           "at_fwd_tol": {"adjoint_ms": t_e, "grad_over_fwd": float(t_e / np.median(tf)),
+                          "grad_rel_err_vs_fp64_adjoint": float(np.linalg.norm(dlog_e - dlog64) /
+                                                                np.linalg.norm(dlog64)),
+                          "adjoint_iters": res_e[3].ravel().tolist()},
+           "fp64_adjoint": {"tol": eps, "iters": it64.ravel().tolist()}}
     if fd_cells:
         rs = np.random.default_rng(seed + 11)
         npad, nc, ncz = 8, 64, 48
@@ -493,6 +508,9 @@ def run_batch(args, rank, world, local):
     eps = args.eps if args.eps else WORKLOADS["cfg3"][1]
     models = syn.config3(seed=rank)
     opts = solve_opts(args.precision, args.solver, args.div_cor, eps, args.corr_intv, 3)
+    # the meshes are not square: receivers through the corrected (untransposed)
+    # interpolation stencil (the reference's transposed one indexes past ny)
+    opts["quirks"] = capi.QUIRKS_REFERENCE & ~4
     plans = [S.Plan(m, **opts) for m in models]
     sig = [torch.from_numpy(np.ascontiguousarray(m.sigma)).to("cuda") for m in models]
     ptrs = [t.data_ptr() for t in sig]
@@ -540,7 +558,9 @@ def run_batch(args, rank, world, local):
         p.close()
     extra = {}
     if args.compare_fp64 and rank == 0:
-        p64 = [S.Plan(m, **solve_opts("fp64", args.solver, args.div_cor, eps, args.corr_intv, 3)) for m in models]
+        o64 = solve_opts("fp64", args.solver, args.div_cor, eps, args.corr_intv, 3)
+        o64["quirks"] = opts["quirks"]
+        p64 = [S.Plan(m, **o64) for m in models]
         t = time.perf_counter()
         S.solve_batch(p64, sigma_device_ptrs=ptrs, allow_noconv=True)
         t64 = time.perf_counter() - t
@@ -564,7 +584,8 @@ def run_batch(args, rank, world, local):
         "config": {"workload": WORKLOADS["cfg3"][0].format(eps=eps),
                    "meshes": [[m.nx, m.ny, m.nz] for m in models], "edges": [int(m.nl) for m in models],
                    "precision": args.precision, "solver": args.solver, "div_cor": args.div_cor,
-                   "systems_per_thread": vs, "systems_per_step": ns, "l2": "working set > L2 (no flush)"},
+                   "systems_per_thread": vs, "systems_per_step": ns, "cuda_graphs": bool(USE_GRAPHS),
+                   "l2": "working set > L2 (no flush)"},
         "e2e": {"value": ns / e2e, "unit": "solves/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": int(launches), "sequential_solves_per_s": ns / seq, "clocks": clk,
         "solve": {"status": status, "fine_iters": iters},
@@ -612,6 +633,8 @@ def main():
     ap.add_argument("--div-cor", dest="div_cor", type=int, default=2, choices=[0, 1, 2],
                     help="0 none, 1 the reference's divergence correction, 2 consistent gradient-space correction")
     ap.add_argument("--no-compare-fp64", dest="compare_fp64", action="store_false")
+    ap.add_argument("--no-graphs", dest="graphs", action="store_false",
+                    help="launch the Krylov iterations one by one instead of replaying captured CUDA graphs")
     ap.add_argument("--no-adjoint", dest="adjoint", action="store_false",
                     help="skip the misfit-gradient measurement (cfg5 workload: forward vs adjoint time, FP64 check)")
     ap.add_argument("--fd-cells", dest="fd_cells", type=int, default=0,
@@ -623,6 +646,8 @@ def main():
                     help="only load the workload's conductivity and time each kernel family a few times "
                          "(a short launch sequence for ncu captures)")
     args = ap.parse_args()
+    global USE_GRAPHS
+    USE_GRAPHS = 1 if args.graphs else 0
     rank, world, local = dist()
     if args.profile:
         run_profile(args)

@@ -46,7 +46,10 @@ extern "C" {
 #define SFDX_QUIRK_RX_TRANSPOSE 4    /* arho_interp2 rd=2 stencil (fdfe_main.f90:763-768)         */
 #define SFDX_QUIRKS_REFERENCE 7
 
-/* solver ids (.fwd line 2, read_input file_opt.f90:102) */
+/* solver ids (.fwd line 2, read_input file_opt.f90:102).  TFQMR, BiCG and COCR
+ * are broken or unreachable in the reference (ptfqmr, pbicg, pcocr); these are
+ * the published algorithms (Freund 1993; Fletcher 1976 with A^H; Sogabe & Zhang
+ * 2007).  TFQMR and BiCG run in FP64 also in mixed-precision plans. */
 #define SFDX_SOLVER_BICGSTAB 1
 #define SFDX_SOLVER_TFQMR 2
 #define SFDX_SOLVER_GPBICG 3
@@ -87,9 +90,12 @@ typedef struct sfdx_opts {
     double coarse_tol;  /* relative residual of the on-device solve replacing PARDISO */
     int coarse_maxit;   /* iteration limit of that solve                               */
     int reliable_every; /* mixed precision: iterations between FP64 residual updates */
-    int batch;          /* systems solved together (0 = all 2*nf)                      */
+    int batch;          /* must be 0: all 2*nf systems of a plan form one batch; to
+                           bound memory, split the frequencies over several plans
+                           (sfdx_plan_solve_batch runs them concurrently)           */
     int verbose;        /* 0 silent, 1 per-level summary on stderr                     */
-    int use_graphs;     /* capture Krylov iterations in CUDA graphs                    */
+    int use_graphs;     /* replay each 8-iteration check interval of the Krylov solves
+                           as a captured CUDA graph (1, default) or launch eagerly (0) */
 } sfdx_opts;
 
 /* Fill *o with the reference defaults. */

@@ -120,17 +120,75 @@ static double dual_volume(const std::vector<double>& h0, const std::vector<doubl
     return h0[i] * (h1[j - 1] + h1[j]) * 0.5 * (h2[k - 1] + h2[k]) * 0.5;
 }
 
+// V^-1 g of the adjoint source on the receiver planes of level L (interior
+// edges), written interleaved [edge][system] into P.b64 (zero elsewhere).
+// cf: [nf][nrec][2][4] receiver cotangents.
+static int adjoint_rhs(Plan& P, const Level& L, int nrec, const double* recv, int transpose,
+                       const std::vector<std::complex<double>>& cf) {
+    const int ns = P.ns, nx = L.nx, ny = L.ny, m = L.nair;
+    const size_t pex = (size_t)nx * (ny + 1), pey = (size_t)(nx + 1) * ny, pez = (size_t)(nx + 1) * (ny + 1);
+    const size_t per = 2 * pex + 2 * pey + pez;
+    std::vector<std::complex<double>> gs(per * ns, 0.0);
+    for (int f = 0; f < P.nf; f++) {
+        SurfaceGrad sg;
+        sg.nx = nx;
+        sg.ny = ny;
+        for (int p = 0; p < 2; p++) {
+            const size_t o = (size_t)(2 * f + p) * per;
+            sg.exs[p] = gs.data() + o;
+            sg.eys[p] = gs.data() + o + 2 * pex;
+            sg.ezs[p] = gs.data() + o + 2 * pex + 2 * pey;
+        }
+        RC(impedance_adjoint_source(sg, m, L.a.data(), L.b.data(), L.c.data(), P.freq[f], nrec, recv, transpose,
+                                    cf.data() + (size_t)f * nrec * 8));
+    }
+    std::vector<std::complex<double>> rx(2 * pex * ns), ry(2 * pey * ns), rz(pez * ns);
+    for (int s = 0; s < ns; s++) {
+        const std::complex<double>* g = gs.data() + (size_t)s * per;
+        for (int pl = 0; pl < 2; pl++)
+            for (int j = 0; j <= ny; j++)
+                for (int i = 0; i < nx; i++) {
+                    const size_t q = (size_t)pl * pex + (size_t)j * nx + i;
+                    const double v = dual_volume(L.a, L.b, L.c, i, j, m + pl);
+                    rx[q * ns + s] = v > 0 ? g[q] / v : 0.0;
+                }
+        for (int pl = 0; pl < 2; pl++)
+            for (int j = 0; j < ny; j++)
+                for (int i = 0; i <= nx; i++) {
+                    const size_t q = (size_t)pl * pey + (size_t)j * (nx + 1) + i;
+                    const double v = dual_volume(L.b, L.a, L.c, j, i, m + pl);
+                    ry[q * ns + s] = v > 0 ? g[2 * pex + q] / v : 0.0;
+                }
+        for (int j = 0; j <= ny; j++)
+            for (int i = 0; i <= nx; i++) {
+                const size_t q = (size_t)j * (nx + 1) + i;
+                const double v = dual_volume(L.c, L.a, L.b, m, i, j);
+                rz[q * ns + s] = v > 0 ? g[2 * pex + 2 * pey + q] / v : 0.0;
+            }
+    }
+    double2* b = P.b64.as<double2>();
+    CK(cudaMemsetAsync(P.b64.p, 0, (size_t)L.nl * ns * sizeof(double2), P.st));
+    CK(cudaMemcpyAsync(b + (size_t)m * pex * ns, rx.data(), rx.size() * 16, cudaMemcpyHostToDevice, P.st));
+    CK(cudaMemcpyAsync(b + ((size_t)L.xnl + (size_t)m * pey) * ns, ry.data(), ry.size() * 16, cudaMemcpyHostToDevice,
+                       P.st));
+    CK(cudaMemcpyAsync(b + ((size_t)L.xnl + L.ynl + (size_t)m * pez) * ns, rz.data(), rz.size() * 16,
+                       cudaMemcpyHostToDevice, P.st));
+    // the host staging vectors go out of scope: finish the copies first
+    CK(cudaStreamSynchronize(P.st));
+    return SFDX_OK;
+}
+
 int misfit_grad(Plan& P, int nrec, const double* recv, const double* zobs, const double* wts, double tol,
                 double* misfit, double* zpred, double* grad, bool grad_on_device, int* adj_iters, double* adj_relres) {
     if (!P.have_solution) return SFDX_ERR_ARG;
     const Level& F = P.lev[P.nlev - 1];
     const int ns = P.ns, nx = F.nx, ny = F.ny, nz = F.nz, m = F.nair;
-    if (m + 2 > nz) return SFDX_ERR_MESH;
+    if (m < 1 || m + 2 > nz) return SFDX_ERR_MESH;
     const size_t nfine = (size_t)F.nl * ns * sizeof(double2);
     // surface planes of every system (system-major copy of the solution)
     const size_t pex = (size_t)nx * (ny + 1), pey = (size_t)(nx + 1) * ny, pez = (size_t)(nx + 1) * (ny + 1);
     const size_t per = 2 * pex + 2 * pey + pez;
-    std::vector<std::complex<double>> surf(per * ns), gs(per * ns, 0.0);
+    std::vector<std::complex<double>> surf(per * ns);
     const std::complex<double>* dev = reinterpret_cast<const std::complex<double>*>(P.ex_out.p);
     for (int s = 0; s < ns; s++) {
         const std::complex<double>* x = dev + (size_t)s * F.nl;
@@ -143,24 +201,21 @@ int misfit_grad(Plan& P, int nrec, const double* recv, const double* zobs, const
     CK(cudaStreamSynchronize(P.st));
     double phi = 0;
     const int transpose = (P.o.quirks & SFDX_QUIRK_RX_TRANSPOSE) ? 1 : 0;
+    std::vector<std::complex<double>> cf((size_t)P.nf * nrec * 8);
     for (int f = 0; f < P.nf; f++) {
         SurfaceView sv;
-        SurfaceGrad sg;
-        sv.nx = sg.nx = nx;
-        sv.ny = sg.ny = ny;
+        sv.nx = nx;
+        sv.ny = ny;
         sv.nair = m;
         for (int p = 0; p < 2; p++) {
             const size_t o = (size_t)(2 * f + p) * per;
             sv.exs[p] = surf.data() + o;
             sv.eys[p] = surf.data() + o + 2 * pex;
             sv.ezs[p] = surf.data() + o + 2 * pex + 2 * pey;
-            sg.exs[p] = gs.data() + o;
-            sg.eys[p] = gs.data() + o + 2 * pex;
-            sg.ezs[p] = gs.data() + o + 2 * pex + 2 * pey;
         }
-        RC(impedance_misfit_adjoint(sv, F.a.data(), F.b.data(), F.c.data(), P.freq[f], nrec, recv, transpose,
-                                    zobs + (size_t)f * nrec * 4, wts ? wts + (size_t)f * nrec * 2 : nullptr, &phi,
-                                    zpred ? zpred + (size_t)f * nrec * 4 : nullptr, sg));
+        RC(impedance_cotangents(sv, F.a.data(), F.b.data(), F.c.data(), P.freq[f], nrec, recv, transpose,
+                                zobs + (size_t)f * nrec * 4, wts ? wts + (size_t)f * nrec * 2 : nullptr, &phi,
+                                zpred ? zpred + (size_t)f * nrec * 4 : nullptr, cf.data() + (size_t)f * nrec * 8));
     }
     *misfit = phi;
     if (!grad) return SFDX_OK;  // misfit (and predicted impedances) only
@@ -170,43 +225,13 @@ int misfit_grad(Plan& P, int nrec, const double* recv, const double* zobs, const
         CK(cudaMemcpyAsync(P.xf.p, P.x64.p, nfine, cudaMemcpyDeviceToDevice, P.st));
         P.xf_valid = true;
     }
-    // adjoint right-hand side V^-1 g on the interior edges of the receiver
-    // planes, interleaved [edge][system]; zero elsewhere
-    std::vector<std::complex<double>> rx(2 * pex * ns), ry(2 * pey * ns), rz(pez * ns);
-    for (int s = 0; s < ns; s++) {
-        const std::complex<double>* g = gs.data() + (size_t)s * per;
-        for (int pl = 0; pl < 2; pl++)
-            for (int j = 0; j <= ny; j++)
-                for (int i = 0; i < nx; i++) {
-                    const size_t q = (size_t)pl * pex + (size_t)j * nx + i;
-                    const double v = dual_volume(F.a, F.b, F.c, i, j, m + pl);
-                    rx[q * ns + s] = v > 0 ? g[q] / v : 0.0;
-                }
-        for (int pl = 0; pl < 2; pl++)
-            for (int j = 0; j < ny; j++)
-                for (int i = 0; i <= nx; i++) {
-                    const size_t q = (size_t)pl * pey + (size_t)j * (nx + 1) + i;
-                    const double v = dual_volume(F.b, F.a, F.c, j, i, m + pl);
-                    ry[q * ns + s] = v > 0 ? g[2 * pex + q] / v : 0.0;
-                }
-        for (int j = 0; j <= ny; j++)
-            for (int i = 0; i <= nx; i++) {
-                const size_t q = (size_t)j * (nx + 1) + i;
-                const double v = dual_volume(F.c, F.a, F.b, m, i, j);
-                rz[q * ns + s] = v > 0 ? g[2 * pex + 2 * pey + q] / v : 0.0;
-            }
-    }
-    double2* b = P.b64.as<double2>();
-    CK(cudaMemsetAsync(P.b64.p, 0, nfine, P.st));
-    CK(cudaMemsetAsync(P.x64.p, 0, nfine, P.st));
-    CK(cudaMemcpyAsync(b + (size_t)m * pex * ns, rx.data(), rx.size() * 16, cudaMemcpyHostToDevice, P.st));
-    CK(cudaMemcpyAsync(b + ((size_t)F.xnl + (size_t)m * pey) * ns, ry.data(), ry.size() * 16, cudaMemcpyHostToDevice,
-                       P.st));
-    CK(cudaMemcpyAsync(b + ((size_t)F.xnl + F.ynl + (size_t)m * pez) * ns, rz.data(), rz.size() * 16,
-                       cudaMemcpyHostToDevice, P.st));
-    // adjoint solve (same solver, precision and corrections as the forward
-    // solve), from zero on the finest mesh
+    // Adjoint solve on the finest mesh from zero.  (An EXCMG cascade with the
+    // same receiver functional on the coarse meshes gives a worse start: the
+    // extrapolation amplifies the coarse-grid error of the point-like receiver
+    // sources -- on cfg5 it needed more iterations than the zero guess.)
     std::vector<int> its, status;
+    RC(adjoint_rhs(P, F, nrec, recv, transpose, cf));
+    CK(cudaMemsetAsync(P.x64.p, 0, nfine, P.st));
     RC(solve_level(P, F, tol > 0 ? tol : P.o.eps, P.o.maxit_plain, false, its, status));
     int rc_conv = SFDX_OK;
     for (int s = 0; s < ns; s++) {

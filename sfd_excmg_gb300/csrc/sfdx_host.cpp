@@ -320,21 +320,17 @@ int impedance_from_surface(const SurfaceView& sv, const double* a, const double*
 }
 
 // Least-squares impedance misfit of one frequency and its derivative with
-// respect to the surface edge values (reverse mode through Z, the receiver
-// interpolation and surface_fields).  phi = sum_r wxy |Zxy - dxy|^2 + wyx |Zyx
-// - dyx|^2; g = d phi / d x in the holomorphic (Wirtinger) sense, so that
-// d phi = 2 Re(g^T dx).
-int impedance_misfit_adjoint(const SurfaceView& sv, const double* a, const double* b, const double* c, double ff,
-                             int nrec, const double* recv, int transpose, const double* zobs, const double* wts,
-                             double* misfit, double* zpred, SurfaceGrad& g) {
+// respect to the receiver fields (reverse mode through Z):
+// phi = sum_r wxy |Zxy - dxy|^2 + wyx |Zyx - dyx|^2, cf[r][p][q] = d phi / d
+// f[p][q] (q = Ex, Ey, Hx, Hy of polarisation p at receiver r) in the
+// holomorphic (Wirtinger) sense, so that d phi = 2 Re(sum cf df).
+int impedance_cotangents(const SurfaceView& sv, const double* a, const double* b, const double* c, double ff,
+                         int nrec, const double* recv, int transpose, const double* zobs, const double* wts,
+                         double* misfit, double* zpred, std::complex<double>* cf_out) {
     const int nx = sv.nx, ny = sv.ny;
-    const size_t n = (size_t)nx * ny;
     const zd iwm = zd(0, 1) * 2.0 * kPi * ff * kMu;
-    SurfFields F[2], dF[2];
-    for (int p = 0; p < 2; p++) {
-        surface_fields(sv, p, a, b, c[sv.nair], iwm, F[p]);
-        dF[p].init(n);
-    }
+    SurfFields F[2];
+    for (int p = 0; p < 2; p++) surface_fields(sv, p, a, b, c[sv.nair], iwm, F[p]);
     std::vector<double> aax, bby;
     cell_centres(nx, ny, a, b, aax, bby);
     double phi = 0;
@@ -358,25 +354,46 @@ int impedance_misfit_adjoint(const SurfaceView& sv, const double* a, const doubl
         }
         // d phi / dZ, then through Z(E, H)
         const zd cxy = wxy * std::conj(rxy), cyx = wyx * std::conj(ryx);
-        zd cf[2][4];
-        cf[0][0] = cxy * (-Hx2 / det);                                              // Ex1
-        cf[1][0] = cxy * (Hx1 / det);                                               // Ex2
-        cf[0][1] = cyx * (Hy2 / det);                                               // Ey1
-        cf[1][1] = cyx * (-Hy1 / det);                                              // Ey2
-        cf[0][2] = cxy * ((Ex2 - zxy * Hy2) / det) + cyx * (-zyx * Hy2 / det);      // Hx1
-        cf[1][2] = cxy * ((-Ex1 + zxy * Hy1) / det) + cyx * (zyx * Hy1 / det);      // Hx2
-        cf[0][3] = cxy * (zxy * Hx2 / det) + cyx * ((-Ey2 + zyx * Hx2) / det);      // Hy1
-        cf[1][3] = cxy * (-zxy * Hx1 / det) + cyx * ((Ey1 - zyx * Hx1) / det);      // Hy2
+        zd* cf = cf_out + (size_t)r * 8;  // [p][q]
+        cf[0] = cxy * (-Hx2 / det);                                         // Ex1
+        cf[4] = cxy * (Hx1 / det);                                          // Ex2
+        cf[1] = cyx * (Hy2 / det);                                          // Ey1
+        cf[5] = cyx * (-Hy1 / det);                                         // Ey2
+        cf[2] = cxy * ((Ex2 - zxy * Hy2) / det) + cyx * (-zyx * Hy2 / det); // Hx1
+        cf[6] = cxy * ((-Ex1 + zxy * Hy1) / det) + cyx * (zyx * Hy1 / det); // Hx2
+        cf[3] = cxy * (zxy * Hx2 / det) + cyx * ((-Ey2 + zyx * Hx2) / det); // Hy1
+        cf[7] = cxy * (-zxy * Hx1 / det) + cyx * ((Ey1 - zyx * Hx1) / det); // Hy2
+    }
+    *misfit += phi;
+    return SFDX_OK;
+}
+
+// The adjoint source of those cotangents on the surface edge planes of a mesh
+// (the transpose of the receiver interpolation and of surface_fields); g is
+// accumulated.  Evaluated on the coarse meshes too, where it is the same
+// functional of the coarse fields.
+int impedance_adjoint_source(SurfaceGrad& g, int nair, const double* a, const double* b, const double* c, double ff,
+                             int nrec, const double* recv, int transpose, const std::complex<double>* cf_in) {
+    const int nx = g.nx, ny = g.ny;
+    const size_t n = (size_t)nx * ny;
+    const zd iwm = zd(0, 1) * 2.0 * kPi * ff * kMu;
+    SurfFields dF[2];
+    for (int p = 0; p < 2; p++) dF[p].init(n);
+    std::vector<double> aax, bby;
+    cell_centres(nx, ny, a, b, aax, bby);
+    for (int r = 0; r < nrec; r++) {
+        RecvStencil S;
+        HRC(receiver_stencil(nx, ny, aax, bby, recv[r], recv[(size_t)nrec + r], transpose, S));
+        const zd* cf = cf_in + (size_t)r * 8;
         for (int p = 0; p < 2; p++)
             for (int t = 0; t < 9; t++) {
-                dF[p].E[0][S.id[t]] += S.w[t] * cf[p][0];
-                dF[p].E[1][S.id[t]] += S.w[t] * cf[p][1];
-                dF[p].H[0][S.id[t]] += S.w[t] * cf[p][2];
-                dF[p].H[1][S.id[t]] += S.w[t] * cf[p][3];
+                dF[p].E[0][S.id[t]] += S.w[t] * cf[4 * p + 0];
+                dF[p].E[1][S.id[t]] += S.w[t] * cf[4 * p + 1];
+                dF[p].H[0][S.id[t]] += S.w[t] * cf[4 * p + 2];
+                dF[p].H[1][S.id[t]] += S.w[t] * cf[4 * p + 3];
             }
     }
-    for (int p = 0; p < 2; p++) surface_fields_adjoint(g, p, a, b, c[sv.nair], iwm, dF[p]);
-    *misfit += phi;
+    for (int p = 0; p < 2; p++) surface_fields_adjoint(g, p, a, b, c[nair], iwm, dF[p]);
     return SFDX_OK;
 }
 

@@ -41,11 +41,15 @@ int impedance_from_surface(const SurfaceView& sv, const double* a, const double*
                            int nrec, const double* recv, int out_type, int transpose, double* out, double* tip);
 
 // Impedance misfit of one frequency (added to *misfit), the predicted Z
-// (optional, [nrec][4]) and its derivative with respect to the surface edge
-// values, accumulated into g.  zobs [nrec][4] = (Re, Im Zxy, Re, Im Zyx);
-// wts [nrec][2] (null: 1).
-int impedance_misfit_adjoint(const SurfaceView& sv, const double* a, const double* b, const double* c, double ff,
-                             int nrec, const double* recv, int transpose, const double* zobs, const double* wts,
-                             double* misfit, double* zpred, SurfaceGrad& g);
+// (optional, [nrec][4]) and its derivative with respect to the receiver fields,
+// cf [nrec][2 polarisations][Ex, Ey, Hx, Hy].  zobs [nrec][4] = (Re, Im Zxy,
+// Re, Im Zyx); wts [nrec][2] (null: 1).
+int impedance_cotangents(const SurfaceView& sv, const double* a, const double* b, const double* c, double ff,
+                         int nrec, const double* recv, int transpose, const double* zobs, const double* wts,
+                         double* misfit, double* zpred, std::complex<double>* cf);
+// d misfit / d (surface edge values) of a mesh from those cotangents,
+// accumulated into g (the adjoint source on that mesh's receiver planes).
+int impedance_adjoint_source(SurfaceGrad& g, int nair, const double* a, const double* b, const double* c, double ff,
+                             int nrec, const double* recv, int transpose, const std::complex<double>* cf);
 
 }  // namespace sfdx

@@ -8,6 +8,7 @@
 #pragma once
 #include <chrono>
 
+#include "sfdx_blas.cuh"
 #include "sfdx_plan.h"
 #include "sfdx_vkern.cuh"
 
@@ -399,6 +400,173 @@ static int cocr_v(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, const 
     return SFDX_OK;
 }
 
+// Right-preconditioned TFQMR (Freund 1993; SFDX_SOLVER_TFQMR -- ptfqmr,
+// solvers.f90:317-519, reads tmp, u and r0 before setting them) for the ns
+// systems of level LV, same calling convention as bicgstab.  Per iteration two
+// operator and two preconditioner applications, two quasi-minimisation
+// half-steps; convergence on the residual bound tau sqrt(m+1).  FP64 only
+// (mixed-precision plans run it in FP64).
+template <class T, int VS>
+static int tfqmr_v(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, const double* tols_host, double tol,
+                   int itmax, const int* mask_host, const Reliable* rel) {
+    if (rel) return SFDX_ERR_UNSUPPORTED;
+    const Lev<T> L = LV.lev<T>();
+    const Mesh& M = LV.mesh;
+    const int ns = P.ns;
+    const size_t vb = (size_t)LV.nl * ns * sizeof(cplx<T>);
+    for (int k = 0; k < 10; k++) RC(P.kv[k].alloc(vb));
+    cplx<T>* V[10];
+    for (int k = 0; k < 10; k++) V[k] = P.kv[k].as<cplx<T>>();
+    cplx<T> *w = V[0], *rt = V[1], *u = V[2], *uh = V[3], *v = V[4], *q = V[5], *qh = V[6], *aq = V[7], *d = V[8];
+    cplx<T>* au = V[9];
+    std::vector<KState> init;
+    init_states(P, tols_host, tol, itmax, mask_host, init);
+    CK(cudaMemcpyAsync(P.d_state.p, init.data(), sizeof(KState) * ns, cudaMemcpyHostToDevice, P.st));
+    const VCfg c = vcfg(P, LV.nl, 2, VS);
+    RC(reserve_partials(P, c, 2));
+    KState* dst = P.d_state.as<KState>();
+    const int64_t W = LV.nl * c.sg.G;
+    const double* wm = P.d_wm.as<double>();
+    const cplx<T>* nul = nullptr;
+    CK(cudaMemsetAsync(d, 0, vb, P.st));
+    vlaunch(k_residual_v<T, T, VS, 3>, W, c.B, c.smem, P.st, L, M, c.sg, dst, b, (const cplx<T>*)x, w, rt, redbuf(P),
+            (double*)nullptr, 0);
+    vlaunch(k_bl_dot<T, VS, FIN_TFQ_INIT>, W, c.B, c.smem, P.st, M, c.sg, dst, (const cplx<T>*)rt, (const cplx<T>*)w,
+            (const cplx<T>*)w, (const cplx<T>*)w, redbuf(P));
+    vlaunch(k_bl_lincomb<T, VS, BC_ONE, BC_ZERO, BC_ZERO>, W, c.B, 0, P.st, M, c.sg, (const KState*)dst, u,
+            (const cplx<T>*)w, nul, nul);
+    // out_h = M^-1 in, out_a = A out_h
+    auto amv = [&](cplx<T>* out_h, cplx<T>* out_a, cplx<T>* in) {
+        precond<T, VS, RHS_VEC>(P, LV, out_h, in, nullptr, nullptr);
+        vlaunch(k_apply_v<T, VS>, W, c.B, 0, P.st, L, M, c.sg, wm, (const cplx<T>*)out_h, out_a);
+    };
+    auto xupd = [&]() {  // x += eta d, then stop the systems that met the test
+        vlaunch(k_bl_lincomb<T, VS, BC_ONE, BC_ETA, BC_ZERO>, W, c.B, 0, P.st, M, c.sg, (const KState*)dst, x,
+                (const cplx<T>*)x, (const cplx<T>*)d, nul);
+        KL(k_bl_commit<<<(ns + 127) / 128, 128, 0, P.st>>>(dst, ns));
+    };
+    amv(uh, v, u);
+    auto body = [&]() {
+        vlaunch(k_bl_dot<T, VS, FIN_TFQ_SIGMA>, W, c.B, c.smem, P.st, M, c.sg, dst, (const cplx<T>*)rt,
+                (const cplx<T>*)v, nul, nul, redbuf(P));
+        vlaunch(k_bl_lincomb<T, VS, BC_ONE, BC_MALPHA, BC_ZERO>, W, c.B, 0, P.st, M, c.sg, (const KState*)dst, q,
+                (const cplx<T>*)u, (const cplx<T>*)v, nul);
+        amv(qh, aq, q);
+        vlaunch(k_tfq_half<T, VS>, W, c.B, c.smem, P.st, M, c.sg, dst, w, (const cplx<T>*)v, d, (const cplx<T>*)uh,
+                redbuf(P), P.hist, P.hist_stride);
+        xupd();
+        vlaunch(k_tfq_half<T, VS>, W, c.B, c.smem, P.st, M, c.sg, dst, w, (const cplx<T>*)aq, d, (const cplx<T>*)qh,
+                redbuf(P), P.hist, P.hist_stride);
+        xupd();
+        vlaunch(k_bl_dot<T, VS, FIN_TFQ_RHO>, W, c.B, c.smem, P.st, M, c.sg, dst, (const cplx<T>*)rt,
+                (const cplx<T>*)w, nul, nul, redbuf(P));
+        vlaunch(k_bl_lincomb<T, VS, BC_ONE, BC_BETA, BC_ZERO>, W, c.B, 0, P.st, M, c.sg, (const KState*)dst, u,
+                (const cplx<T>*)w, (const cplx<T>*)q, nul);
+        amv(uh, au, u);
+        vlaunch(k_bl_lincomb<T, VS, BC_ONE, BC_BETA, BC_BETA2>, W, c.B, 0, P.st, M, c.sg, (const KState*)dst, v,
+                (const cplx<T>*)au, (const cplx<T>*)aq, (const cplx<T>*)v);
+    };
+    for (int it = 1; it <= itmax; it++) {
+        if (graph_interval(P, it, itmax, false)) {
+            RC(graph_run(P, interval_key<T>(P, LV, 2, VS, {(uintptr_t)x, (uintptr_t)b}), [&] {
+                for (int k = 0; k < 8; k++) body();
+            }));
+            it += 7;
+        } else {
+            body();
+        }
+        if (it % 8 == 0 || it == itmax) {
+            CK(cudaGetLastError());
+            RC(sync_state(P));
+            int act = 0;
+            for (int k = 0; k < ns; k++) act += P.hst[k].active;
+            if (!act) break;
+        }
+    }
+    RC(sync_state(P));
+    return SFDX_OK;
+}
+
+// Preconditioned two-sided BiCG for complex systems (Fletcher 1976, in the
+// preconditioned form of the Templates book; SFDX_SOLVER_BICG -- pbicg,
+// solvers.f90:878-1025, never forms zt with SSOR).  The shadow recurrence uses
+// A^H and M^-H, formed through the dual-volume symmetry (k_bl_conj_vscale).
+// FP64 only (mixed-precision plans run it in FP64).
+template <class T, int VS>
+static int bicg2_v(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, const double* tols_host, double tol,
+                   int itmax, const int* mask_host, const Reliable* rel) {
+    if (rel) return SFDX_ERR_UNSUPPORTED;
+    const Lev<T> L = LV.lev<T>();
+    const Mesh& M = LV.mesh;
+    const int ns = P.ns;
+    const size_t vb = (size_t)LV.nl * ns * sizeof(cplx<T>);
+    for (int k = 0; k < 10; k++) RC(P.kv[k].alloc(vb));
+    cplx<T>* V[10];
+    for (int k = 0; k < 10; k++) V[k] = P.kv[k].as<cplx<T>>();
+    cplx<T> *r = V[0], *rt = V[1], *z = V[2], *zt = V[3], *p = V[4], *pt = V[5], *q = V[6], *qt = V[7], *t1 = V[8];
+    cplx<T>* t2 = V[9];
+    std::vector<KState> init;
+    init_states(P, tols_host, tol, itmax, mask_host, init);
+    CK(cudaMemcpyAsync(P.d_state.p, init.data(), sizeof(KState) * ns, cudaMemcpyHostToDevice, P.st));
+    const VCfg c = vcfg(P, LV.nl, 2, VS);
+    RC(reserve_partials(P, c, 2));
+    KState* dst = P.d_state.as<KState>();
+    const int64_t W = LV.nl * c.sg.G;
+    const double* wm = P.d_wm.as<double>();
+    const cplx<T>* nul = nullptr;
+    CK(cudaMemsetAsync(p, 0, vb, P.st));
+    CK(cudaMemsetAsync(pt, 0, vb, P.st));
+    vlaunch(k_residual_v<T, T, VS, 3>, W, c.B, c.smem, P.st, L, M, c.sg, dst, b, (const cplx<T>*)x, r, rt, redbuf(P),
+            (double*)nullptr, 0);
+    vlaunch(k_bl_dot<T, VS, FIN_BICG_INIT>, W, c.B, c.smem, P.st, M, c.sg, dst, (const cplx<T>*)r, (const cplx<T>*)r,
+            nul, nul, redbuf(P));
+    // out = (op)^H in through V conj(op(V^-1 conj(in)))
+    auto herm = [&](cplx<T>* out, const cplx<T>* in, bool prec) {
+        vlaunch(k_bl_conj_vscale<T, VS, true>, W, c.B, 0, P.st, L, M, c.sg, (const KState*)dst, in, t1);
+        if (prec)
+            precond<T, VS, RHS_VEC>(P, LV, t2, t1, nullptr, nullptr);
+        else
+            vlaunch(k_apply_v<T, VS>, W, c.B, 0, P.st, L, M, c.sg, wm, (const cplx<T>*)t1, t2);
+        vlaunch(k_bl_conj_vscale<T, VS, false>, W, c.B, 0, P.st, L, M, c.sg, (const KState*)dst, (const cplx<T>*)t2,
+                out);
+    };
+    auto body = [&]() {
+        precond<T, VS, RHS_VEC>(P, LV, z, r, nullptr, nullptr);
+        herm(zt, rt, true);
+        vlaunch(k_bl_dot<T, VS, FIN_BICG_RHO>, W, c.B, c.smem, P.st, M, c.sg, dst, (const cplx<T>*)rt,
+                (const cplx<T>*)z, nul, nul, redbuf(P));
+        vlaunch(k_bl_lincomb<T, VS, BC_ONE, BC_BETA, BC_ZERO>, W, c.B, 0, P.st, M, c.sg, (const KState*)dst, p,
+                (const cplx<T>*)z, (const cplx<T>*)p, nul);
+        vlaunch(k_bl_lincomb<T, VS, BC_ONE, BC_CBETA, BC_ZERO>, W, c.B, 0, P.st, M, c.sg, (const KState*)dst, pt,
+                (const cplx<T>*)zt, (const cplx<T>*)pt, nul);
+        vlaunch(k_apply_v<T, VS>, W, c.B, 0, P.st, L, M, c.sg, wm, (const cplx<T>*)p, q);
+        herm(qt, pt, false);
+        vlaunch(k_bl_dot<T, VS, FIN_BICG_ALPHA>, W, c.B, c.smem, P.st, M, c.sg, dst, (const cplx<T>*)pt,
+                (const cplx<T>*)q, nul, nul, redbuf(P));
+        vlaunch(k_bicg2_upd<T, VS>, W, c.B, c.smem, P.st, M, c.sg, dst, x, r, rt, (const cplx<T>*)p, (const cplx<T>*)q,
+                (const cplx<T>*)qt, redbuf(P), P.hist, P.hist_stride);
+    };
+    for (int it = 1; it <= itmax; it++) {
+        if (graph_interval(P, it, itmax, false)) {
+            RC(graph_run(P, interval_key<T>(P, LV, 4, VS, {(uintptr_t)x, (uintptr_t)b}), [&] {
+                for (int k = 0; k < 8; k++) body();
+            }));
+            it += 7;
+        } else {
+            body();
+        }
+        if (it % 8 == 0 || it == itmax) {
+            CK(cudaGetLastError());
+            RC(sync_state(P));
+            int act = 0;
+            for (int k = 0; k < ns; k++) act += P.hst[k].active;
+            if (!act) break;
+        }
+    }
+    RC(sync_state(P));
+    return SFDX_OK;
+}
+
 // ------------------------------------------------------------------ corrected restart cycles
 // dst[e][i] = src[e][idx[i]] (i < nd)  /  dst[e][idx[i]] = src[e][i]
 static __global__ void k_gather_cols(int64_t nl, int ns, int nd, const int* __restrict__ idx,
@@ -585,6 +753,34 @@ int cocr(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, const double* t
         return corrected_cycles<T>(P, LV, b, x, itmax, mask_host, rel, run);
     return run(itmax, mask_host, b, x, rel);
 }
+template <class T>
+int tfqmr(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, const double* tols_host, double tol, int itmax,
+          const int* mask_host, const Reliable* rel) {
+    auto run = [&](int itc, const int* m, const cplx<T>* bb, cplx<T>* xx, const Reliable* rr) -> int {
+        switch (plan_vs<T>(P)) {
+            case 4: return tfqmr_v<T, 4>(P, LV, bb, xx, tols_host, tol, itc, m, rr);
+            case 2: return tfqmr_v<T, 2>(P, LV, bb, xx, tols_host, tol, itc, m, rr);
+            default: return tfqmr_v<T, 1>(P, LV, bb, xx, tols_host, tol, itc, m, rr);
+        }
+    };
+    if (P.o.div_cor == 2 && (rel || std::is_same<T, double>::value))
+        return corrected_cycles<T>(P, LV, b, x, itmax, mask_host, rel, run);
+    return run(itmax, mask_host, b, x, rel);
+}
+template <class T>
+int bicg(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, const double* tols_host, double tol, int itmax,
+         const int* mask_host, const Reliable* rel) {
+    auto run = [&](int itc, const int* m, const cplx<T>* bb, cplx<T>* xx, const Reliable* rr) -> int {
+        switch (plan_vs<T>(P)) {
+            case 4: return bicg2_v<T, 4>(P, LV, bb, xx, tols_host, tol, itc, m, rr);
+            case 2: return bicg2_v<T, 2>(P, LV, bb, xx, tols_host, tol, itc, m, rr);
+            default: return bicg2_v<T, 1>(P, LV, bb, xx, tols_host, tol, itc, m, rr);
+        }
+    };
+    if (P.o.div_cor == 2 && (rel || std::is_same<T, double>::value))
+        return corrected_cycles<T>(P, LV, b, x, itmax, mask_host, rel, run);
+    return run(itmax, mask_host, b, x, rel);
+}
 template <class T> int precond_vec(Plan& P, const Level& LV, cplx<T>* out, cplx<T>* q) {
     switch (plan_vs<T>(P)) {
         case 4: precond<T, 4, RHS_VEC>(P, LV, out, q, nullptr, nullptr); break;
@@ -612,6 +808,10 @@ template <class T> int apply_op(Plan& P, const Level& LV, const cplx<T>* x, cplx
     template int gpbicg<T>(Plan&, const Level&, const cplx<T>*, cplx<T>*, const double*, double, int, const int*,      \
                            const Reliable*);                                                                            \
     template int cocr<T>(Plan&, const Level&, const cplx<T>*, cplx<T>*, const double*, double, int, const int*,        \
+                         const Reliable*);                                                                              \
+    template int tfqmr<T>(Plan&, const Level&, const cplx<T>*, cplx<T>*, const double*, double, int, const int*,       \
+                          const Reliable*);                                                                             \
+    template int bicg<T>(Plan&, const Level&, const cplx<T>*, cplx<T>*, const double*, double, int, const int*,        \
                          const Reliable*);                                                                              \
     template int precond_vec<T>(Plan&, const Level&, cplx<T>*, cplx<T>*);                                               \
     template int apply_op<T>(Plan&, const Level&, const cplx<T>*, cplx<T>*);

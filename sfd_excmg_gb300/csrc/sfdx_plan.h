@@ -11,6 +11,7 @@
 #include <tuple>
 #include <cstdlib>
 #include <cstring>
+#include <functional>
 #include <type_traits>
 #include <vector>
 
@@ -360,6 +361,12 @@ int gpbicg(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, const double*
 template <class T>
 int cocr(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, const double* tols_host, double tol, int itmax,
          const int* mask_host, const Reliable* rel = nullptr);
+template <class T>
+int tfqmr(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, const double* tols_host, double tol, int itmax,
+          const int* mask_host, const Reliable* rel = nullptr);
+template <class T>
+int bicg(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, const double* tols_host, double tol, int itmax,
+         const int* mask_host, const Reliable* rel = nullptr);
 // out = M^{-1} q (multi-colour SSOR or Jacobi) for all active systems
 template <class T> int precond_vec(Plan& P, const Level& LV, cplx<T>* out, cplx<T>* q);
 // y = A x for all systems (per-system frequencies in P.d_wm)
@@ -372,6 +379,10 @@ int div_correct(Plan& P, const Level& LV, double2* x);
 // per system)
 int solve_level(Plan& P, const Level& LV, double tol, int itmax, bool coarse, std::vector<int>& its,
                 std::vector<int>& status);
+// EXCMG cascade over all levels; rhs(l) writes level l's right-hand side to
+// P.b64; the finest solution is left in P.x64 (its[], status[]: finest level)
+int excmg_cascade(Plan& P, const std::function<int(int)>& rhs, double eps, bool record, std::vector<int>& its,
+                  std::vector<int>& status);
 // ||b - A x|| / ||b|| per system in FP64
 int true_residual(Plan& P, const Level& LV, const double2* b, const double2* x, double* rel, const int* mask);
 

@@ -25,6 +25,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <ctime>
+#include <functional>
 #include <memory>
 #include <thread>
 #include <type_traits>
@@ -207,6 +208,10 @@ static int solve_level_fp64(Plan& P, const Level& LV, double tol, int itmax, std
         RC(gpbicg<double>(P, LV, P.b64.as<double2>(), P.x64.as<double2>(), nullptr, tol, itmax, nullptr));
     else if (P.o.solver == SFDX_SOLVER_COCR)
         RC(cocr<double>(P, LV, P.b64.as<double2>(), P.x64.as<double2>(), nullptr, tol, itmax, nullptr));
+    else if (P.o.solver == SFDX_SOLVER_TFQMR)
+        RC(tfqmr<double>(P, LV, P.b64.as<double2>(), P.x64.as<double2>(), nullptr, tol, itmax, nullptr));
+    else if (P.o.solver == SFDX_SOLVER_BICG)
+        RC(bicg<double>(P, LV, P.b64.as<double2>(), P.x64.as<double2>(), nullptr, tol, itmax, nullptr));
     else
         return SFDX_ERR_UNSUPPORTED;
     its.resize(P.ns);
@@ -281,7 +286,9 @@ static int solve_level_mixed(Plan& P, const Level& LV, double tol, int itmax, st
 
 int solve_level(Plan& P, const Level& LV, double tol, int itmax, bool coarse, std::vector<int>& its,
                 std::vector<int>& status) {
-    if (coarse || P.o.precision == SFDX_FP64) return solve_level_fp64(P, LV, tol, itmax, its, status);
+    // TFQMR and BiCG have no complex64 / reliable-update form: FP64 in every plan
+    if (coarse || P.o.precision == SFDX_FP64 || P.o.solver == SFDX_SOLVER_TFQMR || P.o.solver == SFDX_SOLVER_BICG)
+        return solve_level_fp64(P, LV, tol, itmax, its, status);
     return solve_level_mixed(P, LV, tol, itmax, its, status);
 }
 
@@ -428,6 +435,57 @@ static void log_level(Plan& P, int l, const std::vector<int>& its, const std::ve
             L.nx, L.ny, L.nz, (long long)L.nl, mn, mx, cnt[ST_CONV], cnt[ST_MAXIT], cnt[ST_NAN], cnt[ST_BREAK], ms);
 }
 
+// EXCMG cascade (doublemode_acc, fdfe_main.f90:1258-1563): levels 1 and 2
+// solved tightly in FP64 from zero (u1u2, the PARDISO replacement), then on
+// each finer level the extrapolated guess from the two previous solutions
+// (extint_v) and a solve to eps 10^(l-N+1).  rhs(l) writes level l's
+// right-hand side into P.b64.  record: keep iterations and times in the plan.
+int excmg_cascade(Plan& P, const std::function<int(int)>& rhs, double eps, bool record, std::vector<int>& its,
+                  std::vector<int>& status) {
+    const int ns = P.ns, N = P.nlev;
+    const size_t nfine = (size_t)P.lev[N - 1].nl * ns * sizeof(double2);
+    RC(P.u0.alloc(nfine));
+    RC(P.u1.alloc(nfine));
+    RC(P.ut.alloc(nfine));
+    double tol = eps * std::pow(10.0, -N + 1);
+    for (int l = 0; l < 2; l++) {
+        const double t0 = now_ms();
+        const Level& L = P.lev[l];
+        RC(rhs(l));
+        CK(cudaMemsetAsync(P.x64.p, 0, (size_t)L.nl * ns * sizeof(double2), P.st));
+        RC(solve_level(P, L, P.o.coarse_tol, P.o.coarse_maxit, true, its, status));
+        double2* dst = l == 0 ? P.u0.as<double2>() : P.u1.as<double2>();
+        CK(cudaMemcpyAsync(dst, P.x64.p, (size_t)L.nl * ns * sizeof(double2), cudaMemcpyDeviceToDevice, P.st));
+        CK(cudaStreamSynchronize(P.st));
+        if (record) {
+            record_iters(P, l, its);
+            P.level_ms[l] = now_ms() - t0;
+            log_level(P, l, its, status, P.level_ms[l]);
+        }
+    }
+    tol = tol * 10;
+    for (int l = 2; l < N; l++) {
+        tol = tol * 10;
+        const double t0 = now_ms();
+        const Level& L = P.lev[l];
+        RC(prolongate(P, l, P.u0.as<double2>(), P.u1.as<double2>(), P.x64.as<double2>()));
+        RC(rhs(l));
+        RC(solve_level(P, L, tol, P.o.maxit_level, false, its, status));
+        CK(cudaStreamSynchronize(P.st));
+        if (record) {
+            record_iters(P, l, its);
+            P.level_ms[l] = now_ms() - t0;
+            log_level(P, l, its, status, P.level_ms[l]);
+        }
+        if (l < N - 1) {
+            std::swap(P.u0.p, P.u1.p);
+            std::swap(P.u0.bytes, P.u1.bytes);
+            CK(cudaMemcpyAsync(P.u1.p, P.x64.p, (size_t)L.nl * ns * sizeof(double2), cudaMemcpyDeviceToDevice, P.st));
+        }
+    }
+    return SFDX_OK;
+}
+
 static int plan_solve(Plan& P) {
     const int ns = P.ns;
     const Level& F = P.lev[P.nlev - 1];
@@ -454,46 +512,12 @@ static int plan_solve(Plan& P) {
         P.level_ms[0] = now_ms() - t0;
         log_level(P, 0, its, status, P.level_ms[0]);
     } else {
-        const int N = P.nlev;
-        RC(P.u0.alloc(nfine));
-        RC(P.u1.alloc(nfine));
-        RC(P.ut.alloc(nfine));
-        double tol = P.o.eps * std::pow(10.0, -N + 1);
-        // levels 1 and 2: tight FP64 solve in place of PARDISO (u1u2)
-        for (int l = 0; l < 2; l++) {
-            double t0 = now_ms();
-            const Level& L = P.lev[l];
-            RC(level_column(P, L, col));
-            RC(level_rhs(P, L, col));
-            CK(cudaMemsetAsync(P.x64.p, 0, (size_t)L.nl * ns * sizeof(double2), P.st));
-            RC(solve_level(P, L, P.o.coarse_tol, P.o.coarse_maxit, true, its, status));
-            record_iters(P, l, its);
-            double2* dst = l == 0 ? P.u0.as<double2>() : P.u1.as<double2>();
-            CK(cudaMemcpyAsync(dst, P.x64.p, (size_t)L.nl * ns * sizeof(double2), cudaMemcpyDeviceToDevice, P.st));
-            CK(cudaStreamSynchronize(P.st));
-            P.level_ms[l] = now_ms() - t0;
-            log_level(P, l, its, status, P.level_ms[l]);
-        }
-        tol = tol * 10;
-        for (int l = 2; l < N; l++) {
-            tol = tol * 10;
-            double t0 = now_ms();
-            const Level& L = P.lev[l];
-            RC(prolongate(P, l, P.u0.as<double2>(), P.u1.as<double2>(), P.x64.as<double2>()));
-            RC(level_column(P, L, col));
-            RC(level_rhs(P, L, col));
-            RC(solve_level(P, L, tol, P.o.maxit_level, false, its, status));
-            record_iters(P, l, its);
-            CK(cudaStreamSynchronize(P.st));
-            P.level_ms[l] = now_ms() - t0;
-            log_level(P, l, its, status, P.level_ms[l]);
-            if (l == N - 1) rc_conv = status_to_rc(status);
-            else {
-                std::swap(P.u0.p, P.u1.p);
-                std::swap(P.u0.bytes, P.u1.bytes);
-                CK(cudaMemcpyAsync(P.u1.p, P.x64.p, (size_t)L.nl * ns * sizeof(double2), cudaMemcpyDeviceToDevice, P.st));
-            }
-        }
+        auto rhs = [&](int l) -> int {
+            RC(level_column(P, P.lev[l], col));
+            return level_rhs(P, P.lev[l], col);
+        };
+        RC(excmg_cascade(P, rhs, P.o.eps, true, its, status));
+        rc_conv = status_to_rc(status);
     }
     RC(true_residual(P, F, P.b64.as<double2>(), P.x64.as<double2>(), P.relres.data(), nullptr));
     // de-interleave into [nf][2][nl] (system-major)
@@ -571,6 +595,7 @@ static int validate_opts(const sfdx_opts& o) {
         o.solver != SFDX_SOLVER_BICG && o.solver != SFDX_SOLVER_COCR)
         return SFDX_ERR_ARG;
     if (o.eps <= 0 || o.maxit_plain <= 0 || o.maxit_level <= 0) return SFDX_ERR_ARG;
+    if (o.batch != 0) return SFDX_ERR_UNSUPPORTED;
     return SFDX_OK;
 }
 

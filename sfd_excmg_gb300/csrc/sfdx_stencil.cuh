@@ -179,58 +179,9 @@ template <class T, int VS> __device__ __forceinline__ void cvzero(CV<T, VS>& a) 
 #pragma unroll
     for (int q = 0; q < VS; q++) a.v[q] = mk<T>(T(0), T(0));
 }
-// 256-bit accesses (sm_100 and later): one instruction moves the 32 bytes of
-// four complex64 or two complex128 values, so a warp touches each 128-byte
-// line of its edges once per instruction instead of twice.  Used only when the
-// address is 32-byte aligned (checked at run time; 16-byte accesses otherwise).
-__device__ __forceinline__ bool al32(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 31) == 0; }
-__device__ __forceinline__ void ld256_nc(const void* p, float4& a, float4& b) {
-    asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-        : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
-        : "l"(p));
-}
-__device__ __forceinline__ void ld256(const void* p, float4& a, float4& b) {
-    asm volatile("ld.global.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-                 : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
-                 : "l"(p)
-                 : "memory");
-}
-__device__ __forceinline__ void st256(void* p, const float4& a, const float4& b) {
-    asm volatile("st.global.v8.f32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"l"(p), "f"(a.x), "f"(a.y), "f"(a.z),
-                 "f"(a.w), "f"(b.x), "f"(b.y), "f"(b.z), "f"(b.w)
-                 : "memory");
-}
-__device__ __forceinline__ void ld256_nc(const void* p, double2& a, double2& b) {
-    asm("ld.global.nc.v4.f64 {%0,%1,%2,%3}, [%4];" : "=d"(a.x), "=d"(a.y), "=d"(b.x), "=d"(b.y) : "l"(p));
-}
-__device__ __forceinline__ void ld256(const void* p, double2& a, double2& b) {
-    asm volatile("ld.global.v4.f64 {%0,%1,%2,%3}, [%4];" : "=d"(a.x), "=d"(a.y), "=d"(b.x), "=d"(b.y) : "l"(p) : "memory");
-}
-__device__ __forceinline__ void st256(void* p, const double2& a, const double2& b) {
-    asm volatile("st.global.v4.f64 [%0], {%1,%2,%3,%4};" ::"l"(p), "d"(a.x), "d"(a.y), "d"(b.x), "d"(b.y) : "memory");
-}
-
 // read-only (non-coherent) vector load of VS consecutive complex values
 template <class T, int VS> __device__ __forceinline__ void cvld(CV<T, VS>& a, const cplx<T>* p) {
-    if (sizeof(T) == 4 && VS % 4 == 0 && al32(p)) {
-#pragma unroll
-        for (int h = 0; h < VS / 4; h++) {
-            float4 f, g;
-            ld256_nc(p + 4 * h, f, g);
-            a.v[4 * h] = mk<T>((T)f.x, (T)f.y);
-            a.v[4 * h + 1] = mk<T>((T)f.z, (T)f.w);
-            a.v[4 * h + 2] = mk<T>((T)g.x, (T)g.y);
-            a.v[4 * h + 3] = mk<T>((T)g.z, (T)g.w);
-        }
-    } else if (sizeof(T) == 8 && VS % 2 == 0 && al32(p)) {
-#pragma unroll
-        for (int h = 0; h < VS / 2; h++) {
-            double2 f, g;
-            ld256_nc(p + 2 * h, f, g);
-            a.v[2 * h] = mk<T>((T)f.x, (T)f.y);
-            a.v[2 * h + 1] = mk<T>((T)g.x, (T)g.y);
-        }
-    } else if (sizeof(T) == 4 && VS % 2 == 0) {
+    if (sizeof(T) == 4 && VS % 2 == 0) {
         const float4* q = reinterpret_cast<const float4*>(p);
 #pragma unroll
         for (int h = 0; h < VS / 2; h++) {
@@ -245,25 +196,7 @@ template <class T, int VS> __device__ __forceinline__ void cvld(CV<T, VS>& a, co
 }
 // coherent load (arrays written by the same kernel)
 template <class T, int VS> __device__ __forceinline__ void cvldw(CV<T, VS>& a, const cplx<T>* p) {
-    if (sizeof(T) == 4 && VS % 4 == 0 && al32(p)) {
-#pragma unroll
-        for (int h = 0; h < VS / 4; h++) {
-            float4 f, g;
-            ld256(p + 4 * h, f, g);
-            a.v[4 * h] = mk<T>((T)f.x, (T)f.y);
-            a.v[4 * h + 1] = mk<T>((T)f.z, (T)f.w);
-            a.v[4 * h + 2] = mk<T>((T)g.x, (T)g.y);
-            a.v[4 * h + 3] = mk<T>((T)g.z, (T)g.w);
-        }
-    } else if (sizeof(T) == 8 && VS % 2 == 0 && al32(p)) {
-#pragma unroll
-        for (int h = 0; h < VS / 2; h++) {
-            double2 f, g;
-            ld256(p + 2 * h, f, g);
-            a.v[2 * h] = mk<T>((T)f.x, (T)f.y);
-            a.v[2 * h + 1] = mk<T>((T)g.x, (T)g.y);
-        }
-    } else if (sizeof(T) == 4 && VS % 2 == 0) {
+    if (sizeof(T) == 4 && VS % 2 == 0) {
         const float4* q = reinterpret_cast<const float4*>(p);
 #pragma unroll
         for (int h = 0; h < VS / 2; h++) {
@@ -277,19 +210,7 @@ template <class T, int VS> __device__ __forceinline__ void cvldw(CV<T, VS>& a, c
     }
 }
 template <class T, int VS> __device__ __forceinline__ void cvst(cplx<T>* p, const CV<T, VS>& a) {
-    if (sizeof(T) == 4 && VS % 4 == 0 && al32(p)) {
-#pragma unroll
-        for (int h = 0; h < VS / 4; h++)
-            st256(p + 4 * h,
-                  make_float4((float)a.v[4 * h].x, (float)a.v[4 * h].y, (float)a.v[4 * h + 1].x, (float)a.v[4 * h + 1].y),
-                  make_float4((float)a.v[4 * h + 2].x, (float)a.v[4 * h + 2].y, (float)a.v[4 * h + 3].x,
-                              (float)a.v[4 * h + 3].y));
-    } else if (sizeof(T) == 8 && VS % 2 == 0 && al32(p)) {
-#pragma unroll
-        for (int h = 0; h < VS / 2; h++)
-            st256(p + 2 * h, make_double2((double)a.v[2 * h].x, (double)a.v[2 * h].y),
-                  make_double2((double)a.v[2 * h + 1].x, (double)a.v[2 * h + 1].y));
-    } else if (sizeof(T) == 4 && VS % 2 == 0) {
+    if (sizeof(T) == 4 && VS % 2 == 0) {
         float4* q = reinterpret_cast<float4*>(p);
 #pragma unroll
         for (int h = 0; h < VS / 2; h++)
