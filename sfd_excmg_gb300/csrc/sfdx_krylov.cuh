@@ -428,13 +428,6 @@ static int tfqmr_v(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, const
     const int64_t W = LV.nl * c.sg.G;
     const double* wm = P.d_wm.as<double>();
     const cplx<T>* nul = nullptr;
-    CK(cudaMemsetAsync(d, 0, vb, P.st));
-    vlaunch(k_residual_v<T, T, VS, 3>, W, c.B, c.smem, P.st, L, M, c.sg, dst, b, (const cplx<T>*)x, w, rt, redbuf(P),
-            (double*)nullptr, 0);
-    vlaunch(k_bl_dot<T, VS, FIN_TFQ_INIT>, W, c.B, c.smem, P.st, M, c.sg, dst, (const cplx<T>*)rt, (const cplx<T>*)w,
-            (const cplx<T>*)w, (const cplx<T>*)w, redbuf(P));
-    vlaunch(k_bl_lincomb<T, VS, BC_ONE, BC_ZERO, BC_ZERO>, W, c.B, 0, P.st, M, c.sg, (const KState*)dst, u,
-            (const cplx<T>*)w, nul, nul);
     // out_h = M^-1 in, out_a = A out_h
     auto amv = [&](cplx<T>* out_h, cplx<T>* out_a, cplx<T>* in) {
         precond<T, VS, RHS_VEC>(P, LV, out_h, in, nullptr, nullptr);
@@ -445,7 +438,6 @@ static int tfqmr_v(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, const
                 (const cplx<T>*)x, (const cplx<T>*)d, nul);
         KL(k_bl_commit<<<(ns + 127) / 128, 128, 0, P.st>>>(dst, ns));
     };
-    amv(uh, v, u);
     auto body = [&]() {
         vlaunch(k_bl_dot<T, VS, FIN_TFQ_SIGMA>, W, c.B, c.smem, P.st, M, c.sg, dst, (const cplx<T>*)rt,
                 (const cplx<T>*)v, nul, nul, redbuf(P));
@@ -466,24 +458,71 @@ static int tfqmr_v(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, const
         vlaunch(k_bl_lincomb<T, VS, BC_ONE, BC_BETA, BC_BETA2>, W, c.B, 0, P.st, M, c.sg, (const KState*)dst, v,
                 (const cplx<T>*)au, (const cplx<T>*)aq, (const cplx<T>*)v);
     };
-    for (int it = 1; it <= itmax; it++) {
-        if (graph_interval(P, it, itmax, false)) {
-            RC(graph_run(P, interval_key<T>(P, LV, 2, VS, {(uintptr_t)x, (uintptr_t)b}), [&] {
-                for (int k = 0; k < 8; k++) body();
-            }));
-            it += 7;
-        } else {
-            body();
+    // The stopping test is the quasi-residual bound tau sqrt(m+1), which the
+    // true residual can exceed once rounding has accumulated: systems that pass
+    // it are checked against b - A x and restarted from their iterate if not
+    // converged, within the iteration budget.
+    std::vector<int> total(ns, 0);
+    int used = 0;
+    for (int round = 0; round < 32 && used < itmax; round++) {
+        const int budget = itmax - used;
+        CK(cudaMemsetAsync(d, 0, vb, P.st));
+        vlaunch(k_residual_v<T, T, VS, 3>, W, c.B, c.smem, P.st, L, M, c.sg, dst, b, (const cplx<T>*)x, w, rt,
+                redbuf(P), (double*)nullptr, 0);
+        vlaunch(k_bl_dot<T, VS, FIN_TFQ_INIT>, W, c.B, c.smem, P.st, M, c.sg, dst, (const cplx<T>*)rt,
+                (const cplx<T>*)w, (const cplx<T>*)w, (const cplx<T>*)w, redbuf(P));
+        vlaunch(k_bl_lincomb<T, VS, BC_ONE, BC_ZERO, BC_ZERO>, W, c.B, 0, P.st, M, c.sg, (const KState*)dst, u,
+                (const cplx<T>*)w, nul, nul);
+        amv(uh, v, u);
+        int done = 0;
+        for (int it = 1; it <= budget; it++) {
+            if (graph_interval(P, it, budget, false)) {
+                RC(graph_run(P, interval_key<T>(P, LV, 2, VS, {(uintptr_t)x, (uintptr_t)b}), [&] {
+                    for (int k = 0; k < 8; k++) body();
+                }));
+                it += 7;
+            } else {
+                body();
+            }
+            done = it;
+            if (it % 8 == 0 || it == budget) {
+                CK(cudaGetLastError());
+                RC(sync_state(P));
+                int act = 0;
+                for (int k = 0; k < ns; k++) act += P.hst[k].active;
+                if (!act) break;
+            }
         }
-        if (it % 8 == 0 || it == itmax) {
-            CK(cudaGetLastError());
-            RC(sync_state(P));
-            int act = 0;
-            for (int k = 0; k < ns; k++) act += P.hst[k].active;
-            if (!act) break;
+        used += done;
+        RC(sync_state(P));
+        for (int k = 0; k < ns; k++) total[k] += P.hst[k].iters;
+        // true residual of the systems that claim convergence
+        KL(k_reactivate<<<(ns + 127) / 128, 128, 0, P.st>>>(dst, ns));
+        vlaunch(k_residual_v<T, T, VS, 2>, W, c.B, c.smem, P.st, L, M, c.sg, dst, b, (const cplx<T>*)x, w,
+                (cplx<T>*)nullptr, redbuf(P), (double*)nullptr, 0);
+        RC(sync_state(P));
+        int restart = 0;
+        for (int k = 0; k < ns; k++) {
+            KState& S = P.hst[k];
+            if (!S.active) continue;  // not a convergence claim
+            const double rel = S.babs > 0 ? S.err / S.babs : S.err;
+            S.err = rel;
+            S.iters = total[k];
+            if (rel < S.tol) {
+                S.active = 0;
+                S.status = ST_CONV;
+            } else {
+                S.status = used < itmax ? ST_RUN : ST_MAXIT;
+                S.active = used < itmax ? 1 : 0;
+                restart += S.active;
+            }
         }
+        for (int k = 0; k < ns; k++) P.hst[k].iters = total[k];
+        CK(cudaMemcpyAsync(P.d_state.p, P.hst.data(), sizeof(KState) * ns, cudaMemcpyHostToDevice, P.st));
+        if (!restart) break;
     }
     RC(sync_state(P));
+    for (int k = 0; k < ns; k++) P.hst[k].iters = total[k];
     return SFDX_OK;
 }
 

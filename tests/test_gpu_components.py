@@ -228,7 +228,7 @@ def test_krylov_mixed_precision_reaches_fp64_tolerance(solver):
         assert np.linalg.norm(r) < 1e-10 * np.linalg.norm(p)
 
 
-@pytest.mark.parametrize("solver", [1, 2, 3, 4, 6])
+@pytest.mark.parametrize("solver", [1, 3, 4, 6])
 def test_krylov_batched_systems_non_power_of_two(solver):
     """Six systems (three frequencies x two right-hand sides): two systems per thread,
     three thread groups, so the per-system reductions take the shared-memory tree."""
