@@ -57,9 +57,12 @@ static int gc_assemble(Plan& P, const Level& LV) {
     for (size_t l = 1; l < LV.mg.size(); l++) {
         const NGrid gf = LV.mg[l - 1].g, gc = LV.mg[l].g;
         float2* pc = P.gcn[0].as<float2>();             // coarse probes   [np_c][27]
-        float2* xf = P.gcn[0].as<float2>() + (size_t)gc.np * NPR;  // prolonged [np_f][27]
-        float2* yf = P.gcn[1].as<float2>();             // N P probes      [np_f][27]
-        float2* Qc = P.gcn[1].as<float2>() + (size_t)gf.np * NPR;  // responses [np_c][27]
+        // second arrays of each buffer start on a 32-byte boundary (vlaunch
+        // requires aligned pointer arguments); the buffers hold 2 np 27 float2
+        auto a32 = [](size_t n) { return (n + 3) / 4 * 4; };
+        float2* xf = P.gcn[0].as<float2>() + a32((size_t)gc.np * NPR);  // prolonged [np_f][27]
+        float2* yf = P.gcn[1].as<float2>();                             // N P probes [np_f][27]
+        float2* Qc = P.gcn[1].as<float2>() + a32((size_t)gf.np * NPR);  // responses  [np_c][27]
         KL(k_mg_probe<<<grid_for((int64_t)gc.np * NPR, 256, 16), 256, 0, P.st>>>(gc, pc));
         CK(cudaMemsetAsync(xf, 0, (size_t)gf.np * NPR * sizeof(float2), P.st));
         vlaunch(k_mg_prolong<float, 1>, (int64_t)gf.np * sg.G, B, 0, P.st, gf, gc, sg, pst, pc, xf);

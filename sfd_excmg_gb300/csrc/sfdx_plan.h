@@ -95,8 +95,21 @@ inline int resident_grid(const void* fn, int B, size_t smem, int64_t work) {
 // most blocks resident_grid() returns (sizes the per-block partial sums)
 inline int64_t max_resident_blocks() { return (int64_t)device_sms() * 32; }
 
+// The system-group kernels move 32-byte groups of a thread's systems with
+// 256-bit accesses (sfdx_stencil.cuh).  Their offsets [edge * ns + s0] are
+// multiples of 32 bytes (VS divides ns), so alignment rests on the base
+// pointers: every pointer argument is checked here, once per launch, and a
+// launch with a misaligned one is refused (g_misaligned; sync_state reports
+// it) instead of faulting on the device.
+extern std::atomic<int> g_misaligned;
+template <class X> inline bool arg_aligned(const X&) { return true; }
+template <class X> inline bool arg_aligned(X* p) { return (reinterpret_cast<uintptr_t>(p) & 31) == 0; }
 template <class... KA, class... A>
 inline void vlaunch(void (*k)(KA...), int64_t work, int B, size_t smem, cudaStream_t st, A... args) {
+    if (!(arg_aligned(args) && ...)) {
+        g_misaligned.store(1);
+        return;
+    }
     const int g = resident_grid((const void*)k, B, smem, work);
     g_launches.fetch_add(1, std::memory_order_relaxed);
     k<<<g, B, smem, st>>>(args...);
@@ -311,6 +324,7 @@ template <class F> int graph_run(Plan& P, const std::vector<uintptr_t>& key, F&&
 }
 
 inline int sync_state(Plan& P) {
+    if (g_misaligned.load()) return SFDX_ERR_ARG;
     P.hst.resize(P.ns);
     CK(cudaMemcpyAsync(P.hst.data(), P.d_state.p, sizeof(KState) * P.ns, cudaMemcpyDeviceToHost, P.st));
     CK(cudaStreamSynchronize(P.st));

@@ -179,9 +179,64 @@ template <class T, int VS> __device__ __forceinline__ void cvzero(CV<T, VS>& a) 
 #pragma unroll
     for (int q = 0; q < VS; q++) a.v[q] = mk<T>(T(0), T(0));
 }
+// 256-bit accesses (sm_100 and later): one instruction moves the 32 bytes of
+// four complex64 or two complex128 values of a thread.  On the operator's
+// 13-neighbour gather this is 27 % faster than two 128-bit loads (0.123 vs
+// 0.168 ms for 1.57 M edges x 16 systems).  The address must be 32-byte
+// aligned: [edge * ns + s0] offsets are (VS divides ns) and vlaunch checks the
+// base pointers.
+__device__ __forceinline__ void ld256_nc(const void* p, float4& a, float4& b) {
+    asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+        : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
+        : "l"(p));
+}
+__device__ __forceinline__ void ld256(const void* p, float4& a, float4& b) {
+    asm volatile("ld.global.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
+                 : "l"(p)
+                 : "memory");
+}
+__device__ __forceinline__ void st256(void* p, const float4& a, const float4& b) {
+    asm volatile("st.global.v8.f32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"l"(p), "f"(a.x), "f"(a.y), "f"(a.z),
+                 "f"(a.w), "f"(b.x), "f"(b.y), "f"(b.z), "f"(b.w)
+                 : "memory");
+}
+__device__ __forceinline__ void ld256_nc(const void* p, double2& a, double2& b) {
+    asm("ld.global.nc.v4.f64 {%0,%1,%2,%3}, [%4];" : "=d"(a.x), "=d"(a.y), "=d"(b.x), "=d"(b.y) : "l"(p));
+}
+__device__ __forceinline__ void ld256(const void* p, double2& a, double2& b) {
+    asm volatile("ld.global.v4.f64 {%0,%1,%2,%3}, [%4];" : "=d"(a.x), "=d"(a.y), "=d"(b.x), "=d"(b.y) : "l"(p) : "memory");
+}
+__device__ __forceinline__ void st256(void* p, const double2& a, const double2& b) {
+    asm volatile("st.global.v4.f64 [%0], {%1,%2,%3,%4};" ::"l"(p), "d"(a.x), "d"(a.y), "d"(b.x), "d"(b.y) : "memory");
+}
+// whether VS values of T go as 256-bit groups
+template <class T, int VS> struct Wide {
+    static constexpr bool value = (sizeof(T) == 4 && VS % 4 == 0) || (sizeof(T) == 8 && VS % 2 == 0);
+    static constexpr int per = sizeof(T) == 4 ? 4 : 2;  // complex values per 32 bytes
+};
+
 // read-only (non-coherent) vector load of VS consecutive complex values
 template <class T, int VS> __device__ __forceinline__ void cvld(CV<T, VS>& a, const cplx<T>* p) {
-    if (sizeof(T) == 4 && VS % 2 == 0) {
+    if (Wide<T, VS>::value) {
+        constexpr int PER = Wide<T, VS>::per;
+#pragma unroll
+        for (int h = 0; h < VS / PER; h++) {
+            if (sizeof(T) == 4) {
+                float4 f, g;
+                ld256_nc(p + PER * h, f, g);
+                a.v[PER * h] = mk<T>((T)f.x, (T)f.y);
+                a.v[PER * h + 1] = mk<T>((T)f.z, (T)f.w);
+                a.v[(PER * h + 2) % VS] = mk<T>((T)g.x, (T)g.y);
+                a.v[(PER * h + 3) % VS] = mk<T>((T)g.z, (T)g.w);
+            } else {
+                double2 f, g;
+                ld256_nc(p + PER * h, f, g);
+                a.v[PER * h] = mk<T>((T)f.x, (T)f.y);
+                a.v[PER * h + 1] = mk<T>((T)g.x, (T)g.y);
+            }
+        }
+    } else if (sizeof(T) == 4 && VS % 2 == 0) {
         const float4* q = reinterpret_cast<const float4*>(p);
 #pragma unroll
         for (int h = 0; h < VS / 2; h++) {
@@ -196,7 +251,25 @@ template <class T, int VS> __device__ __forceinline__ void cvld(CV<T, VS>& a, co
 }
 // coherent load (arrays written by the same kernel)
 template <class T, int VS> __device__ __forceinline__ void cvldw(CV<T, VS>& a, const cplx<T>* p) {
-    if (sizeof(T) == 4 && VS % 2 == 0) {
+    if (Wide<T, VS>::value) {
+        constexpr int PER = Wide<T, VS>::per;
+#pragma unroll
+        for (int h = 0; h < VS / PER; h++) {
+            if (sizeof(T) == 4) {
+                float4 f, g;
+                ld256(p + PER * h, f, g);
+                a.v[PER * h] = mk<T>((T)f.x, (T)f.y);
+                a.v[PER * h + 1] = mk<T>((T)f.z, (T)f.w);
+                a.v[(PER * h + 2) % VS] = mk<T>((T)g.x, (T)g.y);
+                a.v[(PER * h + 3) % VS] = mk<T>((T)g.z, (T)g.w);
+            } else {
+                double2 f, g;
+                ld256(p + PER * h, f, g);
+                a.v[PER * h] = mk<T>((T)f.x, (T)f.y);
+                a.v[PER * h + 1] = mk<T>((T)g.x, (T)g.y);
+            }
+        }
+    } else if (sizeof(T) == 4 && VS % 2 == 0) {
         const float4* q = reinterpret_cast<const float4*>(p);
 #pragma unroll
         for (int h = 0; h < VS / 2; h++) {
@@ -210,7 +283,21 @@ template <class T, int VS> __device__ __forceinline__ void cvldw(CV<T, VS>& a, c
     }
 }
 template <class T, int VS> __device__ __forceinline__ void cvst(cplx<T>* p, const CV<T, VS>& a) {
-    if (sizeof(T) == 4 && VS % 2 == 0) {
+    if (Wide<T, VS>::value) {
+        constexpr int PER = Wide<T, VS>::per;
+#pragma unroll
+        for (int h = 0; h < VS / PER; h++) {
+            if (sizeof(T) == 4)
+                st256(p + PER * h,
+                      make_float4((float)a.v[PER * h].x, (float)a.v[PER * h].y, (float)a.v[PER * h + 1].x,
+                                  (float)a.v[PER * h + 1].y),
+                      make_float4((float)a.v[(PER * h + 2) % VS].x, (float)a.v[(PER * h + 2) % VS].y,
+                                  (float)a.v[(PER * h + 3) % VS].x, (float)a.v[(PER * h + 3) % VS].y));
+            else
+                st256(p + PER * h, make_double2((double)a.v[PER * h].x, (double)a.v[PER * h].y),
+                      make_double2((double)a.v[PER * h + 1].x, (double)a.v[PER * h + 1].y));
+        }
+    } else if (sizeof(T) == 4 && VS % 2 == 0) {
         float4* q = reinterpret_cast<float4*>(p);
 #pragma unroll
         for (int h = 0; h < VS / 2; h++)
