@@ -305,6 +305,13 @@ int sfdx_residual_noalloc(int nx, int ny, int nz, const double* a, const double*
 int sfdx_read_sizes(const char* model_name, int* nx, int* ny, int* nz, int* nair, int* nf, int* nrec);
 int sfdx_read_model(const char* model_name, const sfdx_opts* o, int* level, double* eps, int* solver, int* out_type,
                     double* a, double* b, double* c, double* sigma, double* freq, double* recv, int* abu);
+/* Convergence-history file of one solve, as Bicg_stab_p / pgpbicg write it with
+ * output_ccv (solvers.f90:687-704): <model>_<freq e9.2>_<polar>_<tag>.ccv with
+ * the iteration count, then each non-zero entry of history[n] in e9.2.  polar
+ * "xy" or "yx"; tag the solver name, or "excmg" for EXCMG runs.  The history
+ * comes from sfdx_krylov_solve. */
+int sfdx_write_ccv(const char* model_name, double freq, const char* polar, const char* tag, int iters,
+                   const double* history, int n);
 int sfdx_write_res(const char* model_name, int nf, const double* freq, int nrec, const double* recv,
                    const double* out);
 

@@ -132,6 +132,8 @@ _PROTO = {
     "sfdx_read_model": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_void_p, c_int_p, c_double_p, c_int_p, c_int_p,
                                        c_double_p, c_double_p, c_double_p, c_double_p, c_double_p, c_double_p,
                                        c_int_p]),
+    "sfdx_write_ccv": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_double, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int,
+                                      c_double_p, ctypes.c_int]),
     "sfdx_write_res": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, c_double_p, ctypes.c_int, c_double_p,
                                       c_double_p]),
 }

@@ -561,17 +561,25 @@ extern "C" int sfdx_read_model(const char* name, const sfdx_opts* o, int* level,
 
 // output_data (file_opt.f90:131-158): format 4(e12.5,2x),i1,2x,4(e12.5,2x).
 // The reference prints an unset loop variable in the i1 field; 0 is written.
-static void fortran_e12_5(char* buf, double v) {
-    // Fortran Ew.d: 0.ddddde+xx  (buf holds 32 chars)
-    if (v == 0) { snprintf(buf, 32, " 0.00000E+00"); return; }
-    int ex = (int)std::floor(std::log10(std::fabs(v))) + 1;
-    double m = v / std::pow(10.0, ex);
-    if (std::fabs(m) >= 0.999995) { m /= 10; ex += 1; }
-    if (std::fabs(m) < 0.1) { m *= 10; ex -= 1; }
-    char mant[16];
-    snprintf(mant, sizeof mant, "%.5f", std::fabs(m));
-    snprintf(buf, 32, "%s%s%c%c%02d", v < 0 ? "-" : " ", mant, 'E', ex < 0 ? '-' : '+', std::abs(ex) % 100);
+// Fortran Ew.d edit descriptor: [-]0.d...dE[+-]xx, right-justified in w columns
+static void fortran_e(char* buf, size_t cap, int w, int d, double v) {
+    char body[64];
+    if (v == 0) {
+        snprintf(body, sizeof body, "0.%0*dE+00", d, 0);
+    } else {
+        int ex = (int)std::floor(std::log10(std::fabs(v))) + 1;
+        double m = std::fabs(v) / std::pow(10.0, ex);
+        if (m < 0.1) { m *= 10; ex -= 1; }
+        if (m >= 1.0) { m /= 10; ex += 1; }
+        const double top = 1.0 - 0.5 * std::pow(10.0, -d);  // would print as 1.0...
+        if (m >= top) { m /= 10; ex += 1; }
+        char mant[32];
+        snprintf(mant, sizeof mant, "%.*f", d, m);
+        snprintf(body, sizeof body, "%s%sE%c%02d", v < 0 ? "-" : "", mant, ex < 0 ? '-' : '+', std::abs(ex) % 100);
+    }
+    snprintf(buf, cap, "%*s", w, body);
 }
+static void fortran_e12_5(char* buf, double v) { fortran_e(buf, 32, 12, 5, v); }
 
 extern "C" int sfdx_write_res(const char* name, int nf, const double* freq, int nrec, const double* recv,
                               const double* out) {
@@ -589,6 +597,30 @@ extern "C" int sfdx_write_res(const char* name, int nf, const double* freq, int 
                 fprintf(f, "%s  ", b);
             }
             fprintf(f, "\n");
+        }
+    fclose(f);
+    return SFDX_OK;
+}
+
+// Convergence history file of one solve (Bicg_stab_p / pgpbicg with
+// output_ccv, solvers.f90:687-704, :289-305): named
+// <model>_<freq as e9.2>_<polar>_<tag>.ccv, the iteration count on the first
+// line, then every non-zero relative residual as e9.2.
+extern "C" int sfdx_write_ccv(const char* name, double freq, const char* polar, const char* tag, int iters,
+                              const double* history, int n) {
+    if (!name || !polar || !tag || (n > 0 && !history) || n < 0) return SFDX_ERR_ARG;
+    char fb[32];
+    fortran_e(fb, sizeof fb, 9, 2, freq);
+    const char* ft = fb;
+    while (*ft == ' ') ft++;
+    FILE* f = fopen((std::string(name) + "_" + ft + "_" + polar + "_" + tag + ".ccv").c_str(), "w");
+    if (!f) return SFDX_ERR_IO;
+    fprintf(f, "%12d\n", iters);
+    char b[32];
+    for (int j = 0; j < n; j++)
+        if (history[j] != 0) {
+            fortran_e(b, sizeof b, 9, 2, history[j]);
+            fprintf(f, "%s\n", b);
         }
     fclose(f);
     return SFDX_OK;

@@ -339,6 +339,22 @@ def krylov_solve(nx, ny, nz, a, b, c, sigma, freqs, rhs, x0=None, tol=1e-8, itma
     return out + (hist,) if history else out
 
 
+def write_res(name: str, freqs, recv, res) -> None:
+    """output_data (file_opt.f90:131-158): <name>.res from results[nf, nrec, 4]."""
+    f = _d(np.atleast_1d(freqs))
+    rv = _d(np.asarray(recv).T)
+    r = _d(res)
+    capi.check(capi.lib().sfdx_write_res(name.encode(), len(f), capi.dptr(f), rv.shape[1], capi.dptr(rv),
+                                         capi.dptr(r)), "sfdx_write_res")
+
+
+def write_ccv(name: str, freq: float, polar: str, tag: str, iters: int, history) -> None:
+    """Convergence-history file of one solve (solvers.f90:687-704), history from krylov_solve."""
+    h = _d(np.ravel(history))
+    capi.check(capi.lib().sfdx_write_ccv(name.encode(), float(freq), polar.encode(), tag.encode(), int(iters),
+                                         capi.dptr(h), h.size), "sfdx_write_ccv")
+
+
 def grad_correct(nx, ny, nz, a, b, c, sigma, freqs, rhs, x, tol=1e-8, maxit=2000):
     """Consistent gradient-space correction of x (sfdx_grad_correct): returns
     (x + G phi, nodal PCG iterations)."""

@@ -90,3 +90,17 @@ def test_reader_rejects_bad_level(tmp_path):
         assert e.code == 1
     else:
         raise AssertionError("level < 3 must be rejected (file_opt.f90:22-25)")
+
+
+def test_ccv_and_res_files_use_the_reference_layout(tmp_path):
+    """sfdx_write_ccv / sfdx_write_res: names and Fortran list-directed / Ew.d fields as
+    solvers.f90:687-704 and file_opt.f90:131-158 write them."""
+    import sfd_excmg_gb300 as S
+    base = str(tmp_path / "m")
+    S.write_ccv(base, 0.5, "xy", "excmg", 3, [1.0, 1.234e-3, 0.0, 9.996e-11])
+    lines = open(base + "_0.50E+00_xy_excmg.ccv").read().splitlines()
+    assert lines == ["           3", " 0.10E+01", " 0.12E-02", " 0.10E-09"]
+    S.write_res(base, [10.0], np.array([[1.5, -2.0, 0.0]]), np.array([[[1.0, -0.25, 3.0e-4, 0.0]]]))
+    fields = open(base + ".res").read().split()
+    assert fields == ["0.15000E+01", "-0.20000E+01", "0.00000E+00", "0.10000E+02", "0", "0.10000E+01",
+                      "-0.25000E+00", "0.30000E-03", "0.00000E+00"]
