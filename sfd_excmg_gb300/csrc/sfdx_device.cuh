@@ -73,6 +73,7 @@ template <class T> struct Lev {
     AxisT<T> ax, ay, az;
     const T* sig;  // [6][ncell]
     int aniso;     // 1 if any off-diagonal conductivity is non-zero
+    const T* rc;   // per-row coefficients [nl][12] (sfdx_stencil.cuh row_k_e), or null
 };
 
 // ---------------------------------------------------------------- edges

@@ -83,7 +83,8 @@ static std::vector<uintptr_t> interval_key(const Plan& P, const Level& LV, int s
                                 (uintptr_t)LV.aniso, (uintptr_t)P.o.precond, (uintptr_t)P.d_state.p,
                                 (uintptr_t)P.d_part.p, (uintptr_t)P.d_counter.p, (uintptr_t)P.hist,
                                 (uintptr_t)P.hist_stride, (uintptr_t)LV.sig32.p, (uintptr_t)LV.sig64.p,
-                                (uintptr_t)LV.tab32.p, (uintptr_t)LV.tab64.p};
+                                (uintptr_t)LV.tab32.p, (uintptr_t)LV.tab64.p, (uintptr_t)LV.rc_ok,
+                                (uintptr_t)LV.rc32.p, (uintptr_t)LV.rc64.p};
     for (const DBuf& b : P.kv) k.push_back((uintptr_t)b.p);
     k.insert(k.end(), extra);
     return k;

@@ -175,6 +175,7 @@ extern "C" int sfdx_residual_noalloc(int nx, int ny, int nz, const double* a, co
         cudaStreamSynchronize(st) != cudaSuccess)
         return SFDX_ERR_CUDA;
     L.aniso = aniso;
+    L.rc = nullptr;
     int B = ns;
     while (B < 128 || B < 2 * ns) B *= 2;
     int dev = 0, nsm = 1;

@@ -187,6 +187,8 @@ struct Level {
     int aniso = 0;
     DBuf tab64, tab32;     // [3 axes][6 arrays][stride]
     DBuf sig64, sig32;     // [6][ncell]
+    DBuf rc64, rc32;       // per-row coefficients [nl][12] (k_row_coef), valid if rc_ok
+    bool rc_ok = false;
     DBuf spac;             // a, b, c (device, FP64) for coarsening
     DBuf crd_cubic;        // node coordinates used by cubic_interp on this level
     DBuf crd_quad;         // node coordinates used by quad_interp_e (pairwise sums of a,b,c)
@@ -214,6 +216,7 @@ struct Level {
         L.az = axis_ptrs<T>(base, stride, 2);
         L.sig = std::is_same<T, double>::value ? (const T*)sig64.p : (const T*)sig32.p;
         L.aniso = aniso;
+        L.rc = !rc_ok ? nullptr : std::is_same<T, double>::value ? (const T*)rc64.p : (const T*)rc32.p;
         return L;
     }
 };

@@ -37,6 +37,7 @@
 #include "sfdx_host.h"
 #include "sfdx_kernels.cuh"
 #include "sfdx_plan.h"
+#include "sfdx_vkern.cuh"
 
 using namespace sfdx;
 
@@ -376,6 +377,18 @@ static int set_conductivity(Plan& P, const double* sigma, bool on_device) {
         CK(cudaMemcpyAsync(&flag, P.d_flag.p, sizeof(int), cudaMemcpyDeviceToHost, P.st));
         CK(cudaStreamSynchronize(P.st));
         L.aniso = flag;
+        // per-row coefficients of both precisions (SFDX_ROW_COEF=0: computed
+        // in every row evaluation instead)
+        L.rc_ok = false;
+        const char* env = getenv("SFDX_ROW_COEF");
+        if (!(env && env[0] == '0')) {
+            RC(L.rc64.alloc((size_t)L.nl * 12 * sizeof(double)));
+            RC(L.rc32.alloc((size_t)L.nl * 12 * sizeof(float)));
+            KL(k_row_coef<double><<<grid_for(L.nl, 256, 16), 256, 0, P.st>>>(L.lev<double>(), L.mesh, L.rc64.as<double>()));
+            KL(k_row_coef<float><<<grid_for(L.nl, 256, 16), 256, 0, P.st>>>(L.lev<float>(), L.mesh, L.rc32.as<float>()));
+            CK(cudaGetLastError());
+            L.rc_ok = true;
+        }
     }
     return SFDX_OK;
 }

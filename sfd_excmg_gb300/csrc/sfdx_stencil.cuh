@@ -391,6 +391,38 @@ __device__ __forceinline__ RowK<T> row_k(const Lev<T>& L, int i, int j, int k) {
     return K;
 }
 
+// Coefficients of row e: stored ones when the level has them (built once per
+// conductivity by k_row_coef: 12 values, 48 bytes in complex64 arithmetic,
+// read by the G threads of the edge as one broadcast), else computed from the
+// conductivity and spacing tables as above.
+template <class T, int O, bool SAME, bool CA, bool CB>
+__device__ __forceinline__ RowK<T> row_k_e(const Lev<T>& L, uint32_t e, int i, int j, int k) {
+    if (!L.rc) return row_k<T, O, SAME, CA, CB>(L, i, j, k);
+    RowK<T> K;
+    const T* p = L.rc + (size_t)e * 12;
+    T v[12];
+    if (sizeof(T) == 4) {
+        const float4* q = reinterpret_cast<const float4*>(p);
+#pragma unroll
+        for (int h = 0; h < 3; h++) {
+            const float4 f = __ldg(q + h);
+            v[4 * h] = (T)f.x; v[4 * h + 1] = (T)f.y; v[4 * h + 2] = (T)f.z; v[4 * h + 3] = (T)f.w;
+        }
+    } else {
+        const double2* q = reinterpret_cast<const double2*>(p);
+#pragma unroll
+        for (int h = 0; h < 6; h++) {
+            const double2 f = __ldg(q + h);
+            v[2 * h] = (T)f.x; v[2 * h + 1] = (T)f.y;
+        }
+    }
+    K.cs[0] = v[0]; K.cs[1] = v[1]; K.cs[2] = v[2]; K.cs[3] = v[3];
+    K.dre = v[4]; K.sbar = v[5];
+    K.gA = v[6]; K.sA1 = v[7]; K.sA2 = v[8];
+    K.gB = v[9]; K.sB1 = v[10]; K.sB2 = v[11];
+    return K;
+}
+
 // Neighbour positions and boundary predicates of the interior row (O,i,j,k).
 //   same[q]  : edge index of the q-th same-orientation neighbour, msame bit q
 //   A[0..3]  : first cross group  (v1, v2, v3, v4 of the curl difference)
@@ -515,7 +547,7 @@ __device__ __forceinline__ void row_apply_o(const Lev<T>& L, const Mesh& M, uint
         y = xe;
         return;
     }
-    const RowK<T> K = row_k<T, O, true, true, true>(L, i, j, k);
+    const RowK<T> K = row_k_e<T, O, true, true, true>(L, e, i, j, k);
     const RowN N = row_n<O>(M, e, i, j, k);
     CV<T, VS> C, Mm;
     row_off<T, VS, O, true, true, true, true>(K, N, x, ns, s0, C, Mm);

@@ -210,7 +210,7 @@ __global__ void k_fwd_v(Lev<T> L, Mesh M, SysG sgp, const KState* st, cplx<T>* _
             cvst_m<T, VS>(w + g, rhs, S.act);
             continue;
         }
-        const RowK<T> K = row_k<T, O, P == 1, (O >= OY), (O == OZ)>(L, i, j, k);
+        const RowK<T> K = row_k_e<T, O, P == 1, (O >= OY), (O == OZ)>(L, e, i, j, k);
         const RowN N = row_n<O>(M, e, i, j, k);
         CV<T, VS> C, Mm, out;
         row_off<T, VS, O, P == 1, (O >= OY), (O == OZ), true>(K, N, w, ns, s0, C, Mm);
@@ -233,7 +233,7 @@ __global__ void k_bwd_v(Lev<T> L, Mesh M, SysG sgp, const KState* st, cplx<T>* _
         if (mbnd(M, O, i, j, k)) continue;
         const uint32_t e = medge(M, O, i, j, k);
         const size_t g = (size_t)e * ns + s0;
-        const RowK<T> K = row_k<T, O, P == 0, (O == OX), (O <= OY)>(L, i, j, k);
+        const RowK<T> K = row_k_e<T, O, P == 0, (O == OX), (O <= OY)>(L, e, i, j, k);
         const RowN N = row_n<O>(M, e, i, j, k);
         CV<T, VS> C, Mm, xe;
         row_off<T, VS, O, P == 0, (O == OX), (O <= OY), true>(K, N, x, ns, s0, C, Mm);
@@ -1165,6 +1165,33 @@ __global__ void k_cocr_upd(Mesh M, SysG sgp, KState* st, cplx<XT>* __restrict__ 
             Q.status = ST_MAXIT;
             Q.active = 0;
         }
+    }
+}
+
+// ------------------------------------------------------------------ row coefficients
+// rc[e][12] = the coefficients row_k computes for interior row e (zero for the
+// Dirichlet rows); built after every conductivity change, per level and
+// precision.  L.rc must be null here.
+template <class T>
+__global__ void k_row_coef(Lev<T> L, Mesh M, T* __restrict__ rc) {
+    for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < M.nl; e += gridDim.x * blockDim.x) {
+        int i, j, k;
+        const int o = mdecode(M, e, i, j, k);
+        T v[12];
+#pragma unroll
+        for (int q = 0; q < 12; q++) v[q] = T(0);
+        if (!mbnd(M, o, i, j, k)) {
+            RowK<T> K;
+            if (o == OX) K = row_k<T, OX, true, true, true>(L, i, j, k);
+            else if (o == OY) K = row_k<T, OY, true, true, true>(L, i, j, k);
+            else K = row_k<T, OZ, true, true, true>(L, i, j, k);
+            v[0] = K.cs[0]; v[1] = K.cs[1]; v[2] = K.cs[2]; v[3] = K.cs[3];
+            v[4] = K.dre; v[5] = K.sbar;
+            v[6] = K.gA; v[7] = K.sA1; v[8] = K.sA2;
+            v[9] = K.gB; v[10] = K.sB1; v[11] = K.sB2;
+        }
+#pragma unroll
+        for (int q = 0; q < 12; q++) rc[(size_t)e * 12 + q] = v[q];
     }
 }
 

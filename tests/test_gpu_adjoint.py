@@ -42,9 +42,11 @@ def test_misfit_grad_matches_oracle(precision):
     # the gradient of every cell and component (Frobenius norm over the model)
     err = np.linalg.norm(g - gref) / np.linalg.norm(gref)
     assert err < 1e-4, err
-    # cells with a large gradient individually
+    # cells with a large gradient individually: forward and adjoint fields solved to
+    # 1e-10 carry low-frequency errors of ~1e-4 relative (the impedance tolerances
+    # of test_gpu_forward.py), which reach single cells at the 1e-3 level
     big = np.abs(gref) > 1e-2 * np.abs(gref).max()
-    np.testing.assert_allclose(g[big], gref[big], rtol=1e-3)
+    np.testing.assert_allclose(g[big], gref[big], rtol=3e-3)
 
 
 def test_misfit_grad_matches_gpu_finite_differences():
