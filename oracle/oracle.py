@@ -1,7 +1,7 @@
 """CPU oracle for the SFD_EXCMG forward-solve path -- TEST INFRASTRUCTURE ONLY.
 
 Only tests/, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
-``bench.py`` may import this module, and only as the checker.  The shipped
+``bench.py`` may import this module, and only to check results.  The shipped
 library (``sfd_excmg_gb300``) never imports, loads or calls anything here.
 
 It restates the reference's FP64 algorithms: the heavy loops live in
@@ -423,7 +423,7 @@ def grad_correct(nx, ny, nz, a, b, c, sigma, ff, rhs, x):
     """x + G phi with (G^T V Ms G) phi = G^T V (rhs - K x) / (-i w mu), solved exactly.
 
     No counterpart in the reference (its div_correc removes the divergence of x alone);
-    this is the restatement of the library's consistent correction used as its checker.
+    this is the restatement of the library's consistent correction that its tests compare with.
     Ms, the conductivity part of the assembled rows, is recovered from two assemblies
     (K(w) = C - i w mu Ms)."""
     conv = column_conv(sigma, nx, ny, nz)
@@ -444,7 +444,7 @@ def grad_correct(nx, ny, nz, a, b, c, sigma, ff, rhs, x):
 
 
 # --------------------------------------------------------------------------- adjoint gradient
-# No counterpart in the reference (it has no inversion path).  The checker of the
+# No counterpart in the reference (it has no inversion path).  The oracle's value of the
 # library's misfit gradient, computed independently of the library's route: the
 # transposed system is solved directly (no use of the dual-volume symmetry), the
 # operator derivative comes from re-assembling fd_assemb + dcfast with one cell

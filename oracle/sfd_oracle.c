@@ -2,7 +2,7 @@
  * sfd_oracle.c -- CPU restatement of the SFD_EXCMG forward-solve path.
  *
  * TEST INFRASTRUCTURE ONLY.  This file is the oracle: the parity tests, the
- * smoke check and the CPU-baseline leg of the benchmark call it as the checker.
+ * smoke check and the CPU-baseline leg of the benchmark call it, to check results.
  * Nothing in the shipped library links, loads or calls it.
  *
  * Parity status: unpinned against reference outputs.  The reference Fortran

@@ -645,7 +645,14 @@ static int corrected_cycles(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>*
     double2* x64 = rel ? rel->x64 : reinterpret_cast<double2*>(x);
     std::vector<int> mask(ns), part(ns), used(ns, 0), fin(ns, ST_CONV);
     for (int q = 0; q < ns; q++) part[q] = mask[q] = mask_host ? (mask_host[q] != 0) : 1;
-    const int cyc = P.o.corr_intv > 0 ? P.o.corr_intv : 25;
+    const int cyc0 = P.o.corr_intv > 0 ? P.o.corr_intv : 25;
+    // cycle length grows by this factor per cycle (SFDX_CYCLE_GROWTH): the
+    // systems still running late (high frequencies) lose less Krylov history
+    // to restarts, while the early cycles keep the correction frequent
+    const char* gr_env = getenv("SFDX_CYCLE_GROWTH");
+    const double growth = gr_env ? std::max(1.0, atof(gr_env)) : 1.0;
+    double cyc_f = cyc0;
+    int cyc = cyc0;
     const int gc_maxit = 2000;  // pcg itmax (div_correc.f90:57)
     const std::vector<double> wm_all = P.wm;
     const bool can_pack = P.hist == nullptr;  // residual histories are indexed by the full batch
@@ -736,6 +743,8 @@ static int corrected_cycles(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>*
             }
         }
         if (!left) break;
+        cyc_f *= growth;
+        cyc = (int)std::min(cyc_f, 1e6);
     }
     std::vector<int> last(ns);
     for (int q = 0; q < ns; q++) last[q] = part[q] && fin[q] != ST_NAN && !(fin[q] == ST_BREAK && rel);
