@@ -646,11 +646,12 @@ static int corrected_cycles(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>*
     std::vector<int> mask(ns), part(ns), used(ns, 0), fin(ns, ST_CONV);
     for (int q = 0; q < ns; q++) part[q] = mask[q] = mask_host ? (mask_host[q] != 0) : 1;
     const int cyc0 = P.o.corr_intv > 0 ? P.o.corr_intv : 25;
-    // cycle length grows by this factor per cycle (SFDX_CYCLE_GROWTH): the
+    // cycle length grows by 1.5 per cycle (SFDX_CYCLE_GROWTH overrides): the
     // systems still running late (high frequencies) lose less Krylov history
-    // to restarts, while the early cycles keep the correction frequent
+    // to restarts, while the early cycles keep the correction frequent.  cfg2
+    // at 1e-10: 15.6 solves/s against 13.8 with fixed cycles (2.0: 14.9).
     const char* gr_env = getenv("SFDX_CYCLE_GROWTH");
-    const double growth = gr_env ? std::max(1.0, atof(gr_env)) : 1.0;
+    const double growth = gr_env ? std::max(1.0, atof(gr_env)) : 1.5;
     double cyc_f = cyc0;
     int cyc = cyc0;
     const int gc_maxit = 2000;  // pcg itmax (div_correc.f90:57)
