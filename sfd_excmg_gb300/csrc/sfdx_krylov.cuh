@@ -650,8 +650,10 @@ static int corrected_cycles(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>*
     // systems still running late (high frequencies) lose less Krylov history
     // to restarts, while the early cycles keep the correction frequent.  cfg2
     // at 1e-10: 15.6 solves/s against 13.8 with fixed cycles (2.0: 14.9).
+    // TFQMR keeps fixed cycles: it stagnates without frequent corrections.
     const char* gr_env = getenv("SFDX_CYCLE_GROWTH");
-    const double growth = gr_env ? std::max(1.0, atof(gr_env)) : 1.5;
+    const double growth =
+        P.o.solver == SFDX_SOLVER_TFQMR ? 1.0 : gr_env ? std::max(1.0, atof(gr_env)) : 1.5;
     double cyc_f = cyc0;
     int cyc = cyc0;
     const int gc_maxit = 2000;  // pcg itmax (div_correc.f90:57)
