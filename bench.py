@@ -172,6 +172,10 @@ WORKLOADS = {
 # Reference CPU time for DTM1 (EXCMG, 4 levels, tol 1e-10; Xeon Gold 6248R, serial):
 # 93.62 + 76.84 + 45.95 + 63.31 s for the four frequencies x two polarisations.
 PUBLISHED_SOLVES_PER_S = {"dtm1": 8.0 / (93.62 + 76.84 + 45.95 + 63.31)}
+# DRAM bytes (read + write) of one multi-colour SSOR application on the cfg2
+# finest level, summed over its 11 colour launches from one ncu capture
+# (profiles/mc_ssor_sweep_cfg2.md): 1528.6 MB read + 128.2 MB written.
+SSOR_TRAFFIC = {"cfg2": 1656834048}
 
 
 def make_workload(name):
@@ -387,7 +391,8 @@ def run_ours(args, rank, world, local):
         "e2e": {"value": ns / e2e_s, "unit": "solves/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "achieved": dom["gbs"], "peak": hbm, "unit": "GB/s", "frac": dom["gbs"] / hbm,
-                     "traffic": None, "kernel": "mc_ssor_c64 (11 colour sweeps)", "peak_source": src},
+                     "traffic": SSOR_TRAFFIC.get(args.workload), "kernel": "mc_ssor_c64 (11 colour sweeps)",
+                     "peak_source": src},
         "kernels": kern,
         "cpu_baseline": cpu,
         "clocks": clk,
