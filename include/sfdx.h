@@ -213,6 +213,16 @@ int sfdx_impedance(int nx, int ny, int nz, int nair, const double* a, const doub
 
 /* mt1d_anl (model_selec.f90:266-401), host FP64: conv is Fortran
  * conv(nz,6); edc, hx: 2nz+2 complex; imp: 4 complex. */
+/* Impedance misfit of host fields ex[nf][2][nl] (as sfdx_impedance) against
+ * zobs [nf][nrec][4] with weights wts [nf][nrec][2] (null: 1), misfit = sum
+ * wxy |Zxy - dxy|^2 + wyx |Zyx - dyx|^2, and (grad not null) its derivative
+ * with respect to every edge value, grad[nf][2][nl] complex, in the holomorphic
+ * sense (d misfit = 2 Re sum grad dx): the right-hand side of an adjoint solve
+ * (see sfdx_plan_misfit_grad).  Host FP64, no device use.  No counterpart in
+ * the reference. */
+int sfdx_impedance_misfit(int nx, int ny, int nz, int nair, const double* a, const double* b, const double* c,
+                          int nf, const double* freq, const double* ex, int nrec, const double* recv, int quirks,
+                          const double* zobs, const double* wts, double* misfit, double* grad);
 int sfdx_mt1d(double freq, int nz, const double* conv, const double* c, double* edc, double* hx, double* imp);
 
 /* fd_assemb + dcfast as a matrix-free operator (fdfe_main.f90:226-546,

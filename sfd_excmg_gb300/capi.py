@@ -100,6 +100,10 @@ _PROTO = {
     "sfdx_impedance": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, c_double_p,
                                       c_double_p, c_double_p, ctypes.c_int, c_double_p, c_double_p, ctypes.c_int,
                                       c_double_p, ctypes.c_int, ctypes.c_int, c_double_p, c_double_p]),
+    "sfdx_impedance_misfit": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, c_double_p,
+                                             c_double_p, c_double_p, ctypes.c_int, c_double_p, c_double_p,
+                                             ctypes.c_int, c_double_p, ctypes.c_int, c_double_p, c_double_p,
+                                             c_double_p, c_double_p]),
     "sfdx_mt1d": (ctypes.c_int, [ctypes.c_double, ctypes.c_int, c_double_p, c_double_p, c_double_p, c_double_p,
                                  c_double_p]),
     "sfdx_apply_operator": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, c_double_p, c_double_p,

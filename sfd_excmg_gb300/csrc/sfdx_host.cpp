@@ -5,6 +5,7 @@
 //   * the impedance evaluation (post_process + arho_interp2,
 //     fdfe_main.f90:549-790),
 //   * the reference's model/data/result file formats (file_opt.f90:8-158).
+#include <algorithm>
 #include <cmath>
 #include <complex>
 #include <cstdio>
@@ -599,6 +600,51 @@ extern "C" int sfdx_write_res(const char* name, int nf, const double* freq, int 
             fprintf(f, "\n");
         }
     fclose(f);
+    return SFDX_OK;
+}
+
+// Misfit of host fields and its derivative with respect to every edge value
+// (zero away from the receiver planes): the host part of the adjoint gradient,
+// for callers that run their own adjoint solves.
+extern "C" int sfdx_impedance_misfit(int nx, int ny, int nz, int nair, const double* a, const double* b,
+                                     const double* c, int nf, const double* freq, const double* ex, int nrec,
+                                     const double* recv, int quirks, const double* zobs, const double* wts,
+                                     double* misfit, double* grad) {
+    if (!a || !b || !c || !freq || !ex || !recv || !zobs || !misfit || nrec < 1 || nf < 1 || nair < 1 ||
+        nair + 2 > nz)
+        return SFDX_ERR_ARG;
+    const size_t xnl = (size_t)nx * (ny + 1) * (nz + 1), ynl = (size_t)(nx + 1) * ny * (nz + 1);
+    const size_t nl = xnl + ynl + (size_t)(nx + 1) * (ny + 1) * nz;
+    const size_t pex = (size_t)nx * (ny + 1), pey = (size_t)(nx + 1) * ny, pez = (size_t)(nx + 1) * (ny + 1);
+    const int transpose = (quirks & SFDX_QUIRK_RX_TRANSPOSE) ? 1 : 0;
+    const zd* x = reinterpret_cast<const zd*>(ex);
+    zd* g = reinterpret_cast<zd*>(grad);
+    if (g) std::fill(g, g + (size_t)nf * 2 * nl, zd(0.0));
+    double phi = 0;
+    std::vector<zd> cf((size_t)nrec * 8);
+    for (int f = 0; f < nf; f++) {
+        SurfaceView sv;
+        sv.nx = nx; sv.ny = ny; sv.nair = nair;
+        for (int p = 0; p < 2; p++) {
+            const zd* xp = x + ((size_t)f * 2 + p) * nl;
+            sv.exs[p] = xp + (size_t)nair * pex;
+            sv.eys[p] = xp + xnl + (size_t)nair * pey;
+            sv.ezs[p] = xp + xnl + ynl + (size_t)nair * pez;
+        }
+        HRC(impedance_cotangents(sv, a, b, c, freq[f], nrec, recv, transpose, zobs + (size_t)f * nrec * 4,
+                                 wts ? wts + (size_t)f * nrec * 2 : nullptr, &phi, nullptr, cf.data()));
+        if (!g) continue;
+        SurfaceGrad sg;
+        sg.nx = nx; sg.ny = ny;
+        for (int p = 0; p < 2; p++) {
+            zd* gp = g + ((size_t)f * 2 + p) * nl;
+            sg.exs[p] = gp + (size_t)nair * pex;
+            sg.eys[p] = gp + xnl + (size_t)nair * pey;
+            sg.ezs[p] = gp + xnl + ynl + (size_t)nair * pez;
+        }
+        HRC(impedance_adjoint_source(sg, nair, a, b, c, freq[f], nrec, recv, transpose, cf.data()));
+    }
+    *misfit = phi;
     return SFDX_OK;
 }
 

@@ -817,7 +817,7 @@ extern "C" long long sfdx_plan_device_bytes(const sfdx_plan* plan) {
     long long s = 0;
     const DBuf* bufs[] = {&P.d_state, &P.d_wm, &P.d_pol, &P.d_edc, &P.d_part, &P.d_counter, &P.d_tol, &P.d_mask,
                           &P.d_scale, &P.d_flag, &P.x64, &P.b64, &P.r64, &P.u0, &P.u1, &P.ut, &P.ex_out, &P.errrec,
-                          &P.xf, &P.x32, &P.xb, &P.cb64, &P.cx64, &P.d_idx, &P.d_pst};
+                          &P.xf, &P.x32, &P.xb, &P.cb64, &P.cx64, &P.d_idx, &P.d_pst, &P.xbase};
     for (auto* b : bufs) s += (long long)b->bytes;
     for (auto& b : P.kv) s += (long long)b.bytes;
     for (auto& b : P.dcv) s += (long long)b.bytes;
@@ -825,7 +825,7 @@ extern "C" long long sfdx_plan_device_bytes(const sfdx_plan* plan) {
     for (auto& b : P.gce) s += (long long)b.bytes;
     for (auto& L : P.lev) {
         s += (long long)(L.tab64.bytes + L.tab32.bytes + L.sig64.bytes + L.sig32.bytes + L.spac.bytes +
-                         L.crd_cubic.bytes + L.crd_quad.bytes);
+                         L.crd_cubic.bytes + L.crd_quad.bytes + L.rc64.bytes + L.rc32.bytes);
         for (auto& g : L.mg)
             s += (long long)(g.coef.bytes + g.dinv.bytes + g.x.bytes + g.b.bytes + g.t.bytes + g.r.bytes);
     }

@@ -339,6 +339,25 @@ def krylov_solve(nx, ny, nz, a, b, c, sigma, freqs, rhs, x0=None, tol=1e-8, itma
     return out + (hist,) if history else out
 
 
+def impedance_misfit(model: Model, ex, zobs, wts=None, quirks: int = capi.QUIRKS_REFERENCE, grad: bool = True):
+    """sfdx_impedance_misfit: (misfit, d misfit / d ex [nf, 2, nl] or None) of host fields ex[nf, 2, nl]."""
+    m = model
+    x = _z(ex)
+    f = _d(m.freq)
+    rv = _d(np.asarray(m.recv).T)
+    zo = _d(zobs)
+    wt = None if wts is None else _d(wts)
+    g = np.zeros_like(x) if grad else None
+    mis = ctypes.c_double()
+    capi.check(capi.lib().sfdx_impedance_misfit(m.nx, m.ny, m.nz, m.nair, capi.dptr(_d(m.a)), capi.dptr(_d(m.b)),
+                                                 capi.dptr(_d(m.c)), m.nf, capi.dptr(f), capi.zptr(x), rv.shape[1],
+                                                 capi.dptr(rv), quirks, capi.dptr(zo),
+                                                 capi.dptr(wt) if wt is not None else None, ctypes.byref(mis),
+                                                 capi.zptr(g) if g is not None else None),
+               "sfdx_impedance_misfit")
+    return mis.value, g
+
+
 def write_res(name: str, freqs, recv, res) -> None:
     """output_data (file_opt.f90:131-158): <name>.res from results[nf, nrec, 4]."""
     f = _d(np.atleast_1d(freqs))

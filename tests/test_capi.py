@@ -104,3 +104,44 @@ def test_ccv_and_res_files_use_the_reference_layout(tmp_path):
     fields = open(base + ".res").read().split()
     assert fields == ["0.15000E+01", "-0.20000E+01", "0.00000E+00", "0.10000E+02", "0", "0.10000E+01",
                       "-0.25000E+00", "0.30000E-03", "0.00000E+00"]
+
+
+def test_host_misfit_derivative_matches_finite_differences():
+    """sfdx_impedance_misfit: the misfit equals the oracle's, and its derivative g
+    (d misfit = 2 Re g^T dx) matches central differences in the real and imaginary
+    parts of surface edge values, g = (d/dRe - i d/dIm) / 2."""
+    import sfd_excmg_gb300 as S
+    from oracle import oracle as O
+    from sfd_excmg_gb300 import synthetic as syn
+    m = syn.small_aniso(n=12, seed=2, freqs=(0.5,))
+    om = O.OracleModel(m.nx, m.ny, m.nz, m.nair, m.a, m.b, m.c, m.sigma, m.freq, m.recv)
+    u1, u2, _, _, _ = O.direct_solve(om, 0.5)
+    ex = np.stack([u1, u2])[None]
+    m2 = syn.small_aniso(n=12, seed=3, freqs=(0.5,))
+    om2 = O.OracleModel(m.nx, m.ny, m.nz, m.nair, m.a, m.b, m.c, m2.sigma, m.freq, m.recv)
+    v1, v2, _, _, _ = O.direct_solve(om2, 0.5)
+    zobs = O.impedances(om2, np.stack([v1, v2])[None])
+    phi, g = S.impedance_misfit(m, ex, zobs)
+    assert abs(phi - O.misfit(om, zobs)) <= 1e-10 * phi
+    nx, ny = m.nx, m.ny
+    xnl = nx * (ny + 1) * (m.nz + 1)
+    ynl = (nx + 1) * ny * (m.nz + 1)
+    for p in (0, 1):
+        # per orientation, the edge with the largest derivative (the receiver stencils
+        # touch a few dozen surface edges)
+        a = np.abs(g[0, p])
+        edges = [int(np.argmax(a[:xnl])), xnl + int(np.argmax(a[xnl:xnl + ynl])),
+                 xnl + ynl + int(np.argmax(a[xnl + ynl:]))]
+        assert all(a[e] > 0 for e in edges)
+        for e in edges:
+            h = 1e-6 * np.abs(ex[0, p]).max()
+            d = []
+            for step in (h, 1j * h):
+                xp = ex.copy()
+                xm = ex.copy()
+                xp[0, p, e] += step
+                xm[0, p, e] -= step
+                d.append((S.impedance_misfit(m, xp, zobs, grad=False)[0] -
+                          S.impedance_misfit(m, xm, zobs, grad=False)[0]) / (2 * h))
+            fd = (d[0] - 1j * d[1]) / 2
+            assert abs(g[0, p, e] - fd) <= 1e-5 * abs(fd) + 1e-9 * np.abs(g).max(), (p, e, g[0, p, e], fd)
