@@ -265,7 +265,7 @@ def run_reference(args, rank, world):
         "impl": "reference", "metric": "MT solves/s", "value": v, "unit": "solves/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
         "ms_per_step": float(np.median([s[0] for s in samples]) * 1e3),
-        "config": {"workload": "cfg2 anisotropic+hills 80x80x80 (1,574,640 edges), 8 freqs x 2 pols",
+        "config": {"workload": WORKLOADS["cfg2"][0].format(eps=WORKLOADS["cfg2"][1]),
                    "solver": "SSOR-BiCGStab FP64 CSR (reference algorithm, oracle restatement)"},
         "cpu_baseline": {"value": v, "unit": "solves/s", "cores": threads, "kind": "port",
                          "sample": (f"per system: finest-level assembly + {REF_SAMPLE_ITERS} SSOR-BiCGStab iterations; "
