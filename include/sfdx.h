@@ -185,9 +185,11 @@ int sfdx_plan_set_stream(sfdx_plan* plan, void* stream);
  * algorithmic HBM bytes: 0 operator c64, 1 operator c128, 2 MC-SSOR c64, 3 MC-SSOR c128. */
 int sfdx_plan_kernel_time(sfdx_plan* plan, int kernel, int reps, double* ms, double* bytes);
 /* Pick the number of systems each thread of the hot kernels handles (4, 2
- * or 1 consecutive systems, complex64 and complex128 separately) by timing an
- * operator plus a multi-colour SSOR application per candidate, `reps` times
- * each, on the finest level (conductivity must be loaded).  No counterpart in
+ * or 1 consecutive systems, complex64 and complex128 separately) by timing, per
+ * candidate and `reps` times each on the finest level (conductivity must be
+ * loaded): eight complex64 iterations of the plan's Krylov solver (BiCGStab,
+ * GPBiCG, COCR; other solvers an operator plus a multi-colour SSOR
+ * application), and an operator plus an SSOR application in complex128.  No counterpart in
  * the reference.  The choices are returned in *vs32, *vs64 (optional). */
 int sfdx_plan_autotune(sfdx_plan* plan, int reps, int* vs32, int* vs64);
 /* Wall time (ms) of each level of the last solve, coarsest first (n >= levels). */

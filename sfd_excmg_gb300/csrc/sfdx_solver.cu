@@ -923,6 +923,26 @@ extern "C" int sfdx_plan_autotune(sfdx_plan* plan, int reps, int* vs32, int* vs6
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0));
     CK(cudaEventCreate(&e1));
+    // complex64: eight iterations of the plan's Krylov solver (its fused
+    // operator, sweep and update kernels, as a solve runs them) on a
+    // deterministic right-hand side; complex128 (coarse levels, residual
+    // replacements): an operator plus a preconditioner application
+    DBuf tb, tx;
+    const bool kry = P.o.solver == SFDX_SOLVER_GPBICG || P.o.solver == SFDX_SOLVER_BICGSTAB ||
+                     P.o.solver == SFDX_SOLVER_COCR;
+    if (kry) {
+        RC(tb.alloc(n * sizeof(float2)));
+        RC(tx.alloc(n * sizeof(float2)));
+        KL(k_pattern<float><<<grid_for(n, 256), 256, 0, P.st>>>(n, tb.as<float2>()));
+    }
+    auto iterations = [&]() -> int {
+        CK(cudaMemsetAsync(tx.p, 0, n * sizeof(float2), P.st));
+        const float2* b = tb.as<float2>();
+        float2* x = tx.as<float2>();
+        if (P.o.solver == SFDX_SOLVER_GPBICG) return gpbicg<float>(P, F, b, x, nullptr, 1e-30, 8, nullptr);
+        if (P.o.solver == SFDX_SOLVER_COCR) return cocr<float>(P, F, b, x, nullptr, 1e-30, 8, nullptr);
+        return bicgstab<float>(P, F, b, x, nullptr, 1e-30, 8, nullptr);
+    };
     int best[2] = {P.vs32, P.vs64};
     for (int prec = 0; prec < 2; prec++) {
         double tbest = 1e300;
@@ -933,7 +953,9 @@ extern "C" int sfdx_plan_autotune(sfdx_plan* plan, int reps, int* vs32, int* vs6
             float t = 0;
             for (int r = 0; r <= reps; r++) {  // first pass warms up
                 if (r == 1) CK(cudaEventRecord(e0, P.st));
-                if (prec == 0) {
+                if (prec == 0 && kry) {
+                    RC(iterations());
+                } else if (prec == 0) {
                     RC(apply_op<float>(P, F, P.kv[0].as<float2>(), P.kv[1].as<float2>()));
                     RC(precond_vec<float>(P, F, P.kv[2].as<float2>(), P.kv[1].as<float2>()));
                 } else {
