@@ -648,7 +648,8 @@ def main():
                     help="finest-level relative residual tolerance (default per workload; cfg2: 1e-10, the accuracy "
                          "at which the mixed-precision impedances agree with the FP64 ones to ~1e-5)")
     ap.add_argument("--corr-intv", dest="corr_intv", type=int, default=None,
-                    help="Krylov iterations per restart cycle of the gradient correction (default 25)")
+                    help="Krylov iterations of the first restart cycle of the gradient correction (default 40; each "
+                         "next cycle is 1.5x longer)")
     ap.add_argument("--div-cor", dest="div_cor", type=int, default=2, choices=[0, 1, 2],
                     help="0 none, 1 the reference's divergence correction, 2 consistent gradient-space correction")
     ap.add_argument("--no-compare-fp64", dest="compare_fp64", action="store_false")
