@@ -81,7 +81,7 @@ typedef struct sfdx_opts {
                            in the reference: sfdx_grad_correct below)              */
     int corr_intv;      /* iterations between corrections (corr_intv = 200)            */
     double corr_tol;    /* nodal-Poisson PCG tolerance (corr_tol = 1e-3)               */
-    double ssor_omega;  /* SSOR relaxation (ssor_omg = 1)                              */
+    double ssor_omega;  /* SSOR relaxation in (0, 2) (ssor_omg = 1)                    */
     double sigma_air;   /* conductivity written into air cells by readers (1e-9)      */
     int maxit_plain;    /* iteration limit of the single solve (5000)                  */
     int maxit_level;    /* iteration limit of each EXCMG level (1000)                  */

@@ -20,12 +20,13 @@ static void fwd_one(Plan& P, const Level& LV, const VCfg& c, cplx<T>* w, cplx<T>
                     cplx<T>* aux) {
     const uint32_t W = mcolour_count(LV.mesh, O) * c.sg.G;
     vlaunch(k_fwd_v<T, VS, O, PP, MODE>, W, c.B, 0, P.st, LV.lev<T>(), LV.mesh, c.sg, P.d_state.as<KState>(), w, q, r, v,
-            aux);
+            aux, (T)P.o.ssor_omega);
 }
 template <class T, int VS, int O, int PP>
 static void bwd_one(Plan& P, const Level& LV, const VCfg& c, cplx<T>* x) {
     const uint32_t W = mcolour_count(LV.mesh, O) * c.sg.G;
-    vlaunch(k_bwd_v<T, VS, O, PP>, W, c.B, 0, P.st, LV.lev<T>(), LV.mesh, c.sg, P.d_state.as<KState>(), x);
+    vlaunch(k_bwd_v<T, VS, O, PP>, W, c.B, 0, P.st, LV.lev<T>(), LV.mesh, c.sg, P.d_state.as<KState>(), x,
+            (T)P.o.ssor_omega);
 }
 
 // out = M^{-1} rhs where rhs is produced by MODE (see k_fwd_v).  Multi-colour
@@ -84,7 +85,8 @@ static std::vector<uintptr_t> interval_key(const Plan& P, const Level& LV, int s
                                 (uintptr_t)P.d_part.p, (uintptr_t)P.d_counter.p, (uintptr_t)P.hist,
                                 (uintptr_t)P.hist_stride, (uintptr_t)LV.sig32.p, (uintptr_t)LV.sig64.p,
                                 (uintptr_t)LV.tab32.p, (uintptr_t)LV.tab64.p, (uintptr_t)LV.rc_ok,
-                                (uintptr_t)LV.rc32.p, (uintptr_t)LV.rc64.p};
+                                (uintptr_t)LV.rc32.p, (uintptr_t)LV.rc64.p,
+                                (uintptr_t)(P.o.ssor_omega * 1e6)};
     for (const DBuf& b : P.kv) k.push_back((uintptr_t)b.p);
     k.insert(k.end(), extra);
     return k;

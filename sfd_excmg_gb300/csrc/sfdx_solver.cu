@@ -610,6 +610,7 @@ static int validate_opts(const sfdx_opts& o) {
         return SFDX_ERR_ARG;
     if (o.eps <= 0 || o.maxit_plain <= 0 || o.maxit_level <= 0) return SFDX_ERR_ARG;
     if (o.batch != 0) return SFDX_ERR_UNSUPPORTED;
+    if (!(o.ssor_omega > 0 && o.ssor_omega < 2)) return SFDX_ERR_ARG;
     return SFDX_OK;
 }
 

@@ -153,7 +153,8 @@ __global__ void k_apply_v(Lev<T> L, Mesh M, SysG sgp, const double* wms, const c
 // (the search direction itself), rhs = q).
 template <class T, int VS, int O, int P, int MODE>
 __global__ void k_fwd_v(Lev<T> L, Mesh M, SysG sgp, const KState* st, cplx<T>* __restrict__ w, cplx<T>* __restrict__ q,
-                        const cplx<T>* __restrict__ r, const cplx<T>* __restrict__ v, cplx<T>* __restrict__ aux) {
+                        const cplx<T>* __restrict__ r, const cplx<T>* __restrict__ v, cplx<T>* __restrict__ aux,
+                        T omega) {
     const int ns = sgp.ns, s0 = (threadIdx.x % sgp.G) * VS;
     const SysV<T, VS> S = load_sys<T, VS>(st, s0);
     if (!S.act) return;
@@ -215,15 +216,20 @@ __global__ void k_fwd_v(Lev<T> L, Mesh M, SysG sgp, const KState* st, cplx<T>* _
         CV<T, VS> C, Mm, out;
         row_off<T, VS, O, P == 1, (O >= OY), (O == OZ), true>(K, N, w, ns, s0, C, Mm);
 #pragma unroll
-        for (int u = 0; u < VS; u++)
-            out.v[u] = cdiv<T>(rhs.v[u] - cm_combine<T>(C.v[u], Mm.v[u], S.wm[u]), row_dia<T>(K, S.wm[u]));
+        for (int u = 0; u < VS; u++) {
+            const cplx<T> cm = cm_combine<T>(C.v[u], Mm.v[u], S.wm[u]);
+            out.v[u] = cdiv<T>(rhs.v[u] - mk<T>(omega * cm.x, omega * cm.y), row_dia<T>(K, S.wm[u]));
+        }
         cvst_m<T, VS>(w + g, out, S.act);
     }
 }
 
-// Backward sweep of colour (O,P), in place:  x_e -= D_e^{-1} sum_{later colours} K_en x_n.
+// Backward sweep of colour (O,P), in place:  x_e -= omega D_e^{-1} sum_{later colours} K_en x_n.
+// With the forward sweep's w_e = (rhs_e - omega sum_{earlier} K_en w_n) / D_e this
+// applies M^-1 for M = (D + omega L) D^-1 (D + omega U), the SSOR preconditioner
+// up to the constant factor omega (2 - omega) that Krylov methods do not see.
 template <class T, int VS, int O, int P>
-__global__ void k_bwd_v(Lev<T> L, Mesh M, SysG sgp, const KState* st, cplx<T>* __restrict__ x) {
+__global__ void k_bwd_v(Lev<T> L, Mesh M, SysG sgp, const KState* st, cplx<T>* __restrict__ x, T omega) {
     const int ns = sgp.ns, s0 = (threadIdx.x % sgp.G) * VS;
     const SysV<T, VS> S = load_sys<T, VS>(st, s0);
     if (!S.act) return;
@@ -239,8 +245,10 @@ __global__ void k_bwd_v(Lev<T> L, Mesh M, SysG sgp, const KState* st, cplx<T>* _
         row_off<T, VS, O, P == 0, (O == OX), (O <= OY), true>(K, N, x, ns, s0, C, Mm);
         cvldw<T, VS>(xe, x + g);
 #pragma unroll
-        for (int u = 0; u < VS; u++)
-            xe.v[u] = xe.v[u] - cdiv<T>(cm_combine<T>(C.v[u], Mm.v[u], S.wm[u]), row_dia<T>(K, S.wm[u]));
+        for (int u = 0; u < VS; u++) {
+            const cplx<T> cm = cm_combine<T>(C.v[u], Mm.v[u], S.wm[u]);
+            xe.v[u] = xe.v[u] - cdiv<T>(mk<T>(omega * cm.x, omega * cm.y), row_dia<T>(K, S.wm[u]));
+        }
         cvst_m<T, VS>(x + g, xe, S.act);
     }
 }

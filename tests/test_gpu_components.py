@@ -346,3 +346,18 @@ def test_krylov_iterates_match_multicolour_oracle(ff, solver):
         # so the stopping iteration of these erratic methods may move a little
         assert abs(int(it[s]) - ito) <= max(3, int(0.35 * ito)), (it, ito)
         assert np.linalg.norm(p - K @ x[:, s]) <= 1.01e-8 * np.linalg.norm(p)
+
+
+@pytest.mark.parametrize("omega", [0.8, 1.3])
+def test_ssor_relaxation_converges_to_direct_solution(omega):
+    """The multi-colour SSOR with relaxation omega != 1 (ssor_omg of the reference, fixed
+    at 1 there) still preconditions the solve to the direct solution."""
+    m = _model(0)
+    ff = 1.0
+    K, p1, p2, _ = _csr(m, ff)
+    rhs = np.stack([p1, p2], axis=1)
+    x, it, rr, rc = S.krylov_solve(m.nx, m.ny, m.nz, m.a, m.b, m.c, m.sigma, [ff, ff], rhs, tol=1e-10, itmax=3000,
+                                   div_cor=0, solver=3, ssor_omega=omega)
+    assert rc == 0, (it, rr)
+    for s, p in enumerate((p1, p2)):
+        assert np.linalg.norm(p - K @ x[:, s]) <= 1e-9 * np.linalg.norm(p)
