@@ -124,13 +124,21 @@ def barrier(world):
 
 
 def max_over_ranks(x, world):
+    """The slowest rank's time (replicas run in step; the job takes the longest)."""
     if world == 1:
         return x
     import torch
     import torch.distributed as td
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dev = "cuda" if td.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
     td.all_reduce(t, op=td.ReduceOp.MAX)
     return float(t.item())
+
+
+def whole_job_rate(units_per_rank_step, steps, world, ms_max):
+    """Units per second of the whole job: every rank processes its own replica of the
+    step (weak scaling), timed by the slowest rank."""
+    return units_per_rank_step * steps * world / (ms_max / 1e3)
 
 
 SOLVER = {"bicgstab": 1, "tfqmr": 2, "gpbicg": 3, "bicg": 4, "cocr": 6}
@@ -326,7 +334,7 @@ def run_ours(args, rank, world, local):
     clk = clocks.stop()
     ms = max_over_ranks(ms, world)
     barrier(world)
-    value = ns * args.steps * world / (ms / 1e3)
+    value = whole_job_rate(ns, args.steps, world, ms)
     status, iters, relres, lt = plan.status, plan.iters.copy(), plan.relres.copy(), plan.level_times()
 
     # kernel rooflines on the finest level (CUDA events on the plan's stream)
@@ -595,7 +603,7 @@ def run_batch(args, rank, world, local):
                  "fp64_solves_per_s": ns / t64}
     if rank != 0:
         return
-    value = ns * world / sec
+    value = whole_job_rate(ns, 1, world, sec * 1e3)
     line = {
         "metric": "MT solves/s", "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": True, "scaling": "weak",
