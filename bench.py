@@ -397,6 +397,7 @@ def run_ours(args, rank, world, local):
                    "systems_per_step": ns, "cuda_graphs": bool(USE_GRAPHS),
                    "l2": "working set > L2 (no flush)"},
         "e2e": {"value": ns / e2e_s, "unit": "solves/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+        "per_frequency": {"value": value / 2, "unit": "frequencies/s (both polarisations)"},
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "achieved": dom["gbs"], "peak": hbm, "unit": "GB/s", "frac": dom["gbs"] / hbm,
                      "traffic": SSOR_TRAFFIC.get(args.workload), "kernel": "mc_ssor_c64 (11 colour sweeps)",
