@@ -73,7 +73,8 @@ typedef struct sfdx_opts {
     double eps;         /* finest-level tolerance (.fwd line 2; argv 3)                */
     int solver;         /* SFDX_SOLVER_*                                               */
     int excmg;          /* fwd_acc: 0 single solve from zero guess, 1 EXCMG cascade    */
-    int precond;        /* 'S' multi-colour SSOR, 'J' Jacobi (pre_type)                */
+    int precond;        /* 'S' multi-colour SSOR, 'J' Jacobi (pre_type); 'I' ILU(0) is
+                           not built: SFDX_ERR_UNSUPPORTED                            */
     int div_cor;        /* divergence correction (div_cor): 0 off, 1 the reference's
                            (div_correc every corr_intv iterations), 2 consistent
                            gradient-space correction between restart cycles of

@@ -601,6 +601,7 @@ static int plan_resolve(Plan& P, double tol) {
 
 static int validate_opts(const sfdx_opts& o) {
     if (o.excmg && o.level < 3) return SFDX_ERR_ARG;
+    if (o.precond == 'I') return SFDX_ERR_UNSUPPORTED;  // ILU(0), pre_type = 'I': not built
     if (o.precond != 'S' && o.precond != 'J') return SFDX_ERR_ARG;
     if (o.precision != SFDX_FP64 && o.precision != SFDX_MIXED) return SFDX_ERR_ARG;
     if (o.div_cor < 0 || o.div_cor > 2) return SFDX_ERR_ARG;
@@ -676,8 +677,6 @@ extern "C" int sfdx_plan_create(sfdx_plan** out, const sfdx_opts* opts, int nx, 
     if (opts) o = *opts;
     else sfdx_default_opts(&o);
     RC(validate_opts(o));
-    int ndev = 0;
-    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return SFDX_ERR_CUDA;
     std::unique_ptr<sfdx_plan> h(new sfdx_plan());
     Plan& P = h->P;
     P.o = o;
@@ -701,6 +700,9 @@ extern "C" int sfdx_plan_create(sfdx_plan** out, const sfdx_opts* opts, int nx, 
         if (nx % f || ny % f || nz % f) return SFDX_ERR_MESH;
         if (nx / f < 1 || ny / f < 1 || nz / f < 1) return SFDX_ERR_MESH;
     }
+    // every argument check above runs before the first CUDA call
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return SFDX_ERR_CUDA;
     CK(cudaStreamCreateWithFlags(&P.own_st, cudaStreamNonBlocking));
     P.st = P.own_st;
     P.lev.resize(P.nlev);
@@ -1161,7 +1163,9 @@ extern "C" int sfdx_build_rhs(int nx, int ny, int nz, const double* a, const dou
 extern "C" int sfdx_precond_apply(int nx, int ny, int nz, const double* a, const double* b, const double* c,
                                   const double* sigma, int ns, const double* freqs, int pc, int precision,
                                   const double* y, double* x) {
-    if (!sigma || !y || !x || (pc != 'S' && pc != 'J')) return SFDX_ERR_ARG;
+    if (!sigma || !y || !x) return SFDX_ERR_ARG;
+    if (pc == 'I') return SFDX_ERR_UNSUPPORTED;
+    if (pc != 'S' && pc != 'J') return SFDX_ERR_ARG;
     sfdx_opts o;
     sfdx_default_opts(&o);
     o.precond = pc;

@@ -145,3 +145,44 @@ def test_host_misfit_derivative_matches_finite_differences():
                           S.impedance_misfit(m, xm, zobs, grad=False)[0]) / (2 * h))
             fd = (d[0] - 1j * d[1]) / 2
             assert abs(g[0, p, e] - fd) <= 1e-5 * abs(fd) + 1e-9 * np.abs(g).max(), (p, e, g[0, p, e], fd)
+
+
+def _create(lib, opts, nx=16, ny=16, nz=16, nair=4, freqs=(1.0,)):
+    """sfdx_plan_create on a small uniform mesh; returns (status, handle)."""
+    dp = lambda v: np.ascontiguousarray(v, dtype=np.float64).ctypes.data_as(capi.c_double_p)  # noqa: E731
+    a, b, c = np.full(nx, 50.0), np.full(ny, 50.0), np.full(nz, 50.0)
+    f = np.asarray(freqs, dtype=np.float64)
+    h = ctypes.c_void_p()
+    st = lib.sfdx_plan_create(ctypes.byref(h), ctypes.byref(opts), nx, ny, nz, nair, dp(a), dp(b), dp(c), len(f), dp(f))
+    return st, h.value
+
+
+def test_plan_create_rejects_invalid_arguments_before_any_cuda_call(lib):
+    """Every argument and option check of plan creation answers before the first CUDA
+    call, so each invalid case returns its own status with no handle (also where no
+    device exists)."""
+    arg, mesh, unsup = 1, 2, 8
+    cases = [
+        (dict(ssor_omega=0.0), {}, arg),
+        (dict(ssor_omega=2.0), {}, arg),
+        (dict(ssor_omega=float("nan")), {}, arg),
+        (dict(batch=1), {}, unsup),
+        (dict(precond="I"), {}, unsup),  # ILU(0): a reference option that is not built
+        (dict(precond="X"), {}, arg),
+        (dict(solver=5), {}, arg),
+        (dict(precision=2), {}, arg),
+        (dict(excmg=1, level=2), {}, arg),
+        (dict(div_cor=3), {}, arg),
+        (dict(div_cor=2, corr_tol=0.0), {}, arg),
+        (dict(eps=0.0), {}, arg),
+        (dict(maxit_level=0), {}, arg),
+        ({}, dict(nx=1), arg),
+        ({}, dict(nair=17), arg),
+        ({}, dict(freqs=(1.0, -2.0)), arg),
+        ({}, dict(freqs=tuple(float(k + 1) for k in range(65))), unsup),  # 130 systems: above SFDX_MAX_SYSTEMS
+        (dict(excmg=1, level=3), dict(nx=20), mesh),  # 20 cells do not split into 2^3 blocks
+        (dict(excmg=1, level=4), dict(nx=8, ny=8, nz=8, nair=2), mesh),
+    ]
+    for kw, mesh_kw, want in cases:
+        st, h = _create(lib, S.Opts.defaults(**kw), **mesh_kw)
+        assert (st, h) == (want, None), (kw, mesh_kw, st)
