@@ -43,7 +43,6 @@ import os
 import subprocess
 import sys
 import tempfile
-import threading
 import time
 
 import numpy as np
@@ -258,10 +257,10 @@ def run_reference(args, rank, world):
     its = reference_iterations()
     n_it = float(np.mean(its)) if its else float("nan")
     vals = []
-    for w in range(args.warmup):
+    for _ in range(args.warmup):
         cpu_sample(m, list(range(m.nf)) * 2, threads, iters=2)
     samples = []
-    for k in range(args.steps):
+    for _ in range(args.steps):
         wall, t_it, t_setup = cpu_sample(m, list(range(m.nf)) * 2, threads)
         # projected time of the full solve of all systems on `threads` cores
         per_system = t_setup + n_it * t_it
@@ -381,7 +380,7 @@ def run_ours(args, rank, world, local):
     cpu = None
     if args.cpu_baseline and args.workload == "cfg2":  # the iteration counts of the reference are measured on cfg2
         its = reference_iterations()
-        wall, t_it, t_setup = cpu_sample(m, [0], 1)
+        _, t_it, t_setup = cpu_sample(m, [0], 1)
         n_it = float(np.mean(its)) if its else float("nan")
         cpu = {"value": 1.0 / (t_setup + n_it * t_it), "unit": "solves/s", "cores": 1, "kind": "port",
                "sample": (f"one system: finest-level assembly + {REF_SAMPLE_ITERS} serial SSOR-BiCGStab iterations "
