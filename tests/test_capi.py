@@ -63,8 +63,13 @@ def test_host_impedance_matches_post_process():
     om = O.OracleModel(m.nx, m.ny, m.nz, m.nair, m.a, m.b, m.c, m.sigma, m.freq, m.recv)
     for out_type, rd, q in ((1, 2, 7), (2, 1, 3), (0, 2, 4)):
         ref = O.impedances(om, ex, out_type=out_type, rd=rd)
-        got = S.impedance(m, ex, out_type=out_type, quirks=q)
+        got, tip = S.impedance(m, ex, out_type=out_type, quirks=q, tipper=True)
         np.testing.assert_allclose(got, ref, rtol=1e-13, atol=1e-300)
+        # tippers (Tx, Ty) of post_process (fdfe_main.f90:705-708), written beside the impedances
+        for k, ff in enumerate(m.freq):
+            _, tref, _ = O.post_process(om, ex[k, 0], ex[k, 1], ff, out_type, rd)
+            assert np.abs(tref).max() > 0
+            np.testing.assert_allclose(tip[k], tref, rtol=1e-12, atol=1e-14 * np.abs(tref).max())
 
 
 def test_model_file_roundtrip(tmp_path):
