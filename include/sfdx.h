@@ -325,8 +325,16 @@ int sfdx_read_model(const char* model_name, const sfdx_opts* o, int* level, doub
  * comes from sfdx_krylov_solve. */
 int sfdx_write_ccv(const char* model_name, double freq, const char* polar, const char* tag, int iters,
                    const double* history, int n);
+/* Result file <model>.res as output_data writes it (file_opt.f90:131-158): one
+ * line per frequency and receiver, "x y z f 0 v1 v2 v3 v4" in
+ * 4(e12.5,2x),i1,2x,4(e12.5,2x), with out[nf][nrec][4] from sfdx_impedance;
+ * recv is [3][nrec].  sfdx_write_res_tipper appends the tipper block
+ * tipper[nf][nrec][4] (Re Tx, Im Tx, Re Ty, Im Ty) in the same format, as the
+ * reference does with output_tipper; a null tipper writes the impedances only. */
 int sfdx_write_res(const char* model_name, int nf, const double* freq, int nrec, const double* recv,
                    const double* out);
+int sfdx_write_res_tipper(const char* model_name, int nf, const double* freq, int nrec, const double* recv,
+                          const double* out, const double* tipper);
 
 #ifdef __cplusplus
 }

@@ -582,11 +582,10 @@ static void fortran_e(char* buf, size_t cap, int w, int d, double v) {
 }
 static void fortran_e12_5(char* buf, double v) { fortran_e(buf, 32, 12, 5, v); }
 
-extern "C" int sfdx_write_res(const char* name, int nf, const double* freq, int nrec, const double* recv,
-                              const double* out) {
-    if (!name || !freq || !recv || !out) return SFDX_ERR_ARG;
-    FILE* f = fopen((std::string(name) + ".res").c_str(), "w");
-    if (!f) return SFDX_ERR_IO;
+// output_data (file_opt.f90:131-158): one row per (frequency, receiver) with
+// the receiver position, the frequency, the loop variable the reference prints
+// uninitialised (written as 0) and four values, in format 4(e12.5,2x),i1,2x,4(e12.5,2x).
+static void write_res_rows(FILE* f, int nf, const double* freq, int nrec, const double* recv, const double* v) {
     char b[32];
     for (int k = 0; k < nf; k++)
         for (int i = 0; i < nrec; i++) {
@@ -594,13 +593,28 @@ extern "C" int sfdx_write_res(const char* name, int nf, const double* freq, int 
             fortran_e12_5(b, freq[k]);
             fprintf(f, "%s  0  ", b);
             for (int q = 0; q < 4; q++) {
-                fortran_e12_5(b, out[((size_t)k * nrec + i) * 4 + q]);
+                fortran_e12_5(b, v[((size_t)k * nrec + i) * 4 + q]);
                 fprintf(f, "%s  ", b);
             }
             fprintf(f, "\n");
         }
-    fclose(f);
-    return SFDX_OK;
+}
+
+extern "C" int sfdx_write_res_tipper(const char* name, int nf, const double* freq, int nrec, const double* recv,
+                                     const double* out, const double* tipper) {
+    if (!name || !freq || !recv || !out || nf < 0 || nrec < 0) return SFDX_ERR_ARG;
+    FILE* f = fopen((std::string(name) + ".res").c_str(), "w");
+    if (!f) return SFDX_ERR_IO;
+    write_res_rows(f, nf, freq, nrec, recv, out);
+    // output_tipper (global_para.f90:7): the tipper block follows the impedance block
+    if (tipper) write_res_rows(f, nf, freq, nrec, recv, tipper);
+    const bool bad = ferror(f) != 0;
+    return (fclose(f) != 0 || bad) ? SFDX_ERR_IO : SFDX_OK;
+}
+
+extern "C" int sfdx_write_res(const char* name, int nf, const double* freq, int nrec, const double* recv,
+                              const double* out) {
+    return sfdx_write_res_tipper(name, nf, freq, nrec, recv, out, nullptr);
 }
 
 // Misfit of host fields and its derivative with respect to every edge value

@@ -358,13 +358,18 @@ def impedance_misfit(model: Model, ex, zobs, wts=None, quirks: int = capi.QUIRKS
     return mis.value, g
 
 
-def write_res(name: str, freqs, recv, res) -> None:
-    """output_data (file_opt.f90:131-158): <name>.res from results[nf, nrec, 4]."""
+def write_res(name: str, freqs, recv, res, tipper=None) -> None:
+    """output_data (file_opt.f90:131-158): <name>.res from results[nf, nrec, 4]; with
+    tipper[nf, nrec, 4] the tipper block follows, as with output_tipper."""
     f = _d(np.atleast_1d(freqs))
     rv = _d(np.asarray(recv).T)
     r = _d(res)
-    capi.check(capi.lib().sfdx_write_res(name.encode(), len(f), capi.dptr(f), rv.shape[1], capi.dptr(rv),
-                                         capi.dptr(r)), "sfdx_write_res")
+    t = None if tipper is None else _d(tipper)
+    if t is not None and t.shape != r.shape:
+        raise ValueError(f"tipper shape {t.shape} differs from the results' {r.shape}")
+    capi.check(capi.lib().sfdx_write_res_tipper(name.encode(), len(f), capi.dptr(f), rv.shape[1], capi.dptr(rv),
+                                                capi.dptr(r), capi.dptr(t) if t is not None else None),
+               "sfdx_write_res_tipper")
 
 
 def write_ccv(name: str, freq: float, polar: str, tag: str, iters: int, history) -> None:

@@ -109,6 +109,17 @@ def test_ccv_and_res_files_use_the_reference_layout(tmp_path):
     fields = open(base + ".res").read().split()
     assert fields == ["0.15000E+01", "-0.20000E+01", "0.00000E+00", "0.10000E+02", "0", "0.10000E+01",
                       "-0.25000E+00", "0.30000E-03", "0.00000E+00"]
+    # output_tipper: the tipper block follows the impedance block, row for row
+    recv = np.array([[1.5, -2.0, 0.0], [2.5, 0.0, 0.0]])
+    z = np.arange(16, dtype=float).reshape(2, 2, 4) + 1
+    tip = -z / 100
+    S.write_res(base, [10.0, 100.0], recv, z, tipper=tip)
+    rows = [ln.split() for ln in open(base + ".res").read().splitlines()]
+    assert len(rows) == 8
+    for r, (k, i) in zip(rows, [(k, i) for k in range(2) for i in range(2)] * 2):
+        assert [float(v) for v in r[:3]] == list(recv[i]) and float(r[3]) == [10.0, 100.0][k]
+    np.testing.assert_allclose([[float(v) for v in r[5:]] for r in rows[:4]], z.reshape(4, 4), rtol=1e-5)
+    np.testing.assert_allclose([[float(v) for v in r[5:]] for r in rows[4:]], tip.reshape(4, 4), rtol=1e-5)
 
 
 def test_host_misfit_derivative_matches_finite_differences():
