@@ -767,19 +767,24 @@ extern "C" int sfdx_plan_solve_batch(int nplans, sfdx_plan* const* plans, const 
     std::vector<int> rc(nplans, SFDX_OK);
     std::vector<std::thread> th;
     th.reserve(nplans);
-    for (int q = 0; q < nplans; q++)
-        th.emplace_back([&, q] {
-            try {
-                if (cudaSetDevice(dev) != cudaSuccess) {
-                    rc[q] = SFDX_ERR_CUDA;
-                    return;
+    for (int q = 0; q < nplans; q++) {
+        try {
+            th.emplace_back([&, q] {
+                try {
+                    if (cudaSetDevice(dev) != cudaSuccess) {
+                        rc[q] = SFDX_ERR_CUDA;
+                        return;
+                    }
+                    rc[q] = sfdx_plan_solve(plans[q], sigma[q], sigma_on_device, ex ? ex[q] : nullptr, ex_on_device,
+                                            iters ? iters[q] : nullptr, relres ? relres[q] : nullptr);
+                } catch (...) {
+                    rc[q] = SFDX_ERR_NOMEM;
                 }
-                rc[q] = sfdx_plan_solve(plans[q], sigma[q], sigma_on_device, ex ? ex[q] : nullptr, ex_on_device,
-                                        iters ? iters[q] : nullptr, relres ? relres[q] : nullptr);
-            } catch (...) {
-                rc[q] = SFDX_ERR_NOMEM;
-            }
-        });
+            });
+        } catch (...) {  // no thread for this plan: report it, still join the others
+            rc[q] = SFDX_ERR_NOMEM;
+        }
+    }
     for (auto& t : th) t.join();
     int out = SFDX_OK;
     for (int q = 0; q < nplans; q++) {
