@@ -202,3 +202,34 @@ def test_plan_create_rejects_invalid_arguments_before_any_cuda_call(lib):
     for kw, mesh_kw, want in cases:
         st, h = _create(lib, S.Opts.defaults(**kw), **mesh_kw)
         assert (st, h) == (want, None), (kw, mesh_kw, st)
+
+
+def test_reader_rejects_truncated_and_malformed_files(tmp_path):
+    """read_input on a cut-off or corrupted .fwd / .dat returns an error status (no
+    read past the end, no partial model)."""
+    m = syn.small_aniso()
+    name = str(tmp_path / "mod")
+    m.write(name)
+    good = {ext: open(name + ext).read() for ext in (".fwd", ".dat")}
+    cases = []
+    for ext, txt in good.items():
+        lines = txt.splitlines(keepends=True)
+        for frac in (0.05, 0.3, 0.6, 0.95):
+            # cut at the last whitespace before the point: whole tokens missing (a cut
+            # inside a number can leave a shorter valid number, as in any reader)
+            cut = txt[: int(len(txt) * frac)]
+            cases.append((ext, cut[: max(cut.rfind(" "), cut.rfind("\n"), 0)]))
+        cases.append((ext, "".join(lines[:-1])))              # last line missing
+        cases.append((ext, ""))                                # empty file
+        tok = txt.split()
+        tok[len(tok) // 2] = "abc"                             # a non-number in the middle
+        cases.append((ext, " ".join(tok)))
+    for ext, bad in cases:
+        for e2, t2 in good.items():
+            open(name + e2, "w").write(bad if e2 == ext else t2)
+        try:
+            S.Model.read(name)
+        except capi.SfdxError as e:
+            assert e.code in (1, 7), (ext, len(bad), e.code)
+        else:
+            raise AssertionError(f"{ext} of {len(bad)} bytes accepted")
