@@ -233,3 +233,23 @@ def test_reader_rejects_truncated_and_malformed_files(tmp_path):
             assert e.code in (1, 7), (ext, len(bad), e.code)
         else:
             raise AssertionError(f"{ext} of {len(bad)} bytes accepted")
+
+
+def test_sfd3d_host_reports_usage_and_input_errors(tmp_path):
+    """The drop-in host `sfd3d <model> [level eps]` (sfd_excmg.f90:20-58): usage without
+    a model name, an error status for missing or invalid model files, all before any
+    device work."""
+    import subprocess
+    exe = os.path.join(os.path.dirname(capi.library_path()), "sfd3d")
+    assert os.path.exists(exe), "sfd3d is built beside libsfdx.so"
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 2 and "usage" in r.stderr
+    r = subprocess.run([exe, str(tmp_path / "absent")], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 1 and "missing or malformed" in r.stderr, r.stderr
+    m = syn.small_aniso()
+    m.level = 2  # read_input rejects level < 3 (file_opt.f90:22-25)
+    name = str(tmp_path / "lev2")
+    m.write(name)
+    r = subprocess.run([exe, name], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 1 and "invalid argument" in r.stderr, r.stderr
+    assert not os.path.exists(name + ".res")
