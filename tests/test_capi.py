@@ -253,3 +253,21 @@ def test_sfd3d_host_reports_usage_and_input_errors(tmp_path):
     r = subprocess.run([exe, name], capture_output=True, text=True, timeout=60)
     assert r.returncode == 1 and "invalid argument" in r.stderr, r.stderr
     assert not os.path.exists(name + ".res")
+
+
+def test_opts_layout_agrees_across_c_header_fortran_shim_and_ctypes():
+    """struct sfdx_opts has one layout in include/sfdx.h, the bind(c) type of the
+    Fortran shim and the ctypes mirror: same fields, same order, same C types."""
+    hdr = open(os.path.join(ROOT, "include", "sfdx.h")).read()
+    body = re.search(r"typedef struct sfdx_opts \{(.*?)\} sfdx_opts;", hdr, re.S).group(1)
+    body = re.sub(r"/\*.*?\*/", "", body, flags=re.S)
+    c_fields = [(n, t) for t, n in re.findall(r"\b(int|double)\s+(\w+)\s*;", body)]
+    f90 = open(os.path.join(ROOT, "sfd_excmg_gb300", "fortran", "sfdx_shim.f90")).read()
+    ftype = re.search(r"type, bind\(c\) :: sfdx_opts(.*?)end type", f90, re.S).group(1)
+    kind = {"integer(c_int)": "int", "real(c_double)": "double"}
+    f_fields = [(n, kind[k]) for k, n in re.findall(r"(integer\(c_int\)|real\(c_double\))\s*::\s*(\w+)", ftype)]
+    ct = {ctypes.c_int: "int", ctypes.c_double: "double"}
+    py_fields = [(n, ct[t]) for n, t in capi.Opts._fields_]
+    assert len(c_fields) >= 20
+    assert f_fields == c_fields
+    assert py_fields == c_fields
