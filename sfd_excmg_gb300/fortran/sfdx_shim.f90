@@ -4,8 +4,9 @@
 ! caller's arrays are passed without copies (Fortran sigma(ncell,6) and
 ! ex(2*nl,nf) are exactly the C layouts [6][ncell] and [nf][2][nl]).
 !
-! Build (needs a Fortran 2003 compiler, not present in the build image):
-!   gfortran -c sfdx_shim.f90 && gfortran ... sfdx_shim.o -L<lib dir> -lsfdx
+! Build (needs a Fortran 2003 compiler, not present in the build image), after
+! global_para.f90, whose module global_parameter supplies fwd_acc:
+!   gfortran -c global_para.f90 sfdx_shim.f90 && gfortran ... sfdx_shim.o -L<lib dir> -lsfdx
 module sfdx
   use iso_c_binding
   implicit none
@@ -77,6 +78,7 @@ contains
   ! allocation of ex(nl*2, nf); level/slv/eps come from the .fwd file or argv
   ! exactly as before.  fwd_acc (global_para.f90:19) maps to o%excmg.
   subroutine fwd_solver(modelname, a, b, c, nair, level, slv, eps, sigma, freq, ex)
+    use global_parameter, only: fwd_acc   ! the reference's switch (global_para.f90:19)
     character(len=30) :: modelname
     real(c_double), allocatable :: a(:), b(:), c(:), sigma(:,:), freq(:)
     integer :: nair, level, slv
@@ -93,6 +95,8 @@ contains
     o%level = level
     o%eps = eps
     o%solver = slv
+    o%excmg = 0
+    if (fwd_acc /= 0) o%excmg = 1         ! doublemode_acc instead of doublemode_nor
     rc = sfdx_fwd_solve(o, nx, ny, nz, nair, a, b, c, sigma, nf, freq, ex, c_null_ptr, c_null_ptr)
     if (rc /= SFDX_OK) then
       write(*,*) 'sfdx_fwd_solve failed, status ', rc
