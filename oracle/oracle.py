@@ -72,12 +72,13 @@ def lib():
                 ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, c_double_p, c_double_p, c_double_p,
                 c_double_p, ctypes.c_char, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                 ctypes.c_int64, ctypes.c_void_p, c_int64_p, c_int32_p, ctypes.c_void_p, ctypes.c_void_p,
-                ctypes.c_double, ctypes.c_int, c_double_p]
+                ctypes.c_double, ctypes.c_int, c_double_p, ctypes.c_int64]
             L.orc_bicgstab_fixed.restype = ctypes.c_int
             L.orc_extint_v.restype = ctypes.c_int
             L.orc_post_process.restype = ctypes.c_int
             L.orc_div_correc.restype = ctypes.c_int
             L.orc_ssor_apply.restype = ctypes.c_int
+            L.orc_ilu_apply.restype = ctypes.c_int
     return _LIB
 
 
@@ -121,7 +122,7 @@ class OracleModel:
 @dataclass
 class OracleOpts:
     excmg: bool = False          # fwd_acc (global_para.f90:19), default 0
-    pre: str = "S"               # pre_type (global_para.f90:18)
+    pre: str = "S"               # pre_type (global_para.f90:18): 'S', 'J', 'I' (ILU(0)) or 'M'
     div_cor: bool = True         # global_para.f90:8
     corr_intv: int = 200         # global_para.f90:9
     corr_tol: float = 1e-3       # global_para.f90:10
@@ -191,8 +192,9 @@ def mesh_coarsen(a, b, c, sigma, k, quirk=True):
     return a1, b1, c1, nc
 
 
-def solve_krylov(solver, mesh, K, rhs, x0, eps, itmax, opts: OracleOpts):
-    """Bicg_stab_p (solver 1) or pgpbicg (solver 3) on the CSR system."""
+def solve_krylov(solver, mesh, K, rhs, x0, eps, itmax, opts: OracleOpts, ilu_band=0):
+    """Bicg_stab_p (solver 1) or pgpbicg (solver 3) on the CSR system.  ilu_band is
+    idd(2) of the caller, used by the ILU(0) preconditioner (opts.pre = 'I') only."""
     nx, ny, nz, a, b, c, sigma = mesh
     x = _z(x0).copy()
     err = np.zeros(itmax + 1)
@@ -202,8 +204,23 @@ def solve_krylov(solver, mesh, K, rhs, x0, eps, itmax, opts: OracleOpts):
     it = lib().orc_solve(solver, nx, ny, nz, _p(_d(a)), _p(_d(b)), _p(_d(c)), _p(_d(sigma)), opts.pre.encode(),
                          int(opts.div_cor), opts.corr_intv, opts.corr_tol, opts.omega, K.shape[0],
                          km.ctypes.data, _p(ia, c_int64_p), _p(ja, c_int32_p), _z(rhs).ctypes.data, x.ctypes.data,
-                         eps, itmax, _p(err))
+                         eps, itmax, _p(err), ctypes.c_int64(ilu_band))
     return x, int(it), err[:itmax]
+
+
+def ilu_apply(K, y, band=0):
+    """zilu0 + lusol (pre_type = 'I'): x = (LU)^-1 y with the band filter of zilu0
+    (band = idd(2); 0 keeps every entry)."""
+    ia = np.ascontiguousarray(K.indptr, dtype=np.int64)
+    ja = np.ascontiguousarray(K.indices, dtype=np.int32)
+    km = _z(K.data)
+    x = np.zeros(K.shape[0], np.complex128)
+    ierr = lib().orc_ilu_apply(ctypes.c_int64(K.shape[0]), km.ctypes.data_as(ctypes.c_void_p), _p(ia, c_int64_p),
+                               _p(ja, c_int32_p), ctypes.c_int64(band), _z(y).ctypes.data_as(ctypes.c_void_p),
+                               x.ctypes.data_as(ctypes.c_void_p))
+    if ierr:
+        raise ZeroDivisionError(f"zilu0: zero pivot in row {ierr}")
+    return x
 
 
 def ssor_apply(K, y, omega=1.0):
@@ -293,10 +310,11 @@ def doublemode_nor(nx, ny, nz, a, b, c, sigma, ff, mid, slv, tol, opts: OracleOp
         return u1, u2, info
     maxit = opts.maxit_plain
     nl = K.shape[0]
+    # idd(2) = nl (fdfe_main.f90:994): the ILU(0) keeps every entry
     u1, it1, _ = solve_krylov(slv if slv in (1, 3) else 1, mesh, K, p1, np.zeros(nl) if x0 is None else x0[0],
-                              tol, maxit, opts)
+                              tol, maxit, opts, nl)
     u2, it2, _ = solve_krylov(slv if slv in (1, 3) else 1, mesh, K, p2, np.zeros(nl) if x0 is None else x0[1],
-                              tol, maxit, opts)
+                              tol, maxit, opts, nl)
     info.iters = [it1, it2]
     return u1, u2, info
 
@@ -334,8 +352,9 @@ def doublemode_acc(model: OracleModel, ff, opts: OracleOpts, n_grid=None, eps=No
             raise FloatingPointError("NaN value found in the RHS(p1)")
         mesh = (nx, ny, nz, a1, b1, c1, sf)
         slv = model.solver if model.solver in (1, 3) else 1
-        x1, it1, _ = solve_krylov(slv, mesh, K, p1, u21, tol, opts.maxit_level, opts)
-        x2, it2, _ = solve_krylov(slv, mesh, K, p2, u22, tol, opts.maxit_level, opts)
+        band = (nx + 1) * (ny + 1) * (nz + 1)  # idd(2) = np (fdfe_main.f90:1413)
+        x1, it1, _ = solve_krylov(slv, mesh, K, p1, u21, tol, opts.maxit_level, opts, band)
+        x2, it2, _ = solve_krylov(slv, mesh, K, p2, u22, tol, opts.maxit_level, opts, band)
         infos.append(LevelInfo(i, nx, ny, nz, [it1, it2]))
         u01, u02, u11, u12 = u11, u12, x1, x2
     return u11, u12, infos

@@ -577,6 +577,72 @@ static void jacobifac(int64_t n, const zc *a, const int64_t *ia0, const int32_t 
             if (ja0[j] == i) P->mj[i] = a[j];
 }
 
+/* zilu0 (div_correc.f90:223-317): ILU(0) in MSR form, pre_type = 'I'.  Only
+ * columns within the band |jcol - ii - idd(1)| <= idd(2), idd(1) <= jcol <=
+ * idd(3) enter the factor (:258).  The solvers receive idd = (1, nl, nl, ...)
+ * from doublemode_nor (fdfe_main.f90:994: every entry kept) and (1, np, nl,
+ * ...) from doublemode_acc (:1413: couplings more than np columns apart, the
+ * Ex-Ez blocks, are left out).  band <= 0 keeps every entry.  The elimination
+ * runs over the entries stored before the diagonal in CSR order, which are the
+ * columns < ii because dcfast writes sorted rows.  Returns the zero-pivot row
+ * (1-based) or 0. */
+static int zilu0(int64_t n, int64_t band, const zc *a, const int64_t *ia0, const int32_t *ja0, precond_t *P) {
+    int64_t nnz = ia0[n];
+    if (band <= 0) band = n;
+    P->n = n;
+    P->w = 1.0;
+    P->pre = 'I';
+    P->mj = NULL;
+    P->mc = NULL;
+    P->alu = (zc *)calloc((size_t)(nnz + n + 2), sizeof(zc));
+    P->jlu = (int64_t *)calloc((size_t)(nnz + n + 2), sizeof(int64_t));
+    P->ju = (int64_t *)calloc((size_t)(n + 2), sizeof(int64_t));
+    int64_t *iw = (int64_t *)calloc((size_t)(n + 2), sizeof(int64_t));
+    zc *alu = P->alu;
+    int64_t *jlu = P->jlu, *ju = P->ju;
+    int64_t ju0 = n + 2;
+    jlu[1] = ju0;
+    int ierr = 0;
+    for (int64_t ii = 1; ii <= n && !ierr; ii++) {
+        const int64_t js = ju0;
+        for (int64_t j = ia0[ii - 1] + 1; j <= ia0[ii]; j++) {
+            const int64_t jcol = (int64_t)ja0[j - 1] + 1;
+            const int64_t off = jcol - ii - 1;
+            if (!((off < 0 ? -off : off) <= band && jcol <= n && jcol >= 1)) continue;
+            if (jcol == ii) {
+                alu[ii] = a[j - 1];
+                iw[jcol] = ii;
+                ju[ii] = ju0;
+            } else {
+                alu[ju0] = a[j - 1];
+                jlu[ju0] = jcol;
+                iw[jcol] = ju0;
+                ju0++;
+            }
+        }
+        jlu[ii + 1] = ju0;
+        const int64_t jf = ju0 - 1, jm = ju[ii] - 1;
+        for (int64_t j = js; j <= jm; j++) {  /* row ii of L: eliminate with the rows above */
+            const int64_t jrow = jlu[j];
+            const zc tl = alu[j] * alu[jrow];
+            alu[j] = tl;
+            for (int64_t jj = ju[jrow]; jj <= jlu[jrow + 1] - 1; jj++) {
+                const int64_t jw = iw[jlu[jj]];
+                if (jw != 0) alu[jw] = alu[jw] - tl * alu[jj];
+            }
+        }
+        if (alu[ii] == 0) {
+            ierr = (int)ii;
+            break;
+        }
+        alu[ii] = 1.0 / alu[ii];
+        iw[ii] = 0;
+        for (int64_t i = js; i <= jf; i++) iw[jlu[i]] = 0;
+    }
+    free(iw);
+    return ierr;
+}
+
 static void precond_free(precond_t *P) {
     free(P->alu);
     free(P->jlu);
@@ -657,6 +723,19 @@ static void psolve(const precond_t *P, const zc *y, zc *xo) {
     const int64_t *jlu = P->jlu, *ju = P->ju;
     double w = P->w;
     zc *x = xo - 1; /* 1-based view */
+    if (P->pre == 'I') {  /* lusol with pre_type = 'I': unit L, then U with the inverted pivots */
+        for (int64_t i = 1; i <= n; i++) {
+            zc xi = y[i - 1];
+            for (int64_t k = jlu[i]; k <= ju[i] - 1; k++) xi = xi - alu[k] * x[jlu[k]];
+            x[i] = xi;
+        }
+        for (int64_t i = n; i >= 1; i--) {
+            zc xi = x[i];
+            for (int64_t k = ju[i]; k <= jlu[i + 1] - 1; k++) xi = xi - alu[k] * x[jlu[k]];
+            x[i] = alu[i] * xi;
+        }
+        return;
+    }
     for (int64_t i = 1; i <= n; i++) {
         zc xi = y[i - 1];
         for (int64_t k = jlu[i]; k <= ju[i] - 1; k++) xi = xi - alu[k] * x[jlu[k]];
@@ -668,6 +747,15 @@ static void psolve(const precond_t *P, const zc *y, zc *xo) {
         for (int64_t k = ju[i]; k <= jlu[i + 1] - 1; k++) xi = xi - alu[k] * x[jlu[k]];
         x[i] = alu[i] * xi * w;
     }
+}
+
+/* Exported single application of the ILU(0) preconditioner (tests). */
+int orc_ilu_apply(int64_t n, const zc *a, const int64_t *ia, const int32_t *ja, int64_t band, const zc *y, zc *x) {
+    precond_t P;
+    int ierr = zilu0(n, band, a, ia, ja, &P);
+    if (ierr == 0) psolve(&P, y, x);
+    precond_free(&P);
+    return ierr;
 }
 
 /* Exported single application of the SSOR preconditioner (tests). */
@@ -962,6 +1050,7 @@ typedef struct {
     char pre;
     int div_cor, corr_intv;
     double corr_tol, omega;
+    int64_t ilu_band; /* pre = 'I': idd(2) of the caller; 0 keeps every entry */
 } korc_opts;
 
 /* multi-colour preconditioner data: one per calling thread, colour buffer reused across solves */
@@ -990,6 +1079,7 @@ static int make_precond(const korc_opts *o, int64_t n, const zc *K, const int64_
         P->mc = &t_mc;
         return 0;
     }
+    if (o->pre == 'I') return zilu0(n, o->ilu_band, K, ia, ja, P);
     return ssorfac(n, K, ia, ja, o->omega, P);
 }
 
@@ -1151,8 +1241,9 @@ int orc_gpbicg(const korc_opts *o, int64_t n, const zc *K, const int64_t *ia, co
 /* Flat-argument wrappers for ctypes. */
 int orc_solve(int solver, int nx, int ny, int nz, const double *a, const double *b, const double *c, const double *sig,
               char pre, int div_cor, int corr_intv, double corr_tol, double omega, int64_t n, const zc *K,
-              const int64_t *ia, const int32_t *ja, const zc *rhs, zc *x, double eps, int itmax, double *err_rec) {
-    korc_opts o = {nx, ny, nz, a, b, c, sig, pre, div_cor, corr_intv, corr_tol, omega};
+              const int64_t *ia, const int32_t *ja, const zc *rhs, zc *x, double eps, int itmax, double *err_rec,
+              int64_t ilu_band) {
+    korc_opts o = {nx, ny, nz, a, b, c, sig, pre, div_cor, corr_intv, corr_tol, omega, ilu_band};
     if (solver == 3) return orc_gpbicg(&o, n, K, ia, ja, rhs, x, eps, itmax, err_rec);
     return orc_bicgstab(&o, n, K, ia, ja, rhs, x, eps, itmax, err_rec);
 }
@@ -1161,7 +1252,7 @@ int orc_solve(int solver, int nx, int ny, int nz, const double *a, const double 
  * iterations (no stopping test) and return; used to time the per-iteration
  * cost of the serial SSOR-BiCGStab path on large meshes. */
 int orc_bicgstab_fixed(int64_t n, const zc *K, const int64_t *ia, const int32_t *ja, const zc *b, zc *x, int iters) {
-    korc_opts o = {0, 0, 0, NULL, NULL, NULL, NULL, 'S', 0, 200, 1e-3, 1.0};
+    korc_opts o = {0, 0, 0, NULL, NULL, NULL, NULL, 'S', 0, 200, 1e-3, 1.0, 0};
     double *err = (double *)calloc((size_t)iters + 1, sizeof(double));
     int r = orc_bicgstab(&o, n, K, ia, ja, b, x, -1.0, iters, err);
     free(err);

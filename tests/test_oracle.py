@@ -4,8 +4,9 @@ The reference ships no golden vectors and cannot be compiled here (ifort +
 MKL), so the oracle's restatement is pinned by answers known independently:
 the analytic homogeneous and layered 1-D responses, the half-space apparent
 resistivity and phase of the 3-D discretisation, a 3-D solve of a 1-D model,
-exact reproduction of constant fields by the EXCMG prolongation, and the
-algebraic identities the gradient-space correction relies on.
+exact reproduction of constant fields by the EXCMG prolongation, the
+algebraic identities the gradient-space correction relies on, and the
+identities of the ILU(0) factor (zilu0).
 """
 import numpy as np
 import pytest
@@ -232,3 +233,66 @@ def test_volume_weighted_operator_is_complex_symmetric(ff):
     V = np.where(V > 0, V, 1.0)
     VK = (K.multiply(V[:, None])).tocsr()
     assert abs(VK - VK.T).max() <= 1e-12 * abs(VK).max()
+
+
+def _tiny_aniso_system(ff=1.0, seed=3):
+    """Assembled curl-curl system of a 4x4x6-cell anisotropic model with two air layers
+    (430 edges): small enough for dense checks of a preconditioner."""
+    rng = np.random.default_rng(seed)
+    nx, ny, nz = 4, 4, 6
+    a, b = np.full(nx, 100.0), np.full(ny, 120.0)
+    c = np.array([200.0, 100, 50, 50, 80, 120])
+    ncell = nx * ny * nz
+    sig = np.zeros((6, ncell))
+    sig[0:3] = 10 ** rng.uniform(-3, -1, (3, ncell))
+    sig[3:6] = 0.2 * sig[0] * rng.uniform(-1, 1, (3, ncell))
+    sig[:, : nx * ny * 2] = 0
+    sig[0:3, : nx * ny * 2] = 1e-8
+    edc, _, _ = O.mt1d_anl(ff, O.column_conv(sig, nx, ny, nz), c)
+    K, p1, _ = O.assemble(nx, ny, nz, a, b, c, sig, ff, edc)
+    return (nx, ny, nz, a, b, c, sig), K, p1
+
+
+def test_ilu0_is_the_exact_lu_of_a_tridiagonal_matrix():
+    """zilu0 + lusol (pre_type 'I'): without fill-in ILU(0) is the LU factorisation."""
+    rng = np.random.default_rng(0)
+    n = 50
+    import scipy.sparse as sp
+    d = 4 + rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    T = sp.diags([rng.standard_normal(n - 1) + 0j, d, rng.standard_normal(n - 1) + 0j], [-1, 0, 1], format="csr")
+    y = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    np.testing.assert_allclose(O.ilu_apply(T, y), np.linalg.solve(T.toarray(), y), rtol=1e-13, atol=1e-13)
+
+
+@pytest.mark.parametrize("band_kind", ["all", "np"])
+def test_ilu0_reproduces_the_matrix_on_its_band_pattern(band_kind):
+    """The defining property of ILU(0): M = LU equals A on every entry the factor keeps.
+    zilu0 keeps the columns with |jcol - ii - 1| <= idd(2): every entry for
+    doublemode_nor (idd(2) = nl), only those within np for doublemode_acc (idd(2) = np),
+    which leaves out the Ex-Ez couplings."""
+    mesh, K, _ = _tiny_aniso_system()
+    nx, ny, nz = mesh[:3]
+    n = K.shape[0]
+    band = 0 if band_kind == "all" else (nx + 1) * (ny + 1) * (nz + 1)
+    eye = np.eye(n)
+    M = np.linalg.inv(np.stack([O.ilu_apply(K, eye[:, j], band) for j in range(n)], axis=1))
+    A = K.toarray()
+    i, j = np.nonzero(A)
+    keep = np.abs(j - i - 1) <= (band if band else n)
+    scale = np.abs(A).max()
+    assert np.abs(M[i[keep], j[keep]] - A[i[keep], j[keep]]).max() <= 1e-12 * scale
+    if band_kind == "np":
+        assert (~keep).sum() > 0
+        assert np.abs(M[i[~keep], j[~keep]] - A[i[~keep], j[~keep]]).max() > 1e-6 * scale
+
+
+def test_bicgstab_with_ilu0_solves_a_small_system():
+    """pre = 'I' is wired through Bicg_stab_p: on the 430-edge system the recurrence
+    residual reaches 1e-7 within a few iterations and the true residual agrees.  (Both
+    ILU(0) and SSOR stagnate near 1e-9 on this tiny model with air layers; the
+    tolerance stays above that.)"""
+    mesh, K, p1 = _tiny_aniso_system()
+    x, it, _ = O.solve_krylov(1, mesh, K, p1, np.zeros(K.shape[0]), 1e-7, 100,
+                              O.OracleOpts(pre="I", div_cor=False), ilu_band=0)
+    assert it < 30
+    assert np.linalg.norm(K @ x - p1) <= 2e-7 * np.linalg.norm(p1)
