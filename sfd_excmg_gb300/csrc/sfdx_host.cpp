@@ -8,6 +8,7 @@
 #include <algorithm>
 #include <cmath>
 #include <complex>
+#include <cctype>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -401,23 +402,58 @@ int impedance_adjoint_source(SurfaceGrad& g, int nair, const double* a, const do
 // -------------------------------------------------------------------- files
 // read_input (file_opt.f90:8-95) + read_topo (:97-128): list-directed reads
 // are whitespace-separated numbers; the first line is a free-text title.
+// Values of Fortran list-directed input (the reference reads its files with
+// read(unit,*)): separated by blanks, line ends or commas; D or d as the
+// exponent letter; r*c repeats the constant c r times.
 struct Tok {
     FILE* f;
+    double rep_val = 0;
+    long rep_left = 0;  // values of an r*c item still to hand out
     explicit Tok(FILE* ff) : f(ff) {}
     bool skip_line() {
+        rep_left = 0;
         int ch;
         while ((ch = fgetc(f)) != EOF && ch != '\n') {
         }
         return ch != EOF;
     }
-    bool num(double& v) {
-        char buf[128];
-        if (fscanf(f, "%127s", buf) != 1) return false;
-        for (char* p = buf; *p; p++)
+    static bool parse(char* s, double& v) {
+        for (char* p = s; *p; p++)
             if (*p == 'd' || *p == 'D') *p = 'e';  // Fortran exponent letter
         char* end;
-        v = strtod(buf, &end);
-        return end != buf;
+        v = strtod(s, &end);
+        return end != s && *end == '\0';
+    }
+    bool token(char* buf, int cap) {
+        int ch, n = 0;
+        while ((ch = fgetc(f)) != EOF && (isspace(ch) || ch == ','))
+            ;
+        while (ch != EOF && !isspace(ch) && ch != ',') {
+            if (n + 1 >= cap) return false;
+            buf[n++] = (char)ch;
+            ch = fgetc(f);
+        }
+        buf[n] = '\0';
+        return n > 0;
+    }
+    bool num(double& v) {
+        if (rep_left > 0) {
+            rep_left--;
+            v = rep_val;
+            return true;
+        }
+        char buf[128];
+        if (!token(buf, (int)sizeof buf)) return false;
+        if (char* star = strchr(buf, '*')) {  // r*c
+            *star = '\0';
+            char* end;
+            const long r = strtol(buf, &end, 10);
+            if (end == buf || *end != '\0' || r < 1 || !parse(star + 1, rep_val)) return false;
+            rep_left = r - 1;
+            v = rep_val;
+            return true;
+        }
+        return parse(buf, v);
     }
     bool inum(int& v) {
         double d;

@@ -271,3 +271,33 @@ def test_opts_layout_agrees_across_c_header_fortran_shim_and_ctypes():
     assert len(c_fields) >= 20
     assert f_fields == c_fields
     assert py_fields == c_fields
+
+
+def test_reader_accepts_fortran_list_directed_forms(tmp_path):
+    """The reference reads its inputs with list-directed read(unit,*): commas as
+    separators, D exponents and r*c repeat counts read as the plain file does, and a
+    value with trailing characters is an error."""
+    m = syn.small_aniso()
+    m.a[:] = 50.0
+    name = str(tmp_path / "plain")
+    m.write(name)
+    r0 = S.Model.read(name)
+    lines = open(name + ".fwd").read().splitlines(keepends=True)
+    lines[1] = "%d, %s, %d, %d\n" % (m.level, ("%.6E" % m.eps).replace("E", "D"), m.solver, m.out_type)
+    lines[3] = "%d*5.0D+01\n" % m.nx
+    lines[7] = "6*0\n"
+    alt = str(tmp_path / "listdir")
+    open(alt + ".fwd", "w").write("".join(lines))
+    open(alt + ".dat", "w").write(open(name + ".dat").read().replace(" ", ", "))
+    r1 = S.Model.read(alt)
+    assert (r1.level, r1.eps, r1.solver) == (r0.level, r0.eps, r0.solver)
+    for f in ("a", "b", "c", "sigma", "freq", "recv"):
+        np.testing.assert_array_equal(getattr(r1, f), getattr(r0, f), err_msg=f)
+    lines[3] = "50.0x " * m.nx + "\n"
+    open(alt + ".fwd", "w").write("".join(lines))
+    try:
+        S.Model.read(alt)
+    except capi.SfdxError as e:
+        assert e.code == 7
+    else:
+        raise AssertionError("a value with trailing characters must be rejected")
