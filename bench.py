@@ -21,12 +21,12 @@ sfdx_impedance.  The per-step working set (~4 GB) is far larger than L2, so
 no flush is needed between steps.  The same solve in plain FP64 is timed
 after the run (fp64_solves_per_s) and the impedances of the two compared.
 
-The line also carries `adjoint`: the cfg5 gradient case (the cfg2 mesh without
+The line also carries `adjoint`: the misfit-gradient case (the same mesh without
 hills, isotropic log10 rho Gaussian random field, 6 frequencies, data from a
 perturbed model with 2 % noise) -- forward solve + misfit and adjoint solves +
 per-cell contraction timed with CUDA events, the ratio of the two, and the
 mixed-precision gradient against the FP64 GPU adjoint (`--fd-cells N` adds
-central differences at N random cells).  `--workload cfg3` times 8 models of
+central differences at N random cells).  `--workload multi-model` times 8 models of
 uneven meshes (256 systems) solved concurrently through sfdx_plan_solve_batch
 against the same plans one after another.
 
@@ -165,12 +165,12 @@ def solve_opts(precision, solver="bicgstab", div_cor=2, eps=1e-10, corr_intv=Non
 # (128x128x96 core cells, 4 levels, tol 1e-7) and the reference's own DTM1
 # example (4 levels, tol 1e-10) whose CPU times the reference publishes.
 WORKLOADS = {
-    "cfg2": ("cfg2: anisotropic 20-block model with Gaussian hills, 64x64x48 core cells of 50 m (80x80x80, "
+    "aniso-hills": ("aniso-hills: anisotropic 20-block model with Gaussian hills, 64x64x48 core cells of 50 m (80x80x80, "
              "1,574,640 edges), 8 freqs 1e-3..1e3 Hz x 2 pols, EXCMG 3 levels, tol {eps:g}, 32x32 receivers", 1e-10),
-    "cfg4": ("cfg4: 128x128x96 core cells of 25 m + 16 padding per side, 12 bottom, 36 air (160x160x144, "
+    "large-inclusions": ("large-inclusions: 128x128x96 core cells of 25 m + 16 padding per side, 12 bottom, 36 air (160x160x144, "
              "11,203,024 edges), 3 layers + 10 anisotropic boxes, 6 freqs 0.01..100 Hz x 2 pols, EXCMG 4 levels, "
              "tol {eps:g}", 1e-7),
-    "cfg3": ("cfg3: 8 models per batch, cells per axis drawn from {{48,...,96}} (padding and air included), isotropic "
+    "multi-model": ("multi-model: 8 models per batch, cells per axis drawn from {{48,...,96}} (padding and air included), isotropic "
              "log10 rho GRF (mean 2, std 0.5, corr 5 cells), 16 freqs 1e-3..1e3 Hz x 2 pols = 256 systems, EXCMG 3 "
              "levels, tol {eps:g}, one host thread + stream per model", 1e-10),
     "dtm1": ("dtm1: the reference's DTM1.0 example (input.py), 128x128x192 cells incl. 64 air layers "
@@ -179,19 +179,19 @@ WORKLOADS = {
 # Reference CPU time for DTM1 (EXCMG, 4 levels, tol 1e-10; Xeon Gold 6248R, serial):
 # 93.62 + 76.84 + 45.95 + 63.31 s for the four frequencies x two polarisations.
 PUBLISHED_SOLVES_PER_S = {"dtm1": 8.0 / (93.62 + 76.84 + 45.95 + 63.31)}
-# DRAM bytes (read + write) of one multi-colour SSOR application on the cfg2
+# DRAM bytes (read + write) of one multi-colour SSOR application on the aniso-hills
 # finest level, summed over its 11 colour launches from one ncu capture
-# (profiles/mc_ssor_sweep_cfg2.md): 1528.6 MB read + 128.2 MB written.
-SSOR_TRAFFIC = {"cfg2": 1656834048}
+# (profiles/mc_ssor_sweep_aniso_hills.md): 1528.6 MB read + 128.2 MB written.
+SSOR_TRAFFIC = {"aniso-hills": 1656834048}
 
 
 def make_workload(name):
     from sfd_excmg_gb300 import synthetic as syn
-    if name == "cfg4":
-        return syn.config4(seed=0)
+    if name == "large-inclusions":
+        return syn.large_inclusions(seed=0)
     if name == "dtm1":
         return syn.dtm1()
-    return syn.config2(seed=0)
+    return syn.aniso_hills(seed=0)
 
 
 def cpu_sample(model, freqs_idx, threads, iters=REF_SAMPLE_ITERS):
@@ -235,9 +235,9 @@ def cpu_sample(model, freqs_idx, threads, iters=REF_SAMPLE_ITERS):
 
 
 def reference_iterations():
-    """Iterations the reference algorithm needs per cfg2 system (tests/golden/cfg2_reference, made by
-    tests/golden/make_cfg2_reference.py: plain path, zero guess, lexicographic SSOR + divergence correction)."""
-    d = os.path.join(ROOT, "tests", "golden", "cfg2_reference")
+    """Iterations the reference algorithm needs per aniso-hills system (tests/golden/aniso_hills_reference, made by
+    tests/golden/make_aniso_hills_reference.py: plain path, zero guess, lexicographic SSOR + divergence correction)."""
+    d = os.path.join(ROOT, "tests", "golden", "aniso_hills_reference")
     its = []
     if os.path.isdir(d):
         for fn in sorted(os.listdir(d)):
@@ -251,7 +251,7 @@ def run_reference(args, rank, world):
     if rank != 0:
         return
     from sfd_excmg_gb300 import synthetic as syn
-    m = syn.config2(seed=0)
+    m = syn.aniso_hills(seed=0)
     ns = 2 * m.nf
     threads = max(1, min(ns, os.cpu_count() or 1))
     its = reference_iterations()
@@ -272,12 +272,12 @@ def run_reference(args, rank, world):
         "impl": "reference", "metric": "MT solves/s", "value": v, "unit": "solves/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
         "ms_per_step": float(np.median([s[0] for s in samples]) * 1e3),
-        "config": {"workload": WORKLOADS["cfg2"][0].format(eps=WORKLOADS["cfg2"][1]),
+        "config": {"workload": WORKLOADS["aniso-hills"][0].format(eps=WORKLOADS["aniso-hills"][1]),
                    "solver": "SSOR-BiCGStab FP64 CSR (reference algorithm, oracle restatement)"},
         "cpu_baseline": {"value": v, "unit": "solves/s", "cores": threads, "kind": "port",
                          "sample": (f"per system: finest-level assembly + {REF_SAMPLE_ITERS} SSOR-BiCGStab iterations; "
                                     f"scaled by the reference algorithm's mean iteration count {n_it:.0f} "
-                                    f"(tests/golden/cfg2_reference); {threads} systems in parallel")},
+                                    f"(tests/golden/aniso_hills_reference); {threads} systems in parallel")},
         "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "data": "synthetic",
     }
@@ -378,7 +378,7 @@ def run_ours(args, rank, world, local):
         return
     dom = kern["mc_ssor_c64"]
     cpu = None
-    if args.cpu_baseline and args.workload == "cfg2":  # the iteration counts of the reference are measured on cfg2
+    if args.cpu_baseline and args.workload == "aniso-hills":  # the reference's iteration counts are measured on this workload
         its = reference_iterations()
         _, t_it, t_setup = cpu_sample(m, [0], 1)
         n_it = float(np.mean(its)) if its else float("nan")
@@ -413,7 +413,7 @@ def run_ours(args, rank, world, local):
 
 
 def adjoint_measure(S, syn, torch, stream, solver, eps, fd_cells=0, reps=2, seed=0, adj_tol=1e-8):
-    """cfg5: least-squares impedance misfit of an isotropic GRF model against data from a
+    """Adjoint case: least-squares impedance misfit of an isotropic GRF model against data from a
     perturbed model (+2 % Gaussian noise, weights 1/(0.02|Z|)^2) and its gradient
     d misfit / d log sigma by one adjoint solve per frequency and polarisation.  Times the
     forward solve (+ misfit, tolerance eps) and the adjoint (+ per-cell contraction,
@@ -423,7 +423,7 @@ def adjoint_measure(S, syn, torch, stream, solver, eps, fd_cells=0, reps=2, seed
     with fd_cells > 0, both with central differences (h = 1e-4 in log sigma) of FP64 GPU
     forward solves at that many random core cells (each perturbed solve starts from the base
     fields and solves the correction equation to a 1e-9 reduction, sfdx_plan_resolve)."""
-    m, mt = syn.config5(seed), syn.config5_true(seed)
+    m, mt = syn.grf_inversion(seed), syn.grf_inversion_true(seed)
     opts = solve_opts("mixed", solver, 2, eps, None, m.level)
     opts64 = solve_opts("fp64", solver, 2, eps, None, m.level)
     with S.Plan(mt, **opts) as pt:
@@ -477,7 +477,7 @@ def adjoint_measure(S, syn, torch, stream, solver, eps, fd_cells=0, reps=2, seed
     p64.solve(fetch=False, allow_noconv=True)
     mis64, g64, _, it64, _ = p64.misfit_grad(zobs, wts, allow_noconv=True)
     dlog64 = sg3 * g64[0:3].sum(0)
-    out = {"workload": ("cfg5: cfg2 mesh without hills (80x80x80, 1,574,640 edges), isotropic log10 rho GRF "
+    out = {"workload": ("adjoint: the aniso-hills mesh without hills (80x80x80, 1,574,640 edges), isotropic log10 rho GRF "
                         "(mean 2, std 0.5, corr 5 cells), 6 freqs 1e-3..1e3 Hz x 2 pols, 32x32 receivers, data "
                         "from a perturbed GRF model + 2 % noise, EXCMG 3 levels, tol " + f"{eps:g}"),
            "precision": "mixed", "fwd_tol": eps, "adjoint_tol": adj_tol,
@@ -525,15 +525,15 @@ def adjoint_measure(S, syn, torch, stream, solver, eps, fd_cells=0, reps=2, seed
 
 
 def run_batch(args, rank, world, local):
-    """cfg3: the 8 models solved together (sfdx_plan_solve_batch: one host thread and
+    """multi-model: the 8 models solved together (sfdx_plan_solve_batch: one host thread and
     stream per model) -- value; the same plans one after another -- sequential_solves_per_s."""
     import torch
     torch.cuda.set_device(local)
     import sfd_excmg_gb300 as S
     from sfd_excmg_gb300 import capi
     from sfd_excmg_gb300 import synthetic as syn
-    eps = args.eps if args.eps else WORKLOADS["cfg3"][1]
-    models = syn.config3(seed=rank)
+    eps = args.eps if args.eps else WORKLOADS["multi-model"][1]
+    models = syn.multi_model_batch(seed=rank)
     opts = solve_opts(args.precision, args.solver, args.div_cor, eps, args.corr_intv, 3)
     # the meshes are not square: receivers through the corrected (untransposed)
     # interpolation stencil (the reference's transposed one indexes past ny)
@@ -608,7 +608,7 @@ def run_batch(args, rank, world, local):
         "metric": "MT solves/s", "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "c64+c128" if args.precision == "mixed" else "c128", "data": "synthetic",
-        "config": {"workload": WORKLOADS["cfg3"][0].format(eps=eps),
+        "config": {"workload": WORKLOADS["multi-model"][0].format(eps=eps),
                    "meshes": [[m.nx, m.ny, m.nz] for m in models], "edges": [int(m.nl) for m in models],
                    "precision": args.precision, "solver": args.solver, "div_cor": args.div_cor,
                    "systems_per_thread": vs, "systems_per_step": ns, "cuda_graphs": bool(USE_GRAPHS),
@@ -651,9 +651,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--solver", default="gpbicg", choices=list(SOLVER))
-    ap.add_argument("--workload", default="cfg2", choices=list(WORKLOADS))
+    ap.add_argument("--workload", default="aniso-hills", choices=list(WORKLOADS))
     ap.add_argument("--eps", type=float, default=None,
-                    help="finest-level relative residual tolerance (default per workload; cfg2: 1e-10, the accuracy "
+                    help="finest-level relative residual tolerance (default per workload; aniso-hills: 1e-10, the accuracy "
                          "at which the mixed-precision impedances agree with the FP64 ones to ~1e-5)")
     ap.add_argument("--corr-intv", dest="corr_intv", type=int, default=None,
                     help="Krylov iterations of the first restart cycle of the gradient correction (default 40; each "
@@ -664,10 +664,10 @@ def main():
     ap.add_argument("--no-graphs", dest="graphs", action="store_false",
                     help="launch the Krylov iterations one by one instead of replaying captured CUDA graphs")
     ap.add_argument("--no-adjoint", dest="adjoint", action="store_false",
-                    help="skip the misfit-gradient measurement (cfg5 workload: forward vs adjoint time, FP64 check)")
+                    help="skip the misfit-gradient measurement (adjoint case: forward vs adjoint time, FP64 check)")
     ap.add_argument("--fd-cells", dest="fd_cells", type=int, default=0,
                     help="also check the gradient against central differences of FP64 forward solves at this many "
-                         "random cells (cfg5 asks for 20)")
+                         "random cells (the adjoint case asks for 20)")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     ap.add_argument("--e2e-strict", dest="e2e_allow_noconv", action="store_false")
     ap.add_argument("--profile", action="store_true",
@@ -681,7 +681,7 @@ def main():
         run_profile(args)
     elif args.impl == "reference":
         run_reference(args, rank, world)
-    elif args.workload == "cfg3":
+    elif args.workload == "multi-model":
         run_batch(args, rank, world, local)
     else:
         run_ours(args, rank, world, local)

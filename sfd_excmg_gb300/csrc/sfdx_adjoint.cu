@@ -228,7 +228,7 @@ int misfit_grad(Plan& P, int nrec, const double* recv, const double* zobs, const
     // Adjoint solve on the finest mesh from zero.  (An EXCMG cascade with the
     // same receiver functional on the coarse meshes gives a worse start: the
     // extrapolation amplifies the coarse-grid error of the point-like receiver
-    // sources -- on cfg5 it needed more iterations than the zero guess.)
+    // sources -- on the 80x80x80 GRF adjoint case it needed more iterations than the zero guess.)
     std::vector<int> its, status;
     RC(adjoint_rhs(P, F, nrec, recv, transpose, cf));
     CK(cudaMemsetAsync(P.x64.p, 0, nfine, P.st));

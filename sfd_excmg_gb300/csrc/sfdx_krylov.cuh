@@ -650,8 +650,8 @@ static int corrected_cycles(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>*
     const int cyc0 = P.o.corr_intv > 0 ? P.o.corr_intv : 25;
     // cycle length grows by 1.5 per cycle (SFDX_CYCLE_GROWTH overrides): the
     // systems still running late (high frequencies) lose less Krylov history
-    // to restarts, while the early cycles keep the correction frequent.  cfg2
-    // at 1e-10: 15.6 solves/s against 13.8 with fixed cycles (2.0: 14.9).
+    // to restarts, while the early cycles keep the correction frequent.  On the
+    // 80x80x80 anisotropic model at 1e-10: 15.6 solves/s against 13.8 with fixed cycles (2.0: 14.9).
     // TFQMR keeps fixed cycles: it stagnates without frequent corrections.
     const char* gr_env = getenv("SFDX_CYCLE_GROWTH");
     const double growth =

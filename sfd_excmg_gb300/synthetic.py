@@ -3,7 +3,7 @@
 No public model data ships with the reference beyond the DTM1 generator, so
 the benchmark and tests build their models here: seeded
 ``numpy.random.default_rng`` draws with the sizes, conductivity ranges and
-frequency bands of the five configurations.  Meshes follow the reference's
+frequency bands of the benchmark workloads.  Meshes follow the reference's
 conventions: a core of uniform cells, geometric padding, and air layers that
 mirror the deepest earth layers (read_input, file_opt.f90:52).
 """
@@ -81,7 +81,7 @@ def halfspace(n: int = 16, nair: int = 4, nz_earth: int = 12, h: float = 100.0, 
     return Model(n, n, nz, nair, a, b, c, sig, np.asarray(freqs, float), recv)
 
 
-def config1() -> Model:
+def halfspace_cube() -> Model:
     """Plain EXCMG case: 32^3 core cells of 100 m, 8 padding cells (x1.3) per side,
     8 air layers; 100 ohm-m half-space with a 1 ohm-m cube of 8^3 cells whose
     top is at 400 m depth; 4 frequencies over 0.01-100 Hz; 3 levels, tol 1e-8."""
@@ -100,7 +100,7 @@ def config1() -> Model:
     return Model(nx, ny, nz, nair, a, b, c, sig, freq, recv, level=3, eps=1e-8, solver=1, out_type=1)
 
 
-def config2(seed: int = 0, hills: bool = True, nblocks: int = 20) -> Model:
+def aniso_hills(seed: int = 0, hills: bool = True, nblocks: int = 20) -> Model:
     """Anisotropic model with topography: 64x64x48 core cells of 50 m, 8 lateral
     padding cells, 8 bottom padding cells, 24 air layers (80x80x80); 20 blocks
     with principal resistivities log-uniform in 1-1000 ohm-m and Euler angles
@@ -155,7 +155,7 @@ def grf(shape, corr_len, rng) -> np.ndarray:
     return (f - f.mean()) / (f.std() + 1e-30)
 
 
-def config3(seed: int = 0, nmodels: int = 8, nf: int = 16) -> list:
+def multi_model_batch(seed: int = 0, nmodels: int = 8, nf: int = 16) -> list:
     """Batched multi-model case: `nmodels` models whose cell counts per axis
     (padding and air included) are drawn uniformly from {48, 56, ..., 96}
     (multiples of 8, 3 levels): 50 m core cells, 4 lateral padding cells per
@@ -181,7 +181,7 @@ def config3(seed: int = 0, nmodels: int = 8, nf: int = 16) -> list:
     return models
 
 
-def config4(seed: int = 0) -> Model:
+def large_inclusions(seed: int = 0) -> Model:
     """Large single model: 128x128x96 core cells of 25 m, 16 lateral padding
     cells per side, 12 bottom padding, 36 air layers (160x160x144, 11.2 M edges);
     layers 100/10/1000 ohm-m plus 10 random anisotropic boxes (0.5-5000 ohm-m);
@@ -210,11 +210,11 @@ def config4(seed: int = 0) -> Model:
     return Model(nx, ny, nz, nair, a, b, c, sig, freq, recv, level=4, eps=1e-7, solver=1, out_type=1)
 
 
-def config5(seed: int = 0) -> Model:
-    """Adjoint case: the config-2 mesh without hills, isotropic log10(rho) Gaussian
+def grf_inversion(seed: int = 0) -> Model:
+    """Adjoint case: the aniso_hills mesh without hills, isotropic log10(rho) Gaussian
     random field (mean 2, std 0.5, correlation 5 cells), 6 frequencies."""
     rng = np.random.default_rng(seed)
-    m = config2(seed, hills=False, nblocks=0)
+    m = aniso_hills(seed, hills=False, nblocks=0)
     nze = m.nz - m.nair
     f = 2.0 + 0.5 * grf((nze, m.ny, m.nx), 5.0, rng)
     s3 = m.sigma.reshape(6, m.nz, m.ny, m.nx)
@@ -225,11 +225,11 @@ def config5(seed: int = 0) -> Model:
     return m
 
 
-def config5_true(seed: int = 0) -> Model:
-    """The model that generates the config-5 data: config5(seed) with log10(rho)
+def grf_inversion_true(seed: int = 0) -> Model:
+    """The model that generates the data of the adjoint case: grf_inversion(seed) with log10(rho)
     of the earth perturbed by 0.25 x a second Gaussian random field
     (correlation 5 cells)."""
-    m = config5(seed)
+    m = grf_inversion(seed)
     rng = np.random.default_rng(seed + 1000)
     nze = m.nz - m.nair
     s3 = m.sigma.reshape(6, m.nz, m.ny, m.nx)

@@ -1,9 +1,9 @@
 """Runs the reference algorithm (oracle restatement: lexicographic SSOR-BiCGStab with the
 divergence correction, fwd_acc=0 plain path from a zero guess, maxit 5000, tol 1e-8) on the
 synthetic config-2 model for one frequency and writes iterations, residuals, CPU seconds and
-impedances to tests/golden/cfg2_reference/f<k>.json.
+impedances to tests/golden/aniso_hills_reference/f<k>.json.
 
-Usage: python tests/golden/make_cfg2_reference.py <k> [maxit]
+Usage: python tests/golden/make_aniso_hills_reference.py <k> [maxit]
 The CPU time per iteration and the iteration counts feed the CPU-baseline leg of bench.py.
 """
 import json
@@ -23,7 +23,7 @@ from sfd_excmg_gb300 import synthetic as syn  # noqa: E402
 def main():
     k = int(sys.argv[1])
     maxit = int(sys.argv[2]) if len(sys.argv) > 2 else 5000
-    m = syn.config2(seed=0)
+    m = syn.aniso_hills(seed=0)
     ff = float(m.freq[k])
     t0 = time.process_time()
     conv = O.column_conv(m.sigma, m.nx, m.ny, m.nz)
@@ -44,7 +44,7 @@ def main():
     om = O.OracleModel(m.nx, m.ny, m.nz, m.nair, m.a, m.b, m.c, m.sigma, m.freq, m.recv)
     z, _, _ = O.post_process(om, xs[0], xs[1], ff, 1, 2)
     out["Z"] = z.tolist()
-    d = os.path.join(os.path.dirname(os.path.abspath(__file__)), "cfg2_reference")
+    d = os.path.join(os.path.dirname(os.path.abspath(__file__)), "aniso_hills_reference")
     os.makedirs(d, exist_ok=True)
     with open(os.path.join(d, f"f{k}.json"), "w") as f:
         json.dump(out, f)
