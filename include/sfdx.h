@@ -208,6 +208,15 @@ void sfdx_plan_destroy(sfdx_plan* plan);
 int sfdx_impedance(int nx, int ny, int nz, int nair, const double* a, const double* b, const double* c, int nf,
                    const double* freq, const double* ex, int nrec, const double* recv, int out_type, int quirks,
                    double* out, double* tipper);
+/* The surface fields at the receivers from which sfdx_impedance forms Z and the
+ * tippers (the arho rows of post_process / arho_interp2, fdfe_main.f90:600-700,
+ * 718-790): fields[nf][nrec][2][5] complex (interleaved doubles), (Ex, Ey, Hx,
+ * Hy, Hz) of the xy and the yx polarisation; E from the edge averages on the
+ * receiver plane, H = curl E / (i w mu), both through the 3x3 receiver
+ * stencil (quirks: SFDX_QUIRK_RX_TRANSPOSE as for sfdx_impedance). */
+int sfdx_receiver_fields(int nx, int ny, int nz, int nair, const double* a, const double* b, const double* c, int nf,
+                         const double* freq, const double* ex, int nrec, const double* recv, int quirks,
+                         double* fields);
 
 /* ------------------------------------------------------------------------
  * Component entry points (each one replaces one reference routine; all

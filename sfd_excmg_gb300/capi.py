@@ -140,6 +140,9 @@ _PROTO = {
                                       c_double_p, ctypes.c_int]),
     "sfdx_write_res": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, c_double_p, ctypes.c_int, c_double_p,
                                       c_double_p]),
+    "sfdx_receiver_fields": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, c_double_p,
+                                            c_double_p, c_double_p, ctypes.c_int, c_double_p, c_double_p,
+                                            ctypes.c_int, c_double_p, ctypes.c_int, c_double_p]),
     "sfdx_write_res_tipper": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, c_double_p, ctypes.c_int, c_double_p,
                                              c_double_p, c_double_p]),
 }

@@ -280,7 +280,8 @@ static void receiver_fields(const SurfFields* F, const RecvStencil& S, zd f[2][5
 }
 
 int impedance_from_surface(const SurfaceView& sv, const double* a, const double* b, const double* c, double ff,
-                           int nrec, const double* recv, int out_type, int transpose, double* out, double* tip) {
+                           int nrec, const double* recv, int out_type, int transpose, double* out, double* tip,
+                           zd* fields) {
     const int nx = sv.nx, ny = sv.ny;
     const zd iwm = zd(0, 1) * 2.0 * kPi * ff * kMu;
     SurfFields F[2];
@@ -292,6 +293,9 @@ int impedance_from_surface(const SurfaceView& sv, const double* a, const double*
         HRC(receiver_stencil(nx, ny, aax, bby, recv[r], recv[(size_t)nrec + r], transpose, S));
         zd f[2][5];
         receiver_fields(F, S, f);
+        if (fields)
+            for (int p = 0; p < 2; p++)
+                for (int q = 0; q < 5; q++) fields[(size_t)r * 10 + p * 5 + q] = f[p][q];
         zd det = f[0][2] * f[1][3] - f[1][2] * f[0][3];
         zd zxy = (f[1][0] * f[0][2] - f[0][0] * f[1][2]) / det;
         zd zyx = (f[0][1] * f[1][3] - f[1][1] * f[0][3]) / det;

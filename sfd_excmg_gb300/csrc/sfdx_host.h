@@ -37,8 +37,11 @@ struct SurfaceGrad {
     std::complex<double>& ez(int p, int i, int j) { return ezs[p][(size_t)j * (nx + 1) + i]; }
 };
 
+// fields (optional): [nrec][2][5] complex, (Ex, Ey, Hx, Hy, Hz) of each
+// polarisation interpolated to the receiver (the arho rows of post_process).
 int impedance_from_surface(const SurfaceView& sv, const double* a, const double* b, const double* c, double ff,
-                           int nrec, const double* recv, int out_type, int transpose, double* out, double* tip);
+                           int nrec, const double* recv, int out_type, int transpose, double* out, double* tip,
+                           std::complex<double>* fields = nullptr);
 
 // Impedance misfit of one frequency (added to *misfit), the predicted Z
 // (optional, [nrec][4]) and its derivative with respect to the receiver fields,

@@ -1074,6 +1074,32 @@ extern "C" int sfdx_impedance(int nx, int ny, int nz, int nair, const double* a,
     return SFDX_OK;
 }
 
+extern "C" int sfdx_receiver_fields(int nx, int ny, int nz, int nair, const double* a, const double* b,
+                                    const double* c, int nf, const double* freq, const double* ex, int nrec,
+                                    const double* recv, int quirks, double* fields) {
+    if (!a || !b || !c || !freq || !ex || !recv || !fields || nrec < 1 || nair < 0 || nair + 1 >= nz)
+        return SFDX_ERR_ARG;
+    const int64_t xnl = (int64_t)nx * (ny + 1) * (nz + 1), ynl = (int64_t)(nx + 1) * ny * (nz + 1);
+    const int64_t nl = xnl + ynl + (int64_t)(nx + 1) * (ny + 1) * nz;
+    const size_t pex = (size_t)nx * (ny + 1), pey = (size_t)(nx + 1) * ny, pez = (size_t)(nx + 1) * (ny + 1);
+    const std::complex<double>* X = reinterpret_cast<const std::complex<double>*>(ex);
+    std::complex<double>* F = reinterpret_cast<std::complex<double>*>(fields);
+    std::vector<double> z((size_t)nrec * 4);
+    for (int f = 0; f < nf; f++) {
+        SurfaceView sv;
+        sv.nx = nx; sv.ny = ny; sv.nair = nair;
+        for (int p = 0; p < 2; p++) {
+            const std::complex<double>* x = X + (size_t)(2 * f + p) * nl;
+            sv.exs[p] = x + (size_t)nair * pex;
+            sv.eys[p] = x + xnl + (size_t)nair * pey;
+            sv.ezs[p] = x + xnl + ynl + (size_t)nair * pez;
+        }
+        RC(impedance_from_surface(sv, a, b, c, freq[f], nrec, recv, 1, (quirks & SFDX_QUIRK_RX_TRANSPOSE) ? 1 : 0,
+                                  z.data(), nullptr, F + (size_t)f * nrec * 10));
+    }
+    return SFDX_OK;
+}
+
 // ---------------------------------------------------------------- component entry points
 namespace {
 // A one-level plan over host inputs, ns systems at the given frequencies.

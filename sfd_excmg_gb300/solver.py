@@ -250,6 +250,19 @@ def impedance(model: Model, ex, out_type: int = 1, quirks: int = capi.QUIRKS_REF
     return (out, tip) if tipper else out
 
 
+def receiver_fields(model: Model, ex, quirks: int = capi.QUIRKS_REFERENCE, recv=None) -> np.ndarray:
+    """Surface E and H at the receivers, [nf, nrec, 2, 5] complex: (Ex, Ey, Hx, Hy, Hz)
+    of the xy and yx polarisations, the fields post_process forms Z and the tippers from."""
+    rv = _d(np.asarray(model.recv if recv is None else recv).T)
+    nrec = rv.shape[1]
+    out = np.zeros((model.nf, nrec, 2, 5), np.complex128)
+    capi.check(capi.lib().sfdx_receiver_fields(model.nx, model.ny, model.nz, model.nair, capi.dptr(_d(model.a)),
+                                               capi.dptr(_d(model.b)), capi.dptr(_d(model.c)), model.nf,
+                                               capi.dptr(_d(model.freq)), capi.zptr(_z(ex)), nrec, capi.dptr(rv),
+                                               quirks, capi.zptr(out)), "sfdx_receiver_fields")
+    return out
+
+
 # ---------------------------------------------------------------- components
 def mt1d(freq: float, conv: np.ndarray, c: np.ndarray):
     conv = np.asarray(conv, np.float64)

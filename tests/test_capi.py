@@ -65,11 +65,14 @@ def test_host_impedance_matches_post_process():
         ref = O.impedances(om, ex, out_type=out_type, rd=rd)
         got, tip = S.impedance(m, ex, out_type=out_type, quirks=q, tipper=True)
         np.testing.assert_allclose(got, ref, rtol=1e-13, atol=1e-300)
-        # tippers (Tx, Ty) of post_process (fdfe_main.f90:705-708), written beside the impedances
+        # tippers (Tx, Ty) of post_process (fdfe_main.f90:705-708), written beside the
+        # impedances, and the receiver E and H they and Z are formed from
+        fld = S.receiver_fields(m, ex, quirks=q)
         for k, ff in enumerate(m.freq):
-            _, tref, _ = O.post_process(om, ex[k, 0], ex[k, 1], ff, out_type, rd)
+            _, tref, fref = O.post_process(om, ex[k, 0], ex[k, 1], ff, out_type, rd)
             assert np.abs(tref).max() > 0
             np.testing.assert_allclose(tip[k], tref, rtol=1e-12, atol=1e-14 * np.abs(tref).max())
+            np.testing.assert_allclose(fld[k].reshape(-1, 10), fref, rtol=1e-13, atol=1e-15 * np.abs(fref).max())
 
 
 def test_model_file_roundtrip(tmp_path):
