@@ -459,9 +459,9 @@ struct Tok {
         }
         return parse(buf, v);
     }
-    bool inum(int& v) {
+    bool inum(int& v) {  // an integer item: a whole number within the range of int
         double d;
-        if (!num(d)) return false;
+        if (!num(d) || !(d >= -2147483648.0 && d <= 2147483647.0) || d != std::floor(d)) return false;
         v = (int)d;
         return true;
     }
@@ -504,6 +504,9 @@ extern "C" int sfdx_read_sizes(const char* name, int* nx, int* ny, int* nz, int*
         if (!u.num(d)) { fclose(g); return SFDX_ERR_IO; }
     if (!u.inum(nr)) { fclose(g); return SFDX_ERR_IO; }
     fclose(g);
+    // sizes the caller allocates from: reject what no model can have
+    if (h.nx < 1 || h.ny < 1 || h.nz < 1 || h.nair < 0 || nfr < 1 || nr < 0) return SFDX_ERR_IO;
+    if ((double)h.nx * h.ny * (double)(h.nz + h.nair) * 6.0 > 9.0e15) return SFDX_ERR_IO;
     if (nx) *nx = h.nx;
     if (ny) *ny = h.ny;
     if (nz) *nz = h.nz + h.nair;  // total z cells, air included

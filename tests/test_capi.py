@@ -304,3 +304,32 @@ def test_reader_accepts_fortran_list_directed_forms(tmp_path):
         assert e.code == 7
     else:
         raise AssertionError("a value with trailing characters must be rejected")
+
+
+def test_reader_rejects_impossible_sizes(tmp_path):
+    """Mesh, frequency and receiver counts are whole numbers in range: a negative,
+    fractional or overflowing count is an input error, never an allocation size."""
+    m = syn.small_aniso()
+    name = str(tmp_path / "mod")
+    m.write(name)
+    fwd = open(name + ".fwd").read().splitlines(keepends=True)
+    dat = open(name + ".dat").read().splitlines(keepends=True)
+    nze = m.nz - m.nair
+    bad_fwd = ["%d %d %d %d 0\n" % (-m.nx, m.ny, nze, m.nair), "%s %d %d %d 0\n" % ("16.5", m.ny, nze, m.nair),
+               "%s %d %d %d 0\n" % ("1e30", m.ny, nze, m.nair), "%d %d %d %d 0\n" % (m.nx, m.ny, nze, -1)]
+    for line in bad_fwd:
+        open(name + ".fwd", "w").write("".join(fwd[:2] + [line] + fwd[3:]))
+        try:
+            S.Model.read(name)
+        except capi.SfdxError as e:
+            assert e.code == 7, (line, e.code)
+        else:
+            raise AssertionError(f"accepted mesh line {line!r}")
+    open(name + ".fwd", "w").write("".join(fwd))
+    open(name + ".dat", "w").write("".join(["0\n"] + dat[1 + m.nf:]))  # no frequencies
+    try:
+        S.Model.read(name)
+    except capi.SfdxError as e:
+        assert e.code == 7
+    else:
+        raise AssertionError("a model without frequencies was accepted")
