@@ -333,3 +333,23 @@ def test_reader_rejects_impossible_sizes(tmp_path):
         assert e.code == 7
     else:
         raise AssertionError("a model without frequencies was accepted")
+
+
+def test_product_code_never_uses_the_oracle():
+    """The oracle is test infrastructure: no module of the package imports it and no
+    native source calls into it, so every product result comes from libsfdx."""
+    import ast
+    import glob
+    pkg = os.path.join(ROOT, "sfd_excmg_gb300")
+    for f in glob.glob(os.path.join(pkg, "**", "*.py"), recursive=True):
+        tree = ast.parse(open(f).read())
+        for n in ast.walk(tree):
+            mods = []
+            if isinstance(n, ast.Import):
+                mods = [a.name for a in n.names]
+            elif isinstance(n, ast.ImportFrom):
+                mods = [n.module or ""]
+            assert not any(m == "oracle" or m.startswith("oracle.") for m in mods), f
+    for f in glob.glob(os.path.join(pkg, "**", "*.*"), recursive=True):
+        if f.endswith((".cu", ".cuh", ".cpp", ".h", ".f90")):
+            assert not re.search(r"\borc_\w+\s*\(|sfd_oracle", open(f).read()), f
