@@ -99,15 +99,17 @@ inline int64_t max_resident_blocks() { return (int64_t)device_sms() * 32; }
 // 256-bit accesses (sfdx_stencil.cuh).  Their offsets [edge * ns + s0] are
 // multiples of 32 bytes (VS divides ns), so alignment rests on the base
 // pointers: every pointer argument is checked here, once per launch, and a
-// launch with a misaligned one is refused (g_misaligned; sync_state reports
-// it) instead of faulting on the device.
-extern std::atomic<int> g_misaligned;
+// launch with a misaligned one is refused instead of faulting on the device.
+// The refusal is recorded per host thread (a plan's work runs on one thread)
+// and the next sync_state of that thread reports it as SFDX_ERR_ARG and
+// clears it, so it fails the call that hit it and no other.
+extern thread_local int g_misaligned;
 template <class X> inline bool arg_aligned(const X&) { return true; }
 template <class X> inline bool arg_aligned(X* p) { return (reinterpret_cast<uintptr_t>(p) & 31) == 0; }
 template <class... KA, class... A>
 inline void vlaunch(void (*k)(KA...), int64_t work, int B, size_t smem, cudaStream_t st, A... args) {
     if (!(arg_aligned(args) && ...)) {
-        g_misaligned.store(1);
+        g_misaligned = 1;
         return;
     }
     const int g = resident_grid((const void*)k, B, smem, work);
@@ -327,7 +329,10 @@ template <class F> int graph_run(Plan& P, const std::vector<uintptr_t>& key, F&&
 }
 
 inline int sync_state(Plan& P) {
-    if (g_misaligned.load()) return SFDX_ERR_ARG;
+    if (g_misaligned) {
+        g_misaligned = 0;
+        return SFDX_ERR_ARG;
+    }
     P.hst.resize(P.ns);
     CK(cudaMemcpyAsync(P.hst.data(), P.d_state.p, sizeof(KState) * P.ns, cudaMemcpyDeviceToHost, P.st));
     CK(cudaStreamSynchronize(P.st));

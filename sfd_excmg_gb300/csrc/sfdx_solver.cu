@@ -44,7 +44,7 @@ using namespace sfdx;
 namespace sfdx {
 
 std::atomic<long long> g_launches{0};
-std::atomic<int> g_misaligned{0};
+thread_local int g_misaligned = 0;
 
 static void axis_tables(const std::vector<double>& h, int stride, double* out) {
     const int n = (int)h.size();
