@@ -177,16 +177,19 @@ def check(code: int, where: str) -> None:
 
 
 def dptr(a: np.ndarray):
-    assert a.dtype == np.float64 and a.flags.c_contiguous
+    if a.dtype != np.float64 or not a.flags.c_contiguous:
+        raise TypeError(f"expected a C-contiguous float64 array, got {a.dtype}")
     return a.ctypes.data_as(c_double_p)
 
 
 def zptr(a: np.ndarray):
     """Interleaved (re, im) view of a complex128 array as double*."""
-    assert a.dtype == np.complex128 and a.flags.c_contiguous
+    if a.dtype != np.complex128 or not a.flags.c_contiguous:
+        raise TypeError(f"expected a C-contiguous complex128 array, got {a.dtype}")
     return a.ctypes.data_as(c_double_p)
 
 
 def iptr(a: np.ndarray):
-    assert a.dtype == np.int32 and a.flags.c_contiguous
+    if a.dtype != np.int32 or not a.flags.c_contiguous:
+        raise TypeError(f"expected a C-contiguous int32 array, got {a.dtype}")
     return a.ctypes.data_as(c_int_p)

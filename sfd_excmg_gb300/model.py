@@ -50,9 +50,13 @@ class Model:
         return len(self.freq)
 
     def validate(self) -> None:
-        assert len(self.a) == self.nx and len(self.b) == self.ny and len(self.c) == self.nz
-        assert self.sigma.shape == (6, self.ncell), self.sigma.shape
-        assert self.recv.ndim == 2 and self.recv.shape[1] == 3
+        if not (len(self.a) == self.nx and len(self.b) == self.ny and len(self.c) == self.nz):
+            raise ValueError(f"spacings ({len(self.a)}, {len(self.b)}, {len(self.c)}) do not match the mesh "
+                             f"({self.nx}, {self.ny}, {self.nz})")
+        if np.shape(self.sigma) != (6, self.ncell):
+            raise ValueError(f"sigma has shape {np.shape(self.sigma)}, expected (6, {self.ncell})")
+        if np.ndim(self.recv) != 2 or np.shape(self.recv)[1] != 3:
+            raise ValueError(f"receivers have shape {np.shape(self.recv)}, expected (nrec, 3)")
 
     # ------------------------------------------------------------------ I/O
     @classmethod

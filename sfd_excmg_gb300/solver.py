@@ -23,6 +23,39 @@ def _d(x):
     return np.ascontiguousarray(x, dtype=np.float64)
 
 
+def _sigma(model: Model, sigma=None) -> np.ndarray:
+    """The conductivity handed to the C ABI: [6][ncell] float64, size checked."""
+    sg = _d(model.sigma if sigma is None else sigma)
+    if sg.size != 6 * model.ncell:
+        raise ValueError(f"sigma has {sg.size} values, expected 6 x {model.ncell}")
+    return sg
+
+
+def _nl(nx, ny, nz) -> int:
+    return nx * (ny + 1) * (nz + 1) + (nx + 1) * ny * (nz + 1) + (nx + 1) * (ny + 1) * nz
+
+
+def _mesh(nx, ny, nz, a, b, c, sigma=None):
+    """Spacings (and [6][ncell] conductivity) of an nx x ny x nz mesh for the C ABI, sizes checked."""
+    a, b, c = _d(a), _d(b), _d(c)
+    if (a.size, b.size, c.size) != (nx, ny, nz):
+        raise ValueError(f"spacings of sizes ({a.size}, {b.size}, {c.size}) for a {nx} x {ny} x {nz} mesh")
+    if sigma is None:
+        return a, b, c
+    sg = _d(sigma)
+    if sg.size != 6 * nx * ny * nz:
+        raise ValueError(f"sigma has {sg.size} values, expected 6 x {nx * ny * nz}")
+    return a, b, c, sg
+
+
+def _vec(v, n, ns, name) -> np.ndarray:
+    """n x ns interleaved complex values (system fastest), size checked."""
+    z = _z(v)
+    if z.size != n * ns:
+        raise ValueError(f"{name} has {z.size} values, expected {n} x {ns}")
+    return z.reshape(n, ns)
+
+
 def _z(x):
     return np.ascontiguousarray(x, dtype=np.complex128)
 
@@ -71,8 +104,7 @@ class Plan:
         if sigma_device_ptr is not None:
             sp, son = ctypes.c_void_p(sigma_device_ptr), 1
         else:
-            sg = _d(m.sigma if sigma is None else sigma)
-            assert sg.size == 6 * m.ncell
+            sg = _sigma(m, sigma)
             sp, son = ctypes.c_void_p(sg.ctypes.data), 0
             self._sg = sg
         ex = None
@@ -82,6 +114,9 @@ class Plan:
             op, oon = ctypes.c_void_p(0), 0
         else:
             ex = out if out is not None else np.zeros((m.nf, 2, m.nl), np.complex128)
+            if ex.dtype != np.complex128 or not ex.flags.c_contiguous or ex.size != m.nf * 2 * m.nl:
+                raise ValueError(f"out must be a C-contiguous complex128 array of {m.nf * 2 * m.nl} values "
+                                 f"([nf, 2, nl]), got {ex.dtype} of {ex.size}")
             op, oon = ctypes.c_void_p(ex.ctypes.data), 0
         it = np.zeros(self.iters.size, np.int32)
         rr = np.zeros(self.relres.size)
@@ -101,7 +136,7 @@ class Plan:
         if sigma_device_ptr is not None:
             sp, son = ctypes.c_void_p(sigma_device_ptr), 1
         else:
-            self._sg = _d(self.model.sigma if sigma is None else sigma)
+            self._sg = _sigma(self.model, sigma)
             sp, son = ctypes.c_void_p(self._sg.ctypes.data), 0
         it = np.zeros(self.iters.size, np.int32)
         rr = np.zeros(self.relres.size)
@@ -117,7 +152,7 @@ class Plan:
         if sigma_device_ptr is not None:
             sp, son = ctypes.c_void_p(sigma_device_ptr), 1
         else:
-            self._sg = _d(self.model.sigma if sigma is None else sigma)
+            self._sg = _sigma(self.model, sigma)
             sp, son = ctypes.c_void_p(self._sg.ctypes.data), 0
         capi.check(capi.lib().sfdx_plan_load(self._h, sp, son), "sfdx_plan_load")
 
@@ -205,7 +240,7 @@ def solve_batch(plans, sigmas=None, sigma_device_ptrs=None, allow_noconv: bool =
         sp, son = arr(sigma_device_ptrs), 1
     else:
         for q, p in enumerate(plans):
-            keep.append(_d(p.model.sigma if sigmas is None else sigmas[q]))
+            keep.append(_sigma(p.model, None if sigmas is None else sigmas[q]))
         sp, son = arr([k.ctypes.data for k in keep]), 0
     its = [np.zeros(p.iters.size, np.int32) for p in plans]
     rrs = [np.zeros(p.relres.size) for p in plans]
@@ -242,9 +277,10 @@ def impedance(model: Model, ex, out_type: int = 1, quirks: int = capi.QUIRKS_REF
     nrec = rv.shape[1]
     out = np.zeros((model.nf, nrec, 4))
     tip = np.zeros((model.nf, nrec, 4)) if tipper else None
+    x = _vec(ex, model.nf * 2, model.nl, "ex")
     capi.check(capi.lib().sfdx_impedance(model.nx, model.ny, model.nz, model.nair, capi.dptr(_d(model.a)),
                                          capi.dptr(_d(model.b)), capi.dptr(_d(model.c)), model.nf,
-                                         capi.dptr(_d(model.freq)), capi.zptr(_z(ex)), nrec, capi.dptr(rv), out_type,
+                                         capi.dptr(_d(model.freq)), capi.zptr(x), nrec, capi.dptr(rv), out_type,
                                          quirks, capi.dptr(out), capi.dptr(tip) if tip is not None else None),
                "sfdx_impedance")
     return (out, tip) if tipper else out
@@ -256,9 +292,10 @@ def receiver_fields(model: Model, ex, quirks: int = capi.QUIRKS_REFERENCE, recv=
     rv = _d(np.asarray(model.recv if recv is None else recv).T)
     nrec = rv.shape[1]
     out = np.zeros((model.nf, nrec, 2, 5), np.complex128)
+    x = _vec(ex, model.nf * 2, model.nl, "ex")
     capi.check(capi.lib().sfdx_receiver_fields(model.nx, model.ny, model.nz, model.nair, capi.dptr(_d(model.a)),
                                                capi.dptr(_d(model.b)), capi.dptr(_d(model.c)), model.nf,
-                                               capi.dptr(_d(model.freq)), capi.zptr(_z(ex)), nrec, capi.dptr(rv),
+                                               capi.dptr(_d(model.freq)), capi.zptr(x), nrec, capi.dptr(rv),
                                                quirks, capi.zptr(out)), "sfdx_receiver_fields")
     return out
 
@@ -266,6 +303,8 @@ def receiver_fields(model: Model, ex, quirks: int = capi.QUIRKS_REFERENCE, recv=
 # ---------------------------------------------------------------- components
 def mt1d(freq: float, conv: np.ndarray, c: np.ndarray):
     conv = np.asarray(conv, np.float64)
+    if conv.ndim != 2 or conv.shape[1] != 6 or np.size(c) != conv.shape[0]:
+        raise ValueError(f"conv must be (nz, 6) with nz = len(c), got {conv.shape} and {np.size(c)}")
     nz = conv.shape[0]
     cf = _d(conv.T.ravel())  # Fortran conv(nz,6)
     edc = np.zeros(2 * nz + 2, np.complex128)
@@ -280,20 +319,23 @@ def apply_operator(nx, ny, nz, a, b, c, sigma, freqs, x, precision=capi.FP64):
     """y = K x for ns interleaved systems; x: [nl, ns] complex (or [nl] for one system)."""
     freqs = _d(np.atleast_1d(freqs))
     ns = len(freqs)
-    xx = _z(x).reshape(-1, ns)
+    a, b, c, sigma = _mesh(nx, ny, nz, a, b, c, sigma)
+    xx = _vec(x, _nl(nx, ny, nz), ns, "x")
     y = np.zeros_like(xx)
-    capi.check(capi.lib().sfdx_apply_operator(nx, ny, nz, capi.dptr(_d(a)), capi.dptr(_d(b)), capi.dptr(_d(c)),
-                                              capi.dptr(_d(sigma)), ns, capi.dptr(freqs), precision, capi.zptr(xx),
+    capi.check(capi.lib().sfdx_apply_operator(nx, ny, nz, capi.dptr(a), capi.dptr(b), capi.dptr(c),
+                                              capi.dptr(sigma), ns, capi.dptr(freqs), precision, capi.zptr(xx),
                                               capi.zptr(y)), "sfdx_apply_operator")
     return y.reshape(np.shape(x))
 
 
 def build_rhs(nx, ny, nz, a, b, c, sigma, freq, edc):
-    nl = nx * (ny + 1) * (nz + 1) + (nx + 1) * ny * (nz + 1) + (nx + 1) * (ny + 1) * nz
+    nl = _nl(nx, ny, nz)
+    a, b, c, sigma = _mesh(nx, ny, nz, a, b, c, sigma)
+    e = _vec(edc, 2 * nz + 2, 1, "edc")
     p1 = np.zeros(nl, np.complex128)
     p2 = np.zeros(nl, np.complex128)
-    capi.check(capi.lib().sfdx_build_rhs(nx, ny, nz, capi.dptr(_d(a)), capi.dptr(_d(b)), capi.dptr(_d(c)),
-                                         capi.dptr(_d(sigma)), freq, capi.zptr(_z(edc)), capi.zptr(p1),
+    capi.check(capi.lib().sfdx_build_rhs(nx, ny, nz, capi.dptr(a), capi.dptr(b), capi.dptr(c),
+                                         capi.dptr(sigma), freq, capi.zptr(e), capi.zptr(p1),
                                          capi.zptr(p2)), "sfdx_build_rhs")
     return p1, p2
 
@@ -301,21 +343,23 @@ def build_rhs(nx, ny, nz, a, b, c, sigma, freq, edc):
 def precond_apply(nx, ny, nz, a, b, c, sigma, freqs, y, precond="S", precision=capi.FP64):
     freqs = _d(np.atleast_1d(freqs))
     ns = len(freqs)
-    yy = _z(y).reshape(-1, ns)
+    a, b, c, sigma = _mesh(nx, ny, nz, a, b, c, sigma)
+    yy = _vec(y, _nl(nx, ny, nz), ns, "y")
     x = np.zeros_like(yy)
-    capi.check(capi.lib().sfdx_precond_apply(nx, ny, nz, capi.dptr(_d(a)), capi.dptr(_d(b)), capi.dptr(_d(c)),
-                                             capi.dptr(_d(sigma)), ns, capi.dptr(freqs), ord(precond), precision,
+    capi.check(capi.lib().sfdx_precond_apply(nx, ny, nz, capi.dptr(a), capi.dptr(b), capi.dptr(c),
+                                             capi.dptr(sigma), ns, capi.dptr(freqs), ord(precond), precision,
                                              capi.zptr(yy), capi.zptr(x)), "sfdx_precond_apply")
     return x.reshape(np.shape(y))
 
 
 def mesh_coarsen(a, b, c, sigma, k, quirks=capi.QUIRKS_REFERENCE):
     nx, ny, nz = len(a), len(b), len(c)
+    a, b, c, sigma = _mesh(nx, ny, nz, a, b, c, sigma)
     f = 2 ** k
     a1, b1, c1 = np.zeros(nx // f), np.zeros(ny // f), np.zeros(nz // f)
     s1 = np.zeros((6, (nx // f) * (ny // f) * (nz // f)))
-    capi.check(capi.lib().sfdx_mesh_coarsen(nx, ny, nz, capi.dptr(_d(a)), capi.dptr(_d(b)), capi.dptr(_d(c)),
-                                            capi.dptr(_d(sigma)), k, quirks, capi.dptr(a1), capi.dptr(b1),
+    capi.check(capi.lib().sfdx_mesh_coarsen(nx, ny, nz, capi.dptr(a), capi.dptr(b), capi.dptr(c),
+                                            capi.dptr(sigma), k, quirks, capi.dptr(a1), capi.dptr(b1),
                                             capi.dptr(c1), capi.dptr(s1)), "sfdx_mesh_coarsen")
     return a1, b1, c1, s1
 
@@ -324,10 +368,14 @@ def prolongate(nx, ny, nz, a1, b1, c1, nair, u0, u1, quirks=capi.QUIRKS_REFERENC
     """extint_v on the fine mesh (nx,ny,nz); u0 on the 4h mesh, u1 on the 2h mesh ([n] or [n, ns])."""
     u0 = _z(u0)
     ns = 1 if u0.ndim == 1 else u0.shape[1]
-    nl = nx * (ny + 1) * (nz + 1) + (nx + 1) * ny * (nz + 1) + (nx + 1) * (ny + 1) * nz
-    u = np.zeros((nl, ns), np.complex128)
-    rc = capi.lib().sfdx_prolongate(nx, ny, nz, capi.dptr(_d(a1)), capi.dptr(_d(b1)), capi.dptr(_d(c1)), nair, ns,
-                                    capi.zptr(u0), capi.zptr(_z(u1)), capi.zptr(u), quirks)
+    if nx % 4 or ny % 4 or nz % 4:
+        raise ValueError(f"a {nx} x {ny} x {nz} mesh has no 4h level")
+    a1, b1, c1 = _mesh(nx, ny, nz, a1, b1, c1)
+    v0 = _vec(u0, _nl(nx // 4, ny // 4, nz // 4), ns, "u0")
+    v1 = _vec(u1, _nl(nx // 2, ny // 2, nz // 2), ns, "u1")
+    u = np.zeros((_nl(nx, ny, nz), ns), np.complex128)
+    rc = capi.lib().sfdx_prolongate(nx, ny, nz, capi.dptr(a1), capi.dptr(b1), capi.dptr(c1), nair, ns,
+                                    capi.zptr(v0), capi.zptr(v1), capi.zptr(u), quirks)
     capi.check(rc, "sfdx_prolongate")
     return u[:, 0] if u0.ndim == 1 else u
 
@@ -336,14 +384,15 @@ def krylov_solve(nx, ny, nz, a, b, c, sigma, freqs, rhs, x0=None, tol=1e-8, itma
     """One Krylov solve of ns interleaved systems.  Returns (x, iters, relres, rc[, history[ns, itmax]])."""
     freqs = _d(np.atleast_1d(freqs))
     ns = len(freqs)
-    r = _z(rhs).reshape(-1, ns)
-    x = np.zeros_like(r) if x0 is None else _z(x0).reshape(-1, ns).copy()
+    a, b, c, sigma = _mesh(nx, ny, nz, a, b, c, sigma)
+    r = _vec(rhs, _nl(nx, ny, nz), ns, "rhs")
+    x = np.zeros_like(r) if x0 is None else _vec(x0, _nl(nx, ny, nz), ns, "x0").copy()
     it = np.zeros(ns, np.int32)
     rr = np.zeros(ns)
     hist = np.zeros((ns, itmax)) if history else None
     o = _opts(**opts)
-    rc = capi.lib().sfdx_krylov_solve(ctypes.byref(o), nx, ny, nz, capi.dptr(_d(a)), capi.dptr(_d(b)),
-                                      capi.dptr(_d(c)), capi.dptr(_d(sigma)), ns, capi.dptr(freqs), capi.zptr(r),
+    rc = capi.lib().sfdx_krylov_solve(ctypes.byref(o), nx, ny, nz, capi.dptr(a), capi.dptr(b),
+                                      capi.dptr(c), capi.dptr(sigma), ns, capi.dptr(freqs), capi.zptr(r),
                                       capi.zptr(x), tol, itmax, capi.iptr(it), capi.dptr(rr),
                                       capi.dptr(hist) if hist is not None else None)
     if rc not in (0, 4):
@@ -355,11 +404,12 @@ def krylov_solve(nx, ny, nz, a, b, c, sigma, freqs, rhs, x0=None, tol=1e-8, itma
 def impedance_misfit(model: Model, ex, zobs, wts=None, quirks: int = capi.QUIRKS_REFERENCE, grad: bool = True):
     """sfdx_impedance_misfit: (misfit, d misfit / d ex [nf, 2, nl] or None) of host fields ex[nf, 2, nl]."""
     m = model
-    x = _z(ex)
+    x = _vec(ex, m.nf * 2, m.nl, "ex")
     f = _d(m.freq)
     rv = _d(np.asarray(m.recv).T)
-    zo = _d(zobs)
-    wt = None if wts is None else _d(wts)
+    nrec = rv.shape[1]
+    zo = _d(zobs).reshape(m.nf, nrec, 4)
+    wt = None if wts is None else _d(wts).reshape(m.nf, nrec, 2)
     g = np.zeros_like(x) if grad else None
     mis = ctypes.c_double()
     capi.check(capi.lib().sfdx_impedance_misfit(m.nx, m.ny, m.nz, m.nair, capi.dptr(_d(m.a)), capi.dptr(_d(m.b)),
@@ -368,7 +418,7 @@ def impedance_misfit(model: Model, ex, zobs, wts=None, quirks: int = capi.QUIRKS
                                                  capi.dptr(wt) if wt is not None else None, ctypes.byref(mis),
                                                  capi.zptr(g) if g is not None else None),
                "sfdx_impedance_misfit")
-    return mis.value, g
+    return mis.value, (g.reshape(np.shape(ex)) if g is not None else None)
 
 
 def write_res(name: str, freqs, recv, res, tipper=None) -> None:
@@ -397,10 +447,11 @@ def grad_correct(nx, ny, nz, a, b, c, sigma, freqs, rhs, x, tol=1e-8, maxit=2000
     (x + G phi, nodal PCG iterations)."""
     freqs = _d(np.atleast_1d(freqs))
     ns = len(freqs)
-    r = _z(rhs).reshape(-1, ns)
-    xx = _z(x).reshape(-1, ns).copy()
+    a, b, c, sigma = _mesh(nx, ny, nz, a, b, c, sigma)
+    r = _vec(rhs, _nl(nx, ny, nz), ns, "rhs")
+    xx = _vec(x, _nl(nx, ny, nz), ns, "x").copy()
     it = np.zeros(1, np.int32)
-    capi.check(capi.lib().sfdx_grad_correct(nx, ny, nz, capi.dptr(_d(a)), capi.dptr(_d(b)), capi.dptr(_d(c)),
-                                            capi.dptr(_d(sigma)), ns, capi.dptr(freqs), capi.zptr(r), capi.zptr(xx),
+    capi.check(capi.lib().sfdx_grad_correct(nx, ny, nz, capi.dptr(a), capi.dptr(b), capi.dptr(c),
+                                            capi.dptr(sigma), ns, capi.dptr(freqs), capi.zptr(r), capi.zptr(xx),
                                             tol, maxit, capi.iptr(it)), "sfdx_grad_correct")
     return xx.reshape(np.shape(x)), int(it[0])

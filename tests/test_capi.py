@@ -353,3 +353,33 @@ def test_product_code_never_uses_the_oracle():
     for f in glob.glob(os.path.join(pkg, "**", "*.*"), recursive=True):
         if f.endswith((".cu", ".cuh", ".cpp", ".h", ".f90")):
             assert not re.search(r"\borc_\w+\s*\(|sfd_oracle", open(f).read()), f
+
+
+def test_python_wrappers_check_array_sizes_before_calling_the_library():
+    """Arrays handed to the C ABI are size-checked in Python: a wrong size raises
+    ValueError before any native call (no read or write past a buffer)."""
+    import pytest
+    from sfd_excmg_gb300 import solver as sv
+    m = syn.small_aniso()
+    nx, ny, nz, nl = m.nx, m.ny, m.nz, m.nl
+    x = np.zeros((nl, 2), complex)
+    n0, n1 = sv._nl(nx // 4, ny // 4, nz // 4), sv._nl(nx // 2, ny // 2, nz // 2)
+    bad = [
+        lambda: S.apply_operator(nx, ny, nz, m.a, m.b, m.c, m.sigma, [1.0, 2.0], x[:-1]),
+        lambda: S.apply_operator(nx, ny, nz, m.a[:-1], m.b, m.c, m.sigma, [1.0, 2.0], x),
+        lambda: S.apply_operator(nx, ny, nz, m.a, m.b, m.c, m.sigma[:, :-1], [1.0, 2.0], x),
+        lambda: S.precond_apply(nx, ny, nz, m.a, m.b, m.c, m.sigma, [1.0], np.zeros(nl + 1, complex)),
+        lambda: S.krylov_solve(nx, ny, nz, m.a, m.b, m.c, m.sigma, [1.0, 1.0], x, x0=x[:10]),
+        lambda: S.grad_correct(nx, ny, nz, m.a, m.b, m.c, m.sigma, [1.0, 1.0], x, x[:-2]),
+        lambda: S.prolongate(nx, ny, nz, m.a, m.b, m.c, m.nair, np.zeros(n1, complex), np.zeros(n1, complex)),
+        lambda: S.prolongate(nx + 2, ny, nz, m.a, m.b, m.c, m.nair, np.zeros(n0, complex), np.zeros(n1, complex)),
+        lambda: S.build_rhs(nx, ny, nz, m.a, m.b, m.c, m.sigma, 1.0, np.zeros(nz, complex)),
+        lambda: S.mesh_coarsen(m.a, m.b, m.c, m.sigma[:3], 1),
+        lambda: S.mt1d(1.0, np.zeros((nz, 5)), m.c),
+        lambda: S.impedance(m, np.zeros((m.nf, 1, nl), complex)),
+        lambda: S.receiver_fields(m, np.zeros((m.nf, 2, nl - 1), complex)),
+        lambda: S.impedance_misfit(m, np.zeros((m.nf, 2, nl), complex), np.zeros((m.nf, len(m.recv), 3))),
+    ]
+    for k, f in enumerate(bad):
+        with pytest.raises(ValueError):
+            f()
