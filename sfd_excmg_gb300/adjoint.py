@@ -24,6 +24,15 @@ import torch
 from .solver import Plan
 
 
+def _check(t: torch.Tensor, shape, what: str) -> None:
+    """The conductivity tensor must have exactly the plan's layout: the library copies
+    6 x ncell values from its storage."""
+    if tuple(t.shape) != tuple(shape):
+        raise ValueError(f"{what} has shape {tuple(t.shape)}, expected {tuple(shape)}")
+    if t.is_cuda and torch.cuda.current_device() != t.device.index:
+        raise ValueError(f"{what} is on {t.device}, the plan on cuda:{torch.cuda.current_device()}")
+
+
 def _bind_stream(plan: Plan, t: torch.Tensor) -> None:
     plan.set_stream(torch.cuda.current_stream(t.device).cuda_stream if t.is_cuda else None)
 
@@ -55,6 +64,7 @@ class SigmaMisfit(torch.autograd.Function):
 
     @staticmethod
     def forward(ctx, sigma, plan, zobs, wts):
+        _check(sigma, (6, plan.model.ncell), "sigma")
         ctx.plan, ctx.zobs, ctx.wts = plan, zobs, wts
         ctx.save_for_backward(sigma)
         mis = _forward(plan, sigma, zobs, wts)
@@ -72,6 +82,7 @@ class LogSigmaMisfit(torch.autograd.Function):
 
     @staticmethod
     def forward(ctx, log_sigma, plan, zobs, wts):
+        _check(log_sigma, (plan.model.ncell,), "log_sigma")
         sig = torch.exp(log_sigma.detach().to(torch.float64))
         s6 = torch.zeros((6, sig.numel()), dtype=torch.float64, device=sig.device)
         s6[0:3] = sig

@@ -383,3 +383,19 @@ def test_python_wrappers_check_array_sizes_before_calling_the_library():
     for k, f in enumerate(bad):
         with pytest.raises(ValueError):
             f()
+
+
+def test_autograd_misfit_rejects_tensors_of_the_wrong_layout():
+    """sigma_misfit takes sigma[6, ncell] and log_sigma_misfit log_sigma[ncell]: any
+    other shape (for instance [ncell, 6]) is refused before the plan is touched."""
+    import types
+    import pytest
+    torch = pytest.importorskip("torch")
+    m = syn.small_aniso()
+    fake_plan = types.SimpleNamespace(model=m)  # the check runs before any plan method
+    zobs = np.zeros((m.nf, len(m.recv), 4))
+    for bad in (torch.zeros(m.ncell, 6, dtype=torch.float64), torch.zeros(6, m.ncell - 1, dtype=torch.float64)):
+        with pytest.raises(ValueError):
+            S.sigma_misfit(bad, fake_plan, zobs)
+    with pytest.raises(ValueError):
+        S.log_sigma_misfit(torch.zeros(m.ncell + 1, dtype=torch.float64), fake_plan, zobs)
