@@ -407,3 +407,33 @@ def test_autograd_misfit_rejects_tensors_of_the_wrong_layout():
             S.sigma_misfit(bad, fake_plan, zobs)
     with pytest.raises(ValueError):
         S.log_sigma_misfit(torch.zeros(m.ncell + 1, dtype=torch.float64), fake_plan, zobs)
+
+
+def test_topography_file_fills_the_air_cells_below_the_surface(tmp_path):
+    """read_topo (file_opt.f90:97-128): for the columns n1..n2 x n1..n2, the n3 =
+    int(height / c(nair+1)) air layers directly above the earth take sigma_hhs = 1e-2,
+    written into components xx, xy and yz as the reference writes them."""
+    m = syn.small_aniso()
+    nx, ny, nair = m.nx, m.ny, m.nair
+    cstep = m.c[nair]
+    n1, n2 = 3, 6
+    rng = np.random.default_rng(0)
+    heights = cstep * np.array([0.0, 0.5, 1.0, 1.99, 2.0, 3.7, -1.0, 5.0] * 2)
+    rng.shuffle(heights)
+    m.topo = (n1, n2, heights)
+    name = str(tmp_path / "topo")
+    m.write(name)
+    r = S.Model.read(name)
+    expect = r.sigma.copy()
+    expect[:, : nair * nx * ny] = 0
+    expect[0:3, : nair * nx * ny] = 1e-9  # sigma_air in every air cell first
+    q = 0
+    for j in range(n1, n2 + 1):
+        for i in range(n1, n2 + 1):
+            n3 = int(heights[q] / cstep)
+            q += 1
+            for k in range(1, n3 + 1):
+                cell = (nair - n3 + k - 1) * nx * ny + (j - 1) * nx + (i - 1)
+                expect[[0, 3, 5], cell] = 1e-2
+    np.testing.assert_array_equal(r.sigma, expect)
+    assert (r.sigma[0, : nair * nx * ny] == 1e-2).sum() == sum(max(0, int(h / cstep)) for h in heights)
