@@ -312,7 +312,9 @@ int sfdx_grad_correct(int nx, int ny, int nz, const double* a, const double* b, 
  * SFDX_ERR_NOMEM.  The first call on a device looks up the array's device
  * address (cudaGetSymbolAddress) and must come before any stream capture on
  * that device.  All calls share the array and leave their data in it: calls
- * that overlap on the GPU race and must be serialised by the caller.
+ * that overlap on the GPU race and must be serialised by the caller.  The
+ * device vectors d_rhs, d_x, d_r must be 16-byte aligned and d_sigma 8-byte
+ * aligned (SFDX_ERR_ARG otherwise, before any device work).
  * ------------------------------------------------------------------------ */
 #define SFDX_NOALLOC_MAX_N 1024
 #define SFDX_NOALLOC_MAX_NS 64

@@ -17,6 +17,7 @@
 // SFDX_ERR_NOMEM.  Calls share the array and leave their contents in it, so
 // calls that overlap on the GPU (different streams or threads at the same
 // time) race and must be serialised by the caller.
+#include <cstdint>
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -133,6 +134,11 @@ extern "C" int sfdx_residual_noalloc(int nx, int ny, int nz, const double* a, co
                                      const double* d_x, double* d_r, double* relres, void* stream) {
     if (!a || !b || !c || !d_sigma || !freqs || !d_rhs || !d_x || !d_r || !relres) return SFDX_ERR_ARG;
     if (nx < 2 || ny < 2 || nz < 2 || ns < 1) return SFDX_ERR_ARG;
+    // the kernels read and write the caller's complex vectors as 16-byte
+    // double2 and sigma as double: refuse pointers that would fault
+    if ((reinterpret_cast<uintptr_t>(d_rhs) | reinterpret_cast<uintptr_t>(d_x) | reinterpret_cast<uintptr_t>(d_r)) & 15)
+        return SFDX_ERR_ARG;
+    if (reinterpret_cast<uintptr_t>(d_sigma) & 7) return SFDX_ERR_ARG;
     if (nx > kMaxN || ny > kMaxN || nz > kMaxN || ns > kMaxNS) return SFDX_ERR_NOMEM;
     unsigned char* base = nullptr;
     int rc = scratch_address(&base);

@@ -1037,6 +1037,7 @@ extern "C" int sfdx_plan_misfit_grad(sfdx_plan* plan, int nrec, const double* re
                                      const double* wts, double tol, double* misfit, double* zpred, double* grad,
                                      int grad_on_device, int* adj_iters, double* adj_relres) {
     if (!plan || !recv || !zobs || !misfit || nrec < 1) return SFDX_ERR_ARG;
+    if (grad && grad_on_device && (reinterpret_cast<uintptr_t>(grad) & 7)) return SFDX_ERR_ARG;  // stored as double
     return misfit_grad(plan->P, nrec, recv, zobs, wts, tol, misfit, zpred, grad, grad_on_device != 0, adj_iters,
                        adj_relres);
 }

@@ -437,3 +437,21 @@ def test_topography_file_fills_the_air_cells_below_the_surface(tmp_path):
                 expect[[0, 3, 5], cell] = 1e-2
     np.testing.assert_array_equal(r.sigma, expect)
     assert (r.sigma[0, : nair * nx * ny] == 1e-2).sum() == sum(max(0, int(h / cstep)) for h in heights)
+
+
+def test_noalloc_residual_refuses_misaligned_device_vectors(lib):
+    """sfdx_residual_noalloc reads the caller's complex vectors as 16-byte values and
+    sigma as doubles: misaligned pointers are refused with SFDX_ERR_ARG before any
+    device work (the pointers below are never dereferenced)."""
+    n = 8
+    a = np.full(n, 10.0)
+    f = np.array([1.0])
+    rel = np.zeros(1)
+    dp = lambda v: v.ctypes.data_as(capi.c_double_p)  # noqa: E731
+    vp = ctypes.c_void_p
+    cases = [(0x10000, 0x20008, 0x30000, 0x40000), (0x10000, 0x20000, 0x30004, 0x40000),
+             (0x10000, 0x20000, 0x30000, 0x40008), (0x10004, 0x20000, 0x30000, 0x40000)]
+    for sig, rhs, x, r in cases:
+        st = lib.sfdx_residual_noalloc(n, n, n, dp(a), dp(a), dp(a), vp(sig), 1, dp(f), vp(rhs), vp(x), vp(r),
+                                       dp(rel), None)
+        assert st == 1, (hex(sig), hex(rhs), hex(x), hex(r), st)
