@@ -391,6 +391,13 @@ def test_python_wrappers_check_array_sizes_before_calling_the_library():
     for k, f in enumerate(bad):
         with pytest.raises(ValueError):
             f()
+    # a malformed model is refused by Model.validate before a plan is created
+    import copy
+    for field, value in (("sigma", m.sigma[:, :-1]), ("a", m.a[:-1])):
+        m2 = copy.deepcopy(m)
+        setattr(m2, field, value)
+        with pytest.raises(ValueError):
+            S.Plan(m2)
 
 
 def test_autograd_misfit_rejects_tensors_of_the_wrong_layout():
