@@ -4,7 +4,8 @@
 //
 // Options beyond the reference's argv come from the environment:
 //   SFDX_EXCMG=0|1 (fwd_acc, default 0 as in global_para.f90:19),
-//   SFDX_PRECISION=fp64|mixed, SFDX_VERBOSE=1.
+//   SFDX_PRECISION=fp64|mixed, SFDX_VERBOSE=1, SFDX_TIPPER=1 (output_tipper:
+//   the tippers follow the impedances in <model>.res).
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -59,13 +60,16 @@ int main(int argc, char** argv) {
     }
     if (rc == SFDX_ERR_NOCONV) fprintf(stderr, "sfd3d: warning: %s\n", sfdx_strerror(rc));
     std::vector<double> res((size_t)nf * nrec * 4);
+    // output_tipper (global_para.f90:7, off by default): the tipper block follows
+    const char* te = getenv("SFDX_TIPPER");
+    std::vector<double> tip(te && atoi(te) ? (size_t)nf * nrec * 4 : 0);
     rc = sfdx_impedance(nx, ny, nz, nair, a.data(), b.data(), c.data(), nf, freq.data(), ex.data(), nrec, recv.data(),
-                        out_type, o.quirks, res.data(), nullptr);
+                        out_type, o.quirks, res.data(), tip.empty() ? nullptr : tip.data());
     if (rc) {
         fprintf(stderr, "sfd3d: %s\n", sfdx_strerror(rc));
         return 1;
     }
-    rc = sfdx_write_res(name, nf, freq.data(), nrec, recv.data(), res.data());
+    rc = sfdx_write_res_tipper(name, nf, freq.data(), nrec, recv.data(), res.data(), tip.empty() ? nullptr : tip.data());
     if (rc) {
         fprintf(stderr, "sfd3d: %s\n", sfdx_strerror(rc));
         return 1;
