@@ -307,11 +307,15 @@ int sfdx_grad_correct(int nx, int ny, int nz, const double* a, const double* b, 
  * on `stream` (a cudaStream_t, null = default stream) and the call returns
  * after it completes.  Nothing is allocated: the tables, per-system state and
  * reduction scratch live in one fixed device array of about 4.4 MB that every
- * GPU loading the library holds until the process exits.  Limits: nx, ny, nz
- * <= SFDX_NOALLOC_MAX_N and ns <= SFDX_NOALLOC_MAX_NS, otherwise
- * SFDX_ERR_NOMEM.  The first call on a device looks up the array's device
- * address (cudaGetSymbolAddress) and must come before any stream capture on
- * that device.  All calls share the array and leave their data in it: calls
+ * GPU that ran this entry point holds until the process exits.  Limits: nx,
+ * ny, nz <= SFDX_NOALLOC_MAX_N and ns <= SFDX_NOALLOC_MAX_NS, otherwise
+ * SFDX_ERR_NOMEM.  Every call looks up the array's device address
+ * (cudaGetSymbolAddress).  With CUDA's default lazy module loading the first
+ * call on a device loads this entry point's device code and reserves the
+ * array there, so that first call must come before any stream capture on the
+ * device, and a caller that gives all device memory to its own pool makes it
+ * (any small case) before filling the pool, or sets
+ * CUDA_MODULE_LOADING=EAGER.  All calls share the array and leave their data in it: calls
  * that overlap on the GPU race and must be serialised by the caller.  The
  * device vectors d_rhs, d_x, d_r must be 16-byte aligned and d_sigma 8-byte
  * aligned (SFDX_ERR_ARG otherwise, before any device work).

@@ -180,7 +180,7 @@ static int adjoint_rhs(Plan& P, const Level& L, int nrec, const double* recv, in
 
 int misfit_grad(Plan& P, int nrec, const double* recv, const double* zobs, const double* wts, double tol,
                 double* misfit, double* zpred, double* grad, bool grad_on_device, int* adj_iters, double* adj_relres) {
-    if (!P.have_solution) return SFDX_ERR_ARG;
+    if (!P.solution_current()) return SFDX_ERR_ARG;  // no solve since the conductivity changed
     const Level& F = P.lev[P.nlev - 1];
     const int ns = P.ns, nx = F.nx, ny = F.ny, nz = F.nz, m = F.nair;
     if (m < 1 || m + 2 > nz) return SFDX_ERR_MESH;

@@ -9,8 +9,13 @@
 // conductivity, right-hand side, solution and residual buffers; everything
 // else the kernel needs (spacing tables, per-system state, the partial sums
 // of the reductions and their arrival counter) lives in one file-scope device
-// array of fixed size, reserved when the library is loaded on a device and
-// held by every GPU that loads the library until the process exits.
+// array of fixed size.  The array is reserved on a device when this file's
+// device code is loaded there: with CUDA's default lazy module loading that is
+// the first call of this entry point on the device (its address look-up loads
+// the module).  A caller that hands all device memory to its own pool therefore
+// makes one call (any small case) before filling the pool, or runs with
+// CUDA_MODULE_LOADING=EAGER.  Every GPU that loaded the library holds the
+// array until the process exits.
 //
 // Limits: nx, ny, nz <= SFDX_NOALLOC_MAX_N cells per axis, ns <=
 // SFDX_NOALLOC_MAX_NS systems; larger sizes are rejected with
@@ -19,8 +24,6 @@
 // time) race and must be serialised by the caller.
 #include <cstdint>
 #include <cuda_runtime.h>
-
-#include <mutex>
 
 #include "sfdx.h"
 #include "sfdx_kernels.cuh"
@@ -57,20 +60,15 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
 namespace {
 
-std::mutex g_mu;
-unsigned char* g_dev_ptr[64] = {nullptr};  // device address of the scratch, per device
-
-// Set-up, once per device, with that device current.
+// Device address of the scratch on the current device.  Looked up on every
+// call (cheap once the module is loaded) rather than cached: a cudaDeviceReset
+// by the caller reloads the module, possibly at another address.  The first
+// look-up on a device loads the module there; it must not happen inside a
+// stream capture.
 int scratch_address(unsigned char** out) {
-    int dev = -1;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return SFDX_ERR_CUDA;
-    std::lock_guard<std::mutex> lk(g_mu);
-    if (!g_dev_ptr[dev]) {
-        void* p = nullptr;
-        if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return SFDX_ERR_CUDA;
-        g_dev_ptr[dev] = static_cast<unsigned char*>(p);
-    }
-    *out = g_dev_ptr[dev];
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return SFDX_ERR_CUDA;
+    *out = static_cast<unsigned char*>(p);
     return SFDX_OK;
 }
 

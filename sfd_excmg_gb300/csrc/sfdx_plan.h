@@ -285,6 +285,11 @@ struct Plan {
     std::vector<double> relres;    // [nf][2]
     std::vector<KState> hst;
     bool have_solution = false;
+    // conductivity generation: advanced by every conductivity load; the
+    // solution is current only while sol_gen == sigma_gen (fields of an
+    // earlier conductivity must not feed impedances or gradients)
+    long long sigma_gen = 0, sol_gen = -1;
+    bool solution_current() const { return have_solution && sol_gen == sigma_gen; }
     // systems per thread of the complex64 / complex128 hot kernels (upper
     // bounds; sfdx_plan_autotune measures and sets them)
     int vs32 = 4, vs64 = 2;
@@ -308,6 +313,7 @@ template <class F> int graph_run(Plan& P, const std::vector<uintptr_t>& key, F&&
         return SFDX_OK;
     }
     cudaGraph_t g = nullptr;
+    const int mis0 = g_misaligned;
     CK(cudaStreamBeginCapture(P.st, cudaStreamCaptureModeThreadLocal));
     seq();
     const cudaError_t e = cudaStreamEndCapture(P.st, &g);
@@ -315,6 +321,14 @@ template <class F> int graph_run(Plan& P, const std::vector<uintptr_t>& key, F&&
         if (g) cudaGraphDestroy(g);
         cudaGetLastError();
         return SFDX_ERR_CUDA;
+    }
+    // a launch refused inside the capture (misaligned vector) is missing from
+    // the graph: keep no such graph, and fail this call (the flag is cleared
+    // here, as sync_state would)
+    if (g_misaligned && !mis0) {
+        cudaGraphDestroy(g);
+        g_misaligned = 0;
+        return SFDX_ERR_ARG;
     }
     GraphEntry ge;
     size_t n = 0;

@@ -346,6 +346,7 @@ static int level_column(Plan& P, const Level& LV, std::vector<double>& col) {
 }
 
 static int set_conductivity(Plan& P, const double* sigma, bool on_device) {
+    P.sigma_gen++;  // the last solution (if any) belongs to the previous conductivity
     Level& F = P.lev[P.nlev - 1];
     const size_t nb = (size_t)6 * F.ncell * sizeof(double);
     RC(F.sig64.alloc(nb));
@@ -541,6 +542,7 @@ static int plan_solve(Plan& P) {
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(P.st));
     P.have_solution = true;
+    P.sol_gen = P.sigma_gen;
     return rc_conv;
 }
 
@@ -596,6 +598,7 @@ static int plan_resolve(Plan& P, double tol) {
     P.level_ms.assign(P.nlev, 0.0);
     P.level_ms[P.nlev - 1] = now_ms() - t0;
     P.have_solution = true;
+    P.sol_gen = P.sigma_gen;
     return status_to_rc(status);
 }
 
@@ -815,7 +818,7 @@ extern "C" int sfdx_plan_load(sfdx_plan* plan, const double* sigma, int sigma_on
 }
 
 extern "C" const double* sfdx_plan_fields(sfdx_plan* plan) {
-    if (!plan || !plan->P.have_solution) return nullptr;
+    if (!plan || !plan->P.solution_current()) return nullptr;
     return plan->P.ex_out.as<double>();
 }
 
@@ -1005,7 +1008,7 @@ extern "C" int sfdx_plan_impedance(sfdx_plan* plan, int nrec, const double* recv
                                    double* tipper) {
     if (!plan || !recv || !out || nrec < 1) return SFDX_ERR_ARG;
     Plan& P = plan->P;
-    if (!P.have_solution) return SFDX_ERR_ARG;
+    if (!P.solution_current()) return SFDX_ERR_ARG;
     const Level& F = P.lev[P.nlev - 1];
     const int nx = F.nx, ny = F.ny, m = F.nair;
     const size_t pex = (size_t)nx * (ny + 1), pey = (size_t)(nx + 1) * ny, pez = (size_t)(nx + 1) * (ny + 1);

@@ -94,3 +94,24 @@ def test_autograd_log_sigma_on_device():
     np.testing.assert_allclose(got, ref, rtol=1e-12, atol=1e-14 * np.abs(ref).max())
     om = O.OracleModel(m.nx, m.ny, m.nz, m.nair, m.a, m.b, m.c, m.sigma, m.freq, m.recv)
     assert abs(mis.item() - O.misfit(om, zobs)) <= 1e-4 * mis.item()
+
+
+def test_fields_of_an_earlier_conductivity_are_refused():
+    """After a conductivity load without a solve the plan's fields belong to the previous
+    conductivity: the misfit (gradient) and the impedances are refused (SFDX_ERR_ARG), the
+    field pointer is withheld, and the next solve makes them available again."""
+    from sfd_excmg_gb300 import capi
+    m, zobs = _case(freqs=(1.0,))
+    with S.Plan(m, precision=S.FP64, **SOLVE) as p:
+        p.solve(fetch=False)
+        p.misfit_grad(zobs, with_grad=False)
+        assert p.fields_device_ptr() != 0
+        p.load(sigma=m.sigma * 1.1)
+        for call in (lambda: p.misfit_grad(zobs), lambda: p.misfit_grad(zobs, with_grad=False), p.impedance):
+            with pytest.raises(capi.SfdxError) as e:
+                call()
+            assert e.value.code == 1
+        assert p.fields_device_ptr() == 0
+        p.solve(sigma=m.sigma * 1.1, fetch=False)
+        p.impedance()
+        p.misfit_grad(zobs, with_grad=False)
