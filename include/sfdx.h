@@ -74,7 +74,9 @@ typedef struct sfdx_opts {
     int solver;         /* SFDX_SOLVER_*                                               */
     int excmg;          /* fwd_acc: 0 single solve from zero guess, 1 EXCMG cascade    */
     int precond;        /* 'S' multi-colour SSOR, 'J' Jacobi (pre_type); 'I' ILU(0) is
-                           not built: SFDX_ERR_UNSUPPORTED                            */
+                           not built: SFDX_ERR_UNSUPPORTED.  'G' (no counterpart in
+                           the reference): edge multigrid V-cycle over the EXCMG
+                           mesh levels, multi-colour SSOR + nodal smoother       */
     int div_cor;        /* divergence correction (div_cor): 0 off, 1 the reference's
                            (div_correc every corr_intv iterations), 2 consistent
                            gradient-space correction between restart cycles of
@@ -195,6 +197,13 @@ int sfdx_plan_kernel_time(sfdx_plan* plan, int kernel, int reps, double* ms, dou
 int sfdx_plan_autotune(sfdx_plan* plan, int reps, int* vs32, int* vs64);
 /* Wall time (ms) of each level of the last solve, coarsest first (n >= levels). */
 int sfdx_plan_level_times(const sfdx_plan* plan, double* ms, int n);
+/* Solution of one of the two levels below the finest from the last EXCMG solve
+ * (level = levels-2 or levels-1, 1-based, coarsest = 1), host ex[nf][2][nl_level]
+ * complex.  With 3 levels these are the two coarse solves that replace the
+ * reference's PARDISO calls (u1u2, fdfe_main.f90:1228-1256), the inputs of the
+ * extrapolation of the finest guess (extint_v).  SFDX_ERR_ARG for another
+ * level, a plain (fwd_acc = 0) solve, or a conductivity loaded since. */
+int sfdx_plan_level_fields(sfdx_plan* plan, int level, double* ex);
 void sfdx_plan_destroy(sfdx_plan* plan);
 
 /* ------------------------------------------------------------------------

@@ -79,6 +79,7 @@ def lib():
             L.orc_div_correc.restype = ctypes.c_int
             L.orc_ssor_apply.restype = ctypes.c_int
             L.orc_ilu_apply.restype = ctypes.c_int
+            L.orc_sgs.restype = None
     return _LIB
 
 
@@ -610,3 +611,165 @@ def sigma_grad_local(nx, ny, nz, a, b, c, wm, xs, mus):
     out[:3] *= vol / 4
     out[3:] *= vol / 8
     return out
+
+
+# --------------------------------------------------------------------------- converged solutions of large meshes
+# The exact discrete answer (the solution of the assembled fd_assemb + dcfast
+# system) on meshes too large for SuperLU.  No counterpart in the reference:
+# this is the oracle's own solver, written independently of the library
+# (SciPy sparse matrices, a Gauss-Seidel smoother in C, a direct solve on the
+# coarsest mesh), and it only has to deliver the discrete solution to a
+# relative residual of ~1e-15, which it checks with the assembled matrix.
+# Method: BiCGStab preconditioned by a geometric multigrid V-cycle on the
+# 2x-coarsened meshes (rediscretised with the volume-averaged conductivity
+# of mesh_coarsen without its index shift), lowest-order edge interpolation
+# and its dual-volume transpose, symmetric Gauss-Seidel plus a nodal
+# (gradient-space) Gauss-Seidel step as smoother (Hiptmair 1998).
+def _sgs(K, b, x):
+    x = _z(x).copy()
+    ia = np.ascontiguousarray(K.indptr, dtype=np.int64)
+    ja = np.ascontiguousarray(K.indices, dtype=np.int32)
+    km = _z(K.data)
+    lib().orc_sgs(ctypes.c_int64(K.shape[0]), km.ctypes.data_as(ctypes.c_void_p), _p(ia, c_int64_p), _p(ja, c_int32_p),
+                  _z(b).ctypes.data_as(ctypes.c_void_p), x.ctypes.data_as(ctypes.c_void_p))
+    return x
+
+
+def _node_terms(h):
+    """Fine node m -> (lower coarse node, its weight, upper coarse node, its weight); fine node
+    2I is coarse node I, an odd node lies between two at fraction t = h(m-1)/(h(m-1)+h(m))."""
+    n = len(h) + 1
+    m = np.arange(n)
+    lo = m // 2
+    t = np.zeros(n)
+    odd = m % 2 == 1
+    t[odd] = h[m[odd] - 1] / (h[m[odd] - 1] + h[m[odd]])
+    return lo, 1 - t, np.minimum(lo + 1, (n - 1) // 2), t
+
+
+def edge_prolongation(a, b, c):
+    """Lowest-order edge interpolation from the 2x-coarsened mesh to mesh (a, b, c): a fine
+    edge takes the parallel coarse edges with weight 1 along it and the linear interpolation
+    weights of its transverse node positions."""
+    a, b, c = _d(a), _d(b), _d(c)
+    nx, ny, nz = len(a), len(b), len(c)
+    cx, cy, cz = nx // 2, ny // 2, nz // 2
+    terms = (_node_terms(a), _node_terms(b), _node_terms(c))
+    cxnl, cynl = cx * (cy + 1) * (cz + 1), (cx + 1) * cy * (cz + 1)
+    rows, cols, vals = [], [], []
+    off = 0
+    for o in range(3):
+        sx, sy, sz = nx + (o != 0), ny + (o != 1), nz + (o != 2)
+        k, j, i = np.meshgrid(np.arange(sz), np.arange(sy), np.arange(sx), indexing="ij")
+        ijk = (i.ravel(), j.ravel(), k.ravel())
+        e = off + np.arange(ijk[0].size)
+        off += ijk[0].size
+        ax = [q for q in range(3) if q != o]
+        for pa in (0, 1):
+            for pb in (0, 1):
+                ida = terms[ax[0]][2 * pa][ijk[ax[0]]]
+                wa = terms[ax[0]][2 * pa + 1][ijk[ax[0]]]
+                idb = terms[ax[1]][2 * pb][ijk[ax[1]]]
+                wb = terms[ax[1]][2 * pb + 1][ijk[ax[1]]]
+                w = wa * wb
+                keep = w != 0
+                idx = [None, None, None]
+                idx[o] = ijk[o][keep] // 2
+                idx[ax[0]] = ida[keep]
+                idx[ax[1]] = idb[keep]
+                I, J, Kk = idx
+                if o == 0:
+                    col = (Kk * (cy + 1) + J) * cx + I
+                elif o == 1:
+                    col = cxnl + (Kk * cy + J) * (cx + 1) + I
+                else:
+                    col = cxnl + cynl + (Kk * (cy + 1) + J) * (cx + 1) + I
+                rows.append(e[keep])
+                cols.append(col)
+                vals.append(w[keep])
+    return sp.csr_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))),
+                         shape=(nedges(nx, ny, nz), nedges(cx, cy, cz)))
+
+
+def _boundary_edges(nx, ny, nz):
+    f = np.zeros(nedges(nx, ny, nz), np.uint8)
+    lib().orc_boundary_flags(nx, ny, nz, f.ctypes.data_as(ctypes.POINTER(ctypes.c_ubyte)))
+    return f.astype(bool)
+
+
+class _MGLevel:
+    pass
+
+
+def _mg_hierarchy(model: OracleModel, ff, nlev):
+    levs = []
+    for l in range(nlev):
+        L = _MGLevel()
+        if l == 0:
+            a, b, c, s = _d(model.a), _d(model.b), _d(model.c), _d(model.sigma)
+        else:
+            a, b, c, s = mesh_coarsen(model.a, model.b, model.c, model.sigma, l, quirk=False)
+        nx, ny, nz = len(a), len(b), len(c)
+        L.a, L.b, L.c = a, b, c
+        edc, _, _ = mt1d_anl(ff, column_conv(s, nx, ny, nz), c)
+        L.K, L.p1, L.p2 = assemble(nx, ny, nz, a, b, c, s, ff, edc)
+        L.V = edge_dual_volumes(nx, ny, nz, a, b, c)
+        L.bnd = _boundary_edges(nx, ny, nz)
+        L.G = node_gradient(nx, ny, nz, a, b, c).tocsr()
+        L.GT = L.G.T.tocsr()
+        L.Kn = (L.GT @ sp.diags(L.V) @ L.K @ L.G).tocsr()
+        if l > 0:
+            levs[-1].P = edge_prolongation(levs[-1].a, levs[-1].b, levs[-1].c)
+            levs[-1].PT = levs[-1].P.T.tocsr()
+        levs.append(L)
+    levs[-1].lu = splu(levs[-1].K.tocsc())
+    return levs
+
+
+def _mg_smooth(L, b, x):
+    x = _sgs(L.K, b, x)
+    r = b - L.K @ x
+    phi = _sgs(L.Kn, L.GT @ (L.V * r), np.zeros(L.Kn.shape[0], np.complex128))
+    return x + L.G @ phi
+
+
+def _vcycle(levs, l, b):
+    L = levs[l]
+    if l == len(levs) - 1:
+        return L.lu.solve(b)
+    x = _mg_smooth(L, b, np.zeros_like(b))
+    C = levs[l + 1]
+    rc = L.PT @ (L.V * (b - L.K @ x))
+    rc = np.where(C.bnd, 0, rc / np.where(C.V > 0, C.V, 1))
+    x = x + L.P @ _vcycle(levs, l + 1, rc)
+    return _mg_smooth(L, b, x)
+
+
+def converged_solve(model: OracleModel, ff, tol=1e-15, nlev=None, maxit=200):
+    """Solutions of both polarisations of frequency ff to relative residual `tol`
+    (||p - K x|| / ||p|| with the assembled K); returns (x1, x2, relres1, relres2, iters)."""
+    from scipy.sparse.linalg import LinearOperator, bicgstab
+    if nlev is None:
+        nlev = 1
+        while all(n % 2 ** nlev == 0 and n // 2 ** nlev >= 4 for n in (model.nx, model.ny, model.nz)):
+            nlev += 1
+    levs = _mg_hierarchy(model, ff, nlev)
+    F = levs[0]
+    M = LinearOperator(F.K.shape, lambda v: _vcycle(levs, 0, _z(v)), dtype=np.complex128)
+    out, rr, its = [], [], []
+    for p in (F.p1, F.p2):
+        cnt = [0]
+        x, _ = bicgstab(F.K, p, rtol=tol, atol=0.0, maxiter=maxit, M=M,
+                        callback=lambda xk: cnt.__setitem__(0, cnt[0] + 1))
+        rel = float(np.linalg.norm(p - F.K @ x) / np.linalg.norm(p))
+        # the recurrence residual may claim convergence early: restart from x until the true one passes
+        rounds = 0
+        while rel > tol and rounds < 5:
+            d, _ = bicgstab(F.K, p - F.K @ x, rtol=tol / max(rel, tol), atol=0.0, maxiter=maxit, M=M)
+            x = x + d
+            rel = float(np.linalg.norm(p - F.K @ x) / np.linalg.norm(p))
+            rounds += 1
+        out.append(x)
+        rr.append(rel)
+        its.append(cnt[0])
+    return out[0], out[1], rr[0], rr[1], its

@@ -1618,3 +1618,26 @@ int orc_post_process(int nx, int ny, int nz, int nair, const double *a, const do
     free(arho2);
     return rc;
 }
+
+/* ------------------------------------------------------------------------ */
+/* Symmetric Gauss-Seidel sweep on a CSR matrix, in place: one forward pass  */
+/* then one backward pass of x_i = (b_i - sum_{j != i} a_ij x_j) / a_ii.     */
+/* The smoother of the oracle's converged-solution solver (oracle.py,        */
+/* converged_solve); no counterpart in the reference.                        */
+/* ------------------------------------------------------------------------ */
+void orc_sgs(int64_t n, const zc *a, const int64_t *ia, const int32_t *ja, const zc *b, zc *x) {
+    for (int pass = 0; pass < 2; pass++) {
+        for (int64_t q = 0; q < n; q++) {
+            const int64_t i = pass == 0 ? q : n - 1 - q;
+            zc s = b[i], d = 0;
+            for (int64_t k = ia[i]; k < ia[i + 1]; k++) {
+                const int64_t j = ja[k];
+                if (j == i)
+                    d = a[k];
+                else
+                    s -= a[k] * x[j];
+            }
+            if (d != 0) x[i] = s / d;
+        }
+    }
+}

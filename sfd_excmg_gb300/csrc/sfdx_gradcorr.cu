@@ -137,7 +137,7 @@ static int grad_correct_v(Plan& P, const Level& LV, const double2* b, double2* x
         init[s] = S;
     }
     if (!any) return SFDX_OK;
-    if (!LV.gc_ok) RC(gc_assemble(P, LV));
+    RC(nodal_setup(P, LV));
     const size_t nb = (size_t)np * ns * sizeof(cplx<T>), eb = (size_t)LV.nl * ns * sizeof(double2);
     for (int q = 0; q < 5; q++) RC(P.gcn[q].alloc(nb));
     for (size_t l = 0; l < LV.mg.size(); l++) {
@@ -199,6 +199,12 @@ static int grad_correct_v(Plan& P, const Level& LV, const double2* b, double2* x
     P.gc_calls++;
     P.gc_iters += mx;
     return SFDX_OK;
+}
+
+int nodal_setup(Plan& P, const Level& LV) {
+    if (LV.gc_ok) return SFDX_OK;
+    P.emg_epoch++;  // new stencil buffers: graphs that read the old ones are stale
+    return gc_assemble(P, LV);
 }
 
 int grad_correct(Plan& P, const Level& LV, const double2* b, double2* x, const int* mask, double tol, int maxit,

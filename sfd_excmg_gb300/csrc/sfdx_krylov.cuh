@@ -9,6 +9,7 @@
 #include <chrono>
 
 #include "sfdx_blas.cuh"
+#include "sfdx_mgkern.cuh"
 #include "sfdx_plan.h"
 #include "sfdx_vkern.cuh"
 
@@ -33,14 +34,8 @@ static void bwd_one(Plan& P, const Level& LV, const VCfg& c, cplx<T>* x) {
 // symmetric Gauss-Seidel: colours 0..5 forward, 4..0 backward (the backward
 // step of the last colour is the identity).
 template <class T, int VS, int MODE>
-static void precond(Plan& P, const Level& LV, cplx<T>* out, cplx<T>* q, const cplx<T>* r, const cplx<T>* v,
-                    cplx<T>* aux = nullptr) {
-    if (P.o.precond == 'J') {
-        const int B = block_for(P.ns);
-        KL(k_jacobi<T, MODE><<<grid_for(LV.nl * P.ns, B, 16), B, 0, P.st>>>(LV.lev<T>(), P.d_state.as<KState>(), P.ns, out,
-                                                                            q, r, v));
-        return;
-    }
+static void precond_ssor(Plan& P, const Level& LV, cplx<T>* out, cplx<T>* q, const cplx<T>* r, const cplx<T>* v,
+                         cplx<T>* aux = nullptr) {
     const VCfg c = vcfg(P, LV.nl, 0, VS);
     fwd_one<T, VS, OX, 0, MODE>(P, LV, c, out, q, r, v, aux);
     fwd_one<T, VS, OX, 1, MODE>(P, LV, c, out, q, r, v, aux);
@@ -53,6 +48,112 @@ static void precond(Plan& P, const Level& LV, cplx<T>* out, cplx<T>* q, const cp
     bwd_one<T, VS, OY, 0>(P, LV, c, out);
     bwd_one<T, VS, OX, 1>(P, LV, c, out);
     bwd_one<T, VS, OX, 0>(P, LV, c, out);
+}
+
+// ------------------------------------------------------------------ edge multigrid ('G')
+// V-cycle over the plan's mesh levels (kernels and transfer operators in
+// sfdx_mgkern.cuh).  Per level: pre-smoothing (multi-colour SSOR from zero,
+// nodal step), residual, restriction, the coarser level's V-cycle,
+// prolongation, post-smoothing (residual, SSOR, nodal step); on the coarsest
+// level kEmgCoarseSweeps smoothing steps.  A fixed linear operator, so the
+// Krylov methods see an ordinary (if strong) preconditioner.
+static const int kEmgCoarseSweeps = 4;
+static const double kEmgNodalOmega = 0.7;  // damping of the nodal Jacobi step
+
+static int level_index(const Plan& P, const Level& LV) {
+    for (int l = 0; l < P.nlev; l++)
+        if (&P.lev[l] == &LV) return l;
+    return -1;
+}
+
+// Work vectors of the V-cycle and the nodal operators of levels 0..l (sized
+// for the plan's current batch); must run before any graph capture.
+template <class T> static int emg_prepare(Plan& P, const Level& LV) {
+    if (P.o.precond != 'G') return SFDX_OK;
+    const int l = level_index(P, LV);
+    if (l < 0) return SFDX_ERR_ARG;
+    for (int m = 0; m <= l; m++) {
+        const Level& L = P.lev[m];
+        RC(nodal_setup(P, L));
+        const size_t ev = (size_t)L.nl * P.ns * sizeof(cplx<T>);
+        const size_t nv = (size_t)(L.nx + 1) * (L.ny + 1) * (L.nz + 1) * P.ns * sizeof(cplx<T>);
+        DBuf* bufs[5] = {&L.emg_r, &L.emg_z, &L.emg_phi, &L.emg_b, &L.emg_x};
+        const size_t need[5] = {ev, ev, nv, m < l ? ev : 0, m < l ? ev : 0};
+        for (int q = 0; q < 5; q++) {
+            if (!need[q]) continue;
+            void* before = bufs[q]->p;
+            RC(bufs[q]->alloc(need[q]));
+            if (bufs[q]->p != before) P.emg_epoch++;  // captured graphs hold the old address
+        }
+    }
+    return SFDX_OK;
+}
+
+// nodal step: r = b - A x; phi = w D^-1 G^T V r; x += G phi
+template <class T, int VS>
+static void emg_nodal(Plan& P, const Level& L, const VCfg& c, const cplx<T>* b, cplx<T>* x) {
+    const KState* dst = P.d_state.as<KState>();
+    cplx<T>* r = L.emg_r.as<cplx<T>>();
+    cplx<T>* phi = L.emg_phi.as<cplx<T>>();
+    const uint32_t np = (uint32_t)(L.nx + 1) * (L.ny + 1) * (L.nz + 1);
+    vlaunch(k_mg_res_v<T, VS>, L.nl * c.sg.G, c.B, 0, P.st, L.lev<T>(), L.mesh, c.sg, dst, b, (const cplx<T>*)x, r);
+    vlaunch(k_mg_node_v<T, VS>, (int64_t)np * c.sg.G, c.B, 0, P.st, L.lev<T>(), L.mesh, c.sg, np, dst,
+            (const cplx<T>*)r, L.mg[0].dinv.as<float>(), phi, (T)kEmgNodalOmega);
+    vlaunch(k_mg_gadd_v<T, VS>, L.nl * c.sg.G, c.B, 0, P.st, L.lev<T>(), L.mesh, c.sg, dst, (const cplx<T>*)phi, x);
+}
+
+// smoothing step from the current x: r = b - A x; z = S^-1 r; x += z; nodal step
+template <class T, int VS>
+static void emg_smooth(Plan& P, const Level& L, const VCfg& c, const cplx<T>* b, cplx<T>* x) {
+    const KState* dst = P.d_state.as<KState>();
+    cplx<T>* r = L.emg_r.as<cplx<T>>();
+    cplx<T>* z = L.emg_z.as<cplx<T>>();
+    vlaunch(k_mg_res_v<T, VS>, L.nl * c.sg.G, c.B, 0, P.st, L.lev<T>(), L.mesh, c.sg, dst, b, (const cplx<T>*)x, r);
+    precond_ssor<T, VS, RHS_VEC>(P, L, z, r, nullptr, nullptr);
+    vlaunch(k_mg_add_v<T, VS>, L.nl * c.sg.G, c.B, 0, P.st, L.mesh, c.sg, dst, x, (const cplx<T>*)z);
+    emg_nodal<T, VS>(P, L, c, b, x);
+}
+
+// x = V-cycle(b) on level l.  `pre`: x already holds S^-1 b (the caller fused
+// its Krylov vector update into that first SSOR sweep).
+template <class T, int VS>
+static void emg_vcycle(Plan& P, int l, const cplx<T>* b, cplx<T>* x, bool pre) {
+    const Level& L = P.lev[l];
+    const VCfg c = vcfg(P, L.nl, 0, VS);
+    const KState* dst = P.d_state.as<KState>();
+    if (!pre) precond_ssor<T, VS, RHS_VEC>(P, L, x, const_cast<cplx<T>*>(b), nullptr, nullptr);
+    emg_nodal<T, VS>(P, L, c, b, x);
+    if (l == 0) {
+        for (int s = 1; s < kEmgCoarseSweeps; s++) emg_smooth<T, VS>(P, L, c, b, x);
+        return;
+    }
+    const Level& C = P.lev[l - 1];
+    const VCfg cc = vcfg(P, C.nl, 0, VS);
+    cplx<T>* r = L.emg_r.as<cplx<T>>();
+    cplx<T>* bc = C.emg_b.as<cplx<T>>();
+    cplx<T>* xc = C.emg_x.as<cplx<T>>();
+    vlaunch(k_mg_res_v<T, VS>, L.nl * c.sg.G, c.B, 0, P.st, L.lev<T>(), L.mesh, c.sg, dst, b, (const cplx<T>*)x, r);
+    vlaunch(k_mg_restrict_v<T, VS>, C.nl * cc.sg.G, cc.B, 0, P.st, L.lev<T>(), L.mesh, C.lev<T>(), C.mesh, cc.sg, dst,
+            (const cplx<T>*)r, bc);
+    emg_vcycle<T, VS>(P, l - 1, bc, xc, false);
+    vlaunch(k_mg_prolong_v<T, VS>, L.nl * c.sg.G, c.B, 0, P.st, L.lev<T>(), L.mesh, C.mesh, c.sg, dst,
+            (const cplx<T>*)xc, x);
+    emg_smooth<T, VS>(P, L, c, b, x);
+}
+
+// out = M^{-1} rhs (rhs produced by MODE, see k_fwd_v): Jacobi, multi-colour
+// SSOR, or the edge multigrid V-cycle whose first SSOR sweep carries MODE.
+template <class T, int VS, int MODE>
+static void precond(Plan& P, const Level& LV, cplx<T>* out, cplx<T>* q, const cplx<T>* r, const cplx<T>* v,
+                    cplx<T>* aux = nullptr) {
+    if (P.o.precond == 'J') {
+        const int B = block_for(P.ns);
+        KL(k_jacobi<T, MODE><<<grid_for(LV.nl * P.ns, B, 16), B, 0, P.st>>>(LV.lev<T>(), P.d_state.as<KState>(), P.ns, out,
+                                                                            q, r, v));
+        return;
+    }
+    precond_ssor<T, VS, MODE>(P, LV, out, q, r, v, aux);
+    if (P.o.precond == 'G') emg_vcycle<T, VS>(P, level_index(P, LV), q, out, true);
 }
 
 static void init_states(Plan& P, const double* tols_host, double tol, int itmax, const int* mask_host,
@@ -86,7 +187,7 @@ static std::vector<uintptr_t> interval_key(const Plan& P, const Level& LV, int s
                                 (uintptr_t)P.hist_stride, (uintptr_t)LV.sig32.p, (uintptr_t)LV.sig64.p,
                                 (uintptr_t)LV.tab32.p, (uintptr_t)LV.tab64.p, (uintptr_t)LV.rc_ok,
                                 (uintptr_t)LV.rc32.p, (uintptr_t)LV.rc64.p,
-                                (uintptr_t)(P.o.ssor_omega * 1e6)};
+                                (uintptr_t)(P.o.ssor_omega * 1e6), (uintptr_t)P.emg_epoch};
     for (const DBuf& b : P.kv) k.push_back((uintptr_t)b.p);
     k.insert(k.end(), extra);
     return k;
@@ -768,6 +869,7 @@ static int corrected_cycles(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>*
 template <class T>
 int bicgstab(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, const double* tols_host, double tol, int itmax,
              const int* mask_host, const Reliable* rel) {
+    RC(emg_prepare<T>(P, LV));
     auto run = [&](int itc, const int* m, const cplx<T>* bb, cplx<T>* xx, const Reliable* rr) -> int {
         switch (plan_vs<T>(P)) {
             case 4: return bicgstab_v<T, 4>(P, LV, bb, xx, tols_host, tol, itc, m, rr);
@@ -782,6 +884,7 @@ int bicgstab(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, const doubl
 template <class T>
 int gpbicg(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, const double* tols_host, double tol, int itmax,
            const int* mask_host, const Reliable* rel) {
+    RC(emg_prepare<T>(P, LV));
     auto run = [&](int itc, const int* m, const cplx<T>* bb, cplx<T>* xx, const Reliable* rr) -> int {
         switch (plan_vs<T>(P)) {
             case 4: return gpbicg_v<T, 4>(P, LV, bb, xx, tols_host, tol, itc, m, rr);
@@ -796,6 +899,7 @@ int gpbicg(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, const double*
 template <class T>
 int cocr(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, const double* tols_host, double tol, int itmax,
          const int* mask_host, const Reliable* rel) {
+    RC(emg_prepare<T>(P, LV));
     auto run = [&](int itc, const int* m, const cplx<T>* bb, cplx<T>* xx, const Reliable* rr) -> int {
         switch (plan_vs<T>(P)) {
             case 4: return cocr_v<T, 4>(P, LV, bb, xx, tols_host, tol, itc, m, rr);
@@ -810,6 +914,7 @@ int cocr(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, const double* t
 template <class T>
 int tfqmr(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, const double* tols_host, double tol, int itmax,
           const int* mask_host, const Reliable* rel) {
+    RC(emg_prepare<T>(P, LV));
     auto run = [&](int itc, const int* m, const cplx<T>* bb, cplx<T>* xx, const Reliable* rr) -> int {
         switch (plan_vs<T>(P)) {
             case 4: return tfqmr_v<T, 4>(P, LV, bb, xx, tols_host, tol, itc, m, rr);
@@ -824,6 +929,7 @@ int tfqmr(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, const double* 
 template <class T>
 int bicg(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, const double* tols_host, double tol, int itmax,
          const int* mask_host, const Reliable* rel) {
+    RC(emg_prepare<T>(P, LV));
     auto run = [&](int itc, const int* m, const cplx<T>* bb, cplx<T>* xx, const Reliable* rr) -> int {
         switch (plan_vs<T>(P)) {
             case 4: return bicg2_v<T, 4>(P, LV, bb, xx, tols_host, tol, itc, m, rr);
@@ -836,6 +942,7 @@ int bicg(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, const double* t
     return run(itmax, mask_host, b, x, rel);
 }
 template <class T> int precond_vec(Plan& P, const Level& LV, cplx<T>* out, cplx<T>* q) {
+    RC(emg_prepare<T>(P, LV));
     switch (plan_vs<T>(P)) {
         case 4: precond<T, 4, RHS_VEC>(P, LV, out, q, nullptr, nullptr); break;
         case 2: precond<T, 2, RHS_VEC>(P, LV, out, q, nullptr, nullptr); break;

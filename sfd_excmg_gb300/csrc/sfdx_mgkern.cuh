@@ -1,0 +1,292 @@
+// sfdx_mgkern.cuh -- kernels of the edge multigrid preconditioner
+// (precond = 'G'; no counterpart in the reference, whose pre_type offers
+// SSOR, Jacobi and ILU(0) only, global_para.f90:18).
+//
+// The V-cycle runs on the mesh levels the EXCMG cascade already holds (level
+// l-1 is level l with every pair of cells merged, mesh_coarsen
+// fdfe_main.f90:18-84), each with its own rediscretised operator:
+//   * smoother: the multi-colour SSOR of the Krylov solves, followed by a
+//     nodal (gradient-space) step: r = b - A x, phi = w D^-1 G^T V r with D
+//     the diagonal of G^T V A G = -i w mu N (N the nodal operator of the
+//     gradient correction), x += G phi.  Point smoothers cannot reduce the
+//     error in the near-null space of the curl-curl operator (discrete
+//     gradients: air cells and low frequencies); the nodal step does.
+//   * prolongation P: the lowest-order edge interpolation on nested
+//     non-uniform meshes -- a fine edge takes the coarse edges parallel to it
+//     with weight 1 along the edge and the linear interpolation weights of its
+//     transverse node positions (1 on a coarse node, h-/(h-+h+) and
+//     h+/(h-+h+) between two);
+//   * restriction R = V_c^-1 P^T V_f (V the edge dual volumes), the transpose
+//     with respect to the inner product in which the operator is symmetric.
+// Vectors are [edge][ns] (nodal: [node][ns]) in the precision of the solve;
+// VS systems per thread as in sfdx_vkern.cuh.
+#pragma once
+#include "sfdx_gradcorr.cuh"
+
+namespace sfdx {
+
+// r = b - A x for the active systems (boundary rows: identity)
+template <class T, int VS>
+__global__ void k_mg_res_v(Lev<T> L, Mesh M, SysG sgp, const KState* st, const cplx<T>* __restrict__ b,
+                           const cplx<T>* __restrict__ x, cplx<T>* __restrict__ r) {
+    const int ns = sgp.ns, s0 = (threadIdx.x % sgp.G) * VS;
+    const SysV<T, VS> S = load_sys<T, VS>(st, s0);
+    if (!S.act) return;
+    SFDX_GRID_LOOP(t, M.nl * sgp.G) {
+        uint32_t e;
+        int i, j, k;
+        const int o = mdecode_plane(M, fdiv(sgp.fG, t), e, i, j, k);
+        const size_t g = (size_t)e * ns + s0;
+        CV<T, VS> xe, ax, bv;
+        cvld<T, VS>(xe, x + g);
+        row_apply<T, VS>(L, M, o, e, i, j, k, x, ns, s0, S.wm, xe, ax);
+        cvld<T, VS>(bv, b + g);
+#pragma unroll
+        for (int u = 0; u < VS; u++) ax.v[u] = bv.v[u] - ax.v[u];
+        cvst_m<T, VS>(r + g, ax, S.act);
+    }
+}
+
+// x += z for the active systems
+template <class T, int VS>
+__global__ void k_mg_add_v(Mesh M, SysG sgp, const KState* st, cplx<T>* __restrict__ x, const cplx<T>* __restrict__ z) {
+    const int ns = sgp.ns, s0 = (threadIdx.x % sgp.G) * VS;
+    const SysV<T, VS> S = load_sys<T, VS>(st, s0);
+    if (!S.act) return;
+    SFDX_GRID_LOOP(t, M.nl * sgp.G) {
+        const size_t g = (size_t)fdiv(sgp.fG, t) * ns + s0;
+        CV<T, VS> a, d;
+        cvldw<T, VS>(a, x + g);
+        cvld<T, VS>(d, z + g);
+#pragma unroll
+        for (int u = 0; u < VS; u++) a.v[u] = a.v[u] + d.v[u];
+        cvst_m<T, VS>(x + g, a, S.act);
+    }
+}
+
+// Nodal step, part 1: phi = w D^-1 G^T V r at interior nodes (0 on boundary
+// nodes), D = -i wm N_nn, so phi = (w dinv / wm) * i * (G^T V r).
+// G^T V r at node (i,j,k) = sum over its six edges of +-(V/len) r: + for the
+// edge that ends at the node, - for the one that starts there.
+template <class T, int VS>
+__global__ void k_mg_node_v(Lev<T> L, Mesh M, SysG sgp, uint32_t np, const KState* st, const cplx<T>* __restrict__ r,
+                            const float* __restrict__ dinv, cplx<T>* __restrict__ phi, T omega) {
+    const int ns = sgp.ns, s0 = (threadIdx.x % sgp.G) * VS;
+    const SysV<T, VS> S = load_sys<T, VS>(st, s0);
+    if (!S.act) return;
+    const uint32_t nx1 = M.nx + 1, ny1 = M.ny + 1;
+    SFDX_GRID_LOOP(t, np * sgp.G) {
+        const uint32_t n = fdiv(sgp.fG, t);
+        int i, j, k;
+        node_ijk(M, n, i, j, k);
+        CV<T, VS> out;
+        cvzero<T, VS>(out);
+        if (!node_bnd(M, i, j, k)) {
+            const uint32_t ex = ((uint32_t)k * ny1 + j) * M.nx + i;
+            const uint32_t ey = M.xnl + ((uint32_t)k * M.ny + j) * nx1 + i;
+            const uint32_t ez = M.xnl + M.ynl + ((uint32_t)k * ny1 + j) * nx1 + i;
+            const uint32_t es[6] = {ex - 1, ex, ey - nx1, ey, ez - nx1 * ny1, ez};
+            const T rx = __ldg(L.ax.rs + i), ry = __ldg(L.ay.rs + j), rz = __ldg(L.az.rs + k);
+            const T w[3] = {T(0.25) / (ry * rz), T(0.25) / (rx * rz), T(0.25) / (rx * ry)};
+            CV<T, VS> tn;
+            cvzero<T, VS>(tn);
+#pragma unroll
+            for (int m = 0; m < 6; m++) {
+                CV<T, VS> a;
+                cvld<T, VS>(a, r + (size_t)es[m] * ns + s0);
+                const T f = (m & 1) ? -w[m >> 1] : w[m >> 1];
+#pragma unroll
+                for (int u = 0; u < VS; u++) {
+                    tn.v[u].x += f * a.v[u].x;
+                    tn.v[u].y += f * a.v[u].y;
+                }
+            }
+            const T d = omega * (T)__ldg(dinv + n);
+#pragma unroll
+            for (int u = 0; u < VS; u++) {
+                const T s = d / S.wm[u];
+                out.v[u] = mk<T>(-s * tn.v[u].y, s * tn.v[u].x);
+            }
+        }
+        cvst_m<T, VS>(phi + (size_t)n * ns + s0, out, S.act);
+    }
+}
+
+// Nodal step, part 2: x += G phi on interior edges ((phi_end - phi_start) / len)
+template <class T, int VS>
+__global__ void k_mg_gadd_v(Lev<T> L, Mesh M, SysG sgp, const KState* st, const cplx<T>* __restrict__ phi,
+                            cplx<T>* __restrict__ x) {
+    const int ns = sgp.ns, s0 = (threadIdx.x % sgp.G) * VS;
+    const SysV<T, VS> S = load_sys<T, VS>(st, s0);
+    if (!S.act) return;
+    const uint32_t nx1 = M.nx + 1, pl = nx1 * (M.ny + 1);
+    SFDX_GRID_LOOP(t, M.nl * sgp.G) {
+        const uint32_t e = fdiv(sgp.fG, t);
+        int i, j, k;
+        const int o = mdecode(M, e, i, j, k);
+        if (mbnd(M, o, i, j, k)) continue;
+        const uint32_t n0 = ((uint32_t)k * (M.ny + 1) + j) * nx1 + i;
+        uint32_t n1;
+        T rl;
+        if (o == OX) { n1 = n0 + 1; rl = __ldg(L.ax.rh + i); }
+        else if (o == OY) { n1 = n0 + nx1; rl = __ldg(L.ay.rh + j); }
+        else { n1 = n0 + pl; rl = __ldg(L.az.rh + k); }
+        const size_t g = (size_t)e * ns + s0;
+        CV<T, VS> a, b, xv;
+        cvld<T, VS>(a, phi + (size_t)n0 * ns + s0);
+        cvld<T, VS>(b, phi + (size_t)n1 * ns + s0);
+        cvldw<T, VS>(xv, x + g);
+#pragma unroll
+        for (int u = 0; u < VS; u++)
+            xv.v[u] = mk<T>(xv.v[u].x + rl * (b.v[u].x - a.v[u].x), xv.v[u].y + rl * (b.v[u].y - a.v[u].y));
+        cvst_m<T, VS>(x + g, xv, S.act);
+    }
+}
+
+// Transverse interpolation of one fine node index m onto the coarse nodes
+// of an axis (fine node 2I is coarse node I): 1 or 2 terms (coarse node,
+// weight).  Between two coarse nodes the weights are linear in position:
+// whi(m) = h(m)/(h(m-1)+h(m)) towards the lower one, wlo(m) towards the upper.
+template <class T>
+__device__ __forceinline__ int mg_node_terms(const AxisT<T>& A, int m, int (&c)[2], T (&w)[2]) {
+    if ((m & 1) == 0) {
+        c[0] = m >> 1;
+        w[0] = T(1);
+        return 1;
+    }
+    c[0] = m >> 1;
+    c[1] = (m >> 1) + 1;
+    w[0] = __ldg(A.whi + m);
+    w[1] = __ldg(A.wlo + m);
+    return 2;
+}
+
+// Prolongation with addition: xf += P ec on the interior fine edges.
+template <class T, int VS>
+__global__ void k_mg_prolong_v(Lev<T> Lf, Mesh Mf, Mesh Mc, SysG sgp, const KState* st, const cplx<T>* __restrict__ ec,
+                               cplx<T>* __restrict__ xf) {
+    const int ns = sgp.ns, s0 = (threadIdx.x % sgp.G) * VS;
+    const SysV<T, VS> S = load_sys<T, VS>(st, s0);
+    if (!S.act) return;
+    SFDX_GRID_LOOP(t, Mf.nl * sgp.G) {
+        const uint32_t e = fdiv(sgp.fG, t);
+        int i, j, k;
+        const int o = mdecode(Mf, e, i, j, k);
+        if (mbnd(Mf, o, i, j, k)) continue;
+        int ca[2], cb[2];
+        T wa[2], wb[2];
+        int na, nb;
+        if (o == OX) {
+            na = mg_node_terms<T>(Lf.ay, j, ca, wa);
+            nb = mg_node_terms<T>(Lf.az, k, cb, wb);
+        } else if (o == OY) {
+            na = mg_node_terms<T>(Lf.ax, i, ca, wa);
+            nb = mg_node_terms<T>(Lf.az, k, cb, wb);
+        } else {
+            na = mg_node_terms<T>(Lf.ax, i, ca, wa);
+            nb = mg_node_terms<T>(Lf.ay, j, cb, wb);
+        }
+        CV<T, VS> acc;
+        cvzero<T, VS>(acc);
+        for (int p = 0; p < na; p++)
+            for (int q = 0; q < nb; q++) {
+                uint32_t c;
+                if (o == OX) c = medge(Mc, OX, i >> 1, ca[p], cb[q]);
+                else if (o == OY) c = medge(Mc, OY, ca[p], j >> 1, cb[q]);
+                else c = medge(Mc, OZ, ca[p], cb[q], k >> 1);
+                CV<T, VS> v;
+                cvld<T, VS>(v, ec + (size_t)c * ns + s0);
+                const T w = wa[p] * wb[q];
+#pragma unroll
+                for (int u = 0; u < VS; u++) {
+                    acc.v[u].x += w * v.v[u].x;
+                    acc.v[u].y += w * v.v[u].y;
+                }
+            }
+        const size_t g = (size_t)e * ns + s0;
+        CV<T, VS> xv;
+        cvldw<T, VS>(xv, xf + g);
+#pragma unroll
+        for (int u = 0; u < VS; u++) xv.v[u] = xv.v[u] + acc.v[u];
+        cvst_m<T, VS>(xf + g, xv, S.act);
+    }
+}
+
+// Restriction bc = V_c^-1 P^T V_f rf on the interior coarse edges (0 on the
+// coarse boundary edges, whose rows are identity rows).  A coarse edge
+// gathers the two fine edges along it and their parallel neighbours at the
+// fine nodes 2J-1, 2J, 2J+1 of each transverse axis (18 fine edges, all
+// interior when the coarse edge is).
+template <class T>
+__device__ __forceinline__ void mg_gather_terms(const AxisT<T>& A, int J, int (&m)[3], T (&w)[3]) {
+    m[0] = 2 * J - 1;
+    m[1] = 2 * J;
+    m[2] = 2 * J + 1;
+    w[0] = __ldg(A.wlo + m[0]);  // fine node 2J-1 towards its upper coarse node J
+    w[1] = T(1);
+    w[2] = __ldg(A.whi + m[2]);  // fine node 2J+1 towards its lower coarse node J
+}
+template <class T, int VS>
+__global__ void k_mg_restrict_v(Lev<T> Lf, Mesh Mf, Lev<T> Lc, Mesh Mc, SysG sgp, const KState* st,
+                                const cplx<T>* __restrict__ rf, cplx<T>* __restrict__ bc) {
+    const int ns = sgp.ns, s0 = (threadIdx.x % sgp.G) * VS;
+    const SysV<T, VS> S = load_sys<T, VS>(st, s0);
+    if (!S.act) return;
+    SFDX_GRID_LOOP(t, Mc.nl * sgp.G) {
+        const uint32_t ec = fdiv(sgp.fG, t);
+        int I, J, K;
+        const int o = mdecode(Mc, ec, I, J, K);
+        CV<T, VS> acc;
+        cvzero<T, VS>(acc);
+        if (!mbnd(Mc, o, I, J, K)) {
+            int ma[3], mb[3];
+            T wa[3], wb[3];
+            // transverse weights; the fine dual volume is length x 1/4 (h-+h+)(h-+h+) of the two
+            // transverse axes, 1/(rs rs) / 4
+            T ra[3], rb[3];
+            if (o == OX) {
+                mg_gather_terms<T>(Lf.ay, J, ma, wa);
+                mg_gather_terms<T>(Lf.az, K, mb, wb);
+                for (int q = 0; q < 3; q++) { ra[q] = __ldg(Lf.ay.rs + ma[q]); rb[q] = __ldg(Lf.az.rs + mb[q]); }
+            } else if (o == OY) {
+                mg_gather_terms<T>(Lf.ax, I, ma, wa);
+                mg_gather_terms<T>(Lf.az, K, mb, wb);
+                for (int q = 0; q < 3; q++) { ra[q] = __ldg(Lf.ax.rs + ma[q]); rb[q] = __ldg(Lf.az.rs + mb[q]); }
+            } else {
+                mg_gather_terms<T>(Lf.ax, I, ma, wa);
+                mg_gather_terms<T>(Lf.ay, J, mb, wb);
+                for (int q = 0; q < 3; q++) { ra[q] = __ldg(Lf.ax.rs + ma[q]); rb[q] = __ldg(Lf.ay.rs + mb[q]); }
+            }
+            const AxisT<T>& Al = o == OX ? Lf.ax : (o == OY ? Lf.ay : Lf.az);
+            const int l0 = o == OX ? 2 * I : (o == OY ? 2 * J : 2 * K);
+            const T len0 = T(1) / __ldg(Al.rh + l0), len1 = T(1) / __ldg(Al.rh + l0 + 1);
+            for (int h = 0; h < 2; h++) {
+                const T len = h ? len1 : len0;
+                const int l = l0 + h;
+#pragma unroll
+                for (int p = 0; p < 3; p++)
+#pragma unroll
+                    for (int q = 0; q < 3; q++) {
+                        uint32_t f;
+                        if (o == OX) f = medge(Mf, OX, l, ma[p], mb[q]);
+                        else if (o == OY) f = medge(Mf, OY, ma[p], l, mb[q]);
+                        else f = medge(Mf, OZ, ma[p], mb[q], l);
+                        const T w = wa[p] * wb[q] * len * T(0.25) / (ra[p] * rb[q]);
+                        CV<T, VS> v;
+                        cvld<T, VS>(v, rf + (size_t)f * ns + s0);
+#pragma unroll
+                        for (int u = 0; u < VS; u++) {
+                            acc.v[u].x += w * v.v[u].x;
+                            acc.v[u].y += w * v.v[u].y;
+                        }
+                    }
+            }
+            const T iv = T(1) / edge_vol<T>(Lc, Mc, o, I, J, K);
+#pragma unroll
+            for (int u = 0; u < VS; u++) acc.v[u] = mk<T>(acc.v[u].x * iv, acc.v[u].y * iv);
+        }
+        cvst_m<T, VS>(bc + (size_t)ec * ns + s0, acc, S.act);
+    }
+}
+
+}  // namespace sfdx

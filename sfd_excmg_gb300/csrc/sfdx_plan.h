@@ -199,6 +199,10 @@ struct Level {
     // level's node grid); rebuilt after the conductivity of the level changes
     mutable std::vector<NodeMG> mg;
     mutable bool gc_ok = false;
+    // work vectors of the edge multigrid preconditioner on this level:
+    // residual, smoother output, nodal update, and (below the solve level)
+    // the level's right-hand side and solution
+    mutable DBuf emg_r, emg_z, emg_phi, emg_b, emg_x;
 
     void set_dims(int X, int Y, int Z) {
         nx = X; ny = Y; nz = Z;
@@ -289,11 +293,15 @@ struct Plan {
     // solution is current only while sol_gen == sigma_gen (fields of an
     // earlier conductivity must not feed impedances or gradients)
     long long sigma_gen = 0, sol_gen = -1;
+    long long cascade_gen = -1;  // sigma_gen of the last EXCMG cascade (u0, u1 hold its two sub-finest levels)
     bool solution_current() const { return have_solution && sol_gen == sigma_gen; }
     // systems per thread of the complex64 / complex128 hot kernels (upper
     // bounds; sfdx_plan_autotune measures and sets them)
     int vs32 = 4, vs64 = 2;
     GraphCache graphs;  // captured check intervals (o.use_graphs)
+    // advanced whenever a buffer or nodal operator that the edge multigrid
+    // bakes into captured graphs is (re)allocated: part of every graph key
+    long long emg_epoch = 0;
     Plan() = default;
     Plan(const Plan&) = delete;
     ~Plan() {
@@ -434,5 +442,8 @@ int misfit_grad(Plan& P, int nrec, const double* recv, const double* zobs, const
 // `tol`, at most `maxit` iterations (*iters: the most any system took).
 int grad_correct(Plan& P, const Level& LV, const double2* b, double2* x, const int* mask, double tol, int maxit,
                  int* iters);
+// the nodal operator N = G^T V Ms G of level LV (27-point stencil and its
+// inverse diagonal, LV.mg[0]), assembled if the conductivity changed since
+int nodal_setup(Plan& P, const Level& LV);
 
 }  // namespace sfdx

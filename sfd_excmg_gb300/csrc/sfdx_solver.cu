@@ -533,6 +533,7 @@ static int plan_solve(Plan& P) {
         };
         RC(excmg_cascade(P, rhs, P.o.eps, true, its, status));
         rc_conv = status_to_rc(status);
+        P.cascade_gen = P.sigma_gen;
     }
     RC(true_residual(P, F, P.b64.as<double2>(), P.x64.as<double2>(), P.relres.data(), nullptr));
     // de-interleave into [nf][2][nl] (system-major)
@@ -605,7 +606,7 @@ static int plan_resolve(Plan& P, double tol) {
 static int validate_opts(const sfdx_opts& o) {
     if (o.excmg && o.level < 3) return SFDX_ERR_ARG;
     if (o.precond == 'I') return SFDX_ERR_UNSUPPORTED;  // ILU(0), pre_type = 'I': not built
-    if (o.precond != 'S' && o.precond != 'J') return SFDX_ERR_ARG;
+    if (o.precond != 'S' && o.precond != 'J' && o.precond != 'G') return SFDX_ERR_ARG;
     if (o.precision != SFDX_FP64 && o.precision != SFDX_MIXED) return SFDX_ERR_ARG;
     if (o.div_cor < 0 || o.div_cor > 2) return SFDX_ERR_ARG;
     if (o.div_cor == 2 && (o.corr_intv < 1 || !(o.corr_tol > 0))) return SFDX_ERR_ARG;
@@ -992,6 +993,24 @@ extern "C" int sfdx_plan_autotune(sfdx_plan* plan, int reps, int* vs32, int* vs6
     if (P.o.verbose || getenv("SFDX_VERBOSE"))
         fprintf(stderr, "sfdx: autotune: %d systems per thread (complex64), %d (complex128)\n", vs_pick(ns, P.vs32),
                 vs_pick(ns, P.vs64));
+    return SFDX_OK;
+}
+
+extern "C" int sfdx_plan_level_fields(sfdx_plan* plan, int level, double* ex) {
+    if (!plan || !ex) return SFDX_ERR_ARG;
+    Plan& P = plan->P;
+    const int N = P.nlev;
+    if (N < 3 || (level != N - 2 && level != N - 1) || P.cascade_gen != P.sigma_gen || !P.solution_current())
+        return SFDX_ERR_ARG;
+    const Level& L = P.lev[level - 1];
+    const DBuf& src = level == N - 2 ? P.u0 : P.u1;  // excmg_cascade leaves levels N-2, N-1 there
+    const int ns = P.ns;
+    RC(P.ut.alloc((size_t)L.nl * ns * sizeof(double2)));
+    const int B = block_for(ns);
+    KL(k_scatter_sys<double><<<grid_for(L.nl * ns, B, 16), B, 0, P.st>>>(L.nl, ns, src.as<double2>(), P.ut.as<double2>()));
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(ex, P.ut.p, (size_t)L.nl * ns * sizeof(double2), cudaMemcpyDeviceToHost, P.st));
+    CK(cudaStreamSynchronize(P.st));
     return SFDX_OK;
 }
 

@@ -201,6 +201,17 @@ class Plan:
     def fields_device_ptr(self) -> int:
         return capi.lib().sfdx_plan_fields(self._h) or 0
 
+    def level_fields(self, level: int) -> np.ndarray:
+        """Solution ex[nf, 2, nl_level] of level `level` (1-based; one of the two below the finest) from the
+        last EXCMG solve (sfdx_plan_level_fields)."""
+        m = self.model
+        f = 2 ** (self.nlev - level)
+        nx, ny, nz = m.nx // f, m.ny // f, m.nz // f
+        ex = np.zeros((m.nf, 2, _nl(nx, ny, nz)), np.complex128)
+        capi.check(capi.lib().sfdx_plan_level_fields(self._h, level, capi.dptr(ex.view(np.float64))),
+                   "sfdx_plan_level_fields")
+        return ex
+
     def level_times(self) -> np.ndarray:
         ms = np.zeros(self.nlev)
         capi.check(capi.lib().sfdx_plan_level_times(self._h, capi.dptr(ms), self.nlev), "sfdx_plan_level_times")

@@ -301,3 +301,38 @@ def test_bicgstab_with_ilu0_solves_a_small_system():
                               O.OracleOpts(pre="I", div_cor=False), ilu_band=0)
     assert it < 30
     assert np.linalg.norm(K @ x - p1) <= 2e-7 * np.linalg.norm(p1)
+
+
+def test_converged_solve_matches_superlu():
+    """The oracle's converged-solution solver (multigrid-preconditioned BiCGStab, used for the
+    fixtures of meshes too large for SuperLU) reaches a 1e-15 residual and the impedances of
+    the direct solution."""
+    m = syn.small_aniso(n=16, seed=1, freqs=(0.05, 20.0))
+    om = O.OracleModel(m.nx, m.ny, m.nz, m.nair, m.a, m.b, m.c, m.sigma, m.freq, m.recv)
+    exd = np.zeros((m.nf, 2, m.nl), np.complex128)
+    exm = np.zeros_like(exd)
+    for k, ff in enumerate(m.freq):
+        u1, u2, _, _, _ = O.direct_solve(om, ff)
+        exd[k, 0], exd[k, 1] = u1, u2
+        x1, x2, r1, r2, _ = O.converged_solve(om, ff, tol=1e-15)
+        assert r1 < 1e-14 and r2 < 1e-14, (r1, r2)
+        exm[k, 0], exm[k, 1] = x1, x2
+    zd = O.impedances(om, exd)
+    zm = O.impedances(om, exm)
+    zd, zm = zd[..., 0::2] + 1j * zd[..., 1::2], zm[..., 0::2] + 1j * zm[..., 1::2]
+    assert (np.abs(zm - zd) / np.abs(zd)).max() < 1e-7
+
+
+def test_edge_prolongation_reproduces_constant_fields():
+    """The lowest-order edge interpolation maps a constant coarse field to the same constant
+    on every fine edge whose transverse nodes have both coarse neighbours."""
+    m = syn.small_aniso(n=16, seed=0)
+    P = O.edge_prolongation(m.a, m.b, m.c)
+    cx, cy, cz = m.nx // 2, m.ny // 2, m.nz // 2
+    u = np.concatenate([np.full(cx * (cy + 1) * (cz + 1), 1.0), np.full((cx + 1) * cy * (cz + 1), 2.0),
+                        np.full((cx + 1) * (cy + 1) * cz, 3.0)])
+    v = P @ u
+    xnl, ynl = m.nx * (m.ny + 1) * (m.nz + 1), (m.nx + 1) * m.ny * (m.nz + 1)
+    np.testing.assert_allclose(v[:xnl], 1.0, rtol=1e-14)
+    np.testing.assert_allclose(v[xnl:xnl + ynl], 2.0, rtol=1e-14)
+    np.testing.assert_allclose(v[xnl + ynl:], 3.0, rtol=1e-14)
