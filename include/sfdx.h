@@ -76,7 +76,11 @@ typedef struct sfdx_opts {
     int precond;        /* 'S' multi-colour SSOR, 'J' Jacobi (pre_type); 'I' ILU(0) is
                            not built: SFDX_ERR_UNSUPPORTED.  'G' (no counterpart in
                            the reference): edge multigrid V-cycle over the EXCMG
-                           mesh levels, multi-colour SSOR + nodal smoother       */
+                           mesh levels, multi-colour SSOR + nodal smoother; such
+                           plans coarsen the conductivity without the index shift
+                           of SFDX_QUIRK_COARSEN_SHIFT and, in mixed precision,
+                           replace the complex64 residual at least every 8
+                           iterations                                            */
     int div_cor;        /* divergence correction (div_cor): 0 off, 1 the reference's
                            (div_correc every corr_intv iterations), 2 consistent
                            gradient-space correction between restart cycles of
@@ -185,7 +189,8 @@ long long sfdx_plan_device_bytes(const sfdx_plan* plan);
 /* Issue the plan's work on `stream` (a cudaStream_t; null = the plan's own stream). */
 int sfdx_plan_set_stream(sfdx_plan* plan, void* stream);
 /* CUDA-event time (ms per launch) of one kernel family on the finest level and its
- * algorithmic HBM bytes: 0 operator c64, 1 operator c128, 2 MC-SSOR c64, 3 MC-SSOR c128. */
+ * algorithmic HBM bytes: 0 operator c64, 1 operator c128, 2 MC-SSOR c64, 3 MC-SSOR c128 (the
+ * multi-colour SSOR whatever opts.precond), 4 one edge-multigrid V-cycle c64 over all levels. */
 int sfdx_plan_kernel_time(sfdx_plan* plan, int kernel, int reps, double* ms, double* bytes);
 /* Pick the number of systems each thread of the hot kernels handles (4, 2
  * or 1 consecutive systems, complex64 and complex128 separately) by timing, per

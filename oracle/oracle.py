@@ -28,6 +28,7 @@ import ctypes
 import os
 import subprocess
 import threading
+import time
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -133,6 +134,9 @@ class OracleOpts:
     coarsen_quirk: bool = True   # mesh_coarsen index shift (fdfe_main.f90:64)
     midpoint_quirk: bool = True  # cal_coef along-edge nodes (excmg.f90:685)
     rd: int = 2                  # arho_interp2 stencil (fdfe_main.f90:640,685)
+    # exact solve of EXCMG levels 1-2 (PARDISO in the reference): "splu" (SciPy SuperLU) or
+    # "converged" (converged_solve, the same answer to a 1e-15 residual, for large coarse meshes)
+    coarse_solver: str = "splu"
 
 
 # --------------------------------------------------------------------------
@@ -305,6 +309,10 @@ def doublemode_nor(nx, ny, nz, a, b, c, sigma, ff, mid, slv, tol, opts: OracleOp
     mesh = (nx, ny, nz, a, b, c, sigma)
     info = LevelInfo(0, nx, ny, nz, direct=mid in (1, 2))
     if mid in (1, 2):
+        if opts.coarse_solver == "converged":
+            om = OracleModel(nx, ny, nz, 0, a, b, c, sigma, np.array([ff]), np.zeros((1, 3)))
+            u1, u2, _, _, _ = converged_solve(om, ff)
+            return u1, u2, info
         lu = splu(K.tocsc())
         u1 = lu.solve(p1)
         u2 = lu.solve(p2)
@@ -320,8 +328,10 @@ def doublemode_nor(nx, ny, nz, a, b, c, sigma, ff, mid, slv, tol, opts: OracleOp
     return u1, u2, info
 
 
-def doublemode_acc(model: OracleModel, ff, opts: OracleOpts, n_grid=None, eps=None):
-    """doublemode_acc (fdfe_main.f90:1258-1563) with u1u2 (:1228-1256)."""
+def doublemode_acc(model: OracleModel, ff, opts: OracleOpts, n_grid=None, eps=None, pols=(0, 1)):
+    """doublemode_acc (fdfe_main.f90:1258-1563) with u1u2 (:1228-1256).  `pols` selects the
+    polarisations whose finer levels are solved (both by default, as the reference does; the
+    other's solution is returned as zeros), so that the two can run in separate processes."""
     N = model.level if n_grid is None else n_grid
     tol = (model.eps if eps is None else eps) * 10.0 ** (-N + 1)
     a, b, c, sigma = model.a, model.b, model.c, model.sigma
@@ -354,8 +364,10 @@ def doublemode_acc(model: OracleModel, ff, opts: OracleOpts, n_grid=None, eps=No
         mesh = (nx, ny, nz, a1, b1, c1, sf)
         slv = model.solver if model.solver in (1, 3) else 1
         band = (nx + 1) * (ny + 1) * (nz + 1)  # idd(2) = np (fdfe_main.f90:1413)
-        x1, it1, _ = solve_krylov(slv, mesh, K, p1, u21, tol, opts.maxit_level, opts, band)
-        x2, it2, _ = solve_krylov(slv, mesh, K, p2, u22, tol, opts.maxit_level, opts, band)
+        x1, it1 = (solve_krylov(slv, mesh, K, p1, u21, tol, opts.maxit_level, opts, band)[:2] if 0 in pols
+                   else (np.zeros_like(p1), 0))
+        x2, it2 = (solve_krylov(slv, mesh, K, p2, u22, tol, opts.maxit_level, opts, band)[:2] if 1 in pols
+                   else (np.zeros_like(p2), 0))
         infos.append(LevelInfo(i, nx, ny, nz, [it1, it2]))
         u01, u02, u11, u12 = u11, u12, x1, x2
     return u11, u12, infos
@@ -773,3 +785,29 @@ def converged_solve(model: OracleModel, ff, tol=1e-15, nlev=None, maxit=200):
         rr.append(rel)
         its.append(cnt[0])
     return out[0], out[1], rr[0], rr[1], its
+
+
+# --------------------------------------------------------------------------- the reference algorithm, timed
+def reference_frequency(model: OracleModel, k, eps, pols=(0, 1)):
+    """One frequency (both polarisations) of the reference algorithm as the driver runs it:
+    doublemode_acc (fdfe_main.f90:1258-1563) with the reference's compiled-in options -- levels
+    1-2 solved exactly (PARDISO in u1u2; SuperLU here, or converged_solve where level 2 has more
+    than 20,000 edges and SuperLU takes minutes to hours), levels 3.. by BiCGStab with lexicographic SSOR from
+    the extint_v guess, div_correc every 200 iterations, 1000 iterations per level, tolerance
+    eps 10^(l-N).  Returns (seconds of the solve, (u1, u2) finest-level solutions, relres[2] of
+    the finest level against the assembled matrix (None for a polarisation not solved),
+    [(level, iterations)])."""
+    ff = float(model.freq[k])
+    m = OracleModel(model.nx, model.ny, model.nz, model.nair, model.a, model.b, model.c, model.sigma, model.freq,
+                    model.recv, model.level, eps, 1, 1)
+    # SuperLU's fill on 3-D edge meshes makes it impractical beyond ~10^4 unknowns
+    big = nedges(m.nx // 2 ** (m.level - 2), m.ny // 2 ** (m.level - 2), m.nz // 2 ** (m.level - 2)) > 20000
+    opts = OracleOpts(excmg=True, coarse_solver="converged" if big else "splu")
+    t = time.perf_counter()
+    u1, u2, infos = doublemode_acc(m, ff, opts, pols=pols)
+    secs = time.perf_counter() - t
+    edc, _, _ = mt1d_anl(ff, column_conv(m.sigma, m.nx, m.ny, m.nz), m.c)
+    K, p1, p2 = assemble(m.nx, m.ny, m.nz, m.a, m.b, m.c, m.sigma, ff, edc)
+    rr = [float(np.linalg.norm(p - K @ u) / np.linalg.norm(p)) if q in pols else None
+          for q, (p, u) in enumerate(((p1, u1), (p2, u2)))]
+    return secs, (u1, u2), rr, [(i.level, list(i.iters)) for i in infos]

@@ -55,10 +55,26 @@ static void precond_ssor(Plan& P, const Level& LV, cplx<T>* out, cplx<T>* q, con
 // sfdx_mgkern.cuh).  Per level: pre-smoothing (multi-colour SSOR from zero,
 // nodal step), residual, restriction, the coarser level's V-cycle,
 // prolongation, post-smoothing (residual, SSOR, nodal step); on the coarsest
-// level kEmgCoarseSweeps smoothing steps.  A fixed linear operator, so the
+// level emg_coarse_sweeps() smoothing steps.  A fixed linear operator, so the
 // Krylov methods see an ordinary (if strong) preconditioner.
-static const int kEmgCoarseSweeps = 4;
-static const double kEmgNodalOmega = 0.7;  // damping of the nodal Jacobi step
+// smoothing steps on the coarsest level and the damping of the nodal Jacobi
+// step (SFDX_MG_COARSE, SFDX_MG_OMEGA override them)
+static int emg_coarse_sweeps() {
+    static const int v = [] {
+        const char* e = getenv("SFDX_MG_COARSE");
+        const int n = e ? atoi(e) : 0;
+        return n > 0 ? n : 4;
+    }();
+    return v;
+}
+static double emg_nodal_omega() {
+    static const double v = [] {
+        const char* e = getenv("SFDX_MG_OMEGA");
+        const double w = e ? atof(e) : 0.0;
+        return w > 0 ? w : 0.7;
+    }();
+    return v;
+}
 
 static int level_index(const Plan& P, const Level& LV) {
     for (int l = 0; l < P.nlev; l++)
@@ -98,7 +114,7 @@ static void emg_nodal(Plan& P, const Level& L, const VCfg& c, const cplx<T>* b, 
     const uint32_t np = (uint32_t)(L.nx + 1) * (L.ny + 1) * (L.nz + 1);
     vlaunch(k_mg_res_v<T, VS>, L.nl * c.sg.G, c.B, 0, P.st, L.lev<T>(), L.mesh, c.sg, dst, b, (const cplx<T>*)x, r);
     vlaunch(k_mg_node_v<T, VS>, (int64_t)np * c.sg.G, c.B, 0, P.st, L.lev<T>(), L.mesh, c.sg, np, dst,
-            (const cplx<T>*)r, L.mg[0].dinv.as<float>(), phi, (T)kEmgNodalOmega);
+            (const cplx<T>*)r, L.mg[0].dinv.as<float>(), phi, (T)emg_nodal_omega());
     vlaunch(k_mg_gadd_v<T, VS>, L.nl * c.sg.G, c.B, 0, P.st, L.lev<T>(), L.mesh, c.sg, dst, (const cplx<T>*)phi, x);
 }
 
@@ -124,7 +140,7 @@ static void emg_vcycle(Plan& P, int l, const cplx<T>* b, cplx<T>* x, bool pre) {
     if (!pre) precond_ssor<T, VS, RHS_VEC>(P, L, x, const_cast<cplx<T>*>(b), nullptr, nullptr);
     emg_nodal<T, VS>(P, L, c, b, x);
     if (l == 0) {
-        for (int s = 1; s < kEmgCoarseSweeps; s++) emg_smooth<T, VS>(P, L, c, b, x);
+        for (int s = 1; s < emg_coarse_sweeps(); s++) emg_smooth<T, VS>(P, L, c, b, x);
         return;
     }
     const Level& C = P.lev[l - 1];

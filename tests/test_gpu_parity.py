@@ -8,7 +8,8 @@ complex64 inner iterations, multigrid), so parity is on the converged
 answer: impedances Zxy, Zyx at every receiver and frequency, and the field
 on a sample of earth edges, within the tolerances stated per test.  The
 coarse levels of the EXCMG cascade (the reference's PARDISO solves) are
-compared with SciPy's SuperLU solution of the same coarse systems.
+compared with the exact solution of the same coarse systems (SciPy's SuperLU, or
+the oracle's converged solve to a 1e-15 residual where SuperLU is impractical).
 """
 import os
 
@@ -106,9 +107,9 @@ def test_aniso_hills_converged_matches_oracle(precision):
     assert ez < Z_TOL_CONVERGED and ef < F_TOL_CONVERGED, (ez, ef)
 
 
-def test_coarse_levels_and_guess_match_superlu():
+def test_coarse_levels_and_guess_match_exact_solves():
     """Levels 1 and 2 of a 3-level cascade (the reference solves them with PARDISO,
-    u1u2 fdfe_main.f90:1228-1256) against SuperLU on the same coarse systems, and the
+    u1u2 fdfe_main.f90:1228-1256) against the exact solution of the same coarse systems, and the
     extrapolated finest-level guess (extint_v) built from each, on the earth edges."""
     m = syn.halfspace_cube()
     with S.Plan(m, eps=1e-8, excmg=1, level=3, solver=3, precision=S.FP64, div_cor=2, corr_intv=40,
@@ -123,7 +124,10 @@ def test_coarse_levels_and_guess_match_superlu():
         rl = np.zeros((m.nf, 2, O.nedges(nx, ny, nz)), np.complex128)
         for f, ff in enumerate(m.freq):
             om = O.OracleModel(nx, ny, nz, m.nair // 2 ** k, a1, b1, c1, s1, m.freq, m.recv)
-            x1, x2, _, _, _ = O.direct_solve(om, ff)
+            if rl.shape[2] <= 20000:
+                x1, x2, _, _, _ = O.direct_solve(om, ff)
+            else:  # SuperLU takes hours on 3-D edge meshes of this size: the 1e-15 converged solve
+                x1, x2, _, _, _ = O.converged_solve(om, ff)
             rl[f, 0], rl[f, 1] = x1, x2
         ref.append(rl)
         ea = _earth(nx, ny, nz, m.nair // 2 ** k)
