@@ -215,7 +215,9 @@ void sfdx_plan_destroy(sfdx_plan* plan);
  * Impedances at the receivers.  Replaces post_process + arho_interp2
  * (fdfe_main.f90:549-790).  recv: Fortran recv(nrec,3) = C [3][nrec].
  * out[nf][nrec][4]: out_type 0/1 -> (Re Zxy, Im Zxy, Re Zyx, Im Zyx),
- * out_type 2 -> (rho_xy, rho_yx, phi_xy, phi_yx).  tipper (optional)
+ * out_type 2 -> (rho_xy, rho_yx, phi_xy, phi_yx); out_type 3 (no counterpart in
+ * the reference, which forms Zxy and Zyx only) -> out[nf][nrec][8], the full
+ * tensor (Re, Im) of Zxx, Zxy, Zyx, Zyy.  tipper (optional)
  * [nf][nrec][4] = (Re Tx, Im Tx, Re Ty, Im Ty).  The receiver stencil follows
  * SFDX_QUIRK_RX_TRANSPOSE of `quirks`.
  * ------------------------------------------------------------------------ */

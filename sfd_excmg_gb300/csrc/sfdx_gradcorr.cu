@@ -2,6 +2,7 @@
 // (kernels and derivation in sfdx_gradcorr.cuh; nodal multigrid in
 // sfdx_nodemg.cuh).
 #include "sfdx_gradcorr.cuh"
+#include "sfdx_mgkern.cuh"
 #include "sfdx_plan.h"
 
 namespace sfdx {
@@ -163,9 +164,12 @@ static int grad_correct_v(Plan& P, const Level& LV, const double2* b, double2* x
     const VCfg cnd = vcfg(P, np, 2, VSD);
     const VCfg cn = vcfg(P, np, 2, VS);
     RC(P.d_part.alloc(std::max(P.d_part.bytes, (size_t)max_resident_blocks() * 2 * ns * sizeof(double2))));
-    // r = b - A x (FP64), the nodal right-hand side, z = M^{-1} r, p = z
-    vlaunch(k_residual_v<double, double, VSD, 2>, LV.nl * ce.sg.G, ce.B, ce.smem, P.st, L, M, ce.sg, pst, b, x, re,
-            nullptr, redbuf(P), nullptr, 0);
+    // the gradient-space part of r = b - A x (FP64), formed as b + i w mu Ms x
+    // (k_mg_mres_v: without the curl-curl terms, whose rounding noise the
+    // nodal solve would amplify by 1/(w mu sigma) in air), then the nodal
+    // right-hand side, z = M^{-1} r, p = z
+    vlaunch(k_mg_mres_v<double, VSD>, LV.nl * ce.sg.G, ce.B, 0, P.st, L, M, ce.sg, (const KState*)pst, b,
+            (const double2*)x, re);
     vlaunch(k_gc_rhs<T, VSD, false>, np * cnd.sg.G, cnd.B, cnd.smem, P.st, L, M, cnd.sg, np, pst, re, dinv, rn, z, p, phi,
             redbuf(P));
     vcycle<VS>(P, LV, cn.sg, cn.B, pst, 0, rn, z);

@@ -299,8 +299,18 @@ int impedance_from_surface(const SurfaceView& sv, const double* a, const double*
         zd det = f[0][2] * f[1][3] - f[1][2] * f[0][3];
         zd zxy = (f[1][0] * f[0][2] - f[0][0] * f[1][2]) / det;
         zd zyx = (f[0][1] * f[1][3] - f[1][1] * f[0][3]) / det;
-        double* o = out + (size_t)r * 4;
-        if (out_type == 2) {
+        double* o = out + (size_t)r * (out_type == 3 ? 8 : 4);
+        if (out_type == 3) {
+            // the full tensor Z = E H^-1 of the two polarisations (E, H columns xy, yx);
+            // the reference forms only Zxy and Zyx (fdfe_main.f90:688-705)
+            const zd zxx = (f[0][0] * f[1][3] - f[1][0] * f[0][3]) / det;
+            const zd zyy = (f[1][1] * f[0][2] - f[0][1] * f[1][2]) / det;
+            const zd zz[4] = {zxx, zxy, zyx, zyy};
+            for (int q = 0; q < 4; q++) {
+                o[2 * q] = zz[q].real();
+                o[2 * q + 1] = zz[q].imag();
+            }
+        } else if (out_type == 2) {
             double wmu = 2.0 * kPi * ff * kMu;
             o[0] = std::abs(zxy * zxy * zd(0, 1)) / wmu;
             o[1] = std::abs(zyx * zyx * zd(0, 1)) / wmu;

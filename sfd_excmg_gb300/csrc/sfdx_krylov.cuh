@@ -105,14 +105,15 @@ template <class T> static int emg_prepare(Plan& P, const Level& LV) {
     return SFDX_OK;
 }
 
-// nodal step: r = b - A x; phi = w D^-1 G^T V r; x += G phi
+// nodal step: q = b + i wm Ms x (the gradient-space part of b - A x);
+// phi = w D^-1 G^T V q; x += G phi
 template <class T, int VS>
 static void emg_nodal(Plan& P, const Level& L, const VCfg& c, const cplx<T>* b, cplx<T>* x) {
     const KState* dst = P.d_state.as<KState>();
     cplx<T>* r = L.emg_r.as<cplx<T>>();
     cplx<T>* phi = L.emg_phi.as<cplx<T>>();
     const uint32_t np = (uint32_t)(L.nx + 1) * (L.ny + 1) * (L.nz + 1);
-    vlaunch(k_mg_res_v<T, VS>, L.nl * c.sg.G, c.B, 0, P.st, L.lev<T>(), L.mesh, c.sg, dst, b, (const cplx<T>*)x, r);
+    vlaunch(k_mg_mres_v<T, VS>, L.nl * c.sg.G, c.B, 0, P.st, L.lev<T>(), L.mesh, c.sg, dst, b, (const cplx<T>*)x, r);
     vlaunch(k_mg_node_v<T, VS>, (int64_t)np * c.sg.G, c.B, 0, P.st, L.lev<T>(), L.mesh, c.sg, np, dst,
             (const cplx<T>*)r, L.mg[0].dinv.as<float>(), phi, (T)emg_nodal_omega());
     vlaunch(k_mg_gadd_v<T, VS>, L.nl * c.sg.G, c.B, 0, P.st, L.lev<T>(), L.mesh, c.sg, dst, (const cplx<T>*)phi, x);
@@ -319,6 +320,11 @@ static int bicgstab_v(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, co
             if (rel && (cand || (act && (it - last_rel >= rel->every || it == itmax)))) {
                 RC((reliable_update<T, VS>(P, LV, *rel, x, r, rhat, 1, act)));
                 last_rel = it;
+                if (act && rel && P.o.precond == 'G') {  // fresh recurrences (see gpbicg_v)
+                    for (cplx<T>* q : {p, v, y, z}) CK(cudaMemsetAsync(q, 0, vb, P.st));
+                    vlaunch(k_residual_v<T, double, VSD, 6>, LV.nl * cd.sg.G, cd.B, cd.smem, P.st, LV.lev<double>(), M,
+                            cd.sg, dst, rel->b64, rel->x64, r, rhat, redbuf(P), nullptr, 0);
+                }
             }
             if (!act) break;
         }
@@ -365,6 +371,8 @@ static int gpbicg_v(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, cons
     CK(cudaMemcpyAsync(p, rp, vb, cudaMemcpyDeviceToDevice, P.st));
     int cur = 0, last_rel = 0;
     const bool div1 = !rel && std::is_same<T, double>::value && P.o.div_cor == 1;
+    const bool restart_rel = rel && P.o.precond == 'G';
+    bool fresh = false;
     // one iteration up to the convergence check, with t' in tp[cc]
     auto body = [&](int cc) {
         vlaunch(k_gp_ap_v<T, VS>, LV.nl * c.sg.G, c.B, c.smem, P.st, L, M, c.sg, dst, p, ap, r0, r, redbuf(P));
@@ -414,12 +422,25 @@ static int gpbicg_v(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, cons
             if (rel && (cand || (act && (it - last_rel >= rel->every || it == itmax)))) {
                 RC((reliable_update<T, VS>(P, LV, *rel, x, r, r0, 3, act)));
                 last_rel = it;
+                if (act && restart_rel) {
+                    // fresh recurrences from the FP64 residual (the search directions of a
+                    // strongly preconditioned complex64 iteration carry its rounding noise)
+                    for (cplx<T>* q : {u, w, t, tp[0], tp[1], z}) CK(cudaMemsetAsync(q, 0, vb, P.st));
+                    vlaunch(k_residual_v<T, double, VSD, 5>, LV.nl * cd.sg.G, cd.B, cd.smem, P.st, LV.lev<double>(), M,
+                            cd.sg, dst, rel->b64, rel->x64, r, r0, redbuf(P), nullptr, 0);
+                    precond<T, VS, RHS_VEC>(P, LV, rp, r, nullptr, nullptr);
+                    CK(cudaMemcpyAsync(p, rp, vb, cudaMemcpyDeviceToDevice, P.st));
+                    fresh = true;
+                }
             }
             stop = !act;
         }
         if (stop) break;
-        tail();
-        cur ^= 1;
+        if (!fresh) {
+            tail();
+            cur ^= 1;
+        }
+        fresh = false;
     }
     if (rel) vlaunch(k_flush_v<T, VS, true>, LV.nl * c.sg.G, c.B, 0, P.st, M, c.sg, dst, rel->x64, x, nullptr);
     RC(sync_state(P));

@@ -6,7 +6,8 @@
 // l-1 is level l with every pair of cells merged, mesh_coarsen
 // fdfe_main.f90:18-84), each with its own rediscretised operator:
 //   * smoother: the multi-colour SSOR of the Krylov solves, followed by a
-//     nodal (gradient-space) step: r = b - A x, phi = w D^-1 G^T V r with D
+//     nodal (gradient-space) step: phi = w D^-1 G^T V r with r = b - A x (formed
+//     as b + i w mu Ms x, see k_mg_mres_v) and D
 //     the diagonal of G^T V A G = -i w mu N (N the nodal operator of the
 //     gradient correction), x += G phi.  Point smoothers cannot reduce the
 //     error in the near-null space of the curl-curl operator (discrete
@@ -44,6 +45,52 @@ __global__ void k_mg_res_v(Lev<T> L, Mesh M, SysG sgp, const KState* st, const c
 #pragma unroll
         for (int u = 0; u < VS; u++) ax.v[u] = bv.v[u] - ax.v[u];
         cvst_m<T, VS>(r + g, ax, S.act);
+    }
+}
+
+// Gradient-space residual of the nodal step, q = b + i wm Ms x on interior
+// edges (0 on boundary edges).  G^T V A = -i wm G^T V Ms exactly (V C is
+// symmetric and C G = 0), so G^T V q equals G^T V (b - A x) without the
+// curl-curl terms: the full residual r = b - A x carries rounding noise of the
+// size eps |C x|, which the nodal step divides by wm sigma -- in air (sigma
+// 1e-8) a complex64 V-cycle turned that noise into gradient fields of order
+// one and diverged.
+template <class T, int VS, int O>
+__device__ __forceinline__ void mg_mass_row(const Lev<T>& L, const Mesh& M, uint32_t e, int i, int j, int k,
+                                            const cplx<T>* x, int ns, int s0, const T (&wm)[VS], const CV<T, VS>& bv,
+                                            CV<T, VS>& q) {
+    if (mbnd(M, O, i, j, k)) {
+        cvzero<T, VS>(q);
+        return;
+    }
+    const RowK<T> K = row_k_e<T, O, false, true, true>(L, e, i, j, k);
+    const RowN N = row_n<O>(M, e, i, j, k);
+    CV<T, VS> C, Mm, xe;
+    row_off<T, VS, O, false, true, true, true>(K, N, x, ns, s0, C, Mm);
+    cvld<T, VS>(xe, x + (size_t)e * ns + s0);
+#pragma unroll
+    for (int u = 0; u < VS; u++) {
+        const T mx = Mm.v[u].x + K.sbar * xe.v[u].x, my = Mm.v[u].y + K.sbar * xe.v[u].y;
+        q.v[u] = mk<T>(bv.v[u].x - wm[u] * my, bv.v[u].y + wm[u] * mx);
+    }
+}
+template <class T, int VS>
+__global__ void k_mg_mres_v(Lev<T> L, Mesh M, SysG sgp, const KState* st, const cplx<T>* __restrict__ b,
+                            const cplx<T>* __restrict__ x, cplx<T>* __restrict__ q) {
+    const int ns = sgp.ns, s0 = (threadIdx.x % sgp.G) * VS;
+    const SysV<T, VS> S = load_sys<T, VS>(st, s0);
+    if (!S.act) return;
+    SFDX_GRID_LOOP(t, M.nl * sgp.G) {
+        uint32_t e;
+        int i, j, k;
+        const int o = mdecode_plane(M, fdiv(sgp.fG, t), e, i, j, k);
+        const size_t g = (size_t)e * ns + s0;
+        CV<T, VS> bv, qv;
+        cvld<T, VS>(bv, b + g);
+        if (o == OX) mg_mass_row<T, VS, OX>(L, M, e, i, j, k, x, ns, s0, S.wm, bv, qv);
+        else if (o == OY) mg_mass_row<T, VS, OY>(L, M, e, i, j, k, x, ns, s0, S.wm, bv, qv);
+        else mg_mass_row<T, VS, OZ>(L, M, e, i, j, k, x, ns, s0, S.wm, bv, qv);
+        cvst_m<T, VS>(q + g, qv, S.act);
     }
 }
 

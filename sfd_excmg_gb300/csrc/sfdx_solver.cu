@@ -660,8 +660,12 @@ extern "C" void sfdx_default_opts(sfdx_opts* o) {
     // The two coarsest levels only feed the extrapolated guess: its residual on
     // the next level is the same for a coarse solve to 1e-6 as for an exact
     // (direct) one, so 1e-6 in FP64 stands in for PARDISO.
-    o->coarse_tol = 1e-6;
-    o->coarse_maxit = 1000;
+    // levels 1-2 stand in for PARDISO's direct solves: near-exact, because the
+    // relative residual is dominated by the Dirichlet rows of b (identity rows
+    // solved after one preconditioner application) -- at 1e-6 the interior of the
+    // coarse fields was barely solved
+    o->coarse_tol = 1e-12;
+    o->coarse_maxit = 3000;
     o->reliable_every = 40;
     o->batch = 0;
     o->verbose = 0;
@@ -1076,7 +1080,8 @@ extern "C" int sfdx_plan_impedance(sfdx_plan* plan, int nrec, const double* recv
         }
         CK(cudaStreamSynchronize(P.st));
         RC(impedance_from_surface(sv, F.a.data(), F.b.data(), F.c.data(), P.freq[f], nrec, recv, out_type,
-                                  (P.o.quirks & SFDX_QUIRK_RX_TRANSPOSE) ? 1 : 0, out + (size_t)f * nrec * 4,
+                                  (P.o.quirks & SFDX_QUIRK_RX_TRANSPOSE) ? 1 : 0,
+                                  out + (size_t)f * nrec * (out_type == 3 ? 8 : 4),
                                   tipper ? tipper + (size_t)f * nrec * 4 : nullptr));
     }
     return SFDX_OK;
@@ -1119,7 +1124,8 @@ extern "C" int sfdx_impedance(int nx, int ny, int nz, int nair, const double* a,
             sv.ezs[p] = x + xnl + ynl + (size_t)nair * pez;
         }
         RC(impedance_from_surface(sv, a, b, c, freq[f], nrec, recv, out_type, (quirks & SFDX_QUIRK_RX_TRANSPOSE) ? 1 : 0,
-                                  out + (size_t)f * nrec * 4, tipper ? tipper + (size_t)f * nrec * 4 : nullptr));
+                                  out + (size_t)f * nrec * (out_type == 3 ? 8 : 4),
+                                  tipper ? tipper + (size_t)f * nrec * 4 : nullptr));
     }
     return SFDX_OK;
 }

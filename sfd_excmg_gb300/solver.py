@@ -157,10 +157,12 @@ class Plan:
         capi.check(capi.lib().sfdx_plan_load(self._h, sp, son), "sfdx_plan_load")
 
     def impedance(self, recv=None, out_type: int = 1, tipper: bool = False):
+        """out[nf, nrec, 4] (out_type 0/1: Re/Im Zxy, Zyx; 2: apparent resistivities and phases) or
+        out[nf, nrec, 8] (out_type 3: Re/Im of Zxx, Zxy, Zyx, Zyy)."""
         m = self.model
         rv = _d(np.asarray(m.recv if recv is None else recv).T)  # [3][nrec]
         nrec = rv.shape[1]
-        out = np.zeros((m.nf, nrec, 4))
+        out = np.zeros((m.nf, nrec, 8 if out_type == 3 else 4))
         tip = np.zeros((m.nf, nrec, 4)) if tipper else None
         capi.check(capi.lib().sfdx_plan_impedance(self._h, nrec, capi.dptr(rv), out_type, capi.dptr(out),
                                                    capi.dptr(tip) if tip is not None else None),
@@ -286,7 +288,7 @@ def impedance(model: Model, ex, out_type: int = 1, quirks: int = capi.QUIRKS_REF
               recv=None):
     rv = _d(np.asarray(model.recv if recv is None else recv).T)
     nrec = rv.shape[1]
-    out = np.zeros((model.nf, nrec, 4))
+    out = np.zeros((model.nf, nrec, 8 if out_type == 3 else 4))
     tip = np.zeros((model.nf, nrec, 4)) if tipper else None
     x = _vec(ex, model.nf * 2, model.nl, "ex")
     capi.check(capi.lib().sfdx_impedance(model.nx, model.ny, model.nz, model.nair, capi.dptr(_d(model.a)),

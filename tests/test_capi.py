@@ -81,6 +81,27 @@ def test_host_impedance_matches_post_process():
             np.testing.assert_allclose(fld[k].reshape(-1, 10), fref, rtol=1e-13, atol=1e-15 * np.abs(fref).max())
 
 
+def test_full_impedance_tensor():
+    """out_type 3: the four components Z = E H^-1 of the two polarisations' receiver fields
+    (post_process's E and H, fdfe_main.f90:600-700); Zxy and Zyx equal out_type 1's."""
+    m = syn.small_aniso(freqs=(0.1, 10.0))
+    rng = np.random.default_rng(1)
+    ex = rng.standard_normal((2, 2, m.nl)) + 1j * rng.standard_normal((2, 2, m.nl))
+    om = O.OracleModel(m.nx, m.ny, m.nz, m.nair, m.a, m.b, m.c, m.sigma, m.freq, m.recv)
+    z4 = S.impedance(m, ex, out_type=3)
+    z2 = S.impedance(m, ex, out_type=1)
+    assert z4.shape == (m.nf, m.recv.shape[0], 8)
+    np.testing.assert_allclose(z4[..., 2:6], z2, rtol=1e-14, atol=0)
+    for k, ff in enumerate(m.freq):
+        _, _, f = O.post_process(om, ex[k, 0], ex[k, 1], ff, 1, 2)
+        E = np.stack([f[:, [0, 1]], f[:, [5, 6]]], axis=2)  # [rec][Ex, Ey][pol]
+        H = np.stack([f[:, [2, 3]], f[:, [7, 8]]], axis=2)  # [rec][Hx, Hy][pol]
+        Z = E @ np.linalg.inv(H)
+        ref = np.stack([Z[:, 0, 0], Z[:, 0, 1], Z[:, 1, 0], Z[:, 1, 1]], 1)
+        got = z4[k][:, 0::2] + 1j * z4[k][:, 1::2]
+        np.testing.assert_allclose(got, ref, rtol=1e-11, atol=1e-13 * np.abs(ref).max())
+
+
 def test_model_file_roundtrip(tmp_path):
     m = syn.small_aniso()
     name = str(tmp_path / "mod")
