@@ -44,7 +44,9 @@ extern "C" {
 #define SFDX_QUIRK_COARSEN_SHIFT 1   /* mesh_coarsen fine-cell index (fdfe_main.f90:64)          */
 #define SFDX_QUIRK_EXCMG_MIDPOINT 2  /* cal_coef along-edge nodes (excmg.f90:685,711,737)         */
 #define SFDX_QUIRK_RX_TRANSPOSE 4    /* arho_interp2 rd=2 stencil (fdfe_main.f90:763-768)         */
-#define SFDX_QUIRKS_REFERENCE 7
+#define SFDX_QUIRK_TOPO_PLANE 8      /* topography receiver plane one cell deep and c(nair+1) as
+                                        its vertical step (fdfe_main.f90:604-616, 627-629)       */
+#define SFDX_QUIRKS_REFERENCE 15
 
 /* solver ids (.fwd line 2, read_input file_opt.f90:102).  TFQMR, BiCG and COCR
  * are broken or unreachable in the reference (ptfqmr, pbicg, pcocr); these are
@@ -79,8 +81,8 @@ typedef struct sfdx_opts {
                            mesh levels, multi-colour SSOR + nodal smoother; such
                            plans coarsen the conductivity without the index shift
                            of SFDX_QUIRK_COARSEN_SHIFT and, in mixed precision,
-                           replace the complex64 residual at least every 8
-                           iterations                                            */
+                           run complex128 Krylov iterations preconditioned by a
+                           complex64 V-cycle                                     */
     int div_cor;        /* divergence correction (div_cor): 0 off, 1 the reference's
                            (div_correc every corr_intv iterations), 2 consistent
                            gradient-space correction between restart cycles of
@@ -224,6 +226,21 @@ void sfdx_plan_destroy(sfdx_plan* plan);
 int sfdx_impedance(int nx, int ny, int nz, int nair, const double* a, const double* b, const double* c, int nf,
                    const double* freq, const double* ex, int nrec, const double* recv, int out_type, int quirks,
                    double* out, double* tipper);
+/* Impedances with topography: the receivers of each surface column sit on that
+ * column's earth surface instead of the flat plane nair (the topo branch of
+ * post_process, fdfe_main.f90:604-616, which the shipped driver never reaches
+ * because it passes no topo).  abr[6] = (i1, i2, j1, j2, k1, k2), 1-based: the
+ * column window and the range of cells searched; topo[(i2-i1+1)(j2-j1+1)] the
+ * elevation (m, positive up) of each window column, x fastest.  A column's
+ * plane is set by the first cell of k1..k2 whose centre lies at or below -topo:
+ * with SFDX_QUIRK_TOPO_PLANE (reference) its lower node plane and the vertical
+ * step c(nair+1) for every column, without it its upper node plane (the top of
+ * the first earth cell) and the cell below that plane.  Columns outside the
+ * window, or with no such cell, use nair.  Other arguments and the output as
+ * sfdx_impedance. */
+int sfdx_impedance_topo(int nx, int ny, int nz, int nair, const double* a, const double* b, const double* c, int nf,
+                        const double* freq, const double* ex, int nrec, const double* recv, int out_type, int quirks,
+                        const int* abr, const double* topo, double* out, double* tipper);
 /* The surface fields at the receivers from which sfdx_impedance forms Z and the
  * tippers (the arho rows of post_process / arho_interp2, fdfe_main.f90:600-700,
  * 718-790): fields[nf][nrec][2][5] complex (interleaved doubles), (Ex, Ey, Hx,

@@ -77,6 +77,7 @@ def lib():
             L.orc_bicgstab_fixed.restype = ctypes.c_int
             L.orc_extint_v.restype = ctypes.c_int
             L.orc_post_process.restype = ctypes.c_int
+            L.orc_post_process_topo.restype = ctypes.c_int
             L.orc_div_correc.restype = ctypes.c_int
             L.orc_ssor_apply.restype = ctypes.c_int
             L.orc_ilu_apply.restype = ctypes.c_int
@@ -283,6 +284,55 @@ def post_process(model: OracleModel, x1, x2, ff, out_type=1, rd=2):
                                 _p(_d(model.c)), ctypes.c_double(ff), _z(x1).ctypes.data_as(ctypes.c_void_p),
                                 _z(x2).ctypes.data_as(ctypes.c_void_p), nrec, _p(recv), out_type, rd, _p(out),
                                 _p(tip), fld.ctypes.data_as(ctypes.c_void_p))
+    if rc != 0:
+        raise ValueError(f"receiver {-rc} lies outside the interpolation stencil")
+    return out, tip, fld
+
+
+def receiver_planes(model: OracleModel, abr, topo, corrected=False):
+    """The receiver plane of every surface column with topography (post_process,
+    fdfe_main.f90:604-616): inside the window abr = (i1, i2, j1, j2, k1, k2) (1-based) a
+    column's plane is the first cell k in k1..k2 whose centre ccz(k) lies at or below the
+    surface -topo (topo = elevation, positive up; ccz of the reference, :593-595), outside it
+    nair.  The reference takes that cell's lower node plane (m = k) and the vertical step
+    c(nair+1) for every column; corrected = True takes its upper plane (m = k - 1, the top of
+    the first earth cell, which is nair on flat ground) and the cell below that plane
+    (c(m+1)).  A column with no such cell keeps nair.  Returns (mcol[ny*nx], czcol[ny*nx])."""
+    nx, ny, nair = model.nx, model.ny, model.nair
+    c = _d(model.c)
+    ccz = -c[:nair].sum() + np.cumsum(c) - c / 2
+    i1, i2, j1, j2, k1, k2 = (int(v) for v in abr)
+    mcol = np.full(nx * ny, nair, np.int32)
+    czcol = np.full(nx * ny, c[nair])
+    for j in range(1, ny + 1):
+        for i in range(1, nx + 1):
+            if not (i1 <= i <= i2 and j1 <= j <= j2):
+                continue
+            t = topo[(j - j1) * (i2 - i1 + 1) + i - i1]
+            for k in range(k1, k2 + 1):
+                if ccz[k - 1] >= -t:
+                    m = k - 1 if corrected else k
+                    mcol[(j - 1) * nx + i - 1] = m
+                    if corrected:
+                        czcol[(j - 1) * nx + i - 1] = c[m]
+                    break
+    return mcol, czcol
+
+
+def post_process_topo(model: OracleModel, x1, x2, ff, mcol, czcol, out_type=1, rd=2):
+    """post_process with a receiver plane per column (receiver_planes)."""
+    nrec = model.recv.shape[0]
+    recv = np.asfortranarray(model.recv, dtype=np.float64).ravel(order="F").copy()
+    out = np.zeros((nrec, 4))
+    tip = np.zeros((nrec, 4))
+    fld = np.zeros((nrec, 10), np.complex128)
+    mc = np.ascontiguousarray(mcol, np.int32)
+    cz = _d(czcol)
+    rc = lib().orc_post_process_topo(model.nx, model.ny, model.nz, model.nair, _p(_d(model.a)), _p(_d(model.b)),
+                                     _p(_d(model.c)), ctypes.c_double(ff), _z(x1).ctypes.data_as(ctypes.c_void_p),
+                                     _z(x2).ctypes.data_as(ctypes.c_void_p), nrec, _p(recv), out_type, rd, _p(out),
+                                     _p(tip), fld.ctypes.data_as(ctypes.c_void_p),
+                                     mc.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), _p(cz))
     if rc != 0:
         raise ValueError(f"receiver {-rc} lies outside the interpolation stencil")
     return out, tip, fld

@@ -1531,15 +1531,33 @@ static int arho_interp2(int mode, int rd, int nx, int ny, const double *ax, cons
 #undef F
 }
 
+/* post_process with an optional receiver plane per surface column (the
+ * topography branch, fdfe_main.f90:604-616): mcol[(j-1)*nx+i-1] is the node
+ * plane m of column (i,j) (NULL: nair everywhere) and czcol the vertical step of
+ * its H derivatives (NULL: c(nair+1), as the reference uses for every column). */
+static int post_process_cols(int nx, int ny, int nz, int nair, const double *a, const double *b, const double *c,
+                             double ff, const zc *x1, const zc *x2, int nrec, const double *recv, int out_type, int rd,
+                             double *out, double *tip, zc *fields_out, const int *mcol, const double *czcol);
 int orc_post_process(int nx, int ny, int nz, int nair, const double *a, const double *b, const double *c, double ff,
                      const zc *x1, const zc *x2, int nrec, const double *recv, int out_type, int rd, double *out,
                      double *tip, zc *fields_out) {
+    return post_process_cols(nx, ny, nz, nair, a, b, c, ff, x1, x2, nrec, recv, out_type, rd, out, tip, fields_out,
+                             NULL, NULL);
+}
+int orc_post_process_topo(int nx, int ny, int nz, int nair, const double *a, const double *b, const double *c,
+                          double ff, const zc *x1, const zc *x2, int nrec, const double *recv, int out_type, int rd,
+                          double *out, double *tip, zc *fields_out, const int *mcol, const double *czcol) {
+    return post_process_cols(nx, ny, nz, nair, a, b, c, ff, x1, x2, nrec, recv, out_type, rd, out, tip, fields_out,
+                             mcol, czcol);
+}
+static int post_process_cols(int nx, int ny, int nz, int nair, const double *a, const double *b, const double *c,
+                             double ff, const zc *x1, const zc *x2, int nrec, const double *recv, int out_type, int rd,
+                             double *out, double *tip, zc *fields_out, const int *mcol, const double *czcol) {
     const int64_t n1 = (int64_t)nx * (ny + 1) * (nz + 1), n2 = (int64_t)ny * (nz + 1) * (nx + 1);
     size_t nxy = (size_t)nx * ny;
     zc *ex = (zc *)calloc(nxy * 2, sizeof(zc)), *ey = (zc *)calloc(nxy * 2, sizeof(zc));
     zc *hx = (zc *)calloc(nxy * 2, sizeof(zc)), *hy = (zc *)calloc(nxy * 2, sizeof(zc)), *hz = (zc *)calloc(nxy * 2, sizeof(zc));
     zc *arho = (zc *)calloc((size_t)nrec * 5, sizeof(zc)), *arho2 = (zc *)calloc((size_t)nrec * 5, sizeof(zc));
-    const int m = nair;
     const zc iwm = I * 2.0 * PI * ff * MU;
 #define X(v, n) v[(n)-1]
 #define FLD(arr, i, j, md) arr[((size_t)((md)-1) * ny + (j)-1) * nx + (i)-1]
@@ -1547,6 +1565,8 @@ int orc_post_process(int nx, int ny, int nz, int nair, const double *a, const do
         const zc *xv = pol == 1 ? x1 : x2;
         for (int j = 1; j <= ny; j++)
             for (int i = 1; i <= nx; i++) {
+                const int m = mcol ? mcol[(size_t)(j - 1) * nx + i - 1] : nair;
+                const double cz = czcol ? czcol[(size_t)(j - 1) * nx + i - 1] : c[nair];
                 int64_t idx = (int64_t)m * nx * (ny + 1) + (int64_t)(j - 1) * nx + i;
                 int64_t idx2 = n1 + (int64_t)m * ny * (nx + 1) + (int64_t)(j - 1) * (nx + 1) + i;
                 int64_t idx3 = n1 + n2 + (int64_t)m * (nx + 1) * (ny + 1) + (int64_t)(j - 1) * (nx + 1) + i;
@@ -1557,10 +1577,10 @@ int orc_post_process(int nx, int ny, int nz, int nair, const double *a, const do
                     FLD(ey, i, j, 2) = (X(x2, idx2) + X(x2, idx2 + 1)) / 2.0;
                 }
                 zc exz = ((X(xv, idx + (int64_t)nx * (ny + 1)) + X(xv, idx + (int64_t)nx * (ny + 1) + nx)) / 2.0 -
-                          FLD(ex, i, j, pol)) / c[nair];
+                          FLD(ex, i, j, pol)) / cz;
                 zc ezx = ((X(xv, idx3 + 1) + X(xv, idx3 + nx + 2)) / 2.0 - (X(xv, idx3 + nx + 1) + X(xv, idx3)) / 2.0) / a[i - 1];
                 zc eyz = ((X(xv, idx2 + (int64_t)ny * (nx + 1)) + X(xv, idx2 + (int64_t)ny * (nx + 1) + 1)) / 2.0 -
-                          FLD(ey, i, j, pol)) / c[nair];
+                          FLD(ey, i, j, pol)) / cz;
                 zc ezy = (-(X(xv, idx3) + X(xv, idx3 + 1)) / 2.0 + (X(xv, idx3 + nx + 1) + X(xv, idx3 + nx + 2)) / 2.0) / b[j - 1];
                 zc exy = (X(xv, idx + nx) - X(xv, idx)) / b[j - 1];
                 zc eyx = (X(xv, idx2 + 1) - X(xv, idx2)) / a[i - 1];

@@ -28,7 +28,8 @@ ERRORS = {
 QUIRK_COARSEN_SHIFT = 1
 QUIRK_EXCMG_MIDPOINT = 2
 QUIRK_RX_TRANSPOSE = 4
-QUIRKS_REFERENCE = 7
+QUIRK_TOPO_PLANE = 8
+QUIRKS_REFERENCE = 15
 FP64 = 0
 MIXED = 1
 
@@ -101,6 +102,10 @@ _PROTO = {
     "sfdx_impedance": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, c_double_p,
                                       c_double_p, c_double_p, ctypes.c_int, c_double_p, c_double_p, ctypes.c_int,
                                       c_double_p, ctypes.c_int, ctypes.c_int, c_double_p, c_double_p]),
+    "sfdx_impedance_topo": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, c_double_p,
+                                           c_double_p, c_double_p, ctypes.c_int, c_double_p, c_double_p,
+                                           ctypes.c_int, c_double_p, ctypes.c_int, ctypes.c_int, c_int_p,
+                                           c_double_p, c_double_p, c_double_p]),
     "sfdx_impedance_misfit": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, c_double_p,
                                              c_double_p, c_double_p, ctypes.c_int, c_double_p, c_double_p,
                                              ctypes.c_int, c_double_p, ctypes.c_int, c_double_p, c_double_p,

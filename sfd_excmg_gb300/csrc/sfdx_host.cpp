@@ -279,13 +279,99 @@ static void receiver_fields(const SurfFields* F, const RecvStencil& S, zd f[2][5
     }
 }
 
+static int impedance_from_fields(const SurfFields (&F)[2], int nx, int ny, const double* a, const double* b,
+                                 double ff, int nrec, const double* recv, int out_type, int transpose, double* out,
+                                 double* tip, zd* fields);
+
 int impedance_from_surface(const SurfaceView& sv, const double* a, const double* b, const double* c, double ff,
                            int nrec, const double* recv, int out_type, int transpose, double* out, double* tip,
                            zd* fields) {
-    const int nx = sv.nx, ny = sv.ny;
     const zd iwm = zd(0, 1) * 2.0 * kPi * ff * kMu;
     SurfFields F[2];
     for (int p = 0; p < 2; p++) surface_fields(sv, p, a, b, c[sv.nair], iwm, F[p]);
+    return impedance_from_fields(F, sv.nx, sv.ny, a, b, ff, nrec, recv, out_type, transpose, out, tip, fields);
+}
+
+// Receiver plane per surface column with topography (post_process,
+// fdfe_main.f90:604-616): inside the window abr = (i1, i2, j1, j2, k1, k2)
+// (1-based) the first cell k of k1..k2 whose centre lies at or below the
+// surface -topo (elevation, positive up) marks the column's plane; outside the
+// window, or with no such cell, the plane is nair.  `reference`: the cell's
+// lower node plane (m = k) and the vertical step c(nair+1) for every column, as
+// the reference computes them; otherwise its upper plane (m = k - 1, the top of
+// the first earth cell, nair on flat ground) and the cell below it (c(m+1)).
+int receiver_planes(int nx, int ny, int nz, int nair, const double* c, const int* abr, const double* topo,
+                    int reference, int* mcol, double* czcol) {
+    if (abr[0] < 1 || abr[1] > nx || abr[0] > abr[1] || abr[2] < 1 || abr[3] > ny || abr[2] > abr[3] ||
+        abr[4] < 1 || abr[5] >= nz || abr[4] > abr[5])
+        return SFDX_ERR_ARG;
+    std::vector<double> ccz(nz);
+    double air = 0, acc = 0;
+    for (int k = 0; k < nair; k++) air += c[k];
+    for (int k = 0; k < nz; k++) {
+        acc += c[k];
+        ccz[k] = -air + acc - c[k] / 2;
+    }
+    for (int j = 1; j <= ny; j++)
+        for (int i = 1; i <= nx; i++) {
+            const size_t id = (size_t)(j - 1) * nx + i - 1;
+            mcol[id] = nair;
+            czcol[id] = c[nair];
+            if (i < abr[0] || i > abr[1] || j < abr[2] || j > abr[3]) continue;
+            const double t = topo[(size_t)(j - abr[2]) * (abr[1] - abr[0] + 1) + i - abr[0]];
+            for (int k = abr[4]; k <= abr[5]; k++)
+                if (ccz[k - 1] >= -t) {
+                    mcol[id] = reference ? k : k - 1;
+                    if (!reference) czcol[id] = c[k - 1];
+                    break;
+                }
+        }
+    return SFDX_OK;
+}
+
+// surface_fields with a plane per column: x is the whole field of one
+// polarisation (Ex, Ey, Ez blocks of the reference order)
+static void surface_fields_cols(const zd* x, int nx, int ny, int nz, const int* mcol, const double* czcol,
+                                const double* a, const double* b, zd iwm, SurfFields& F) {
+    const size_t xnl = (size_t)nx * (ny + 1) * (nz + 1), ynl = (size_t)(nx + 1) * ny * (nz + 1);
+    auto EX = [&](int k, int i, int j) { return x[((size_t)k * (ny + 1) + j) * nx + i]; };
+    auto EY = [&](int k, int i, int j) { return x[xnl + ((size_t)k * ny + j) * (nx + 1) + i]; };
+    auto EZ = [&](int k, int i, int j) { return x[xnl + ynl + ((size_t)k * (ny + 1) + j) * (nx + 1) + i]; };
+    F.init((size_t)nx * ny);
+    for (int j = 0; j < ny; j++)
+        for (int i = 0; i < nx; i++) {
+            const size_t id = (size_t)j * nx + i;
+            const int m = mcol[id];
+            const double cz = czcol[id];
+            zd ex0 = (EX(m, i, j) + EX(m, i, j + 1)) / 2.0;
+            zd ey0 = (EY(m, i, j) + EY(m, i + 1, j)) / 2.0;
+            F.E[0][id] = ex0;
+            F.E[1][id] = ey0;
+            zd exz = ((EX(m + 1, i, j) + EX(m + 1, i, j + 1)) / 2.0 - ex0) / cz;
+            zd ezx = ((EZ(m, i + 1, j) + EZ(m, i + 1, j + 1)) / 2.0 - (EZ(m, i, j + 1) + EZ(m, i, j)) / 2.0) / a[i];
+            zd eyz = ((EY(m + 1, i, j) + EY(m + 1, i + 1, j)) / 2.0 - ey0) / cz;
+            zd ezy = (-(EZ(m, i, j) + EZ(m, i + 1, j)) / 2.0 + (EZ(m, i, j + 1) + EZ(m, i + 1, j + 1)) / 2.0) / b[j];
+            zd exy = (EX(m, i, j + 1) - EX(m, i, j)) / b[j];
+            zd eyx = (EY(m, i + 1, j) - EY(m, i, j)) / a[i];
+            F.H[1][id] = (exz - ezx) / iwm;
+            F.H[0][id] = (ezy - eyz) / iwm;
+            F.H[2][id] = (exy - eyx) / iwm;
+        }
+}
+
+int impedance_topo(const zd* x1, const zd* x2, int nx, int ny, int nz, const int* mcol, const double* czcol,
+                   const double* a, const double* b, double ff, int nrec, const double* recv, int out_type,
+                   int transpose, double* out, double* tip) {
+    const zd iwm = zd(0, 1) * 2.0 * kPi * ff * kMu;
+    SurfFields F[2];
+    surface_fields_cols(x1, nx, ny, nz, mcol, czcol, a, b, iwm, F[0]);
+    surface_fields_cols(x2, nx, ny, nz, mcol, czcol, a, b, iwm, F[1]);
+    return impedance_from_fields(F, nx, ny, a, b, ff, nrec, recv, out_type, transpose, out, tip, nullptr);
+}
+
+static int impedance_from_fields(const SurfFields (&F)[2], int nx, int ny, const double* a, const double* b,
+                                 double ff, int nrec, const double* recv, int out_type, int transpose, double* out,
+                                 double* tip, zd* fields) {
     std::vector<double> aax, bby;
     cell_centres(nx, ny, a, b, aax, bby);
     for (int r = 0; r < nrec; r++) {

@@ -47,6 +47,13 @@ int impedance_from_surface(const SurfaceView& sv, const double* a, const double*
 // (optional, [nrec][4]) and its derivative with respect to the receiver fields,
 // cf [nrec][2 polarisations][Ex, Ey, Hx, Hy].  zobs [nrec][4] = (Re, Im Zxy,
 // Re, Im Zyx); wts [nrec][2] (null: 1).
+// receiver plane per surface column with topography and the impedances formed
+// there (post_process, fdfe_main.f90:604-616); sfdx_host.cpp
+int receiver_planes(int nx, int ny, int nz, int nair, const double* c, const int* abr, const double* topo,
+                    int reference, int* mcol, double* czcol);
+int impedance_topo(const std::complex<double>* x1, const std::complex<double>* x2, int nx, int ny, int nz,
+                   const int* mcol, const double* czcol, const double* a, const double* b, double ff, int nrec,
+                   const double* recv, int out_type, int transpose, double* out, double* tip);
 int impedance_cotangents(const SurfaceView& sv, const double* a, const double* b, const double* c, double ff,
                          int nrec, const double* recv, int transpose, const double* zobs, const double* wts,
                          double* misfit, double* zpred, std::complex<double>* cf);

@@ -88,6 +88,13 @@ template <class T> static int emg_prepare(Plan& P, const Level& LV) {
     if (P.o.precond != 'G') return SFDX_OK;
     const int l = level_index(P, LV);
     if (l < 0) return SFDX_ERR_ARG;
+    if (P.pf32) {  // complex64 copies of the preconditioner's input and output
+        for (DBuf* b : {&P.emg_q32, &P.emg_o32}) {
+            void* before = b->p;
+            RC(b->alloc((size_t)LV.nl * P.ns * sizeof(float2)));
+            if (b->p != before) P.emg_epoch++;
+        }
+    }
     for (int m = 0; m <= l; m++) {
         const Level& L = P.lev[m];
         RC(nodal_setup(P, L));
@@ -158,11 +165,40 @@ static void emg_vcycle(Plan& P, int l, const cplx<T>* b, cplx<T>* x, bool pre) {
     emg_smooth<T, VS>(P, L, c, b, x);
 }
 
+// Complex64 V-cycle for a complex128 Krylov solve (P.pf32): MODE's vector
+// update in FP64 with the result rounded to complex64, the V-cycle with the
+// complex64 grouping of the plan, the output widened to FP64.  The Krylov
+// vectors and the operator stay FP64, so the V-cycle's large discrete-gradient
+// components (cheap in the operator's norm, costly under a rounded operator)
+// never meet complex64 operator arithmetic.
+template <int VS, int MODE>
+static void emg_precond32(Plan& P, const Level& LV, double2* out, double2* q, const double2* r, const double2* v,
+                          double2* aux) {
+    const int l = level_index(P, LV);
+    const VCfg c = vcfg(P, LV.nl, 0, VS);
+    const KState* dst = P.d_state.as<KState>();
+    float2* q32 = P.emg_q32.as<float2>();
+    float2* o32 = P.emg_o32.as<float2>();
+    vlaunch(k_mg_to32_v<VS, MODE>, LV.nl * c.sg.G, c.B, 0, P.st, LV.mesh, c.sg, dst, q, r, v, aux, q32);
+    switch (plan_vs<float>(P)) {
+        case 4: emg_vcycle<float, 4>(P, l, q32, o32, false); break;
+        case 2: emg_vcycle<float, 2>(P, l, q32, o32, false); break;
+        default: emg_vcycle<float, 1>(P, l, q32, o32, false); break;
+    }
+    vlaunch(k_mg_to64_v<VS>, LV.nl * c.sg.G, c.B, 0, P.st, LV.mesh, c.sg, dst, (const float2*)o32, out);
+}
+
 // out = M^{-1} rhs (rhs produced by MODE, see k_fwd_v): Jacobi, multi-colour
 // SSOR, or the edge multigrid V-cycle whose first SSOR sweep carries MODE.
 template <class T, int VS, int MODE>
 static void precond(Plan& P, const Level& LV, cplx<T>* out, cplx<T>* q, const cplx<T>* r, const cplx<T>* v,
                     cplx<T>* aux = nullptr) {
+    if constexpr (std::is_same<T, double>::value) {
+        if (P.o.precond == 'G' && P.pf32) {
+            emg_precond32<VS, MODE>(P, LV, out, q, r, v, aux);
+            return;
+        }
+    }
     if (P.o.precond == 'J') {
         const int B = block_for(P.ns);
         KL(k_jacobi<T, MODE><<<grid_for(LV.nl * P.ns, B, 16), B, 0, P.st>>>(LV.lev<T>(), P.d_state.as<KState>(), P.ns, out,
@@ -204,7 +240,7 @@ static std::vector<uintptr_t> interval_key(const Plan& P, const Level& LV, int s
                                 (uintptr_t)P.hist_stride, (uintptr_t)LV.sig32.p, (uintptr_t)LV.sig64.p,
                                 (uintptr_t)LV.tab32.p, (uintptr_t)LV.tab64.p, (uintptr_t)LV.rc_ok,
                                 (uintptr_t)LV.rc32.p, (uintptr_t)LV.rc64.p,
-                                (uintptr_t)(P.o.ssor_omega * 1e6), (uintptr_t)P.emg_epoch};
+                                (uintptr_t)(P.o.ssor_omega * 1e6), (uintptr_t)P.emg_epoch, (uintptr_t)P.pf32};
     for (const DBuf& b : P.kv) k.push_back((uintptr_t)b.p);
     k.insert(k.end(), extra);
     return k;
@@ -320,11 +356,6 @@ static int bicgstab_v(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, co
             if (rel && (cand || (act && (it - last_rel >= rel->every || it == itmax)))) {
                 RC((reliable_update<T, VS>(P, LV, *rel, x, r, rhat, 1, act)));
                 last_rel = it;
-                if (act && rel && P.o.precond == 'G') {  // fresh recurrences (see gpbicg_v)
-                    for (cplx<T>* q : {p, v, y, z}) CK(cudaMemsetAsync(q, 0, vb, P.st));
-                    vlaunch(k_residual_v<T, double, VSD, 6>, LV.nl * cd.sg.G, cd.B, cd.smem, P.st, LV.lev<double>(), M,
-                            cd.sg, dst, rel->b64, rel->x64, r, rhat, redbuf(P), nullptr, 0);
-                }
             }
             if (!act) break;
         }
@@ -371,8 +402,6 @@ static int gpbicg_v(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, cons
     CK(cudaMemcpyAsync(p, rp, vb, cudaMemcpyDeviceToDevice, P.st));
     int cur = 0, last_rel = 0;
     const bool div1 = !rel && std::is_same<T, double>::value && P.o.div_cor == 1;
-    const bool restart_rel = rel && P.o.precond == 'G';
-    bool fresh = false;
     // one iteration up to the convergence check, with t' in tp[cc]
     auto body = [&](int cc) {
         vlaunch(k_gp_ap_v<T, VS>, LV.nl * c.sg.G, c.B, c.smem, P.st, L, M, c.sg, dst, p, ap, r0, r, redbuf(P));
@@ -422,25 +451,12 @@ static int gpbicg_v(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, cons
             if (rel && (cand || (act && (it - last_rel >= rel->every || it == itmax)))) {
                 RC((reliable_update<T, VS>(P, LV, *rel, x, r, r0, 3, act)));
                 last_rel = it;
-                if (act && restart_rel) {
-                    // fresh recurrences from the FP64 residual (the search directions of a
-                    // strongly preconditioned complex64 iteration carry its rounding noise)
-                    for (cplx<T>* q : {u, w, t, tp[0], tp[1], z}) CK(cudaMemsetAsync(q, 0, vb, P.st));
-                    vlaunch(k_residual_v<T, double, VSD, 5>, LV.nl * cd.sg.G, cd.B, cd.smem, P.st, LV.lev<double>(), M,
-                            cd.sg, dst, rel->b64, rel->x64, r, r0, redbuf(P), nullptr, 0);
-                    precond<T, VS, RHS_VEC>(P, LV, rp, r, nullptr, nullptr);
-                    CK(cudaMemcpyAsync(p, rp, vb, cudaMemcpyDeviceToDevice, P.st));
-                    fresh = true;
-                }
             }
             stop = !act;
         }
         if (stop) break;
-        if (!fresh) {
-            tail();
-            cur ^= 1;
-        }
-        fresh = false;
+        tail();
+        cur ^= 1;
     }
     if (rel) vlaunch(k_flush_v<T, VS, true>, LV.nl * c.sg.G, c.B, 0, P.st, M, c.sg, dst, rel->x64, x, nullptr);
     RC(sync_state(P));

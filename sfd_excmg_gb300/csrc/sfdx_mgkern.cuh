@@ -94,6 +94,77 @@ __global__ void k_mg_mres_v(Lev<T> L, Mesh M, SysG sgp, const KState* st, const 
     }
 }
 
+// Complex64 preconditioning of a complex128 Krylov solve: the vector update
+// of MODE (as the first sweep of k_fwd_v applies it) in FP64, its result
+// rounded to complex64 for the V-cycle; and the V-cycle's output widened back.
+template <int VS, int MODE>
+__global__ void k_mg_to32_v(Mesh M, SysG sgp, const KState* st, double2* __restrict__ q, const double2* __restrict__ r,
+                            const double2* __restrict__ v, double2* __restrict__ aux, float2* __restrict__ q32) {
+    const int ns = sgp.ns, s0 = (threadIdx.x % sgp.G) * VS;
+    const SysV<double, VS> S = load_sys<double, VS>(st, s0);
+    if (!S.act) return;
+    double2 c1[VS], c2[VS];
+#pragma unroll
+    for (int u = 0; u < VS; u++) {
+        c1[u] = MODE == RHS_PUPD || MODE == RHS_COCR ? st[s0 + u].beta : st[s0 + u].alpha;
+        c2[u] = st[s0 + u].omega;
+    }
+    SFDX_GRID_LOOP(t, M.nl * sgp.G) {
+        const size_t g = (size_t)fdiv(sgp.fG, t) * ns + s0;
+        CV<double, VS> rhs;
+        if (MODE == RHS_PUPD) {
+            CV<double, VS> rr, qq, vv;
+            cvld<double, VS>(rr, r + g);
+            cvldw<double, VS>(qq, q + g);
+            cvld<double, VS>(vv, v + g);
+#pragma unroll
+            for (int u = 0; u < VS; u++) rhs.v[u] = rr.v[u] + cmul<double>(c1[u], qq.v[u] - cmul<double>(c2[u], vv.v[u]));
+            cvst_m<double, VS>(q + g, rhs, S.act);
+        } else if (MODE == RHS_SUPD) {
+            CV<double, VS> rr, vv;
+            cvld<double, VS>(rr, r + g);
+            cvld<double, VS>(vv, v + g);
+#pragma unroll
+            for (int u = 0; u < VS; u++) rhs.v[u] = rr.v[u] - cmul<double>(c1[u], vv.v[u]);
+            cvst_m<double, VS>(q + g, rhs, S.act);
+        } else if (MODE == RHS_COCR) {
+            CV<double, VS> uu, qq, zz, pp;
+            cvld<double, VS>(uu, r + g);
+            cvldw<double, VS>(qq, q + g);
+            cvld<double, VS>(zz, v + g);
+            cvldw<double, VS>(pp, aux + g);
+#pragma unroll
+            for (int u = 0; u < VS; u++) {
+                rhs.v[u] = uu.v[u] + cmul<double>(c1[u], qq.v[u]);
+                pp.v[u] = zz.v[u] + cmul<double>(c1[u], pp.v[u]);
+            }
+            cvst_m<double, VS>(q + g, rhs, S.act);
+            cvst_m<double, VS>(aux + g, pp, S.act);
+        } else {
+            cvldw<double, VS>(rhs, q + g);
+        }
+        CV<float, VS> f;
+#pragma unroll
+        for (int u = 0; u < VS; u++) f.v[u] = make_float2((float)rhs.v[u].x, (float)rhs.v[u].y);
+        cvst_m<float, VS>(q32 + g, f, S.act);
+    }
+}
+template <int VS>
+__global__ void k_mg_to64_v(Mesh M, SysG sgp, const KState* st, const float2* __restrict__ x32, double2* __restrict__ x) {
+    const int ns = sgp.ns, s0 = (threadIdx.x % sgp.G) * VS;
+    const SysV<double, VS> S = load_sys<double, VS>(st, s0);
+    if (!S.act) return;
+    SFDX_GRID_LOOP(t, M.nl * sgp.G) {
+        const size_t g = (size_t)fdiv(sgp.fG, t) * ns + s0;
+        CV<float, VS> f;
+        cvld<float, VS>(f, x32 + g);
+        CV<double, VS> d;
+#pragma unroll
+        for (int u = 0; u < VS; u++) d.v[u] = make_double2((double)f.v[u].x, (double)f.v[u].y);
+        cvst_m<double, VS>(x + g, d, S.act);
+    }
+}
+
 // x += z for the active systems
 template <class T, int VS>
 __global__ void k_mg_add_v(Mesh M, SysG sgp, const KState* st, cplx<T>* __restrict__ x, const cplx<T>* __restrict__ z) {

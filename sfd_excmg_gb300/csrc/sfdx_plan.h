@@ -302,6 +302,11 @@ struct Plan {
     // advanced whenever a buffer or nodal operator that the edge multigrid
     // bakes into captured graphs is (re)allocated: part of every graph key
     long long emg_epoch = 0;
+    // complex128 Krylov iteration with the complex64 multigrid V-cycle as its
+    // preconditioner (mixed-precision plans with precond 'G', finer levels);
+    // emg_q32 / emg_o32: the V-cycle's complex64 input and output
+    bool pf32 = false;
+    DBuf emg_q32, emg_o32;
     Plan() = default;
     Plan(const Plan&) = delete;
     ~Plan() {

@@ -234,13 +234,8 @@ static int solve_level_mixed(Plan& P, const Level& LV, double tol, int itmax, st
     DBuf& x32 = P.x32;
     RC(x32.alloc(n * sizeof(float2)));
     RC(P.xb.alloc(n * sizeof(double2)));
-    // With the multigrid preconditioner eight iterations already reduce the
-    // complex64 residual by ~1e-4 -- about what complex64 arithmetic carries --
-    // so the FP64 residual replaces it at every check (8 iterations) at most;
-    // with 40 the recurrence ran into rounding noise and diverged.
-    int every = P.o.reliable_every > 0 ? P.o.reliable_every : 40;
-    if (P.o.precond == 'G') every = std::min(every, 8);
-    Reliable rel{P.b64.as<double2>(), P.x64.as<double2>(), every, P.xb.as<double2>()};
+    Reliable rel{P.b64.as<double2>(), P.x64.as<double2>(), P.o.reliable_every > 0 ? P.o.reliable_every : 40,
+                 P.xb.as<double2>()};
     if (P.o.solver == SFDX_SOLVER_GPBICG)
         RC(gpbicg<float>(P, LV, nullptr, x32.as<float2>(), nullptr, tol, itmax, nullptr, &rel));
     else if (P.o.solver == SFDX_SOLVER_BICGSTAB)
@@ -296,6 +291,17 @@ int solve_level(Plan& P, const Level& LV, double tol, int itmax, bool coarse, st
     // TFQMR and BiCG have no complex64 / reliable-update form: FP64 in every plan
     if (coarse || P.o.precision == SFDX_FP64 || P.o.solver == SFDX_SOLVER_TFQMR || P.o.solver == SFDX_SOLVER_BICG)
         return solve_level_fp64(P, LV, tol, itmax, its, status);
+    // mixed precision with the multigrid preconditioner: complex128 Krylov
+    // vectors and operator, complex64 V-cycle (a complex64 Krylov iteration
+    // under the V-cycle met the rounding of its complex64 operator on the
+    // V-cycle's large discrete-gradient components: FP64 residuals grew and
+    // every system fell back to FP64)
+    if (P.o.precond == 'G') {
+        P.pf32 = true;
+        const int rc = solve_level_fp64(P, LV, tol, itmax, its, status);
+        P.pf32 = false;
+        return rc;
+    }
     return solve_level_mixed(P, LV, tol, itmax, its, status);
 }
 
@@ -1127,6 +1133,27 @@ extern "C" int sfdx_impedance(int nx, int ny, int nz, int nair, const double* a,
                                   out + (size_t)f * nrec * (out_type == 3 ? 8 : 4),
                                   tipper ? tipper + (size_t)f * nrec * 4 : nullptr));
     }
+    return SFDX_OK;
+}
+
+extern "C" int sfdx_impedance_topo(int nx, int ny, int nz, int nair, const double* a, const double* b, const double* c,
+                                   int nf, const double* freq, const double* ex, int nrec, const double* recv,
+                                   int out_type, int quirks, const int* abr, const double* topo, double* out,
+                                   double* tipper) {
+    if (!a || !b || !c || !freq || !ex || !recv || !out || !abr || !topo || nrec < 1 || nair < 0 || nair + 1 >= nz)
+        return SFDX_ERR_ARG;
+    const int64_t xnl = (int64_t)nx * (ny + 1) * (nz + 1), ynl = (int64_t)(nx + 1) * ny * (nz + 1);
+    const int64_t nl = xnl + ynl + (int64_t)(nx + 1) * (ny + 1) * nz;
+    std::vector<int> mcol((size_t)nx * ny);
+    std::vector<double> czcol((size_t)nx * ny);
+    RC(receiver_planes(nx, ny, nz, nair, c, abr, topo, (quirks & SFDX_QUIRK_TOPO_PLANE) ? 1 : 0, mcol.data(),
+                       czcol.data()));
+    const std::complex<double>* X = reinterpret_cast<const std::complex<double>*>(ex);
+    for (int f = 0; f < nf; f++)
+        RC(impedance_topo(X + (size_t)(2 * f) * nl, X + (size_t)(2 * f + 1) * nl, nx, ny, nz, mcol.data(), czcol.data(),
+                          a, b, freq[f], nrec, recv, out_type, (quirks & SFDX_QUIRK_RX_TRANSPOSE) ? 1 : 0,
+                          out + (size_t)f * nrec * (out_type == 3 ? 8 : 4),
+                          tipper ? tipper + (size_t)f * nrec * 4 : nullptr));
     return SFDX_OK;
 }
 

@@ -256,8 +256,7 @@ __global__ void k_bwd_v(Lev<T> L, Mesh M, SysG sgp, const KState* st, cplx<T>* _
 // ------------------------------------------------------------------ residual
 // r = b - A x (x, b in XT; r, rhat in T).  MODE as k_residual (sfdx_kernels.cuh):
 // 0 BiCGStab start, 1 BiCGStab restart, 2 absolute residual, 3 GPBiCG start,
-// 4 residual restart only, 5 GPBiCG / 6 BiCGStab fresh start from the FP64
-// residual inside a mixed-precision solve (iteration counts kept).
+// 4 residual restart only.
 template <class T, class XT, int VS, int MODE>
 __global__ void k_residual_v(Lev<XT> L, Mesh M, SysG sgp, KState* st, const cplx<XT>* __restrict__ bvec,
                              const cplx<XT>* __restrict__ x, cplx<T>* __restrict__ r, cplx<T>* __restrict__ rhat, RedBuf rb,
@@ -330,24 +329,6 @@ __global__ void k_residual_v(Lev<XT> L, Mesh M, SysG sgp, KState* st, const cplx
         } else if (MODE == 2) {
             Q.err = nr;
             Q.babs = sqrt(v.y);
-        } else if (MODE == 5 || MODE == 6) {  // recurrences restarted, counts kept
-            Q.babs = sqrt(v.y);
-            Q.err = nr / Q.babs;
-            Q.errv = Q.err;
-            if (isnan(Q.err)) {
-                Q.status = ST_NAN;
-                Q.active = 0;
-                continue;
-            }
-            if (MODE == 5) {
-                Q.beta = make_double2(0.0, 0.0);
-            } else {
-                Q.alpha = make_double2(1.0, 0.0);
-                Q.omega = make_double2(1.0, 0.0);
-                Q.rhoold = make_double2(1.0, 0.0);
-                Q.rho = make_double2(v.x, 0.0);  // rhat == r
-                Q.beta = Q.rho;
-            }
         } else if (MODE == 3) {  // GPBiCG start (solvers.f90:203-221)
             Q.babs = sqrt(v.y);
             Q.err = nr / Q.babs;

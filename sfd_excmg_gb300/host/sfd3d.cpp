@@ -5,7 +5,9 @@
 // Options beyond the reference's argv come from the environment:
 //   SFDX_EXCMG=0|1 (fwd_acc, default 0 as in global_para.f90:19),
 //   SFDX_PRECISION=fp64|mixed, SFDX_VERBOSE=1, SFDX_TIPPER=1 (output_tipper:
-//   the tippers follow the impedances in <model>.res).
+//   the tippers follow the impedances in <model>.res), SFDX_DIV_COR=0|1|2
+//   (div_cor, default 1), SFDX_PRECOND=S|J|G (pre_type, default S; G the edge
+//   multigrid).
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -48,6 +50,14 @@ int main(int argc, char** argv) {
     if (const char* e = getenv("SFDX_EXCMG")) o.excmg = atoi(e);
     if (const char* p = getenv("SFDX_PRECISION")) o.precision = strcmp(p, "mixed") == 0 ? SFDX_MIXED : SFDX_FP64;
     if (getenv("SFDX_VERBOSE")) o.verbose = 1;
+    if (const char* d = getenv("SFDX_DIV_COR")) {
+        o.div_cor = atoi(d);
+        if (o.div_cor == 2) {  // the consistent correction's cycle length and nodal tolerance
+            o.corr_intv = 40;
+            o.corr_tol = 1e-2;
+        }
+    }
+    if (const char* p = getenv("SFDX_PRECOND")) o.precond = p[0];
     const long long nl = (long long)nx * (ny + 1) * (nz + 1) + (long long)(nx + 1) * ny * (nz + 1) +
                          (long long)(nx + 1) * (ny + 1) * nz;
     std::vector<double> ex((size_t)nf * 2 * nl * 2);

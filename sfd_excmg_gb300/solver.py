@@ -299,6 +299,28 @@ def impedance(model: Model, ex, out_type: int = 1, quirks: int = capi.QUIRKS_REF
     return (out, tip) if tipper else out
 
 
+def impedance_topo(model: Model, ex, abr, topo, out_type: int = 1, quirks: int = capi.QUIRKS_REFERENCE,
+                   tipper: bool = False, recv=None):
+    """Impedances with the receivers of each surface column on its own earth surface
+    (sfdx_impedance_topo): abr = (i1, i2, j1, j2, k1, k2) 1-based window, topo the elevation
+    (m) of every window column, x fastest."""
+    rv = _d(np.asarray(model.recv if recv is None else recv).T)
+    nrec = rv.shape[1]
+    ab = np.ascontiguousarray(abr, dtype=np.int32)
+    tp = _d(topo)
+    if ab.size != 6 or tp.size != (ab[1] - ab[0] + 1) * (ab[3] - ab[2] + 1):
+        raise ValueError("abr must hold 6 indices and topo one elevation per window column")
+    out = np.zeros((model.nf, nrec, 8 if out_type == 3 else 4))
+    tip = np.zeros((model.nf, nrec, 4)) if tipper else None
+    x = _vec(ex, model.nf * 2, model.nl, "ex")
+    capi.check(capi.lib().sfdx_impedance_topo(model.nx, model.ny, model.nz, model.nair, capi.dptr(_d(model.a)),
+                                              capi.dptr(_d(model.b)), capi.dptr(_d(model.c)), model.nf,
+                                              capi.dptr(_d(model.freq)), capi.zptr(x), nrec, capi.dptr(rv), out_type,
+                                              quirks, capi.iptr(ab), capi.dptr(tp), capi.dptr(out),
+                                              capi.dptr(tip) if tip is not None else None), "sfdx_impedance_topo")
+    return (out, tip) if tipper else out
+
+
 def receiver_fields(model: Model, ex, quirks: int = capi.QUIRKS_REFERENCE, recv=None) -> np.ndarray:
     """Surface E and H at the receivers, [nf, nrec, 2, 5] complex: (Ex, Ey, Hx, Hy, Hz)
     of the xy and yx polarisations, the fields post_process forms Z and the tippers from."""

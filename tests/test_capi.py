@@ -481,3 +481,26 @@ def test_noalloc_residual_refuses_misaligned_device_vectors(lib):
         st = lib.sfdx_residual_noalloc(n, n, n, dp(a), dp(a), dp(a), vp(sig), 1, dp(f), vp(rhs), vp(x), vp(r),
                                        dp(rel), None)
         assert st == 1, (hex(sig), hex(rhs), hex(x), hex(r), st)
+
+
+def test_topography_receiver_planes_match_oracle():
+    """sfdx_impedance_topo: receivers on each column's earth surface (the topo branch of
+    post_process, fdfe_main.f90:604-616) in the reference form (plane one cell deep,
+    vertical step c(nair+1)) and the corrected one, against the oracle; on flat ground the
+    corrected form is the flat impedance."""
+    m = syn.small_aniso(n=16, nair=8, freqs=(0.1, 10.0))
+    rng = np.random.default_rng(3)
+    ex = rng.standard_normal((2, 2, m.nl)) + 1j * rng.standard_normal((2, 2, m.nl))
+    om = O.OracleModel(m.nx, m.ny, m.nz, m.nair, m.a, m.b, m.c, m.sigma, m.freq, m.recv)
+    abr = np.array([3, 14, 2, 15, 2, 12], np.int32)
+    cols = (abr[1] - abr[0] + 1) * (abr[3] - abr[2] + 1)
+    topo = rng.uniform(0.0, 0.8 * m.c[:m.nair].sum(), cols)
+    for q, corrected in ((capi.QUIRKS_REFERENCE, False), (capi.QUIRKS_REFERENCE & ~capi.QUIRK_TOPO_PLANE, True)):
+        got = S.impedance_topo(m, ex, abr, topo, quirks=q)
+        mcol, czcol = O.receiver_planes(om, abr, topo, corrected=corrected)
+        assert len(set(mcol.tolist())) > 2  # the planes follow the surface
+        for k, ff in enumerate(m.freq):
+            ref, _, _ = O.post_process_topo(om, ex[k, 0], ex[k, 1], ff, mcol, czcol, 1, 2)
+            np.testing.assert_allclose(got[k], ref, rtol=1e-12, atol=1e-14 * np.abs(ref).max())
+    flat = S.impedance_topo(m, ex, abr, np.zeros(cols), quirks=capi.QUIRKS_REFERENCE & ~capi.QUIRK_TOPO_PLANE)
+    np.testing.assert_allclose(flat, S.impedance(m, ex), rtol=1e-14, atol=0)
