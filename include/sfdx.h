@@ -202,6 +202,13 @@ int sfdx_plan_kernel_time(sfdx_plan* plan, int kernel, int reps, double* ms, dou
  * application), and an operator plus an SSOR application in complex128.  No counterpart in
  * the reference.  The choices are returned in *vs32, *vs64 (optional). */
 int sfdx_plan_autotune(sfdx_plan* plan, int reps, int* vs32, int* vs64);
+/* Relative residual history of the finest-level solve of the last sfdx_plan_solve,
+ * hist[nf*2][maxit] (system 2f + pol), the value at iteration i (0-based, counted
+ * over all restart cycles) where the host checked it -- every 8th iteration and at
+ * the end -- and 0 elsewhere: the .ccv history of Bicg_stab_p / pgpbicg
+ * (solvers.f90:687-704) at the library's check points.  Write it with
+ * sfdx_write_ccv, which keeps the non-zero entries. */
+int sfdx_plan_history(const sfdx_plan* plan, double* hist, int maxit);
 /* Wall time (ms) of each level of the last solve, coarsest first (n >= levels). */
 int sfdx_plan_level_times(const sfdx_plan* plan, double* ms, int n);
 /* Solution of one of the two levels below the finest from the last EXCMG solve

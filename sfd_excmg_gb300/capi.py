@@ -97,6 +97,7 @@ _PROTO = {
     "sfdx_plan_destroy": (None, [ctypes.c_void_p]),
     "sfdx_plan_level_times": (ctypes.c_int, [ctypes.c_void_p, c_double_p, ctypes.c_int]),
     "sfdx_plan_level_fields": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, c_double_p]),
+    "sfdx_plan_history": (ctypes.c_int, [ctypes.c_void_p, c_double_p, ctypes.c_int]),
     "sfdx_plan_set_stream": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "sfdx_plan_kernel_time": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, c_double_p, c_double_p]),
     "sfdx_impedance": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, c_double_p,

@@ -836,6 +836,7 @@ static int corrected_cycles(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>*
                                                                               P.cx64.as<double2>()));
             bc = P.cb64.as<double2>();
             xc = P.cx64.as<double2>();
+            if (P.rec_on) P.rec_map = idx;
             P.ns = nd;
             P.wm.resize(nd);
             for (int i = 0; i < nd; i++) P.wm[i] = wm_all[idx[i]];
@@ -865,6 +866,7 @@ static int corrected_cycles(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>*
                                                                                P.cx64.as<double2>(), x64));
             P.ns = ns;
             P.wm = wm_all;
+            P.rec_map.clear();
             if (rc == SFDX_OK)
                 for (int i = 0; i < nd; i++) hs[idx[i]] = P.hst[i];
         } else if (rc == SFDX_OK) {
@@ -891,6 +893,7 @@ static int corrected_cycles(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>*
         for (int q : idx) {
             const int st = hs[q].status;
             used[q] += std::max(1, hs[q].iters);
+            if (P.rec_on && q < (int)P.rec_off.size()) P.rec_off[q] = used[q];
             if (st == ST_CONV || st == ST_VCONV || st == ST_NAN || (st == ST_BREAK && rel)) {
                 mask[q] = 0;  // converged, failed, or handed to the caller's FP64 finish
                 fin[q] = st;

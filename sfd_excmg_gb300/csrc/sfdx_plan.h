@@ -302,6 +302,14 @@ struct Plan {
     // advanced whenever a buffer or nodal operator that the edge multigrid
     // bakes into captured graphs is (re)allocated: part of every graph key
     long long emg_epoch = 0;
+    // residual history of the finest-level solves, recorded at every host
+    // check (8 iterations): rec_hist[system][iteration] (0: not recorded);
+    // rec_map: full-batch index of each system of a packed batch (empty: the
+    // identity); rec_off: iterations of earlier restart cycles per system
+    bool rec_on = false;
+    int rec_len = 0;
+    std::vector<double> rec_hist;
+    std::vector<int> rec_map, rec_off;
     // complex128 Krylov iteration with the complex64 multigrid V-cycle as its
     // preconditioner (mixed-precision plans with precond 'G', finer levels);
     // emg_q32 / emg_o32: the V-cycle's complex64 input and output
@@ -363,6 +371,16 @@ inline int sync_state(Plan& P) {
     P.hst.resize(P.ns);
     CK(cudaMemcpyAsync(P.hst.data(), P.d_state.p, sizeof(KState) * P.ns, cudaMemcpyDeviceToHost, P.st));
     CK(cudaStreamSynchronize(P.st));
+    if (P.rec_on) {
+        for (int s = 0; s < P.ns; s++) {
+            const KState& Q = P.hst[s];
+            if (Q.status == ST_SKIP || !(Q.err > 0)) continue;
+            const int full = P.rec_map.empty() ? s : P.rec_map[s];
+            const long long gi = (long long)P.rec_off[full] + (Q.it > 0 ? Q.it - 1 : 0);
+            if (full < (int)P.rec_off.size() && gi >= 0 && gi < P.rec_len)
+                P.rec_hist[(size_t)full * P.rec_len + gi] = Q.err;
+        }
+    }
     return SFDX_OK;
 }
 

@@ -262,6 +262,9 @@ static int solve_level_mixed(Plan& P, const Level& LV, double tol, int itmax, st
     }
     if (nleft) {
         std::vector<int> its64, st64;
+        if (P.rec_on)
+            for (int q = 0; q < ns; q++)
+                if (left[q] && q < (int)P.rec_off.size()) P.rec_off[q] = its[q];
         const int save = P.o.div_cor;
         if (save == 1) P.o.div_cor = 0;  // the FP64 finish is a continuation, not a reference restart
         int rc;
@@ -470,6 +473,15 @@ static void log_level(Plan& P, int l, const std::vector<int>& its, const std::ve
             L.nx, L.ny, L.nz, (long long)L.nl, mn, mx, cnt[ST_CONV], cnt[ST_MAXIT], cnt[ST_NAN], cnt[ST_BREAK], ms);
 }
 
+// residual history of the next finest-level solve (sync_state records it)
+static void history_start(Plan& P, int len) {
+    P.rec_on = true;
+    P.rec_len = len;
+    P.rec_hist.assign((size_t)P.ns * len, 0.0);
+    P.rec_off.assign(P.ns, 0);
+    P.rec_map.clear();
+}
+
 // EXCMG cascade (doublemode_acc, fdfe_main.f90:1258-1563): levels 1 and 2
 // solved tightly in FP64 from zero (u1u2, the PARDISO replacement), then on
 // each finer level the extrapolated guess from the two previous solutions
@@ -505,7 +517,10 @@ int excmg_cascade(Plan& P, const std::function<int(int)>& rhs, double eps, bool 
         const Level& L = P.lev[l];
         RC(prolongate(P, l, P.u0.as<double2>(), P.u1.as<double2>(), P.x64.as<double2>()));
         RC(rhs(l));
-        RC(solve_level(P, L, tol, P.o.maxit_level, false, its, status));
+        if (record && l == N - 1) history_start(P, P.o.maxit_level);
+        const int rcs = solve_level(P, L, tol, P.o.maxit_level, false, its, status);
+        P.rec_on = false;
+        RC(rcs);
         CK(cudaStreamSynchronize(P.st));
         if (record) {
             record_iters(P, l, its);
@@ -540,7 +555,10 @@ static int plan_solve(Plan& P) {
         RC(level_column(P, F, col));
         RC(level_rhs(P, F, col));
         CK(cudaMemsetAsync(P.x64.p, 0, nfine, P.st));
-        RC(solve_level(P, F, P.o.eps, P.o.maxit_plain, false, its, status));
+        history_start(P, P.o.maxit_plain);
+        const int rcs = solve_level(P, F, P.o.eps, P.o.maxit_plain, false, its, status);
+        P.rec_on = false;
+        RC(rcs);
         record_iters(P, P.nlev - 1, its);
         rc_conv = status_to_rc(status);
         CK(cudaStreamSynchronize(P.st));
@@ -1048,6 +1066,16 @@ extern "C" int sfdx_plan_level_fields(sfdx_plan* plan, int level, double* ex) {
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(ex, P.ut.p, (size_t)L.nl * ns * sizeof(double2), cudaMemcpyDeviceToHost, P.st));
     CK(cudaStreamSynchronize(P.st));
+    return SFDX_OK;
+}
+
+extern "C" int sfdx_plan_history(const sfdx_plan* plan, double* hist, int maxit) {
+    if (!plan || !hist || maxit < 1) return SFDX_ERR_ARG;
+    const Plan& P = plan->P;
+    if (!P.solution_current() || P.rec_len < 1) return SFDX_ERR_ARG;
+    for (int s = 0; s < P.ns; s++)
+        for (int i = 0; i < maxit; i++)
+            hist[(size_t)s * maxit + i] = i < P.rec_len ? P.rec_hist[(size_t)s * P.rec_len + i] : 0.0;
     return SFDX_OK;
 }
 

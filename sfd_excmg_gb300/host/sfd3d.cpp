@@ -7,7 +7,8 @@
 //   SFDX_PRECISION=fp64|mixed, SFDX_VERBOSE=1, SFDX_TIPPER=1 (output_tipper:
 //   the tippers follow the impedances in <model>.res), SFDX_DIV_COR=0|1|2
 //   (div_cor, default 1), SFDX_PRECOND=S|J|G (pre_type, default S; G the edge
-//   multigrid).
+//   multigrid), SFDX_CCV=1 (output_ccv: the finest-level residual history of
+//   every solve in <model>_<freq>_<polar>_<solver|excmg>.ccv).
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -62,8 +63,33 @@ int main(int argc, char** argv) {
                          (long long)(nx + 1) * (ny + 1) * nz;
     std::vector<double> ex((size_t)nf * 2 * nl * 2);
     std::vector<double> relres((size_t)nf * 2);
-    rc = sfdx_fwd_solve(&o, nx, ny, nz, nair, a.data(), b.data(), c.data(), sigma.data(), nf, freq.data(), ex.data(),
-                        nullptr, relres.data());
+    const char* ccv = getenv("SFDX_CCV");
+    if (ccv && atoi(ccv)) {
+        // the plan keeps the histories that the one-shot call discards
+        sfdx_plan* plan = nullptr;
+        rc = sfdx_plan_create(&plan, &o, nx, ny, nz, nair, a.data(), b.data(), c.data(), nf, freq.data());
+        const int nlev = o.excmg ? o.level : 1;
+        std::vector<int> its((size_t)nf * 2 * nlev);
+        if (rc == SFDX_OK) rc = sfdx_plan_solve(plan, sigma.data(), 0, ex.data(), 0, its.data(), relres.data());
+        if (rc == SFDX_OK || rc == SFDX_ERR_NOCONV) {
+            const int maxit = o.excmg ? o.maxit_level : o.maxit_plain;
+            std::vector<double> hist((size_t)nf * 2 * maxit);
+            const int hrc = sfdx_plan_history(plan, hist.data(), maxit);
+            static const char* names[7] = {"", "bicgstab", "tfqmr", "gpbicg", "bicg", "", "cocr"};
+            const char* tag = o.excmg ? "excmg" : (o.solver >= 0 && o.solver < 7 ? names[o.solver] : "");
+            for (int f = 0; f < nf && hrc == SFDX_OK; f++)
+                for (int p = 0; p < 2; p++) {
+                    const double* h = hist.data() + (size_t)(2 * f + p) * maxit;
+                    const int n_it = its[(size_t)(2 * f + p) * nlev + nlev - 1];  // iters(1) of the finest level
+                    if (sfdx_write_ccv(name, freq[f], p ? "yx" : "xy", tag, n_it, h, maxit) != SFDX_OK)
+                        fprintf(stderr, "sfd3d: cannot write the .ccv file\n");
+                }
+        }
+        sfdx_plan_destroy(plan);
+    } else {
+        rc = sfdx_fwd_solve(&o, nx, ny, nz, nair, a.data(), b.data(), c.data(), sigma.data(), nf, freq.data(),
+                            ex.data(), nullptr, relres.data());
+    }
     if (rc && rc != SFDX_ERR_NOCONV) {
         fprintf(stderr, "sfd3d: %s\n", sfdx_strerror(rc));
         return 1;

@@ -214,6 +214,15 @@ class Plan:
                    "sfdx_plan_level_fields")
         return ex
 
+    def history(self, maxit: int | None = None) -> np.ndarray:
+        """Finest-level residual history of the last solve, [nf, 2, maxit] (sfdx_plan_history; values at the
+        host's check points, 0 elsewhere)."""
+        m = self.model
+        n = maxit or (self.opts.maxit_level if self.opts.excmg else self.opts.maxit_plain)
+        h = np.zeros((m.nf, 2, n))
+        capi.check(capi.lib().sfdx_plan_history(self._h, capi.dptr(h), n), "sfdx_plan_history")
+        return h
+
     def level_times(self) -> np.ndarray:
         ms = np.zeros(self.nlev)
         capi.check(capi.lib().sfdx_plan_level_times(self._h, capi.dptr(ms), self.nlev), "sfdx_plan_level_times")

@@ -151,7 +151,7 @@ def test_sfd3d_end_to_end_matches_oracle(tmp_path):
     name = str(tmp_path / "mod")
     m.write(name)
     exe = os.path.join(os.path.dirname(capi.library_path()), "sfd3d")
-    env = dict(os.environ, SFDX_EXCMG="1", SFDX_DIV_COR="2", SFDX_PRECOND="G")
+    env = dict(os.environ, SFDX_EXCMG="1", SFDX_DIV_COR="2", SFDX_PRECOND="G", SFDX_CCV="1")
     r = subprocess.run([exe, name, "3", "1e-10"], env=env, capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stderr
     rows = np.array([[float(v) for v in ln.split()] for ln in open(name + ".res").read().splitlines()])
@@ -164,3 +164,15 @@ def test_sfd3d_end_to_end_matches_oracle(tmp_path):
     err = np.abs(_zc(z) - _zc(zref)) / np.abs(_zc(zref))
     # the file holds 5 significant digits (Ew.d with d = 5)
     assert np.all(err < z_tol_corrected(m.freq) + 2e-5), err
+    # output_ccv (solvers.f90:687-704): one history per frequency and polarisation, the
+    # finest level's iteration count, then the residuals at the check points, falling to
+    # the tolerance
+    import glob
+    for pol in ("xy", "yx"):
+        files = sorted(glob.glob(name + "_*_" + pol + "_excmg.ccv"))
+        assert len(files) == m.nf, files
+        for fn in files:
+            lines = open(fn).read().split()
+            n_it, vals = int(lines[0]), [float(v) for v in lines[1:]]
+            assert n_it > 0 and len(vals) >= 1
+            assert vals[-1] < 1e-10 and min(vals) > 0, vals
