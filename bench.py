@@ -54,7 +54,7 @@ sys.path.insert(0, ROOT)
 FALLBACK_HBM_GBS = 6800.0
 REF_SAMPLE_ITERS = 5  # BiCGStab-SSOR iterations of the bounded cpu_baseline sample
 REF_STEPS = 1  # whole reference forward solves timed per --impl reference run
-REF_FREQS = None  # frequency indices of the reference arm's sample (None: lowest and highest)
+REF_FREQS = None  # frequency indices of the reference arm's sample (None: the highest frequency)
 
 
 def peaks():
@@ -289,15 +289,17 @@ def reference_forward(name, eps, freqs, procs):
 def run_reference(args, rank, world):
     """The reference algorithm on the host cores (oracle restatement; the Fortran/MKL build is not
     available): whole solves at the configuration's own tolerance of a bounded sample of the
-    workload's systems (REF_FREQS: by default the lowest and the highest frequency, both
-    polarisations), one system per process.  One solve takes minutes, so the line carries
+    workload's systems (REF_FREQS: by default the highest frequency, both polarisations: the
+    reference's fastest solves, so the rate is an upper bound of its rate over the whole workload;
+    a complete run of large-inclusions, tests/golden/large_inclusions_reference.json, takes 228-2066 s
+    per system), one system per process.  One solve takes minutes, so the line carries
     REF_STEPS timed steps whatever --steps asks (reported as steps) and no warm-up (nothing to
     warm on a CPU).  Rank 0 only."""
     if rank != 0:
         return
     m = make_workload(args.workload)
     eps = m.eps  # the configuration's tolerance for the reference run
-    freqs = sorted({0, m.nf - 1}) if REF_FREQS is None else REF_FREQS
+    freqs = [m.nf - 1] if REF_FREQS is None else REF_FREQS
     procs = max(1, min(2 * len(freqs), os.cpu_count() or 1))
     walls = []
     for _ in range(REF_STEPS):

@@ -76,6 +76,20 @@ static double emg_nodal_omega() {
     return v;
 }
 
+// Nodal steps of complex64 V-cycles skip the nodes inside air (all eight
+// cells below this conductivity, S/m; SFDX_MG_AIR overrides, 0 keeps them):
+// there the step's gradient corrections scale like 1/(w mu sigma) and, stored
+// in complex64 beside the field, swamp it; as near-null modes they barely
+// change the residual, and the FP64 gradient correction after each restart
+// cycle removes them where the impedances see them.
+static double emg_air_cut() {
+    static const double v = [] {
+        const char* e = getenv("SFDX_MG_AIR");
+        return e ? atof(e) : 1e-6;
+    }();
+    return v;
+}
+
 static int level_index(const Plan& P, const Level& LV) {
     for (int l = 0; l < P.nlev; l++)
         if (&P.lev[l] == &LV) return l;
@@ -122,7 +136,8 @@ static void emg_nodal(Plan& P, const Level& L, const VCfg& c, const cplx<T>* b, 
     const uint32_t np = (uint32_t)(L.nx + 1) * (L.ny + 1) * (L.nz + 1);
     vlaunch(k_mg_mres_v<T, VS>, L.nl * c.sg.G, c.B, 0, P.st, L.lev<T>(), L.mesh, c.sg, dst, b, (const cplx<T>*)x, r);
     vlaunch(k_mg_node_v<T, VS>, (int64_t)np * c.sg.G, c.B, 0, P.st, L.lev<T>(), L.mesh, c.sg, np, dst,
-            (const cplx<T>*)r, L.mg[0].dinv.as<float>(), phi, (T)emg_nodal_omega());
+            (const cplx<T>*)r, L.mg[0].dinv.as<float>(), phi, (T)emg_nodal_omega(),
+            (T)(sizeof(T) == 4 ? emg_air_cut() : 0.0));
     vlaunch(k_mg_gadd_v<T, VS>, L.nl * c.sg.G, c.B, 0, P.st, L.lev<T>(), L.mesh, c.sg, dst, (const cplx<T>*)phi, x);
 }
 

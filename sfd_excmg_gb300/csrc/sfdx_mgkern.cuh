@@ -186,9 +186,12 @@ __global__ void k_mg_add_v(Mesh M, SysG sgp, const KState* st, cplx<T>* __restri
 // nodes), D = -i wm N_nn, so phi = (w dinv / wm) * i * (G^T V r).
 // G^T V r at node (i,j,k) = sum over its six edges of +-(V/len) r: + for the
 // edge that ends at the node, - for the one that starts there.
+// air_max > 0: nodes whose eight cells all have sigma_xx below air_max get no
+// correction (their gradients are near-null modes of any size -- see
+// emg_air_cut).
 template <class T, int VS>
 __global__ void k_mg_node_v(Lev<T> L, Mesh M, SysG sgp, uint32_t np, const KState* st, const cplx<T>* __restrict__ r,
-                            const float* __restrict__ dinv, cplx<T>* __restrict__ phi, T omega) {
+                            const float* __restrict__ dinv, cplx<T>* __restrict__ phi, T omega, T air_max) {
     const int ns = sgp.ns, s0 = (threadIdx.x % sgp.G) * VS;
     const SysV<T, VS> S = load_sys<T, VS>(st, s0);
     if (!S.act) return;
@@ -199,7 +202,17 @@ __global__ void k_mg_node_v(Lev<T> L, Mesh M, SysG sgp, uint32_t np, const KStat
         node_ijk(M, n, i, j, k);
         CV<T, VS> out;
         cvzero<T, VS>(out);
-        if (!node_bnd(M, i, j, k)) {
+        bool air = false;
+        if (air_max > T(0) && !node_bnd(M, i, j, k)) {
+            T smax = T(0);
+#pragma unroll
+            for (int q = 0; q < 8; q++) {
+                const int64_t cidx = ((int64_t)(k - 1 + (q >> 2)) * M.ny + (j - 1 + ((q >> 1) & 1))) * M.nx + (i - 1 + (q & 1));
+                smax = fmax(smax, __ldg(L.sig + cidx));
+            }
+            air = smax < air_max;
+        }
+        if (!node_bnd(M, i, j, k) && !air) {
             const uint32_t ex = ((uint32_t)k * ny1 + j) * M.nx + i;
             const uint32_t ey = M.xnl + ((uint32_t)k * M.ny + j) * nx1 + i;
             const uint32_t ez = M.xnl + M.ynl + ((uint32_t)k * ny1 + j) * nx1 + i;

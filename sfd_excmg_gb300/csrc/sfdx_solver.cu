@@ -295,11 +295,13 @@ int solve_level(Plan& P, const Level& LV, double tol, int itmax, bool coarse, st
     if (coarse || P.o.precision == SFDX_FP64 || P.o.solver == SFDX_SOLVER_TFQMR || P.o.solver == SFDX_SOLVER_BICG)
         return solve_level_fp64(P, LV, tol, itmax, its, status);
     // mixed precision with the multigrid preconditioner: complex128 Krylov
-    // vectors and operator, complex64 V-cycle (a complex64 Krylov iteration
-    // under the V-cycle met the rounding of its complex64 operator on the
-    // V-cycle's large discrete-gradient components: FP64 residuals grew and
-    // every system fell back to FP64)
-    if (P.o.precond == 'G') {
+    // vectors and operator, complex64 V-cycle (SFDX_MG_PF32=0: the complex64
+    // Krylov iteration with FP64 reliable updates of the SSOR plans instead)
+    static const bool krylov64 = [] {
+        const char* e = getenv("SFDX_MG_PF32");
+        return !(e && e[0] == '0');
+    }();
+    if (P.o.precond == 'G' && krylov64) {
         P.pf32 = true;
         const int rc = solve_level_fp64(P, LV, tol, itmax, its, status);
         P.pf32 = false;
