@@ -288,6 +288,16 @@ static __global__ void k_restore(int64_t nl, const KState* st, int ns, double2* 
     }
 }
 
+// x64 = xb for the systems that ended in NaN or a breakdown
+static __global__ void k_restore_failed(int64_t nl, const KState* st, int ns, double2* __restrict__ x64,
+                                        const double2* __restrict__ xb) {
+    const int64_t W = nl * ns;
+    for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < W; g += (int64_t)gridDim.x * blockDim.x) {
+        const int s = (int)(g % ns);
+        if (st[s].status == ST_NAN || st[s].status == ST_BREAK) x64[g] = xb[g];
+    }
+}
+
 // ------------------------------------------------------------------ misc vector kernels
 template <class A, class B>
 __global__ void k_convert(int64_t n, const cplx<A>* __restrict__ src, cplx<B>* __restrict__ dst) {

@@ -302,10 +302,44 @@ int solve_level(Plan& P, const Level& LV, double tol, int itmax, bool coarse, st
         return !(e && e[0] == '0');
     }();
     if (P.o.precond == 'G' && krylov64) {
+        // the starting iterate, for systems whose complex64 V-cycle fails them
+        // (NaN or breakdown): those restart from it with the FP64 V-cycle
+        const size_t n = (size_t)LV.nl * P.ns;
+        RC(P.xb.alloc(n * sizeof(double2)));
+        CK(cudaMemcpyAsync(P.xb.p, P.x64.p, n * sizeof(double2), cudaMemcpyDeviceToDevice, P.st));
         P.pf32 = true;
         const int rc = solve_level_fp64(P, LV, tol, itmax, its, status);
         P.pf32 = false;
-        return rc;
+        RC(rc);
+        std::vector<int> left(P.ns, 0);
+        int nleft = 0;
+        for (int q = 0; q < P.ns; q++)
+            if (status[q] == ST_NAN || status[q] == ST_BREAK) {
+                left[q] = 1;
+                nleft++;
+            }
+        if (!nleft) return SFDX_OK;
+        const int B = block_for(P.ns);
+        KL(k_restore_failed<<<grid_for(n, B, 16), B, 0, P.st>>>(LV.nl, P.d_state.as<KState>(), P.ns,
+                                                                  P.x64.as<double2>(), P.xb.as<double2>()));
+        CK(cudaGetLastError());
+        if (P.rec_on)
+            for (int q = 0; q < P.ns; q++)
+                if (left[q] && q < (int)P.rec_off.size()) P.rec_off[q] = its[q];
+        if (P.o.verbose || getenv("SFDX_VERBOSE"))
+            fprintf(stderr, "sfdx:   %d system(s) restarted with the FP64 V-cycle\n", nleft);
+        if (P.o.solver == SFDX_SOLVER_GPBICG)
+            RC(gpbicg<double>(P, LV, P.b64.as<double2>(), P.x64.as<double2>(), nullptr, tol, itmax, left.data()));
+        else if (P.o.solver == SFDX_SOLVER_COCR)
+            RC(cocr<double>(P, LV, P.b64.as<double2>(), P.x64.as<double2>(), nullptr, tol, itmax, left.data()));
+        else
+            RC(bicgstab<double>(P, LV, P.b64.as<double2>(), P.x64.as<double2>(), nullptr, tol, itmax, left.data()));
+        for (int q = 0; q < P.ns; q++) {
+            if (!left[q]) continue;
+            its[q] += P.hst[q].iters;
+            status[q] = P.hst[q].status;
+        }
+        return SFDX_OK;
     }
     return solve_level_mixed(P, LV, tol, itmax, its, status);
 }

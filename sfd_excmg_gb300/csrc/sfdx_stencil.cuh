@@ -490,6 +490,13 @@ __device__ __forceinline__ void ld_nb(CV<T, VS>& a, const cplx<T>* x, uint32_t e
     }
 }
 
+// both coefficients +0 (bit test on the integer pipe: the off-diagonal
+// conductivity weights are sums of non-negative products, never -0)
+__device__ __forceinline__ bool both_zero(float a, float b) { return (__float_as_uint(a) | __float_as_uint(b)) == 0u; }
+__device__ __forceinline__ bool both_zero(double a, double b) {
+    return (__double_as_longlong(a) | __double_as_longlong(b)) == 0ll;
+}
+
 template <class T, int VS, int PAIR, bool RO>
 __device__ __forceinline__ void acc_cross(CV<T, VS>& C, CV<T, VS>& Mm, T g, T s1, T s2, const uint32_t (&idx)[4],
                                           unsigned msk, const cplx<T>* x, int ns, int s0) {
@@ -501,10 +508,17 @@ __device__ __forceinline__ void acc_cross(CV<T, VS>& C, CV<T, VS>& Mm, T g, T s1
 #pragma unroll
     for (int q = 0; q < VS; q++) {
         cplx<T> cu = (v1.v[q] - v2.v[q]) + (v4.v[q] - v3.v[q]);
-        cplx<T> m1 = PAIR == 0 ? v1.v[q] + v2.v[q] : v1.v[q] + v3.v[q];
-        cplx<T> m2 = PAIR == 0 ? v3.v[q] + v4.v[q] : v2.v[q] + v4.v[q];
         C.v[q].x += g * cu.x;
         C.v[q].y += g * cu.y;
+    }
+    // rows whose cells are all isotropic have no cross-orientation mass terms
+    // (adding 0 * m would leave Mm bit-identical): skip the 8 adds and fused
+    // multiply-adds per system, a third of the FP64 operator's instructions
+    if (both_zero(s1, s2)) return;
+#pragma unroll
+    for (int q = 0; q < VS; q++) {
+        cplx<T> m1 = PAIR == 0 ? v1.v[q] + v2.v[q] : v1.v[q] + v3.v[q];
+        cplx<T> m2 = PAIR == 0 ? v3.v[q] + v4.v[q] : v2.v[q] + v4.v[q];
         Mm.v[q].x += s1 * m1.x + s2 * m2.x;
         Mm.v[q].y += s1 * m1.y + s2 * m2.y;
     }
