@@ -298,6 +298,30 @@ static int reliable_update(Plan& P, const Level& LV, const Reliable& rel, cplx<T
     return SFDX_OK;
 }
 
+// Under the complex64 V-cycle (P.pf32) a system whose FP64 residual has grown
+// 1e4-fold above the smallest it reached met the V-cycle's rounding (gradient
+// corrections of very low induction numbers, 1e-3 Hz in resistive ground):
+// stop it as a breakdown, so that solve_level restarts it from its starting
+// iterate with the FP64 V-cycle.  `emin` holds each system's smallest residual.
+static int pf32_divergence(Plan& P, std::vector<double>& emin) {
+    if (!P.pf32) return SFDX_OK;
+    if ((int)emin.size() != P.ns) emin.assign(P.ns, INFINITY);
+    KState* dst = P.d_state.as<KState>();
+    for (int q = 0; q < P.ns; q++) {
+        KState& S = P.hst[q];
+        if (!S.active) continue;
+        if (!(S.err <= 1e4 * emin[q])) {  // also NaN
+            S.active = 0;
+            S.status = ST_BREAK;
+            CK(cudaMemcpyAsync(dst + q, &S, sizeof(KState), cudaMemcpyHostToDevice, P.st));
+        } else {
+            emin[q] = std::min(emin[q], S.err);
+        }
+    }
+    CK(cudaStreamSynchronize(P.st));
+    return SFDX_OK;
+}
+
 // Bicg_stab_p (solvers.f90:522-719) for the ns systems of level LV: A x = b.
 // Plain: x holds the initial guess (precision T).  With `rel` (mixed
 // precision) b/x are the complex64 work vectors and the FP64 b64/x64 of
@@ -337,6 +361,7 @@ static int bicgstab_v(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, co
     CK(cudaGetLastError());
     const int check_every = 8;
     int last_rel = 0;
+    std::vector<double> emin;  // smallest residual per system (pf32_divergence)
     const bool div1 = !rel && std::is_same<T, double>::value && P.o.div_cor == 1;
     auto body = [&]() {
         precond<T, VS, RHS_PUPD>(P, LV, y, p, r, v);
@@ -363,6 +388,7 @@ static int bicgstab_v(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, co
         if (it % check_every == 0 || it == itmax) {
             CK(cudaGetLastError());
             RC(sync_state(P));
+            RC(pf32_divergence(P, emin));
             int act = 0, cand = 0;
             for (int q = 0; q < ns; q++) {
                 act += P.hst[q].active;
@@ -416,6 +442,7 @@ static int gpbicg_v(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, cons
     precond<T, VS, RHS_VEC>(P, LV, rp, r, nullptr, nullptr);
     CK(cudaMemcpyAsync(p, rp, vb, cudaMemcpyDeviceToDevice, P.st));
     int cur = 0, last_rel = 0;
+    std::vector<double> emin;  // smallest residual per system (pf32_divergence)
     const bool div1 = !rel && std::is_same<T, double>::value && P.o.div_cor == 1;
     // one iteration up to the convergence check, with t' in tp[cc]
     auto body = [&](int cc) {
@@ -458,6 +485,7 @@ static int gpbicg_v(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, cons
         if (it % 8 == 0 || it == itmax) {
             CK(cudaGetLastError());
             RC(sync_state(P));
+            RC(pf32_divergence(P, emin));
             int act = 0, cand = 0;
             for (int q = 0; q < ns; q++) {
                 act += P.hst[q].active;
@@ -521,6 +549,7 @@ static int cocr_v(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, const 
     RC(restart());
     bool first = true;
     int last_rel = 0;
+    std::vector<double> emin;  // smallest residual per system (pf32_divergence)
     auto body = [&](bool fst) {
         if (fst)
             vlaunch(k_cocr_u<T, VS, true>, W, c.B, c.smem, P.st, L, M, c.sg, dst, (const cplx<T>*)z, u, redbuf(P));
@@ -551,6 +580,7 @@ static int cocr_v(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, const 
         if (it % 8 == 0 || it == itmax) {
             CK(cudaGetLastError());
             RC(sync_state(P));
+            RC(pf32_divergence(P, emin));
             int act = 0, cand = 0;
             for (int k = 0; k < ns; k++) {
                 act += P.hst[k].active;
