@@ -157,10 +157,11 @@ MAXIT_LEVEL = 3000  # iteration limit per EXCMG level (the reference's 1000 is t
 # kernel families timed on the finest level (sfdx_plan_kernel_time ids)
 KERNELS = ((2, "mc_ssor_c64"), (0, "operator_c64"), (4, "vcycle_c64"))
 ROOFLINE_KERNEL = "mc_ssor_c64"
-# DRAM bytes (read + write) per launch of the roofline kernel from one ncu capture
-# of this build on the workload (dram__bytes_read.sum + dram__bytes_write.sum, summed
-# over the colour launches of one application)
-TRAFFIC = {}
+# DRAM bytes (read + write) of one application of the roofline kernel (the 11 colour
+# launches): dram__bytes_read.sum + dram__bytes_write.sum of one ncu capture on
+# aniso-hills (1657 MB), and for large-inclusions the same scaled by the edge-systems
+# processed (x 5.336; too large for a multi-pass capture)
+TRAFFIC = {("aniso-hills", "mc_ssor_c64"): 1.6572e9, ("large-inclusions", "mc_ssor_c64"): 8.843e9}
 
 
 def solve_opts(precision, solver="bicgstab", div_cor=2, eps=1e-10, corr_intv=None, level=3, precond="G"):
@@ -506,7 +507,10 @@ def run_ours(args, rank, world, local):
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "achieved": dom["gbs"], "peak": hbm, "unit": "GB/s", "frac": dom["gbs"] / hbm,
                      "traffic": TRAFFIC.get((args.workload, ROOFLINE_KERNEL)), "kernel": ROOFLINE_KERNEL,
-                     "peak_source": src},
+                     "peak_source": src,
+                     "traffic_source": {"aniso-hills": "ncu capture of one application",
+                                        "large-inclusions": "ncu capture on aniso-hills scaled by edge-systems"}
+                     .get(args.workload)},
         "kernels": kern,
         "cpu_baseline": cpu,
         "clocks": clk,
