@@ -288,13 +288,13 @@ static __global__ void k_restore(int64_t nl, const KState* st, int ns, double2* 
     }
 }
 
-// x64 = xb for the systems that ended in NaN or a breakdown
-static __global__ void k_restore_failed(int64_t nl, const KState* st, int ns, double2* __restrict__ x64,
-                                        const double2* __restrict__ xb) {
+// x64 = xb for the systems selected by sel[s] != 0
+static __global__ void k_restore_sel(int64_t nl, const int* __restrict__ sel, int ns, double2* __restrict__ x64,
+                                     const double2* __restrict__ xb) {
     const int64_t W = nl * ns;
     for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < W; g += (int64_t)gridDim.x * blockDim.x) {
         const int s = (int)(g % ns);
-        if (st[s].status == ST_NAN || st[s].status == ST_BREAK) x64[g] = xb[g];
+        if (sel[s]) x64[g] = xb[g];
     }
 }
 

@@ -299,26 +299,39 @@ static int reliable_update(Plan& P, const Level& LV, const Reliable& rel, cplx<T
 }
 
 // Under the complex64 V-cycle (P.pf32) a system whose FP64 residual has grown
-// 1e4-fold above the smallest it reached met the V-cycle's rounding (gradient
-// corrections of very low induction numbers, 1e-3 Hz in resistive ground):
-// stop it as a breakdown, so that solve_level restarts it from its starting
-// iterate with the FP64 V-cycle.  `emin` holds each system's smallest residual.
-static int pf32_divergence(Plan& P, std::vector<double>& emin) {
+// 1e4-fold above the smallest it reached, or has not reached a new smallest
+// residual for 160 iterations, met the V-cycle's rounding (gradient
+// corrections of very low induction numbers, 1e-3 Hz in resistive ground;
+// the multigrid iteration otherwise converges in tens of iterations): stop it
+// as a breakdown, so that solve_level restarts it from its starting iterate
+// with the FP64 V-cycle.  `emin` holds each system's smallest residual and the
+// iteration that reached it.
+struct ResMin {
+    std::vector<double> e;
+    std::vector<int> it;
+};
+static int pf32_divergence(Plan& P, ResMin& m) {
     if (!P.pf32) return SFDX_OK;
-    if ((int)emin.size() != P.ns) emin.assign(P.ns, INFINITY);
+    if ((int)m.e.size() != P.ns) {
+        m.e.assign(P.ns, INFINITY);
+        m.it.assign(P.ns, 0);
+    }
     KState* dst = P.d_state.as<KState>();
+    bool sent = false;
     for (int q = 0; q < P.ns; q++) {
         KState& S = P.hst[q];
         if (!S.active) continue;
-        if (!(S.err <= 1e4 * emin[q])) {  // also NaN
+        if (!(S.err <= 1e4 * m.e[q]) || S.it - m.it[q] > 160) {  // also NaN
             S.active = 0;
             S.status = ST_BREAK;
             CK(cudaMemcpyAsync(dst + q, &S, sizeof(KState), cudaMemcpyHostToDevice, P.st));
-        } else {
-            emin[q] = std::min(emin[q], S.err);
+            sent = true;
+        } else if (S.err < m.e[q]) {
+            m.e[q] = S.err;
+            m.it[q] = S.it;
         }
     }
-    CK(cudaStreamSynchronize(P.st));
+    if (sent) CK(cudaStreamSynchronize(P.st));
     return SFDX_OK;
 }
 
@@ -361,7 +374,7 @@ static int bicgstab_v(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, co
     CK(cudaGetLastError());
     const int check_every = 8;
     int last_rel = 0;
-    std::vector<double> emin;  // smallest residual per system (pf32_divergence)
+    ResMin emin;  // smallest residual per system (pf32_divergence)
     const bool div1 = !rel && std::is_same<T, double>::value && P.o.div_cor == 1;
     auto body = [&]() {
         precond<T, VS, RHS_PUPD>(P, LV, y, p, r, v);
@@ -442,7 +455,7 @@ static int gpbicg_v(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, cons
     precond<T, VS, RHS_VEC>(P, LV, rp, r, nullptr, nullptr);
     CK(cudaMemcpyAsync(p, rp, vb, cudaMemcpyDeviceToDevice, P.st));
     int cur = 0, last_rel = 0;
-    std::vector<double> emin;  // smallest residual per system (pf32_divergence)
+    ResMin emin;  // smallest residual per system (pf32_divergence)
     const bool div1 = !rel && std::is_same<T, double>::value && P.o.div_cor == 1;
     // one iteration up to the convergence check, with t' in tp[cc]
     auto body = [&](int cc) {
@@ -549,7 +562,7 @@ static int cocr_v(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, const 
     RC(restart());
     bool first = true;
     int last_rel = 0;
-    std::vector<double> emin;  // smallest residual per system (pf32_divergence)
+    ResMin emin;  // smallest residual per system (pf32_divergence)
     auto body = [&](bool fst) {
         if (fst)
             vlaunch(k_cocr_u<T, VS, true>, W, c.B, c.smem, P.st, L, M, c.sg, dst, (const cplx<T>*)z, u, redbuf(P));
@@ -939,7 +952,9 @@ static int corrected_cycles(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>*
             const int st = hs[q].status;
             used[q] += std::max(1, hs[q].iters);
             if (P.rec_on && q < (int)P.rec_off.size()) P.rec_off[q] = used[q];
-            if (st == ST_CONV || st == ST_VCONV || st == ST_NAN || (st == ST_BREAK && rel)) {
+            // a breakdown under complex64 iterations or the complex64 V-cycle is
+            // handed to the caller's FP64 finish / FP64 V-cycle restart
+            if (st == ST_CONV || st == ST_VCONV || st == ST_NAN || (st == ST_BREAK && (rel || P.pf32))) {
                 mask[q] = 0;  // converged, failed, or handed to the caller's FP64 finish
                 fin[q] = st;
             } else if (used[q] >= itmax) {
@@ -954,7 +969,7 @@ static int corrected_cycles(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>*
         cyc = (int)std::min(cyc_f, 1e6);
     }
     std::vector<int> last(ns);
-    for (int q = 0; q < ns; q++) last[q] = part[q] && fin[q] != ST_NAN && !(fin[q] == ST_BREAK && rel);
+    for (int q = 0; q < ns; q++) last[q] = part[q] && fin[q] != ST_NAN && !(fin[q] == ST_BREAK && (rel || P.pf32));
     RC(grad_correct(P, LV, b64, x64, last.data(), P.o.corr_tol, gc_maxit, nullptr));
     P.hst.resize(ns);
     for (int q = 0; q < ns; q++) {

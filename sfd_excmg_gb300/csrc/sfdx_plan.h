@@ -268,6 +268,7 @@ struct Plan {
     // mixed precision: complex64 partial solution and the FP64 iterate saved
     // before each reliable update
     DBuf x32, xb;
+    DBuf d_sel;  // per-system selection flags (int) of the complex64 V-cycle fallback
     // Krylov vectors (precision of the active solve)
     DBuf kv[14];
     // divergence correction: t, r, p, v, phi (nodes) and the PCG state

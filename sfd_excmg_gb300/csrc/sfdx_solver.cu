@@ -320,8 +320,10 @@ int solve_level(Plan& P, const Level& LV, double tol, int itmax, bool coarse, st
             }
         if (!nleft) return SFDX_OK;
         const int B = block_for(P.ns);
-        KL(k_restore_failed<<<grid_for(n, B, 16), B, 0, P.st>>>(LV.nl, P.d_state.as<KState>(), P.ns,
-                                                                  P.x64.as<double2>(), P.xb.as<double2>()));
+        RC(P.d_sel.alloc(sizeof(int) * P.ns));
+        CK(cudaMemcpyAsync(P.d_sel.p, left.data(), sizeof(int) * P.ns, cudaMemcpyHostToDevice, P.st));
+        KL(k_restore_sel<<<grid_for(n, B, 16), B, 0, P.st>>>(LV.nl, P.d_sel.as<int>(), P.ns, P.x64.as<double2>(),
+                                                               P.xb.as<double2>()));
         CK(cudaGetLastError());
         if (P.rec_on)
             for (int q = 0; q < P.ns; q++)
