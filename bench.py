@@ -147,8 +147,11 @@ SOLVER = {"bicgstab": 1, "tfqmr": 2, "gpbicg": 3, "bicg": 4, "cocr": 6}
 
 
 # Divergence handling of the benchmark solves: the consistent gradient-space
-# correction between GPBiCG restart cycles of 40 iterations (nodal PCG to 1e-2).
-GC_OPTS = dict(div_cor=2, corr_intv=40, corr_tol=1e-2)
+# correction (nodal PCG to 1e-2) before Krylov restart cycles of 20 iterations,
+# each next cycle 1.5x longer.  Large-inclusions at 1e-12: 5.41 s per solve with
+# a first cycle of 20, 5.67 with 24, 6.14 with 40, 5.72 with 16; 26.2 with the
+# correction only at the end (2000).
+GC_OPTS = dict(div_cor=2, corr_intv=20, corr_tol=1e-2)
 
 
 USE_GRAPHS = 1  # CUDA-graph capture of the Krylov check intervals (--no-graphs: 0)
