@@ -86,10 +86,17 @@ __global__ void k_interp(int nx, int ny, int nz, const double* __restrict__ X, c
     const int64_t xnl = (int64_t)nx * (ny + 1) * (nz + 1), ynl = (int64_t)(nx + 1) * ny * (nz + 1);
     const int64_t nl = xnl + ynl + (int64_t)(nx + 1) * (ny + 1) * nz;
     const int64_t cxnl = (int64_t)cx * (cy + 1) * (cz + 1), cynl = (int64_t)(cx + 1) * cy * (cz + 1);
-    const int64_t W = nl * ns;
+    // one thread per fine edge and group of up to SG systems: the Lagrange
+    // weights are computed once per group (the same products, in the same
+    // order, for every system: results do not depend on the grouping)
+    constexpr int SG = 4;
+    const int ngrp = (ns + SG - 1) / SG;
+    const int64_t W = nl * ngrp;
     for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < W; g += (int64_t)gridDim.x * blockDim.x) {
-        const int s = (int)(g % ns);
-        const int64_t e = g / ns;
+        const int s0 = (int)(g % ngrp) * SG;
+        const int cnt = min(SG, ns - s0);
+        const int64_t e = g / ngrp;
+        cplx<T>* out = uf + e * ns + s0;
         int o, i, j, k;
         if (e < xnl) {
             o = 0; i = (int)(e % nx); int64_t r = e / nx; j = (int)(r % (ny + 1)); k = (int)(r / (ny + 1));
@@ -107,7 +114,7 @@ __global__ void k_interp(int nx, int ny, int nz, const double* __restrict__ X, c
         int be = pe / bs;
         int b1 = node_block(p1, bs, nb1), b2 = node_block(p2, bs, nb2);
         if (be >= nbe || b1 < 0 || b2 < 0) {
-            uf[g] = zero<T>();
+            for (int u = 0; u < cnt; u++) out[u] = zero<T>();
             continue;
         }
         double cx1[M + 1], cx2[M + 1], cx3[M];
@@ -124,7 +131,9 @@ __global__ void k_interp(int nx, int ny, int nz, const double* __restrict__ X, c
         lagrange<M>(cx3, (Ce[pe] + Ce[pe + 1]) / 2, w3);
         // coarse edge (ce along, c1 across-1, c2 across-2) -> coarse index
         const int ce0 = be * M, c10 = b1 * M, c20 = b2 * M;
-        double ar = 0.0, ai = 0.0;
+        double ar[SG], ai[SG];
+#pragma unroll
+        for (int u = 0; u < SG; u++) ar[u] = ai[u] = 0.0;
         for (int kk = 0; kk < M; kk++)
             for (int jj = 0; jj <= M; jj++)
                 for (int ii = 0; ii <= M; ii++) {
@@ -136,11 +145,16 @@ __global__ void k_interp(int nx, int ny, int nz, const double* __restrict__ X, c
                         ci = cxnl + ((int64_t)(c20 + jj) * cy + (ce0 + kk)) * (cx + 1) + (c10 + ii);
                     else
                         ci = cxnl + cynl + ((int64_t)(ce0 + kk) * (cy + 1) + (c20 + jj)) * (cx + 1) + (c10 + ii);
-                    cplx<T> u = uc[ci * ns + s];
-                    ar += w * (double)u.x;
-                    ai += w * (double)u.y;
+                    const cplx<T>* up = uc + ci * ns + s0;
+#pragma unroll
+                    for (int u = 0; u < SG; u++)
+                        if (u < cnt) {
+                            const cplx<T> v = up[u];
+                            ar[u] += w * (double)v.x;
+                            ai[u] += w * (double)v.y;
+                        }
                 }
-        uf[g] = mk<T>((T)ar, (T)ai);
+        for (int u = 0; u < cnt; u++) out[u] = mk<T>((T)ar[u], (T)ai[u]);
     }
 }
 

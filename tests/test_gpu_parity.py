@@ -109,6 +109,20 @@ def test_aniso_hills_converged_matches_oracle(precision, solver):
     assert ez < Z_TOL_CONVERGED and ef < F_TOL_CONVERGED, (ez, ef)
 
 
+def test_large_inclusions_converged_matches_oracle():
+    """Config 4, the benchmark workload (128x128x96 core cells, 160x160x144 with padding and
+    air, 11.2 M edges, 6 frequencies, 4 EXCMG levels), as the benchmark solves it: mixed
+    precision (complex64 V-cycle under complex128 BiCGStab), tolerance 1e-12."""
+    fx = _fixture("large_inclusions")
+    m = syn.large_inclusions(seed=0)
+    with S.Plan(m, eps=1e-12, excmg=1, level=m.level, solver=1, precision=S.MIXED, precond="G", div_cor=2,
+                corr_intv=20, corr_tol=1e-2, maxit_level=3000) as p:
+        ex = p.solve()
+        ez, ef = _errors(p, ex, fx)
+    print(f"large-inclusions mixed: Z {ez:.2e}, fields {ef:.2e}")
+    assert ez < 1e-5 and ef < F_TOL_CONVERGED, (ez, ef)
+
+
 def test_coarse_levels_and_guess_match_exact_solves():
     """Levels 1 and 2 of a 3-level cascade (the reference solves them with PARDISO,
     u1u2 fdfe_main.f90:1228-1256) against the exact solution of the same coarse systems, and the
