@@ -64,9 +64,14 @@ __device__ __forceinline__ void mg_mass_row(const Lev<T>& L, const Mesh& M, uint
         return;
     }
     const RowK<T> K = row_k_e<T, O, false, true, true>(L, e, i, j, k);
-    const RowN N = row_n<O>(M, e, i, j, k);
-    CV<T, VS> C, Mm, xe;
-    row_off<T, VS, O, false, true, true, true>(K, N, x, ns, s0, C, Mm);
+    CV<T, VS> Mm, xe;
+    if (both_zero(K.sA1, K.sA2) && both_zero(K.sB1, K.sB2)) {
+        cvzero<T, VS>(Mm);  // isotropic cells around the edge: diagonal mass only, no neighbour reads
+    } else {
+        const RowN N = row_n<O>(M, e, i, j, k);
+        CV<T, VS> C;
+        row_off<T, VS, O, false, true, true, true>(K, N, x, ns, s0, C, Mm);
+    }
     cvld<T, VS>(xe, x + (size_t)e * ns + s0);
 #pragma unroll
     for (int u = 0; u < VS; u++) {
