@@ -298,7 +298,7 @@ def run_reference(args, rank, world):
     available): whole solves at the configuration's own tolerance of a bounded sample of the
     workload's systems (REF_FREQS: by default the highest frequency, both polarisations: the
     reference's fastest solves, so the rate is an upper bound of its rate over the whole workload;
-    a complete run of large-inclusions, tests/golden/large_inclusions_reference.json, takes 228-2066 s
+    a complete run of large-inclusions, tests/golden/large_inclusions_reference.json, takes 228-4319 s
     per system), one system per process.  One solve takes minutes, so the line carries
     REF_STEPS timed steps whatever --steps asks (reported as steps) and no warm-up (nothing to
     warm on a CPU).  Rank 0 only."""
