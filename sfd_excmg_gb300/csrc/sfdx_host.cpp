@@ -283,6 +283,22 @@ static int impedance_from_fields(const SurfFields (&F)[2], int nx, int ny, const
                                  double ff, int nrec, const double* recv, int out_type, int transpose, double* out,
                                  double* tip, zd* fields);
 
+int receiver_stencils(int nx, int ny, const double* a, const double* b, int nrec, const double* recv, int transpose,
+                      int* id, int* idz, double* w) {
+    std::vector<double> aax, bby;
+    cell_centres(nx, ny, a, b, aax, bby);
+    for (int r = 0; r < nrec; r++) {
+        RecvStencil S;
+        HRC(receiver_stencil(nx, ny, aax, bby, recv[r], recv[(size_t)nrec + r], transpose, S));
+        for (int t = 0; t < 9; t++) {
+            id[(size_t)r * 9 + t] = (int)S.id[t];
+            idz[(size_t)r * 9 + t] = (int)S.idz[t];
+            w[(size_t)r * 9 + t] = S.w[t];
+        }
+    }
+    return SFDX_OK;
+}
+
 int impedance_from_surface(const SurfaceView& sv, const double* a, const double* b, const double* c, double ff,
                            int nrec, const double* recv, int out_type, int transpose, double* out, double* tip,
                            zd* fields) {

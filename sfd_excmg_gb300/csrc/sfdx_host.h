@@ -39,6 +39,14 @@ struct SurfaceGrad {
 
 // fields (optional): [nrec][2][5] complex, (Ex, Ey, Hx, Hy, Hz) of each
 // polarisation interpolated to the receiver (the arho rows of post_process).
+// The 3x3 receiver stencils of arho_interp2 (rd=2, fdfe_main.f90:718-790) for
+// the device evaluation: per receiver r, id[9r..9r+8] are the surface cells
+// [j*nx+i] of E, Hx and Hy (transposed with `transpose`), idz[] those of Hz,
+// w[] their weights.  SFDX_ERR_RECEIVER for a receiver outside the
+// interpolable area.
+int receiver_stencils(int nx, int ny, const double* a, const double* b, int nrec, const double* recv, int transpose,
+                      int* id, int* idz, double* w);
+
 int impedance_from_surface(const SurfaceView& sv, const double* a, const double* b, const double* c, double ff,
                            int nrec, const double* recv, int out_type, int transpose, double* out, double* tip,
                            std::complex<double>* fields = nullptr);

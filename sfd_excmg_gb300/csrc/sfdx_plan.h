@@ -269,6 +269,7 @@ struct Plan {
     // before each reliable update
     DBuf x32, xb;
     DBuf d_sel;  // per-system selection flags (int) of the complex64 V-cycle fallback
+    DBuf d_imp;  // workspace of the device impedance evaluation (sfdx_plan_impedance)
     // Krylov vectors (precision of the active solve)
     DBuf kv[14];
     // divergence correction: t, r, p, v, phi (nodes) and the PCG state

@@ -1126,36 +1126,147 @@ extern "C" int sfdx_plan_level_times(const sfdx_plan* plan, double* ms, int n) {
 
 // impedance from the plan's device-resident solution: copy only the edge
 // planes the evaluation reads.
+// Impedances (and tippers) at the receivers from the plan's device fields:
+// post_process + arho_interp2 (fdfe_main.f90:549-790) evaluated as
+// impedance_from_fields does on the host (sfdx_host.cpp), one thread per
+// (receiver, frequency).  The surface E and H of the nine stencil cells come
+// straight from the edge planes nair and nair+1 of both polarisations.
+struct ImpGeom {
+    int nx, ny, nair, nrec, nf, out_type, ncomp;
+    int64_t nl, xnl, ynl;
+    double cz;
+};
+// surface E (x, y) and H (x, y, z) of one polarisation at cell (i, j)
+__device__ __forceinline__ void imp_cell(const double2* __restrict__ x, const ImpGeom& g, const double* a,
+                                         const double* b, double2 iwm, int i, int j, double2 E[2], double2 H[3]) {
+    const int nx = g.nx, ny = g.ny;
+    const int64_t pex = (int64_t)nx * (ny + 1), pey = (int64_t)(nx + 1) * ny, pez = (int64_t)(nx + 1) * (ny + 1);
+    auto ex = [&](int pl, int ii, int jj) { return x[(int64_t)(g.nair + pl) * pex + (int64_t)jj * nx + ii]; };
+    auto ey = [&](int pl, int ii, int jj) {
+        return x[g.xnl + (int64_t)(g.nair + pl) * pey + (int64_t)jj * (nx + 1) + ii];
+    };
+    auto ez = [&](int ii, int jj) { return x[g.xnl + g.ynl + (int64_t)g.nair * pez + (int64_t)jj * (nx + 1) + ii]; };
+    auto half = [](double2 u, double2 v) { return mk<double>((u.x + v.x) / 2.0, (u.y + v.y) / 2.0); };
+    auto over = [](double2 u, double d) { return mk<double>(u.x / d, u.y / d); };
+    const double2 ex0 = half(ex(0, i, j), ex(0, i, j + 1));
+    const double2 ey0 = half(ey(0, i, j), ey(0, i + 1, j));
+    E[0] = ex0;
+    E[1] = ey0;
+    const double2 exz = over(half(ex(1, i, j), ex(1, i, j + 1)) - ex0, g.cz);
+    const double2 ezx = over(half(ez(i + 1, j), ez(i + 1, j + 1)) - half(ez(i, j + 1), ez(i, j)), a[i]);
+    const double2 eyz = over(half(ey(1, i, j), ey(1, i + 1, j)) - ey0, g.cz);
+    const double2 ezy = over(half(ez(i, j + 1), ez(i + 1, j + 1)) - half(ez(i, j), ez(i + 1, j)), b[j]);
+    const double2 exy = over(ex(0, i, j + 1) - ex(0, i, j), b[j]);
+    const double2 eyx = over(ey(0, i + 1, j) - ey(0, i, j), a[i]);
+    H[1] = cdiv<double>(exz - ezx, iwm);
+    H[0] = cdiv<double>(ezy - eyz, iwm);
+    H[2] = cdiv<double>(exy - eyx, iwm);
+}
+
+static __global__ void k_impedance(ImpGeom g, const double2* __restrict__ fields, const double* __restrict__ a,
+                                   const double* __restrict__ b, const double* __restrict__ wmu,
+                                   const int* __restrict__ id, const int* __restrict__ idz,
+                                   const double* __restrict__ w, double* __restrict__ out, double* __restrict__ tip) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= g.nrec * g.nf) return;
+    const int f = t / g.nrec, r = t - f * g.nrec;
+    const double2 iwm = mk<double>(0.0, wmu[f]);
+    double2 fr[2][5];
+    for (int p = 0; p < 2; p++) {
+        const double2* x = fields + (int64_t)(2 * f + p) * g.nl;
+        for (int q = 0; q < 5; q++) fr[p][q] = zero<double>();
+        for (int s = 0; s < 9; s++) {
+            const double ws = w[r * 9 + s];
+            double2 E[2], H[3];
+            const int c = id[r * 9 + s];
+            imp_cell(x, g, a, b, iwm, c % g.nx, c / g.nx, E, H);
+            fr[p][0] = fr[p][0] + rmul<double>(ws, E[0]);
+            fr[p][1] = fr[p][1] + rmul<double>(ws, E[1]);
+            fr[p][2] = fr[p][2] + rmul<double>(ws, H[0]);
+            fr[p][3] = fr[p][3] + rmul<double>(ws, H[1]);
+            const int cz = idz[r * 9 + s];
+            imp_cell(x, g, a, b, iwm, cz % g.nx, cz / g.nx, E, H);
+            fr[p][4] = fr[p][4] + rmul<double>(ws, H[2]);
+        }
+    }
+    const double2 det = cmul<double>(fr[0][2], fr[1][3]) - cmul<double>(fr[1][2], fr[0][3]);
+    const double2 zxy = cdiv<double>(cmul<double>(fr[1][0], fr[0][2]) - cmul<double>(fr[0][0], fr[1][2]), det);
+    const double2 zyx = cdiv<double>(cmul<double>(fr[0][1], fr[1][3]) - cmul<double>(fr[1][1], fr[0][3]), det);
+    double* o = out + ((int64_t)f * g.nrec + r) * g.ncomp;
+    if (g.out_type == 3) {
+        // the full tensor Z = E H^-1 (the reference forms Zxy and Zyx only)
+        const double2 zxx = cdiv<double>(cmul<double>(fr[0][0], fr[1][3]) - cmul<double>(fr[1][0], fr[0][3]), det);
+        const double2 zyy = cdiv<double>(cmul<double>(fr[1][1], fr[0][2]) - cmul<double>(fr[0][1], fr[1][2]), det);
+        const double2 zz[4] = {zxx, zxy, zyx, zyy};
+        for (int q = 0; q < 4; q++) {
+            o[2 * q] = zz[q].x;
+            o[2 * q + 1] = zz[q].y;
+        }
+    } else if (g.out_type == 2) {
+        const double2 a2 = cmul<double>(zxy, zxy), b2 = cmul<double>(zyx, zyx);
+        o[0] = sqrt(cabs2<double>(a2)) / wmu[f];  // |i Z^2| = |Z^2|
+        o[1] = sqrt(cabs2<double>(b2)) / wmu[f];
+        o[2] = -atan(zxy.y / zxy.x) * 180.0 / 3.141592653589793238462643;
+        o[3] = -atan(zyx.y / zyx.x) * 180.0 / 3.141592653589793238462643;
+    } else {
+        o[0] = zxy.x;
+        o[1] = zxy.y;
+        o[2] = zyx.x;
+        o[3] = zyx.y;
+    }
+    if (tip) {
+        const double2 tx = cdiv<double>(cmul<double>(fr[1][3], fr[0][4]) - cmul<double>(fr[0][3], fr[1][4]), det);
+        const double2 ty = cdiv<double>(cmul<double>(fr[0][2], fr[1][4]) - cmul<double>(fr[1][2], fr[0][4]), det);
+        double* tp = tip + ((int64_t)f * g.nrec + r) * 4;
+        tp[0] = tx.x;
+        tp[1] = tx.y;
+        tp[2] = ty.x;
+        tp[3] = ty.y;
+    }
+}
+
 extern "C" int sfdx_plan_impedance(sfdx_plan* plan, int nrec, const double* recv, int out_type, double* out,
                                    double* tipper) {
     if (!plan || !recv || !out || nrec < 1) return SFDX_ERR_ARG;
     Plan& P = plan->P;
     if (!P.solution_current()) return SFDX_ERR_ARG;
     const Level& F = P.lev[P.nlev - 1];
-    const int nx = F.nx, ny = F.ny, m = F.nair;
-    const size_t pex = (size_t)nx * (ny + 1), pey = (size_t)(nx + 1) * ny, pez = (size_t)(nx + 1) * (ny + 1);
-    std::vector<std::complex<double>> buf((2 * pex + 2 * pey + pez) * 2);
-    const std::complex<double>* dev = reinterpret_cast<const std::complex<double>*>(P.ex_out.p);
-    for (int f = 0; f < P.nf; f++) {
-        SurfaceView sv;
-        sv.nx = nx; sv.ny = ny; sv.nair = m;
-        for (int p = 0; p < 2; p++) {
-            const std::complex<double>* x = dev + (size_t)(2 * f + p) * F.nl;
-            std::complex<double>* base = buf.data() + (size_t)p * (2 * pex + 2 * pey + pez);
-            CK(cudaMemcpyAsync(base, x + (size_t)m * pex, 2 * pex * 16, cudaMemcpyDeviceToHost, P.st));
-            CK(cudaMemcpyAsync(base + 2 * pex, x + F.xnl + (size_t)m * pey, 2 * pey * 16, cudaMemcpyDeviceToHost, P.st));
-            CK(cudaMemcpyAsync(base + 2 * pex + 2 * pey, x + F.xnl + F.ynl + (size_t)m * pez, pez * 16,
-                               cudaMemcpyDeviceToHost, P.st));
-            sv.exs[p] = base;
-            sv.eys[p] = base + 2 * pex;
-            sv.ezs[p] = base + 2 * pex + 2 * pey;
-        }
-        CK(cudaStreamSynchronize(P.st));
-        RC(impedance_from_surface(sv, F.a.data(), F.b.data(), F.c.data(), P.freq[f], nrec, recv, out_type,
-                                  (P.o.quirks & SFDX_QUIRK_RX_TRANSPOSE) ? 1 : 0,
-                                  out + (size_t)f * nrec * (out_type == 3 ? 8 : 4),
-                                  tipper ? tipper + (size_t)f * nrec * 4 : nullptr));
-    }
+    const int transpose = (P.o.quirks & SFDX_QUIRK_RX_TRANSPOSE) ? 1 : 0;
+    const int ncomp = out_type == 3 ? 8 : 4;
+    std::vector<int> id((size_t)nrec * 9), idz((size_t)nrec * 9);
+    std::vector<double> w((size_t)nrec * 9), wmu(P.nf);
+    RC(receiver_stencils(F.nx, F.ny, F.a.data(), F.b.data(), nrec, recv, transpose, id.data(), idz.data(), w.data()));
+    const double pi = 3.141592653589793238462643, mu = 4.0 * pi * 1e-7;
+    for (int f = 0; f < P.nf; f++) wmu[f] = 2.0 * pi * P.freq[f] * mu;
+    // device workspace: a, b, wmu, w, out, tip (doubles), id, idz (ints)
+    const size_t nd = (size_t)F.nx + F.ny + P.nf + w.size() + (size_t)P.nf * nrec * (ncomp + 4);
+    RC(P.d_imp.alloc(nd * sizeof(double) + 2 * id.size() * sizeof(int)));
+    double* da = P.d_imp.as<double>();
+    double* db = da + F.nx;
+    double* dwm = db + F.ny;
+    double* dw = dwm + P.nf;
+    double* dout = dw + w.size();
+    double* dtip = dout + (size_t)P.nf * nrec * ncomp;
+    int* did = reinterpret_cast<int*>(da + nd);
+    int* didz = did + id.size();
+    CK(cudaMemcpyAsync(da, F.a.data(), F.nx * sizeof(double), cudaMemcpyHostToDevice, P.st));
+    CK(cudaMemcpyAsync(db, F.b.data(), F.ny * sizeof(double), cudaMemcpyHostToDevice, P.st));
+    CK(cudaMemcpyAsync(dwm, wmu.data(), P.nf * sizeof(double), cudaMemcpyHostToDevice, P.st));
+    CK(cudaMemcpyAsync(dw, w.data(), w.size() * sizeof(double), cudaMemcpyHostToDevice, P.st));
+    CK(cudaMemcpyAsync(did, id.data(), id.size() * sizeof(int), cudaMemcpyHostToDevice, P.st));
+    CK(cudaMemcpyAsync(didz, idz.data(), idz.size() * sizeof(int), cudaMemcpyHostToDevice, P.st));
+    ImpGeom g;
+    g.nx = F.nx; g.ny = F.ny; g.nair = F.nair; g.nrec = nrec; g.nf = P.nf; g.out_type = out_type; g.ncomp = ncomp;
+    g.nl = F.nl; g.xnl = F.xnl; g.ynl = F.ynl;
+    g.cz = F.c[F.nair];
+    const int n = nrec * P.nf;
+    KL(k_impedance<<<(n + 127) / 128, 128, 0, P.st>>>(g, P.ex_out.as<double2>(), da, db, dwm, did, didz, dw, dout,
+                                                       tipper ? dtip : nullptr));
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(out, dout, (size_t)P.nf * nrec * ncomp * sizeof(double), cudaMemcpyDeviceToHost, P.st));
+    if (tipper)
+        CK(cudaMemcpyAsync(tipper, dtip, (size_t)P.nf * nrec * 4 * sizeof(double), cudaMemcpyDeviceToHost, P.st));
+    CK(cudaStreamSynchronize(P.st));
     return SFDX_OK;
 }
 

@@ -113,7 +113,27 @@ def test_plan_reuse_and_device_impedance():
     assert np.array_equal(ex1, ex2)
     np.testing.assert_array_equal(z1, z2)
     zh = S.impedance(m, ex1)
-    np.testing.assert_allclose(z1, zh, rtol=0, atol=1e-14 * np.abs(zh).max())
+    # device evaluation against the host one: the same formulas, different rounding
+    np.testing.assert_allclose(z1, zh, rtol=1e-11, atol=1e-14 * np.abs(zh).max())
+
+
+@pytest.mark.parametrize("transpose", [True, False])
+def test_device_impedance_matches_host_evaluation(transpose):
+    """sfdx_plan_impedance evaluates Z on the device (post_process + arho_interp2, fdfe_main.f90:549-790,
+    one thread per receiver and frequency); sfdx_impedance evaluates it on the host from fetched
+    fields.  Every output type (Zxy/Zyx, apparent resistivity and phase, the full tensor) and the
+    tippers agree to rounding, with the reference's transposed receiver stencil and without."""
+    from sfd_excmg_gb300 import capi
+    quirks = capi.QUIRKS_REFERENCE if transpose else capi.QUIRKS_REFERENCE & ~capi.QUIRK_RX_TRANSPOSE
+    m = syn.small_aniso(n=16, seed=2, freqs=(0.05, 1.0, 20.0))
+    with S.Plan(m, eps=1e-9, excmg=1, level=3, solver=3, precision=S.FP64, div_cor=2, corr_intv=25, corr_tol=1e-2,
+                quirks=quirks) as p:
+        ex = p.solve()
+        for ot in (1, 2, 3):
+            zd, td = p.impedance(out_type=ot, tipper=True)
+            zh, th = S.impedance(m, ex, out_type=ot, quirks=quirks, tipper=True)
+            np.testing.assert_allclose(zd, zh, rtol=1e-11, atol=1e-14 * np.abs(zh).max())
+            np.testing.assert_allclose(td, th, rtol=1e-10, atol=1e-13 * np.abs(th).max())
 
 
 def test_solve_batch_matches_single_solves():
