@@ -336,3 +336,42 @@ def test_edge_prolongation_reproduces_constant_fields():
     np.testing.assert_allclose(v[:xnl], 1.0, rtol=1e-14)
     np.testing.assert_allclose(v[xnl:xnl + ynl], 2.0, rtol=1e-14)
     np.testing.assert_allclose(v[xnl + ynl:], 3.0, rtol=1e-14)
+
+
+def test_edge_prolongation_commutes_with_the_gradient():
+    """The edge interpolation of the multigrid preconditioner maps discrete gradients to discrete
+    gradients: P G_c phi = G_f (Pn phi) with Pn the trilinear nodal interpolation on the same nested
+    non-uniform meshes -- the property that lets the coarse levels correct the gradient part of the
+    error (and the nodal step's corrections survive the transfer)."""
+    import scipy.sparse as sp
+    m = syn.small_aniso(n=16, seed=0)
+    nx, ny, nz = m.nx, m.ny, m.nz
+    a1, b1, c1, _ = O.mesh_coarsen(m.a, m.b, m.c, m.sigma, 1, quirk=False)
+    cx, cy, cz = len(a1), len(b1), len(c1)
+
+    def interp_1d(h):
+        lo, wlo, hi, whi = O._node_terms(np.asarray(h, float))
+        n = len(h) + 1
+        return sp.csr_matrix((np.concatenate([wlo, whi]), (np.tile(np.arange(n), 2), np.concatenate([lo, hi]))),
+                             shape=(n, len(h) // 2 + 1))
+
+    Pn = sp.kron(interp_1d(m.c), sp.kron(interp_1d(m.b), interp_1d(m.a))).tocsr()
+
+    def interior(nx_, ny_, nz_):
+        n = np.arange((nx_ + 1) * (ny_ + 1) * (nz_ + 1))
+        i, j, k = n % (nx_ + 1), (n // (nx_ + 1)) % (ny_ + 1), n // ((nx_ + 1) * (ny_ + 1))
+        return (i > 0) & (i < nx_) & (j > 0) & (j < ny_) & (k > 0) & (k < nz_)
+
+    ic, ifn = interior(cx, cy, cz), interior(nx, ny, nz)
+    Gc = O.node_gradient(cx, cy, cz, a1, b1, c1)
+    Gf = O.node_gradient(nx, ny, nz, m.a, m.b, m.c)
+    P = O.edge_prolongation(m.a, m.b, m.c)
+    rng = np.random.default_rng(3)
+    phi = rng.standard_normal(int(ic.sum())) + 1j * rng.standard_normal(int(ic.sum()))
+    full = np.zeros(ic.size, complex)
+    full[ic] = phi
+    phif = (Pn @ full)
+    assert np.abs(phif[~ifn]).max() == 0.0  # zero coarse boundary -> zero fine boundary
+    lhs = P @ (Gc @ phi)
+    rhs = Gf @ phif[ifn]
+    np.testing.assert_allclose(lhs, rhs, rtol=0, atol=1e-12 * np.abs(rhs).max())
