@@ -289,6 +289,16 @@ int sfdx_apply_operator(int nx, int ny, int nz, const double* a, const double* b
 int sfdx_build_rhs(int nx, int ny, int nz, const double* a, const double* b, const double* c, const double* sigma,
                    double freq, const double* edc, double* p1, double* p2);
 
+/* One application of the edge multigrid V-cycle (precond 'G'; no reference
+ * counterpart: pre_type offers SSOR, Jacobi and ILU(0) only,
+ * global_para.f90:18) on the finest of `levels` 2x-coarsened meshes:
+ * x = M^{-1} y for ns systems (y, x: [nl][ns] complex, freqs[ns]).  precision
+ * SFDX_FP64 runs the FP64 V-cycle, SFDX_MIXED the complex64 one of mixed
+ * plans (whose nodal steps leave out all-air nodes). */
+int sfdx_vcycle_apply(int nx, int ny, int nz, int nair, const double* a, const double* b, const double* c,
+                      const double* sigma, int ns, const double* freqs, int levels, int precision, const double* y,
+                      double* x);
+
 /* One preconditioner application x = M^{-1} y (replaces ssorfac + lusol,
  * div_correc.f90:171-220 / solvers.f90:721-762, with the multi-colour
  * ordering; 'J' replaces diagcsr). */

@@ -837,6 +837,90 @@ def converged_solve(model: OracleModel, ff, tol=1e-15, nlev=None, maxit=200):
     return out[0], out[1], rr[0], rr[1], its
 
 
+# --------------------------------------------------------------------------- the GPU's edge multigrid V-cycle
+# Restatement of the V-cycle of precond = 'G' (sfdx_mgkern.cuh, emg_* in
+# sfdx_krylov.cuh) on the assembled matrices, the oracle of sfdx_vcycle_apply.
+# No reference counterpart (pre_type offers SSOR, Jacobi and ILU(0) only).
+# Per level: x = S^-1 b with the multi-colour symmetric Gauss-Seidel of the
+# Krylov preconditioner ('M', colours Ex (j+k)&1, Ey (i+k)&1, Ez (i+j)&1,
+# orientation-major), a nodal step (q = b + i w mu Ms x on interior edges,
+# phi = omega (G^T V q) / diag(G^T V K G), x += G phi), then the residual
+# restricted by V_c^-1 P^T V_f, the coarser V-cycle from zero, x += P x_c,
+# and one smoothing step (r = b - K x, x += S^-1 r, nodal step); the coarsest
+# level takes `coarse_sweeps` smoothing steps.  Coarse meshes: mesh_coarsen
+# without its index shift.
+def _mc_colour_rows(nx, ny, nz):
+    col = np.zeros(nedges(nx, ny, nz), np.int8)
+    k, j, i = np.meshgrid(np.arange(nz + 1), np.arange(ny + 1), np.arange(nx), indexing="ij")
+    xnl = i.size
+    col[:xnl] = ((j + k) & 1).ravel()
+    k, j, i = np.meshgrid(np.arange(nz + 1), np.arange(ny), np.arange(nx + 1), indexing="ij")
+    ynl = i.size
+    col[xnl:xnl + ynl] = 2 + ((i + k) & 1).ravel()
+    k, j, i = np.meshgrid(np.arange(nz), np.arange(ny + 1), np.arange(nx + 1), indexing="ij")
+    col[xnl + ynl:] = 4 + ((i + j) & 1).ravel()
+    return [np.flatnonzero(col == c) for c in range(6)], col
+
+
+def _mc_sgs(L, b):
+    """x = (D+U)^-1 D (D+L)^-1 b (the multi-colour SSOR with omega = 1), vectorised per colour."""
+    x = np.zeros_like(b)
+    for c in range(6):
+        R = L.rows[c]
+        x[R] = (b[R] - L.K[R] @ x) / L.D[R]  # later colours and the own colour are still zero
+    for c in range(4, -1, -1):
+        R = L.rows[c]
+        later = np.where(L.col > c, x, 0)
+        x[R] = x[R] - (L.K[R] @ later) / L.D[R]
+    return x
+
+
+def _gpu_nodal(L, b, x, omega):
+    q = b + 1j * L.wm * (L.Ms @ x)
+    q[L.bnd] = 0
+    phi = omega * (L.GT @ (L.V * q)) / L.Kn_diag
+    return x + L.G @ phi
+
+
+def _gpu_smooth(L, b, x, omega):
+    r = b - L.K @ x
+    return _gpu_nodal(L, b, x + _mc_sgs(L, r), omega)
+
+
+def _gpu_vcycle(levs, l, b, omega, coarse_sweeps):
+    L = levs[l]
+    x = _gpu_nodal(L, b, _mc_sgs(L, b), omega)
+    if l == len(levs) - 1:
+        for _ in range(coarse_sweeps - 1):
+            x = _gpu_smooth(L, b, x, omega)
+        return x
+    C = levs[l + 1]
+    rc = L.PT @ (L.V * (b - L.K @ x))
+    rc = np.where(C.bnd, 0, rc / np.where(C.V > 0, C.V, 1))
+    x = x + L.P @ _gpu_vcycle(levs, l + 1, rc, omega, coarse_sweeps)
+    return _gpu_smooth(L, b, x, omega)
+
+
+def gpu_vcycle(model: OracleModel, ff, y, nlev=3, omega=0.7, coarse_sweeps=4):
+    """x = M^-1 y for one system of frequency ff with the V-cycle above (levels: the model's
+    mesh and nlev - 1 coarser ones)."""
+    levs = _mg_hierarchy(model, ff, nlev)
+    wm = 2 * np.pi * ff * 4e-7 * np.pi
+    for l, L in enumerate(levs):
+        nx, ny, nz = len(L.a), len(L.b), len(L.c)
+        s = _d(model.sigma) if l == 0 else mesh_coarsen(model.a, model.b, model.c, model.sigma, l, quirk=False)[3]
+        # the mass part from a second assembly at twice the frequency: K(f) = C - i w mu Ms
+        edc2, _, _ = mt1d_anl(2 * ff, column_conv(s, nx, ny, nz), L.c)
+        K2, _, _ = assemble(nx, ny, nz, L.a, L.b, L.c, s, 2 * ff, edc2)
+        L.K = L.K.tocsr()
+        L.Ms = ((K2 - L.K) / (-1j * wm)).tocsr()
+        L.wm = wm
+        L.D = L.K.diagonal()
+        L.rows, L.col = _mc_colour_rows(nx, ny, nz)
+        L.Kn_diag = L.Kn.diagonal()
+    return _gpu_vcycle(levs, 0, _z(y), omega, coarse_sweeps)
+
+
 # --------------------------------------------------------------------------- the reference algorithm, timed
 def reference_frequency(model: OracleModel, k, eps, pols=(0, 1)):
     """One frequency (both polarisations) of the reference algorithm as the driver runs it:

@@ -9,14 +9,14 @@ from .capi import FP64, MIXED, QUIRKS_REFERENCE, Opts, SfdxError
 from .model import Model
 from .solver import (Plan, apply_operator, build_rhs, fwd_solve, grad_correct, impedance, impedance_topo, krylov_solve,
                      mesh_coarsen,
-                     mt1d, precond_apply, prolongate, receiver_fields, solve_batch, write_ccv, write_res,
+                     mt1d, precond_apply, vcycle_apply, prolongate, receiver_fields, solve_batch, write_ccv, write_res,
                      impedance_misfit)
 
 __all__ = [
     "capi", "Opts", "SfdxError", "FP64", "MIXED", "QUIRKS_REFERENCE", "Model", "Plan", "fwd_solve", "impedance",
     "impedance_topo",
     "receiver_fields",
-    "mt1d", "apply_operator", "build_rhs", "precond_apply", "mesh_coarsen", "prolongate", "krylov_solve",
+    "mt1d", "apply_operator", "build_rhs", "precond_apply", "vcycle_apply", "mesh_coarsen", "prolongate", "krylov_solve",
     "grad_correct", "solve_batch", "write_res", "write_ccv", "impedance_misfit", "sigma_misfit", "log_sigma_misfit",
 ]
 

@@ -118,6 +118,9 @@ _PROTO = {
                                            c_double_p, c_double_p]),
     "sfdx_build_rhs": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, c_double_p, c_double_p, c_double_p,
                                       c_double_p, ctypes.c_double, c_double_p, c_double_p, c_double_p]),
+    "sfdx_vcycle_apply": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, c_double_p,
+                                         c_double_p, c_double_p, c_double_p, ctypes.c_int, c_double_p, ctypes.c_int,
+                                         ctypes.c_int, c_double_p, c_double_p]),
     "sfdx_precond_apply": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, c_double_p, c_double_p,
                                           c_double_p, c_double_p, ctypes.c_int, c_double_p, ctypes.c_int,
                                           ctypes.c_int, c_double_p, c_double_p]),

@@ -1364,16 +1364,19 @@ extern "C" int sfdx_receiver_fields(int nx, int ny, int nz, int nair, const doub
 namespace {
 // A one-level plan over host inputs, ns systems at the given frequencies.
 int component_plan(sfdx_plan** h, const sfdx_opts* o, int nx, int ny, int nz, const double* a, const double* b,
-                   const double* c, const double* sigma, int ns, const double* freqs) {
+                   const double* c, const double* sigma, int ns, const double* freqs, int nair = 0,
+                   int levels = 0) {
     if (ns < 1 || ns > SFDX_MAX_SYSTEMS || !freqs) return SFDX_ERR_ARG;
     sfdx_opts oo;
     if (o) oo = *o;
     else sfdx_default_opts(&oo);
-    oo.excmg = 0;
+    // one mesh level, or `levels` 2x-coarsened ones (the edge multigrid's)
+    oo.excmg = levels > 1 ? 1 : 0;
+    if (levels > 1) oo.level = levels;
     // nf systems pairs: reuse plan_create with one frequency per pair, then
     // override the per-system table with the requested frequencies.
     std::vector<double> fr((ns + 1) / 2, 1.0);
-    RC(sfdx_plan_create(h, &oo, nx, ny, nz, 0, a, b, c, (int)fr.size(), fr.data()));
+    RC(sfdx_plan_create(h, &oo, nx, ny, nz, nair, a, b, c, (int)fr.size(), fr.data()));
     Plan& P = (*h)->P;
     P.ns = ns;
     if (P.lev[0].nl * ns >= (1LL << 31)) return SFDX_ERR_UNSUPPORTED;
@@ -1464,6 +1467,48 @@ extern "C" int sfdx_precond_apply(int nx, int ny, int nz, const double* a, const
     RC(component_plan(&g.p, &o, nx, ny, nz, a, b, c, sigma, ns, freqs));
     Plan& P = g.p->P;
     const Level& L = P.lev[0];
+    const size_t n = (size_t)L.nl * ns;
+    std::vector<KState> init(ns);
+    for (int q = 0; q < ns; q++) {
+        memset(&init[q], 0, sizeof(KState));
+        init[q].wm = P.wm[q];
+        init[q].active = 1;
+    }
+    CK(cudaMemcpyAsync(P.d_state.p, init.data(), sizeof(KState) * ns, cudaMemcpyHostToDevice, P.st));
+    DBuf dy, dx;
+    RC(dy.alloc(n * 16));
+    RC(dx.alloc(n * 16));
+    CK(cudaMemcpyAsync(dy.p, y, n * 16, cudaMemcpyHostToDevice, P.st));
+    if (precision == SFDX_FP64) {
+        RC(precond_vec<double>(P, L, dx.as<double2>(), dy.as<double2>()));
+    } else {
+        DBuf fy, fx;
+        RC(fy.alloc(n * 8));
+        RC(fx.alloc(n * 8));
+        KL(k_convert<double, float><<<grid_for(n, 256), 256, 0, P.st>>>(n, dy.as<double2>(), fy.as<float2>()));
+        RC(precond_vec<float>(P, L, fx.as<float2>(), fy.as<float2>()));
+        KL(k_convert<float, double><<<grid_for(n, 256), 256, 0, P.st>>>(n, fx.as<float2>(), dx.as<double2>()));
+        CK(cudaStreamSynchronize(P.st));
+    }
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(x, dx.p, n * 16, cudaMemcpyDeviceToHost, P.st));
+    CK(cudaStreamSynchronize(P.st));
+    return SFDX_OK;
+}
+
+extern "C" int sfdx_vcycle_apply(int nx, int ny, int nz, int nair, const double* a, const double* b, const double* c,
+                                 const double* sigma, int ns, const double* freqs, int levels, int precision,
+                                 const double* y, double* x) {
+    if (!sigma || !y || !x || levels < 2 || nair < 0) return SFDX_ERR_ARG;
+    if (precision != SFDX_FP64 && precision != SFDX_MIXED) return SFDX_ERR_ARG;
+    sfdx_opts o;
+    sfdx_default_opts(&o);
+    o.precond = 'G';
+    o.precision = precision;
+    PlanGuard g;
+    RC(component_plan(&g.p, &o, nx, ny, nz, a, b, c, sigma, ns, freqs, nair, levels));
+    Plan& P = g.p->P;
+    const Level& L = P.lev[P.nlev - 1];
     const size_t n = (size_t)L.nl * ns;
     std::vector<KState> init(ns);
     for (int q = 0; q < ns; q++) {

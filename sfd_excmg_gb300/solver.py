@@ -396,6 +396,21 @@ def precond_apply(nx, ny, nz, a, b, c, sigma, freqs, y, precond="S", precision=c
     return x.reshape(np.shape(y))
 
 
+def vcycle_apply(model: Model, freqs, y, levels: int = 3, precision=capi.FP64):
+    """One edge-multigrid V-cycle x = M^{-1} y (sfdx_vcycle_apply) on the model's mesh and the
+    `levels` - 1 coarser ones; y[nl, ns] complex with one frequency per system."""
+    freqs = _d(np.atleast_1d(freqs))
+    ns = len(freqs)
+    nx, ny, nz = model.nx, model.ny, model.nz
+    a, b, c, sigma = _mesh(nx, ny, nz, model.a, model.b, model.c, model.sigma)
+    yy = _vec(y, _nl(nx, ny, nz), ns, "y")
+    x = np.zeros_like(yy)
+    capi.check(capi.lib().sfdx_vcycle_apply(nx, ny, nz, model.nair, capi.dptr(a), capi.dptr(b), capi.dptr(c),
+                                            capi.dptr(sigma), ns, capi.dptr(freqs), levels, precision,
+                                            capi.zptr(yy), capi.zptr(x)), "sfdx_vcycle_apply")
+    return x.reshape(np.shape(y))
+
+
 def mesh_coarsen(a, b, c, sigma, k, quirks=capi.QUIRKS_REFERENCE):
     nx, ny, nz = len(a), len(b), len(c)
     a, b, c, sigma = _mesh(nx, ny, nz, a, b, c, sigma)

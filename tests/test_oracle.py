@@ -375,3 +375,20 @@ def test_edge_prolongation_commutes_with_the_gradient():
     lhs = P @ (Gc @ phi)
     rhs = Gf @ phif[ifn]
     np.testing.assert_allclose(lhs, rhs, rtol=0, atol=1e-12 * np.abs(rhs).max())
+
+
+def test_gpu_vcycle_restatement_preconditions_bicgstab():
+    """The oracle's restatement of the GPU's edge multigrid V-cycle is a working preconditioner:
+    BiCGStab with it reaches a 1e-10 residual on the 16^3 anisotropic model with air at 0.01 and
+    10 Hz in a few tens of iterations (the oracle of sfdx_vcycle_apply)."""
+    from scipy.sparse.linalg import LinearOperator, bicgstab
+    m = syn.small_aniso(n=16, nair=8, nz_earth=24, seed=0, freqs=(0.01, 10.0))
+    om = O.OracleModel(m.nx, m.ny, m.nz, m.nair, m.a, m.b, m.c, m.sigma, m.freq, m.recv)
+    for ff in m.freq:
+        edc, _, _ = O.mt1d_anl(ff, O.column_conv(m.sigma, m.nx, m.ny, m.nz), m.c)
+        K, p1, _ = O.assemble(m.nx, m.ny, m.nz, m.a, m.b, m.c, m.sigma, ff, edc)
+        Mv = LinearOperator(K.shape, lambda v, ff=ff: O.gpu_vcycle(om, ff, v), dtype=np.complex128)
+        its = [0]
+        x, info = bicgstab(K, p1, rtol=1e-10, atol=0.0, maxiter=80, M=Mv, callback=lambda _: its.__setitem__(0, its[0] + 1))
+        rel = np.linalg.norm(p1 - K @ x) / np.linalg.norm(p1)
+        assert rel < 1e-9 and its[0] < 60, (ff, rel, its[0])
