@@ -876,10 +876,11 @@ def _mc_sgs(L, b):
 
 
 def _gpu_nodal(L, b, x, omega):
+    # phi = omega D^-1 G^T V q with D = diag(G^T V K G) = -i w mu N_nn; the GPU keeps 1/N_nn in
+    # float (nodal_setup), and so does this restatement
     q = b + 1j * L.wm * (L.Ms @ x)
     q[L.bnd] = 0
-    phi = omega * (L.GT @ (L.V * q)) / L.Kn_diag
-    return x + L.G @ phi
+    return x + L.G @ (omega * 1j * (L.dinv32 / L.wm) * (L.GT @ (L.V * q)))
 
 
 def _gpu_smooth(L, b, x, omega):
@@ -917,7 +918,8 @@ def gpu_vcycle(model: OracleModel, ff, y, nlev=3, omega=0.7, coarse_sweeps=4):
         L.wm = wm
         L.D = L.K.diagonal()
         L.rows, L.col = _mc_colour_rows(nx, ny, nz)
-        L.Kn_diag = L.Kn.diagonal()
+        n32 = (1j * L.Kn.diagonal() / wm).real.astype(np.float32)  # N_nn rounded to float, then 1.f / N
+        L.dinv32 = (np.float32(1.0) / n32).astype(np.float64)
     return _gpu_vcycle(levs, 0, _z(y), omega, coarse_sweeps)
 
 
