@@ -918,7 +918,10 @@ def gpu_vcycle(model: OracleModel, ff, y, nlev=3, omega=0.7, coarse_sweeps=4):
         L.wm = wm
         L.D = L.K.diagonal()
         L.rows, L.col = _mc_colour_rows(nx, ny, nz)
-        n32 = (1j * L.Kn.diagonal() / wm).real.astype(np.float32)  # N_nn rounded to float, then 1.f / N
+        # N = G^T V Ms G directly (G^T V K G / (-i w mu) carries the rounding of C G = 0 divided by
+        # w mu); N_nn rounded to float, then 1.f / N, as the GPU does
+        nd = (L.GT @ (sp.diags(L.V) @ (L.Ms.real @ L.G))).diagonal()
+        n32 = nd.astype(np.float32)
         L.dinv32 = (np.float32(1.0) / n32).astype(np.float64)
     return _gpu_vcycle(levs, 0, _z(y), omega, coarse_sweeps)
 
