@@ -926,6 +926,117 @@ def gpu_vcycle(model: OracleModel, ff, y, nlev=3, omega=0.7, coarse_sweeps=4):
     return _gpu_vcycle(levs, 0, _z(y), omega, coarse_sweeps)
 
 
+# --------------------------------------------------------------------------- complex64 Krylov on a split V-cycle
+# Numerical premise of a complex64 Krylov iteration under the edge multigrid
+# (not built on the GPU yet): storage of every vector in complex64 is emulated
+# by rounding after each step.  The V-cycle above, run with that storage, either
+# adds its nodal corrections G phi into x (split=False) or carries them as a nodal
+# potential psi beside x (split=True): residuals then take A(x + G psi) =
+# K x - i w mu Ms G psi (C G = 0), and the prolongation moves psi by the
+# trilinear nodal interpolation, which commutes with G.  BiCGStab runs on complex64
+# vectors with an FP64 iterate and an FP64 residual every 8 iterations.
+def _c64(v):
+    return v.astype(np.complex64).astype(np.complex128)
+
+
+def _node_interp_1d(h):
+    lo, wlo, hi, whi = _node_terms(_d(h))
+    n = len(h) + 1
+    return sp.csr_matrix((np.concatenate([wlo, whi]), (np.tile(np.arange(n), 2), np.concatenate([lo, hi]))),
+                         shape=(n, len(h) // 2 + 1))
+
+
+def _interior_nodes(nx, ny, nz):
+    n = np.arange((nx + 1) * (ny + 1) * (nz + 1))
+    i, j, k = n % (nx + 1), (n // (nx + 1)) % (ny + 1), n // ((nx + 1) * (ny + 1))
+    return (i > 0) & (i < nx) & (j > 0) & (j < ny) & (k > 0) & (k < nz)
+
+
+def _split_levels(model, ff, nlev):
+    levs = _mg_hierarchy(model, ff, nlev)
+    wm = 2 * np.pi * ff * 4e-7 * np.pi
+    for l, L in enumerate(levs):
+        nx, ny, nz = len(L.a), len(L.b), len(L.c)
+        s = _d(model.sigma) if l == 0 else mesh_coarsen(model.a, model.b, model.c, model.sigma, l, quirk=False)[3]
+        edc2, _, _ = mt1d_anl(2 * ff, column_conv(s, nx, ny, nz), L.c)
+        K2, _, _ = assemble(nx, ny, nz, L.a, L.b, L.c, s, 2 * ff, edc2)
+        L.K = L.K.tocsr()
+        L.Ms = ((K2 - L.K) / (-1j * wm)).tocsr()
+        L.wm = wm
+        L.inner = _interior_nodes(nx, ny, nz)
+        if l > 0:
+            F = levs[l - 1]
+            Pn = sp.kron(_node_interp_1d(F.c), sp.kron(_node_interp_1d(F.b), _node_interp_1d(F.a))).tocsr()
+            F.Pn = Pn[F.inner][:, L.inner].tocsr()
+    return levs
+
+
+def _split_smooth(L, b, x, psi, split):
+    r = b - L.K @ x + 1j * L.wm * (L.Ms @ (L.G @ psi))
+    x = _c64(x + _sgs(L.K, r, np.zeros_like(r)))
+    r = b - L.K @ x + 1j * L.wm * (L.Ms @ (L.G @ psi))
+    phi = _sgs(L.Kn, L.GT @ (L.V * r), np.zeros(L.Kn.shape[0], np.complex128))
+    return (x, _c64(psi + phi)) if split else (_c64(x + L.G @ phi), psi)
+
+
+def _split_vcycle(levs, l, b, split):
+    L = levs[l]
+    x, psi = np.zeros_like(b), np.zeros(L.G.shape[1], np.complex128)
+    if l == len(levs) - 1:
+        for _ in range(4):
+            x, psi = _split_smooth(L, b, x, psi, split)
+        return x, psi
+    x, psi = _split_smooth(L, b, x, psi, split)
+    C = levs[l + 1]
+    rc = L.PT @ (L.V * (b - L.K @ x + 1j * L.wm * (L.Ms @ (L.G @ psi))))
+    rc = np.where(C.bnd, 0, rc / np.where(C.V > 0, C.V, 1))
+    xc, psic = _split_vcycle(levs, l + 1, rc, split)
+    x, psi = _c64(x + L.P @ xc), _c64(psi + L.Pn @ psic)
+    return _split_smooth(L, b, x, psi, split)
+
+
+def complex64_vcycle_bicgstab(model: OracleModel, ff, split=True, nlev=3, tol=1e-12, maxit=200, every=8):
+    """BiCGStab with complex64 storage under the V-cycle above for the xy system of frequency ff;
+    returns (iterations, final FP64 relative residual, FP64 residuals every `every` iterations)."""
+    levs = _split_levels(model, ff, nlev)
+    F = levs[0]
+    K, K32 = F.K, F.K.astype(np.complex64)
+    b = F.p1
+    nb = np.linalg.norm(b)
+
+    def op(yc, psi):  # A (y_c + G psi) in complex64 arithmetic on y_c, the mass part on G psi
+        return _c64((K32 @ yc.astype(np.complex64)).astype(np.complex128) - 1j * F.wm * (F.Ms @ (F.G @ psi)))
+
+    x = np.zeros_like(b)
+    r = b.copy()
+    rhat = r.copy()
+    p = np.zeros_like(b)
+    v = np.zeros_like(b)
+    rho = alpha = omega = 1.0
+    its, hist = 0, []
+    while its < maxit:
+        rho1 = np.vdot(rhat, r)
+        p = _c64(r + rho1 / rho * alpha / omega * (p - omega * v))
+        yc, ypsi = _split_vcycle(levs, 0, p, split)
+        v = op(yc, ypsi)
+        alpha = rho1 / np.vdot(rhat, v)
+        s = _c64(r - alpha * v)
+        zc, zpsi = _split_vcycle(levs, 0, s, split)
+        t = op(zc, zpsi)
+        omega = np.vdot(t, s) / np.vdot(t, t)
+        x = x + alpha * (yc + F.G @ ypsi) + omega * (zc + F.G @ zpsi)
+        r = _c64(s - omega * t)
+        rho = rho1
+        its += 1
+        if its % every == 0:
+            rr = b - K @ x
+            hist.append(float(np.linalg.norm(rr) / nb))
+            r = _c64(rr)
+            if hist[-1] < tol or not np.isfinite(hist[-1]):
+                break
+    return its, float(np.linalg.norm(b - K @ x) / nb), hist
+
+
 # --------------------------------------------------------------------------- the reference algorithm, timed
 def reference_frequency(model: OracleModel, k, eps, pols=(0, 1)):
     """One frequency (both polarisations) of the reference algorithm as the driver runs it:

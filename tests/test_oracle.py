@@ -392,3 +392,18 @@ def test_gpu_vcycle_restatement_preconditions_bicgstab():
         x, info = bicgstab(K, p1, rtol=1e-10, atol=0.0, maxiter=80, M=Mv, callback=lambda _: its.__setitem__(0, its[0] + 1))
         rel = np.linalg.norm(p1 - K @ x) / np.linalg.norm(p1)
         assert rel < 1e-9 and its[0] < 60, (ff, rel, its[0])
+
+
+def test_complex64_krylov_needs_the_split_vcycle():
+    """Numerical premise of a complex64 Krylov iteration under the edge multigrid: with every
+    vector stored in complex64, the V-cycle that carries its nodal corrections as a potential
+    psi beside x (A(x + G psi) = K x - i w mu Ms G psi) lets BiCGStab reach 1e-12 as in FP64,
+    while the same V-cycle adding G phi into x stalls (its gradient parts, ~1/(w mu sigma) in
+    air, swamp the curl parts in complex64)."""
+    m = syn.small_aniso(n=16, nair=8, nz_earth=24, seed=0, freqs=(0.01, 1.0))
+    om = O.OracleModel(m.nx, m.ny, m.nz, m.nair, m.a, m.b, m.c, m.sigma, m.freq, m.recv)
+    for ff in m.freq:
+        its, rel, hist = O.complex64_vcycle_bicgstab(om, ff, split=True)
+        assert rel < 1e-12 and its <= 32, (ff, its, rel, hist)
+    its, rel, hist = O.complex64_vcycle_bicgstab(om, 0.01, split=False, maxit=40)
+    assert rel > 1e-8, (its, rel, hist)
