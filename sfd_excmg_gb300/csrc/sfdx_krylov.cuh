@@ -109,6 +109,21 @@ template <class T> static int emg_prepare(Plan& P, const Level& LV) {
             if (b->p != before) P.emg_epoch++;
         }
     }
+    if (P.split && std::is_same<T, float>::value) {
+        for (int m = 0; m <= l; m++) {
+            const Level& L = P.lev[m];
+            const size_t ev = (size_t)L.nl * P.ns * sizeof(cplx<T>);
+            const size_t nv = (size_t)(L.nx + 1) * (L.ny + 1) * (L.nz + 1) * P.ns * sizeof(cplx<T>);
+            DBuf* bufs[3] = {&L.emg_g, &L.emg_t, &L.emg_psi};
+            const size_t need[3] = {ev, ev, m < l ? nv : 0};
+            for (int q = 0; q < 3; q++) {
+                if (!need[q]) continue;
+                void* before = bufs[q]->p;
+                RC(bufs[q]->alloc(need[q]));
+                if (bufs[q]->p != before) P.emg_epoch++;
+            }
+        }
+    }
     for (int m = 0; m <= l; m++) {
         const Level& L = P.lev[m];
         RC(nodal_setup(P, L));
@@ -180,6 +195,75 @@ static void emg_vcycle(Plan& P, int l, const cplx<T>* b, cplx<T>* x, bool pre) {
     emg_smooth<T, VS>(P, L, c, b, x);
 }
 
+// ---- split V-cycle (P.split): x and the nodal potential psi of each level
+// q = b + i wm Ms (x + G psi) ; phi = w D^-1 G^T V q ; psi += phi
+template <class T, int VS>
+static void emg_nodal_split(Plan& P, const Level& L, const VCfg& c, const cplx<T>* b, const cplx<T>* x, cplx<T>* psi) {
+    const KState* dst = P.d_state.as<KState>();
+    cplx<T>* xs = L.emg_g.as<cplx<T>>();
+    cplx<T>* q = L.emg_r.as<cplx<T>>();
+    cplx<T>* phi = L.emg_phi.as<cplx<T>>();
+    const uint32_t np = (uint32_t)(L.nx + 1) * (L.ny + 1) * (L.nz + 1);
+    // the mass product has no curl-curl cancellation: x + G psi in one vector is fine here
+    vlaunch(k_mg_xpg_v<T, VS>, L.nl * c.sg.G, c.B, 0, P.st, L.lev<T>(), L.mesh, c.sg, dst, x, (const cplx<T>*)psi, xs);
+    vlaunch(k_mg_mres_v<T, VS>, L.nl * c.sg.G, c.B, 0, P.st, L.lev<T>(), L.mesh, c.sg, dst, b, (const cplx<T>*)xs, q);
+    vlaunch(k_mg_node_v<T, VS>, (int64_t)np * c.sg.G, c.B, 0, P.st, L.lev<T>(), L.mesh, c.sg, np, dst,
+            (const cplx<T>*)q, L.mg[0].dinv.as<float>(), phi, (T)emg_nodal_omega(), (T)0);
+    vlaunch(k_mg_nadd_v<T, VS>, (int64_t)np * c.sg.G, c.B, 0, P.st, c.sg, dst, np, psi, (const cplx<T>*)phi);
+}
+// r = b - A x + i wm Ms G psi  (= b - A (x + G psi)) into L.emg_r
+template <class T, int VS>
+static void emg_res_split(Plan& P, const Level& L, const VCfg& c, const cplx<T>* b, const cplx<T>* x,
+                          const cplx<T>* psi) {
+    const KState* dst = P.d_state.as<KState>();
+    cplx<T>* t = L.emg_t.as<cplx<T>>();
+    cplx<T>* g = L.emg_g.as<cplx<T>>();
+    vlaunch(k_mg_res_v<T, VS>, L.nl * c.sg.G, c.B, 0, P.st, L.lev<T>(), L.mesh, c.sg, dst, b, x, t);
+    vlaunch(k_mg_xpg_v<T, VS>, L.nl * c.sg.G, c.B, 0, P.st, L.lev<T>(), L.mesh, c.sg, dst, (const cplx<T>*)nullptr,
+            psi, g);
+    vlaunch(k_mg_mres_v<T, VS>, L.nl * c.sg.G, c.B, 0, P.st, L.lev<T>(), L.mesh, c.sg, dst, (const cplx<T>*)t,
+            (const cplx<T>*)g, L.emg_r.as<cplx<T>>());
+}
+// smoothing step: r = b - A(x + G psi); x += S^-1 r; nodal step
+template <class T, int VS>
+static void emg_smooth_split(Plan& P, const Level& L, const VCfg& c, const cplx<T>* b, cplx<T>* x, cplx<T>* psi) {
+    const KState* dst = P.d_state.as<KState>();
+    cplx<T>* z = L.emg_z.as<cplx<T>>();
+    emg_res_split<T, VS>(P, L, c, b, x, psi);
+    precond_ssor<T, VS, RHS_VEC>(P, L, z, L.emg_r.as<cplx<T>>(), nullptr, nullptr);
+    vlaunch(k_mg_add_v<T, VS>, L.nl * c.sg.G, c.B, 0, P.st, L.mesh, c.sg, dst, x, (const cplx<T>*)z);
+    emg_nodal_split<T, VS>(P, L, c, b, x, psi);
+}
+// (x, psi) = V-cycle(b) on level l, psi from zero; `pre`: x already holds S^-1 b
+template <class T, int VS>
+static void emg_vcycle_split(Plan& P, int l, const cplx<T>* b, cplx<T>* x, cplx<T>* psi, bool pre) {
+    const Level& L = P.lev[l];
+    const VCfg c = vcfg(P, L.nl, 0, VS);
+    const KState* dst = P.d_state.as<KState>();
+    const uint32_t np = (uint32_t)(L.nx + 1) * (L.ny + 1) * (L.nz + 1);
+    vlaunch(k_psi_zero_v<T, VS, false>, (int64_t)np * c.sg.G, c.B, 0, P.st, c.sg, dst, np, psi);
+    if (!pre) precond_ssor<T, VS, RHS_VEC>(P, L, x, const_cast<cplx<T>*>(b), nullptr, nullptr);
+    emg_nodal_split<T, VS>(P, L, c, b, x, psi);
+    if (l == 0) {
+        for (int s = 1; s < emg_coarse_sweeps(); s++) emg_smooth_split<T, VS>(P, L, c, b, x, psi);
+        return;
+    }
+    const Level& C = P.lev[l - 1];
+    const VCfg cc = vcfg(P, C.nl, 0, VS);
+    cplx<T>* bc = C.emg_b.as<cplx<T>>();
+    cplx<T>* xc = C.emg_x.as<cplx<T>>();
+    cplx<T>* pc = C.emg_psi.as<cplx<T>>();
+    emg_res_split<T, VS>(P, L, c, b, x, psi);
+    vlaunch(k_mg_restrict_v<T, VS>, C.nl * cc.sg.G, cc.B, 0, P.st, L.lev<T>(), L.mesh, C.lev<T>(), C.mesh, cc.sg, dst,
+            (const cplx<T>*)L.emg_r.as<cplx<T>>(), bc);
+    emg_vcycle_split<T, VS>(P, l - 1, bc, xc, pc, false);
+    vlaunch(k_mg_prolong_v<T, VS>, L.nl * c.sg.G, c.B, 0, P.st, L.lev<T>(), L.mesh, C.mesh, c.sg, dst,
+            (const cplx<T>*)xc, x);
+    vlaunch(k_mg_nprolong_v<T, VS>, (int64_t)np * c.sg.G, c.B, 0, P.st, L.lev<T>(), L.mesh, C.mesh, c.sg, dst, np,
+            (const cplx<T>*)pc, psi);
+    emg_smooth_split<T, VS>(P, L, c, b, x, psi);
+}
+
 // Complex64 V-cycle for a complex128 Krylov solve (P.pf32): MODE's vector
 // update in FP64 with the result rounded to complex64, the V-cycle with the
 // complex64 grouping of the plan, the output widened to FP64.  The Krylov
@@ -211,6 +295,13 @@ static void precond(Plan& P, const Level& LV, cplx<T>* out, cplx<T>* q, const cp
     if constexpr (std::is_same<T, double>::value) {
         if (P.o.precond == 'G' && P.pf32) {
             emg_precond32<VS, MODE>(P, LV, out, q, r, v, aux);
+            return;
+        }
+    }
+    if constexpr (std::is_same<T, float>::value) {
+        if (P.o.precond == 'G' && P.split) {
+            precond_ssor<T, VS, MODE>(P, LV, out, q, r, v, aux);
+            emg_vcycle_split<T, VS>(P, level_index(P, LV), q, out, static_cast<cplx<T>*>(P.psi_out), true);
             return;
         }
     }
@@ -255,7 +346,9 @@ static std::vector<uintptr_t> interval_key(const Plan& P, const Level& LV, int s
                                 (uintptr_t)P.hist_stride, (uintptr_t)LV.sig32.p, (uintptr_t)LV.sig64.p,
                                 (uintptr_t)LV.tab32.p, (uintptr_t)LV.tab64.p, (uintptr_t)LV.rc_ok,
                                 (uintptr_t)LV.rc32.p, (uintptr_t)LV.rc64.p,
-                                (uintptr_t)(P.o.ssor_omega * 1e6), (uintptr_t)P.emg_epoch, (uintptr_t)P.pf32};
+                                (uintptr_t)(P.o.ssor_omega * 1e6), (uintptr_t)P.emg_epoch, (uintptr_t)P.pf32,
+                                (uintptr_t)P.split, (uintptr_t)P.psi_y.p, (uintptr_t)P.psi_z.p, (uintptr_t)P.psi_x.p,
+                                (uintptr_t)P.g_y.p, (uintptr_t)P.g_z.p};
     for (const DBuf& b : P.kv) k.push_back((uintptr_t)b.p);
     k.insert(k.end(), extra);
     return k;
@@ -266,6 +359,20 @@ static std::vector<uintptr_t> interval_key(const Plan& P, const Level& LV, int s
 // correction runs on the host every corr_intv iterations)
 static bool graph_interval(const Plan& P, int it, int itmax, bool host_work) {
     return P.o.use_graphs && !host_work && it > 8 && (it - 1) % 8 == 0 && it + 7 <= itmax;
+}
+
+// x64 += G psi_x, psi_x = 0 (split Krylov vectors: the nodal part of the
+// complex64 partial solution)
+template <class T, int VS, bool ALL>
+static void split_flush(Plan& P, const Level& LV, const VCfg& c, double2* x64) {
+    if constexpr (std::is_same<T, float>::value) {
+        const KState* dst = P.d_state.as<KState>();
+        const uint32_t np = (uint32_t)(LV.nx + 1) * (LV.ny + 1) * (LV.nz + 1);
+        cplx<T>* px = P.psi_x.as<cplx<T>>();
+        vlaunch(k_flush_psi_v<T, VS, ALL>, LV.nl * c.sg.G, c.B, 0, P.st, LV.lev<double>(), LV.mesh, c.sg, dst, x64,
+                (const cplx<T>*)px);
+        vlaunch(k_psi_zero_v<T, VS, ALL>, (int64_t)np * c.sg.G, c.B, 0, P.st, c.sg, dst, np, px);
+    }
 }
 
 // FP64 residual replacement for the systems still running or whose complex64
@@ -281,6 +388,7 @@ static int reliable_update(Plan& P, const Level& LV, const Reliable& rel, cplx<T
     KState* dst = P.d_state.as<KState>();
     KL(k_reactivate<<<(ns + 127) / 128, 128, 0, P.st>>>(dst, ns));
     vlaunch(k_flush_v<T, VS, false>, LV.nl * c.sg.G, c.B, 0, P.st, LV.mesh, c.sg, dst, rel.x64, x32, rel.xb);
+    if (P.split) split_flush<T, VS, false>(P, LV, c, rel.x64);
     vlaunch(k_reliable_v<T, VSD>, LV.nl * cd.sg.G, cd.B, cd.smem, P.st, LV.lev<double>(), LV.mesh, cd.sg, dst, rel.b64, rel.x64, r, rhat, solver, redbuf(P));
     CK(cudaGetLastError());
     RC(sync_state(P));
@@ -376,7 +484,41 @@ static int bicgstab_v(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, co
     int last_rel = 0;
     ResMin emin;  // smallest residual per system (pf32_divergence)
     const bool div1 = !rel && std::is_same<T, double>::value && P.o.div_cor == 1;
+    // split Krylov vectors (P.split, complex64 iteration under the split V-cycle):
+    // y + G psi_y, z + G psi_z, partial solution x + G psi_x
+    const bool split = rel && P.split && std::is_same<T, float>::value;
+    const uint32_t npn = (uint32_t)(LV.nx + 1) * (LV.ny + 1) * (LV.nz + 1);
+    cplx<T> *py = nullptr, *pz = nullptr, *px = nullptr, *gy = nullptr, *gz = nullptr;
+    if (split) {
+        const size_t nb = (size_t)npn * ns * sizeof(cplx<T>);
+        for (DBuf* d : {&P.psi_y, &P.psi_z, &P.psi_x}) RC(d->alloc(nb));
+        for (DBuf* d : {&P.g_y, &P.g_z}) RC(d->alloc(vb));
+        py = P.psi_y.as<cplx<T>>();
+        pz = P.psi_z.as<cplx<T>>();
+        px = P.psi_x.as<cplx<T>>();
+        gy = P.g_y.as<cplx<T>>();
+        gz = P.g_z.as<cplx<T>>();
+        CK(cudaMemsetAsync(px, 0, nb, P.st));
+    }
     auto body = [&]() {
+        if (split) {
+            P.psi_out = py;
+            precond<T, VS, RHS_PUPD>(P, LV, y, p, r, v);
+            vlaunch(k_mg_xpg_v<T, VS>, LV.nl * c.sg.G, c.B, 0, P.st, L, M, c.sg, dst, (const cplx<T>*)nullptr,
+                    (const cplx<T>*)py, gy);
+            vlaunch(k_bicg_v_split_v<T, VS>, LV.nl * c.sg.G, c.B, c.smem, P.st, L, M, c.sg, dst, y, gy, v, rhat,
+                    redbuf(P));
+            P.psi_out = pz;
+            precond<T, VS, RHS_SUPD>(P, LV, z, s, r, v);
+            vlaunch(k_mg_xpg_v<T, VS>, LV.nl * c.sg.G, c.B, 0, P.st, L, M, c.sg, dst, (const cplx<T>*)nullptr,
+                    (const cplx<T>*)pz, gz);
+            vlaunch(k_bicg_t_split_v<T, VS>, LV.nl * c.sg.G, c.B, c.smem, P.st, L, M, c.sg, dst, z, gz, t, s,
+                    redbuf(P));
+            vlaunch(k_split_psi_upd_v<T, VS>, (int64_t)npn * c.sg.G, c.B, 0, P.st, c.sg, dst, npn, px,
+                    (const cplx<T>*)py, (const cplx<T>*)pz);
+            vlaunch(k_bicg_upd_v<T, T, VS>, LV.nl * c.sg.G, c.B, c.smem, P.st, M, c.sg, dst, x, y, z, s, t, r, rhat, redbuf(P), P.hist, P.hist_stride);
+            return;
+        }
         precond<T, VS, RHS_PUPD>(P, LV, y, p, r, v);
         vlaunch(k_bicg_v_v<T, VS>, LV.nl * c.sg.G, c.B, c.smem, P.st, L, M, c.sg, dst, y, v, rhat, redbuf(P));
         precond<T, VS, RHS_SUPD>(P, LV, z, s, r, v);
@@ -414,8 +556,10 @@ static int bicgstab_v(Plan& P, const Level& LV, const cplx<T>* b, cplx<T>* x, co
             if (!act) break;
         }
     }
-    if (rel)
+    if (rel) {
         vlaunch(k_flush_v<T, VS, true>, LV.nl * c.sg.G, c.B, 0, P.st, M, c.sg, dst, rel->x64, x, nullptr);
+        if (split) split_flush<T, VS, true>(P, LV, c, rel->x64);
+    }
     RC(sync_state(P));
     return SFDX_OK;
 }

@@ -425,4 +425,304 @@ __global__ void k_mg_restrict_v(Lev<T> Lf, Mesh Mf, Lev<T> Lc, Mesh Mc, SysG sgp
     }
 }
 
+// ------------------------------------------------------------------ split V-cycle
+// For a complex64 Krylov iteration under the multigrid (SFDX_MG_SPLIT): the
+// V-cycle carries its nodal corrections as a potential psi beside x instead
+// of adding G phi into x, and A(x + G psi) = A x - i wm Ms G psi (C G = 0), so
+// no complex64 vector holds a curl part beside a much larger gradient part.
+
+// out = x + G psi on interior edges, x on boundary edges (x == nullptr: 0)
+template <class T, int VS>
+__global__ void k_mg_xpg_v(Lev<T> L, Mesh M, SysG sgp, const KState* st, const cplx<T>* __restrict__ x,
+                           const cplx<T>* __restrict__ psi, cplx<T>* __restrict__ out) {
+    const int ns = sgp.ns, s0 = (threadIdx.x % sgp.G) * VS;
+    const SysV<T, VS> S = load_sys<T, VS>(st, s0);
+    if (!S.act) return;
+    const uint32_t nx1 = M.nx + 1, pl = nx1 * (M.ny + 1);
+    SFDX_GRID_LOOP(t, M.nl * sgp.G) {
+        const uint32_t e = fdiv(sgp.fG, t);
+        int i, j, k;
+        const int o = mdecode(M, e, i, j, k);
+        const size_t g = (size_t)e * ns + s0;
+        CV<T, VS> xv;
+        if (x) cvld<T, VS>(xv, x + g);
+        else cvzero<T, VS>(xv);
+        if (!mbnd(M, o, i, j, k)) {
+            const uint32_t n0 = ((uint32_t)k * (M.ny + 1) + j) * nx1 + i;
+            uint32_t n1;
+            T rl;
+            if (o == OX) { n1 = n0 + 1; rl = __ldg(L.ax.rh + i); }
+            else if (o == OY) { n1 = n0 + nx1; rl = __ldg(L.ay.rh + j); }
+            else { n1 = n0 + pl; rl = __ldg(L.az.rh + k); }
+            CV<T, VS> a, b;
+            cvld<T, VS>(a, psi + (size_t)n0 * ns + s0);
+            cvld<T, VS>(b, psi + (size_t)n1 * ns + s0);
+#pragma unroll
+            for (int u = 0; u < VS; u++)
+                xv.v[u] = mk<T>(xv.v[u].x + rl * (b.v[u].x - a.v[u].x), xv.v[u].y + rl * (b.v[u].y - a.v[u].y));
+        }
+        cvst_m<T, VS>(out + g, xv, S.act);
+    }
+}
+
+// psi += phi (node vectors [node][ns])
+template <class T, int VS>
+__global__ void k_mg_nadd_v(SysG sgp, const KState* st, uint32_t np, cplx<T>* __restrict__ psi,
+                            const cplx<T>* __restrict__ phi) {
+    const int ns = sgp.ns, s0 = (threadIdx.x % sgp.G) * VS;
+    const SysV<T, VS> S = load_sys<T, VS>(st, s0);
+    if (!S.act) return;
+    SFDX_GRID_LOOP(t, np * sgp.G) {
+        const size_t g = (size_t)fdiv(sgp.fG, t) * ns + s0;
+        CV<T, VS> a, d;
+        cvldw<T, VS>(a, psi + g);
+        cvld<T, VS>(d, phi + g);
+#pragma unroll
+        for (int u = 0; u < VS; u++) a.v[u] = a.v[u] + d.v[u];
+        cvst_m<T, VS>(psi + g, a, S.act);
+    }
+}
+
+// psi_f += Pn psi_c at the interior fine nodes: the trilinear interpolation on
+// the nested non-uniform node grids (the node terms of the edge prolongation,
+// with which it commutes: P G_c = G_f Pn)
+template <class T, int VS>
+__global__ void k_mg_nprolong_v(Lev<T> Lf, Mesh Mf, Mesh Mc, SysG sgp, const KState* st, uint32_t npf,
+                                const cplx<T>* __restrict__ psic, cplx<T>* __restrict__ psif) {
+    const int ns = sgp.ns, s0 = (threadIdx.x % sgp.G) * VS;
+    const SysV<T, VS> S = load_sys<T, VS>(st, s0);
+    if (!S.act) return;
+    const uint32_t cx1 = Mc.nx + 1, cy1 = Mc.ny + 1;
+    SFDX_GRID_LOOP(t, npf * sgp.G) {
+        const uint32_t n = fdiv(sgp.fG, t);
+        int i, j, k;
+        node_ijk(Mf, n, i, j, k);
+        if (node_bnd(Mf, i, j, k)) continue;
+        int ca[2], cb[2], cc[2];
+        T wa[2], wb[2], wc[2];
+        const int na = mg_node_terms<T>(Lf.ax, i, ca, wa);
+        const int nb = mg_node_terms<T>(Lf.ay, j, cb, wb);
+        const int nc = mg_node_terms<T>(Lf.az, k, cc, wc);
+        CV<T, VS> acc;
+        cvzero<T, VS>(acc);
+        for (int c = 0; c < nc; c++)
+            for (int b = 0; b < nb; b++)
+                for (int a = 0; a < na; a++) {
+                    const uint32_t cn = ((uint32_t)cc[c] * cy1 + (uint32_t)cb[b]) * cx1 + (uint32_t)ca[a];
+                    const T w = wa[a] * wb[b] * wc[c];
+                    CV<T, VS> v;
+                    cvld<T, VS>(v, psic + (size_t)cn * ns + s0);
+#pragma unroll
+                    for (int u = 0; u < VS; u++) {
+                        acc.v[u].x += w * v.v[u].x;
+                        acc.v[u].y += w * v.v[u].y;
+                    }
+                }
+        const size_t g = (size_t)n * ns + s0;
+        CV<T, VS> pv;
+        cvldw<T, VS>(pv, psif + g);
+#pragma unroll
+        for (int u = 0; u < VS; u++) pv.v[u] = pv.v[u] + acc.v[u];
+        cvst_m<T, VS>(psif + g, pv, S.act);
+    }
+}
+
+// Krylov side of the split: psi_x += alpha psi_y + omega psi_z (this
+// iteration's BiCGStab scalars; before k_bicg_upd_v retires converged systems)
+template <class T, int VS>
+__global__ void k_split_psi_upd_v(SysG sgp, const KState* st, uint32_t np, cplx<T>* __restrict__ px,
+                                  const cplx<T>* __restrict__ py, const cplx<T>* __restrict__ pz) {
+    const int ns = sgp.ns, s0 = (threadIdx.x % sgp.G) * VS;
+    const SysV<T, VS> S = load_sys<T, VS>(st, s0);
+    if (!S.act) return;
+    cplx<T> al[VS], om[VS];
+#pragma unroll
+    for (int u = 0; u < VS; u++) {
+        al[u] = cst<T>(st[s0 + u].alpha);
+        om[u] = cst<T>(st[s0 + u].omega);
+    }
+    SFDX_GRID_LOOP(t, np * sgp.G) {
+        const size_t g = (size_t)fdiv(sgp.fG, t) * ns + s0;
+        CV<T, VS> a, y, z;
+        cvldw<T, VS>(a, px + g);
+        cvld<T, VS>(y, py + g);
+        cvld<T, VS>(z, pz + g);
+#pragma unroll
+        for (int u = 0; u < VS; u++) a.v[u] = a.v[u] + cmul<T>(al[u], y.v[u]) + cmul<T>(om[u], z.v[u]);
+        cvst_m<T, VS>(px + g, a, S.act);
+    }
+}
+
+// x64 += G psi (FP64) on interior edges: the nodal part of the complex64
+// partial solution folded into the FP64 solution.  ALL: every system that is
+// not NaN (the final fold), else the active ones (reliable updates), as k_flush_v.
+template <class T, int VS, bool ALL>
+__global__ void k_flush_psi_v(Lev<double> L, Mesh M, SysG sgp, const KState* st, double2* __restrict__ x64,
+                              const cplx<T>* __restrict__ psi) {
+    const int ns = sgp.ns, s0 = (threadIdx.x % sgp.G) * VS;
+    SysV<T, VS> S = load_sys<T, VS>(st, s0);
+    if (ALL) {
+        S.act = 0;
+#pragma unroll
+        for (int v = 0; v < VS; v++) S.act |= (st[s0 + v].status != ST_NAN ? 1u : 0u) << v;
+    }
+    if (!S.act) return;
+    const uint32_t nx1 = M.nx + 1, pl = nx1 * (M.ny + 1);
+    SFDX_GRID_LOOP(t, M.nl * sgp.G) {
+        const uint32_t e = fdiv(sgp.fG, t);
+        int i, j, k;
+        const int o = mdecode(M, e, i, j, k);
+        if (mbnd(M, o, i, j, k)) continue;
+        const uint32_t n0 = ((uint32_t)k * (M.ny + 1) + j) * nx1 + i;
+        uint32_t n1;
+        double rl;
+        if (o == OX) { n1 = n0 + 1; rl = __ldg(L.ax.rh + i); }
+        else if (o == OY) { n1 = n0 + nx1; rl = __ldg(L.ay.rh + j); }
+        else { n1 = n0 + pl; rl = __ldg(L.az.rh + k); }
+        const size_t g = (size_t)e * ns + s0;
+        CV<T, VS> a, b;
+        cvld<T, VS>(a, psi + (size_t)n0 * ns + s0);
+        cvld<T, VS>(b, psi + (size_t)n1 * ns + s0);
+        CV<double, VS> xv;
+        cvldw<double, VS>(xv, x64 + g);
+#pragma unroll
+        for (int u = 0; u < VS; u++)
+            xv.v[u] = make_double2(xv.v[u].x + rl * ((double)b.v[u].x - (double)a.v[u].x),
+                                   xv.v[u].y + rl * ((double)b.v[u].y - (double)a.v[u].y));
+        cvst_m<double, VS>(x64 + g, xv, S.act);
+    }
+}
+// psi = 0 for the systems k_flush_psi_v<T, VS, ALL> folded
+template <class T, int VS, bool ALL>
+__global__ void k_psi_zero_v(SysG sgp, const KState* st, uint32_t np, cplx<T>* __restrict__ psi) {
+    const int ns = sgp.ns, s0 = (threadIdx.x % sgp.G) * VS;
+    SysV<T, VS> S = load_sys<T, VS>(st, s0);
+    if (ALL) {
+        S.act = 0;
+#pragma unroll
+        for (int v = 0; v < VS; v++) S.act |= (st[s0 + v].status != ST_NAN ? 1u : 0u) << v;
+    }
+    if (!S.act) return;
+    SFDX_GRID_LOOP(t, np * sgp.G) {
+        const size_t g = (size_t)fdiv(sgp.fG, t) * ns + s0;
+        CV<T, VS> z;
+        cvzero<T, VS>(z);
+        cvst_m<T, VS>(psi + g, z, S.act);
+    }
+}
+
+// A (y + G psi) = A y - i wm Ms g with g = G psi materialised (k_mg_xpg_v):
+// the row's operator on y plus the mass row on g, boundary rows y
+template <class T, int VS>
+__device__ __forceinline__ void split_row(const Lev<T>& L, const Mesh& M, int o, uint32_t e, int i, int j, int k,
+                                          const cplx<T>* y, const cplx<T>* gv, int ns, int s0, const T (&wm)[VS],
+                                          CV<T, VS>& val) {
+    CV<T, VS> ye, mq, zb;
+    cvld<T, VS>(ye, y + (size_t)e * ns + s0);
+    row_apply<T, VS>(L, M, o, e, i, j, k, y, ns, s0, wm, ye, val);
+    cvzero<T, VS>(zb);
+    if (o == OX) mg_mass_row<T, VS, OX>(L, M, e, i, j, k, gv, ns, s0, wm, zb, mq);
+    else if (o == OY) mg_mass_row<T, VS, OY>(L, M, e, i, j, k, gv, ns, s0, wm, zb, mq);
+    else mg_mass_row<T, VS, OZ>(L, M, e, i, j, k, gv, ns, s0, wm, zb, mq);
+#pragma unroll
+    for (int u = 0; u < VS; u++) val.v[u] = val.v[u] - mq.v[u];  // mq = i wm Ms g
+}
+
+// k_bicg_v_v on the split vector: v = A (y + G psi_y) ; alpha = rho / <rhat, v>
+template <class T, int VS>
+__global__ void k_bicg_v_split_v(Lev<T> L, Mesh M, SysG sgp, KState* st, const cplx<T>* __restrict__ y,
+                                 const cplx<T>* __restrict__ gy, cplx<T>* __restrict__ v,
+                                 const cplx<T>* __restrict__ rhat, RedBuf rb) {
+    extern __shared__ double2 smem[];
+    typedef typename AccOf<T>::type A;
+    const int ns = sgp.ns, s0 = (threadIdx.x % sgp.G) * VS;
+    const SysV<T, VS> S = load_sys<T, VS>(st, s0);
+    A ar[VS], ai[VS];
+#pragma unroll
+    for (int u = 0; u < VS; u++) ar[u] = ai[u] = 0;
+    if (S.act)
+        SFDX_GRID_LOOP(t, M.nl * sgp.G) {
+            uint32_t e;
+            int i, j, k;
+            const int o = mdecode_plane(M, fdiv(sgp.fG, t), e, i, j, k);
+            const size_t g = (size_t)e * ns + s0;
+            CV<T, VS> val, h;
+            split_row<T, VS>(L, M, o, e, i, j, k, y, gy, ns, s0, S.wm, val);
+            cvst_m<T, VS>(v + g, val, S.act);
+            cvld<T, VS>(h, rhat + g);
+#pragma unroll
+            for (int u = 0; u < VS; u++) {
+                cplx<T> d = cdot<T>(h.v[u], val.v[u]);
+                ar[u] += d.x;
+                ai[u] += d.y;
+            }
+        }
+    double2 acc[1][VS];
+#pragma unroll
+    for (int u = 0; u < VS; u++) acc[0][u] = make_double2(ar[u], ai[u]);
+    if (!vreduce_last<1, VS>(acc, sgp, rb, smem)) return;
+    const int B = blockDim.x;
+    for (int ss = threadIdx.x; ss < ns; ss += B) {
+        if (!st[ss].active) continue;
+        double2 d = smem[B + ss];
+        double2 rho = st[ss].rho;
+        double den = d.x * d.x + d.y * d.y;
+        st[ss].alpha = make_double2((rho.x * d.x + rho.y * d.y) / den, (rho.y * d.x - rho.x * d.y) / den);
+        if (!isfinite(st[ss].alpha.x) || !isfinite(st[ss].alpha.y)) {
+            st[ss].active = 0;
+            st[ss].status = ST_BREAK;
+        }
+    }
+}
+
+// k_bicg_t_v on the split vector: t = A (z + G psi_z) ; omega = <t,s>/<t,t>
+template <class T, int VS>
+__global__ void k_bicg_t_split_v(Lev<T> L, Mesh M, SysG sgp, KState* st, const cplx<T>* __restrict__ z,
+                                 const cplx<T>* __restrict__ gz, cplx<T>* __restrict__ tv,
+                                 const cplx<T>* __restrict__ sv, RedBuf rb) {
+    extern __shared__ double2 smem[];
+    typedef typename AccOf<T>::type A;
+    const int ns = sgp.ns, s0 = (threadIdx.x % sgp.G) * VS;
+    const SysV<T, VS> S = load_sys<T, VS>(st, s0);
+    A a0r[VS], a0i[VS], a1[VS];
+#pragma unroll
+    for (int u = 0; u < VS; u++) a0r[u] = a0i[u] = a1[u] = 0;
+    if (S.act)
+        SFDX_GRID_LOOP(t, M.nl * sgp.G) {
+            uint32_t e;
+            int i, j, k;
+            const int o = mdecode_plane(M, fdiv(sgp.fG, t), e, i, j, k);
+            const size_t g = (size_t)e * ns + s0;
+            CV<T, VS> val, ss;
+            split_row<T, VS>(L, M, o, e, i, j, k, z, gz, ns, s0, S.wm, val);
+            cvst_m<T, VS>(tv + g, val, S.act);
+            cvld<T, VS>(ss, sv + g);
+#pragma unroll
+            for (int u = 0; u < VS; u++) {
+                cplx<T> d = cdot<T>(val.v[u], ss.v[u]);
+                a0r[u] += d.x;
+                a0i[u] += d.y;
+                a1[u] += cabs2<T>(val.v[u]);
+            }
+        }
+    double2 acc[2][VS];
+#pragma unroll
+    for (int u = 0; u < VS; u++) {
+        acc[0][u] = make_double2(a0r[u], a0i[u]);
+        acc[1][u] = make_double2(a1[u], 0.0);
+    }
+    if (!vreduce_last<2, VS>(acc, sgp, rb, smem)) return;
+    const int B = blockDim.x;
+    for (int ss = threadIdx.x; ss < ns; ss += B) {
+        if (!st[ss].active) continue;
+        double2 ts = smem[B + ss];
+        double tt = smem[B + ns + ss].x;
+        st[ss].omega = make_double2(ts.x / tt, ts.y / tt);
+        if (!isfinite(st[ss].omega.x) || !isfinite(st[ss].omega.y) || (st[ss].omega.x == 0.0 && st[ss].omega.y == 0.0)) {
+            st[ss].active = 0;
+            st[ss].status = ST_BREAK;
+        }
+    }
+}
+
 }  // namespace sfdx

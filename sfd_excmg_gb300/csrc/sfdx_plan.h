@@ -203,6 +203,7 @@ struct Level {
     // residual, smoother output, nodal update, and (below the solve level)
     // the level's right-hand side and solution
     mutable DBuf emg_r, emg_z, emg_phi, emg_b, emg_x;
+    mutable DBuf emg_psi, emg_g, emg_t;  // split V-cycle: nodal potential, edge temporaries
 
     void set_dims(int X, int Y, int Z) {
         nx = X; ny = Y; nz = Z;
@@ -317,6 +318,13 @@ struct Plan {
     // emg_q32 / emg_o32: the V-cycle's complex64 input and output
     bool pf32 = false;
     DBuf emg_q32, emg_o32;
+    // complex64 Krylov iteration on split vectors y + G psi under the split
+    // V-cycle (SFDX_MG_SPLIT): psi_out receives the V-cycle's nodal potential;
+    // psi_y, psi_z those of the two preconditioned vectors, psi_x the partial
+    // solution's; g_y, g_z = G psi_y, G psi_z on the edges
+    bool split = false;
+    void* psi_out = nullptr;
+    DBuf psi_y, psi_z, psi_x, g_y, g_z;
     Plan() = default;
     Plan(const Plan&) = delete;
     ~Plan() {

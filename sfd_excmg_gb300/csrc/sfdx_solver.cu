@@ -294,9 +294,23 @@ int solve_level(Plan& P, const Level& LV, double tol, int itmax, bool coarse, st
     // TFQMR and BiCG have no complex64 / reliable-update form: FP64 in every plan
     if (coarse || P.o.precision == SFDX_FP64 || P.o.solver == SFDX_SOLVER_TFQMR || P.o.solver == SFDX_SOLVER_BICG)
         return solve_level_fp64(P, LV, tol, itmax, its, status);
-    // mixed precision with the multigrid preconditioner: complex128 Krylov
-    // vectors and operator, complex64 V-cycle (SFDX_MG_PF32=0: the complex64
-    // Krylov iteration with FP64 reliable updates of the SSOR plans instead)
+    // mixed precision with the multigrid preconditioner and the other solvers
+    // (or SFDX_MG_SPLIT=0): complex128 Krylov vectors and operator, complex64
+    // V-cycle (SFDX_MG_PF32=0: the complex64 Krylov iteration with FP64
+    // reliable updates of the SSOR plans instead)
+    // mixed precision, multigrid, BiCGStab: complex64 BiCGStab on split vectors
+    // (y + G psi) under the split V-cycle, FP64 reliable updates
+    // (SFDX_MG_SPLIT=0: the complex128 Krylov iteration below instead)
+    static const bool split = [] {
+        const char* e = getenv("SFDX_MG_SPLIT");
+        return !(e && e[0] == '0');
+    }();
+    if (P.o.precond == 'G' && split && P.o.solver == SFDX_SOLVER_BICGSTAB) {
+        P.split = true;
+        const int rc = solve_level_mixed(P, LV, tol, itmax, its, status);
+        P.split = false;
+        return rc;
+    }
     static const bool krylov64 = [] {
         const char* e = getenv("SFDX_MG_PF32");
         return !(e && e[0] == '0');

@@ -119,10 +119,11 @@ def test_fields_of_an_earlier_conductivity_are_refused():
 
 def test_mixed_multigrid_adjoint_at_low_frequency_matches_fp64():
     """The complex64 multigrid V-cycle under 1e-3 Hz adjoint solves on resistive ground (the
-    grf-inversion model: isotropic GRF, 1e-3..1e3 Hz).  Its gradient corrections there are
-    large enough for complex64 rounding to make the adjoint residual grow; such systems are
-    stopped and restarted with the FP64 V-cycle, so every adjoint system meets the tolerance
-    and the gradient agrees with the FP64 adjoint."""
+    grf-inversion model: isotropic GRF, 1e-3..1e3 Hz), where its gradient corrections are
+    largest.  The default mixed path (complex64 BiCGStab on split vectors, the nodal part kept
+    as a potential) converges there; under the complex128-Krylov path (SFDX_MG_SPLIT=0) such
+    systems stall, are stopped and restart with the FP64 V-cycle.  Either way every adjoint
+    system meets the tolerance and the gradient agrees with the FP64 adjoint."""
     m, mt = syn.grf_inversion(0), syn.grf_inversion_true(0)
     opts = dict(eps=1e-10, excmg=1, level=m.level, div_cor=2, corr_intv=40, corr_tol=1e-2, solver=1, precond="G")
     with S.Plan(mt, precision=S.FP64, **opts) as pt:
