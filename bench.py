@@ -9,9 +9,11 @@ with 4 levels.  Synthetic and seeded (numpy default_rng(0)): the reference
 publishes no model files for it.  Finest-level tolerance: the relative residual
 at which the impedances agree with the oracle's exact discrete answer to 1e-5
 (1e-12; the configuration's own 1e-7 leaves errors of ~1e-2).  Solver:
-BiCGStab with complex128 vectors and operator, right-preconditioned by a
-complex64 edge multigrid V-cycle (multi-colour SSOR + nodal smoother) over the
-EXCMG levels, consistent gradient correction between restart cycles.
+complex64 BiCGStab on split vectors (field plus nodal potential) with FP64
+reliable updates, right-preconditioned by the split edge multigrid V-cycle
+(multi-colour SSOR + nodal smoother) over the EXCMG levels, consistent
+gradient correction between restart cycles (SFDX_MG_SPLIT=0: complex128
+BiCGStab under a complex64 V-cycle).
 
 A step = one complete forward solve of all systems (both coarse levels,
 prolongations, the finer levels) followed by the impedances at the 1024
